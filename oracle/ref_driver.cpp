@@ -1,0 +1,311 @@
+// ref_driver.cpp -- runs the PANSFEM2 reference itself (its headers, compiled
+// here with g++) on the SIMP configurations and dumps full-precision results,
+// so the C oracle and the GPU library can be pinned against the real thing.
+//
+// TEST INFRASTRUCTURE: built by oracle/build_ref.sh into oracle/_ref/ only where
+// the reference source tree is present; the outputs become the committed
+// fixtures under tests/golden/.
+//
+// The SIMP loop is the call sequence of
+// sample/optimize/sample_optimize_density_oc.cpp:93-207 (OC) and
+// sample/optimize/sample_optimize_density_mma.cpp:98-203 (MMA), with the
+// configuration's parameters in place of the sample's literals, the linear
+// DensityFilter (or the sample's HeavisideFilter with heaviside=1) and no VTK
+// output.  Usage:  ref_driver <mode> out=<file> key=value ...
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <numeric>
+#include <cassert>
+#include <sstream>
+
+// CSR keeps indptr/indices/data private (CSR.h:71-74); the harness reads them
+// through an access-only remap while compiling the unmodified headers.
+#define private public
+#include "src/LinearAlgebra/Models/Vector.h"
+#include "src/FEM/Equation/PlaneStrain.h"
+#include "src/FEM/Equation/HeatTransfer.h"
+#include "src/FEM/Equation/Solid.h"
+#include "src/FEM/Controller/ShapeFunction.h"
+#include "src/FEM/Controller/GaussIntegration.h"
+#include "src/FEM/Controller/BoundaryCondition.h"
+#include "src/FEM/Controller/Assembling.h"
+#include "src/LinearAlgebra/Solvers/CG.h"
+#include "src/Optimize/Solver/OC.h"
+#include "src/Optimize/Solver/MMA.h"
+#include "src/Optimize/Filter/DensityFilter.h"
+#include "src/Optimize/Filter/HeavisideFilter.h"
+#include "src/PrePost/Mesher/SquareMesh.h"
+#include "src/FEM/Equation/General.h"
+
+using namespace PANSFEM2;
+
+// ---------------- tiny binary container: [namelen][name][type][count][data] ----------------
+struct Dump {
+    FILE* f;
+    explicit Dump(const std::string& path) { f = fopen(path.c_str(), "wb"); if (!f) { perror("open"); exit(2); } }
+    ~Dump() { fclose(f); }
+    void put(const std::string& name, int type, long long count, const void* data, size_t elem) {
+        int nl = (int)name.size();
+        fwrite(&nl, 4, 1, f); fwrite(name.data(), 1, nl, f);
+        fwrite(&type, 4, 1, f); fwrite(&count, 8, 1, f);
+        if (count) fwrite(data, elem, (size_t)count, f);
+    }
+    void d(const std::string& n, const std::vector<double>& v) { put(n, 0, (long long)v.size(), v.data(), 8); }
+    void i(const std::string& n, const std::vector<int>& v) { put(n, 1, (long long)v.size(), v.data(), 4); }
+};
+
+static std::map<std::string, std::string> g_args;
+static double argd(const char* k, double dflt) { auto it = g_args.find(k); return it == g_args.end() ? dflt : atof(it->second.c_str()); }
+static int argi(const char* k, int dflt) { auto it = g_args.find(k); return it == g_args.end() ? dflt : atoi(it->second.c_str()); }
+static std::string args(const char* k, const char* dflt) { auto it = g_args.find(k); return it == g_args.end() ? dflt : it->second; }
+
+// 3D structured grid in the SquareMesh i-major convention (no 3D mesher exists in the reference)
+static void grid3d(double lx, double ly, double lz, int nx, int ny, int nz, std::vector<Vector<double> >& x,
+                   std::vector<std::vector<int> >& el) {
+    auto nid = [&](int i, int j, int k) { return ((ny + 1) * i + j) * (nz + 1) + k; };
+    x.assign((size_t)(nx + 1) * (ny + 1) * (nz + 1), Vector<double>(3));
+    for (int i = 0; i <= nx; i++) for (int j = 0; j <= ny; j++) for (int k = 0; k <= nz; k++)
+        x[nid(i, j, k)] = {lx * (i / (double)nx), ly * (j / (double)ny), lz * (k / (double)nz)};
+    el.assign((size_t)nx * ny * nz, std::vector<int>());
+    for (int i = 0; i < nx; i++) for (int j = 0; j < ny; j++) for (int k = 0; k < nz; k++)
+        el[(ny * i + j) * nz + k] = {nid(i, j, k), nid(i + 1, j, k), nid(i + 1, j + 1, k), nid(i, j + 1, k),
+                                     nid(i, j, k + 1), nid(i + 1, j, k + 1), nid(i + 1, j + 1, k + 1), nid(i, j + 1, k + 1)};
+}
+
+typedef std::vector<std::pair<std::pair<int, int>, double> > BCList;
+
+static void element_matrix(int kind, Matrix<double>& Ke, std::vector<std::vector<std::pair<int, int> > >& n2e,
+                           const std::vector<int>& el, std::vector<Vector<double> >& x, double E, double V, double t) {
+    if (kind == 0) PlaneStrainStiffness<double, ShapeFunction4Square, Gauss4Square>(Ke, n2e, el, {0, 1}, x, E, V, t);
+    else if (kind == 1) HeatTransfer<double, ShapeFunction4Square, Gauss4Square>(Ke, n2e, el, {0}, x, E, t);
+    else SolidLinearIsotropicElastic<double, ShapeFunction8Cubic, Gauss8Cubic>(Ke, n2e, el, {0, 1, 2}, x, E, V);
+}
+
+// ------------------------------- SIMP -------------------------------
+static int run_simp() {
+    int kind = argi("kind", 0), nx = argi("nx", 12), ny = argi("ny", 6), nz = argi("nz", 0);
+    double lx = argd("lx", nx), ly = argd("ly", ny), lz = argd("lz", nz);
+    double V = argd("V", 0.3), t = argd("t", 1.0), E1 = argd("E1", 1.0), E0 = argd("E0", 1e-9), p = argd("p", 3.0);
+    double vf = argd("vf", 0.5), R = argd("R", 1.5), scale0 = argd("scale0", 1.0), scale1 = argd("scale1", 1.0);
+    double rho0 = argd("rho0", vf);
+    int optimizer = argi("opt", 0), iters = argi("iters", 5), heav = argi("heaviside", 0);
+    double move = argd("move", 0.2), cg_eps = argd("cg_eps", 1e-10);
+    int cg_itmax = argi("cg_itmax", 100000);
+    std::string bc = args("bc", "cantilever");
+    int ndof = kind == 0 ? 2 : (kind == 1 ? 1 : 3);
+
+    std::vector<Vector<double> > x;
+    std::vector<std::vector<int> > elements;
+    BCList ufixed, qfixed;
+    if (kind != 2) {
+        SquareMesh<double> mesh(lx, ly, nx, ny);
+        x = mesh.GenerateNodes();
+        elements = mesh.GenerateElements();
+        if (bc == "cantilever") {
+            std::vector<int> dl = kind == 0 ? std::vector<int>{0, 1} : std::vector<int>{0};
+            ufixed = mesh.GenerateFixedlist(dl, [](Vector<double> _x) { return std::abs(_x(0)) < 1.0e-5; });
+            qfixed = mesh.GenerateFixedlist({kind == 0 ? 1 : 0}, [&](Vector<double> _x) {
+                return std::abs(_x(0) - lx) < 1.0e-5 && std::abs(_x(1) - 0.5 * ly) < 1.0e-5; });
+            for (auto& q : qfixed) q.second = -1.0;
+        } else if (bc == "mbb") {
+            ufixed = mesh.GenerateFixedlist({0}, [](Vector<double> _x) { return std::abs(_x(0)) < 1.0e-5; });
+            BCList u2 = mesh.GenerateFixedlist({1}, [&](Vector<double> _x) {
+                return std::abs(_x(0) - lx) < 1.0e-5 && std::abs(_x(1)) < 1.0e-5; });
+            ufixed.insert(ufixed.end(), u2.begin(), u2.end());
+            qfixed = mesh.GenerateFixedlist({1}, [&](Vector<double> _x) {
+                return std::abs(_x(0)) < 1.0e-5 && std::abs(_x(1) - ly) < 1.0e-5; });
+            for (auto& q : qfixed) q.second = -1.0;
+        } else if (bc == "heatsink") {
+            // zero temperature on a patch of the bottom edge; uniform unit source as nodal loads
+            int w = argi("patch_w", std::max(1, nx / 10)), p0 = argi("patch_i0", (nx - w) / 2);
+            for (int i = p0; i <= p0 + w; i++) ufixed.push_back({{(ny + 1) * i + 0, 0}, 0.0});
+            double h2 = (lx / nx) * (ly / ny) * 0.25;
+            for (int i = 0; i <= nx; i++) for (int j = 0; j <= ny; j++) {
+                int c = (i > 0 && j > 0) + (i < nx && j > 0) + (i > 0 && j < ny) + (i < nx && j < ny);
+                qfixed.push_back({{(ny + 1) * i + j, 0}, c * h2});
+            }
+        }
+    } else {
+        grid3d(lx, ly, lz, nx, ny, nz, x, elements);
+        for (int j = 0; j <= ny; j++) for (int k = 0; k <= nz; k++)
+            for (int d = 0; d < 3; d++) ufixed.push_back({{(ny + 1) * 0 * (nz + 1) + j * (nz + 1) + k, d}, 0.0});
+        for (int j = 0; j <= ny; j++) qfixed.push_back({{((ny + 1) * nx + j) * (nz + 1) + 0, 2}, -1.0 / (ny + 1)});
+    }
+    int dim = kind == 2 ? 3 : 2;
+
+    // neighbour lists exactly as sample_optimize_density_oc.cpp:43-60 (all pairs)
+    std::vector<Vector<double> > cg(elements.size());
+    for (size_t i = 0; i < elements.size(); i++) cg[i] = CenterOfGravity(x, elements[i]);
+    std::vector<std::vector<int> > neighbors(elements.size());
+    std::vector<std::vector<double> > w(elements.size());
+    for (size_t i = 0; i < elements.size(); i++)
+        for (size_t j = 0; j < elements.size(); j++)
+            if ((cg[i] - cg[j]).Norm() <= R) {
+                neighbors[i].push_back((int)j);
+                w[i].push_back((R - (cg[i] - cg[j]).Norm()) / R);
+            }
+    DensityFilter<double> dfilter(elements.size(), neighbors, w);
+    HeavisideFilter<double> hfilter(elements.size(), neighbors, w);
+    double beta = 0.5;
+
+    std::vector<double> s(elements.size(), rho0);
+    OC<double> oc(s.size(), argd("iota", 0.5), argd("lmin", 0.0), argd("lmax", 1.0e4), argd("leps", 1.0e-3), move,
+                  std::vector<double>(s.size(), 0.01), std::vector<double>(s.size(), 1.0));
+    MMA<double> mma(s.size(), 1, argd("a0", 1.0), std::vector<double>(1, 0.0), std::vector<double>(1, argd("mma_c", 10000.0)),
+                    std::vector<double>(1, 0.0), std::vector<double>(s.size(), argd("xmin", 0.01)),
+                    std::vector<double>(s.size(), argd("xmax", 1.0)));
+    mma.SetParameters(argd("raa0", 1.0e-5), argd("albefa", 0.1), move, argd("asyinit", 0.5), argd("asydecr", 0.7),
+                      argd("asyincr", 1.2), argd("mma_eps", 1.0e-6));
+
+    Dump out(args("out", "ref.bin"));
+    {
+        std::vector<int> nfix, dfix, nl, dl; std::vector<double> vl;
+        for (auto& u : ufixed) { nfix.push_back(u.first.first); dfix.push_back(u.first.second); }
+        for (auto& q : qfixed) { nl.push_back(q.first.first); dl.push_back(q.first.second); vl.push_back(q.second); }
+        out.i("fix_node", nfix); out.i("fix_dof", dfix); out.i("load_node", nl); out.i("load_dof", dl); out.d("load_val", vl);
+        std::vector<int> nptr(1, 0), nidx; std::vector<double> nw;
+        for (size_t i = 0; i < neighbors.size(); i++) {
+            nidx.insert(nidx.end(), neighbors[i].begin(), neighbors[i].end());
+            nw.insert(nw.end(), w[i].begin(), w[i].end());
+            nptr.push_back((int)nidx.size());
+        }
+        out.i("nb_ptr", nptr); out.i("nb_idx", nidx); out.d("nb_w", nw);
+        std::vector<double> xc, cgc;
+        for (auto& xi : x) for (int k = 0; k < dim; k++) xc.push_back(xi(k));
+        for (auto& ci : cg) for (int k = 0; k < dim; k++) cgc.push_back(ci(k));
+        out.d("coords", xc); out.d("centroids", cgc);
+        std::vector<int> conn;
+        for (auto& e : elements) conn.insert(conn.end(), e.begin(), e.end());
+        out.i("conn", conn);
+        Matrix<double> Ke; std::vector<std::vector<std::pair<int, int> > > n2e;
+        element_matrix(kind, Ke, n2e, elements[0], x, 1.0, V, t);
+        std::vector<double> kv;
+        for (int a = 0; a < Ke.ROW(); a++) for (int b = 0; b < Ke.COL(); b++) kv.push_back(Ke(a, b));
+        out.d("Ke0", kv);
+        element_matrix(kind, Ke, n2e, elements.back(), x, 0.37, V, t);
+        kv.clear();
+        for (int a = 0; a < Ke.ROW(); a++) for (int b = 0; b < Ke.COL(); b++) kv.push_back(Ke(a, b));
+        out.d("Ke_last_E037", kv);
+    }
+    std::vector<double> F_hist, f_hist, g_hist, rho_hist, dfdrho_hist, dfds_hist, s_hist, u_hist, r_hist;
+    for (int k = 0; k < iters; k++) {
+        if (heav && k % 40 == 0) { beta *= 2.0; hfilter.UpdateBeta(beta); }
+        std::vector<double> rho = heav ? hfilter.GetFilteredVariables(s) : dfilter.GetFilteredVariables(s);
+        double g = 0.0;
+        std::vector<double> dgdrho(s.size(), 0.0);
+        for (size_t i = 0; i < elements.size(); i++) {
+            g += scale1 * rho[i] / (vf * elements.size());
+            dgdrho[i] = scale1 / (vf * elements.size());
+        }
+        g -= 1.0 * scale1;
+
+        std::vector<Vector<double> > u(x.size(), Vector<double>(ndof));
+        std::vector<std::vector<int> > nodetoglobal(x.size(), std::vector<int>(ndof, 0));
+        SetDirichlet(u, nodetoglobal, ufixed);
+        int KDEGREE = Renumbering(nodetoglobal);
+        LILCSR<double> K(KDEGREE, KDEGREE);
+        std::vector<double> F(KDEGREE, 0.0);
+        for (size_t i = 0; i < elements.size(); i++) {
+            double E = E1 * pow(rho[i], p) + E0 * (1.0 - pow(rho[i], p));
+            std::vector<std::vector<std::pair<int, int> > > nodetoelement;
+            Matrix<double> Ke;
+            element_matrix(kind, Ke, nodetoelement, elements[i], x, E, V, t);
+            Assembling(K, F, u, Ke, nodetoglobal, nodetoelement, elements[i]);
+        }
+        Assembling(F, qfixed, nodetoglobal);
+        CSR<double> Kmod(K);
+        if (k == 0) {
+            std::vector<int> n2g;
+            for (auto& nd : nodetoglobal) n2g.insert(n2g.end(), nd.begin(), nd.end());
+            out.i("n2g", n2g);
+            out.i("indptr", Kmod.indptr);
+            out.i("indices", Kmod.indices);
+            out.d("data", Kmod.data);
+            out.d("F0", F);
+        }
+        if (k == 0 && argi("solvers", 0)) {
+            // the other Krylov solvers and ILU(0) of CG.h on the first system
+            out.d("sol_cg", CG(Kmod, F, cg_itmax, cg_eps));
+            out.d("sol_bicgstab", BiCGSTAB(Kmod, F, cg_itmax, cg_eps));
+            out.d("sol_bicgstab2", BiCGSTAB2(Kmod, F, cg_itmax, cg_eps));
+            CSR<double> M = ILU0(Kmod);
+            out.i("ilu_indptr", M.indptr);
+            out.i("ilu_indices", M.indices);
+            out.d("ilu_data", M.data);
+            std::vector<double> Fc = F;
+            out.d("ilu_apply_F", PreILU0(M, Fc));
+            out.d("sol_ilu0cg", ILU0CG(Kmod, M, F, cg_itmax, cg_eps));
+        }
+        std::vector<double> result = ScalingCG(Kmod, F, cg_itmax, cg_eps);
+        Disassembling(u, result, nodetoglobal);
+        if (k == 0) out.d("result0", result);
+
+        RemoveBoundaryConditions(nodetoglobal);
+        KDEGREE = Renumbering(nodetoglobal);
+        std::vector<double> RF(KDEGREE, 0.0);
+        std::vector<Vector<double> > r(x.size(), Vector<double>(ndof));
+        for (size_t i = 0; i < elements.size(); i++) {
+            double E = E1 * pow(rho[i], p) + E0 * (1.0 - pow(rho[i], p));
+            std::vector<std::vector<std::pair<int, int> > > nodetoelement;
+            Matrix<double> Ke;
+            element_matrix(kind, Ke, nodetoelement, elements[i], x, E, V, t);
+            Vector<double> Keue = Ke * ElementVector(u, nodetoelement, elements[i]);
+            Assembling(RF, Keue, nodetoglobal, nodetoelement, elements[i]);
+        }
+        Disassembling(r, RF, nodetoglobal);
+        double f = scale0 * std::inner_product(u.begin(), u.end(), r.begin(), 0.0);
+        std::vector<double> dfdrho(s.size(), 0.0);
+        for (size_t i = 0; i < elements.size(); i++) {
+            std::vector<std::vector<std::pair<int, int> > > nodetoelement;
+            Matrix<double> Ke;
+            element_matrix(kind, Ke, nodetoelement, elements[i], x, 1.0, V, t);
+            Vector<double> ue = ElementVector(u, nodetoelement, elements[i]);
+            dfdrho[i] = -scale0 * p * (-E0 + E1) * pow(rho[i], p - 1.0) * (ue * (Ke * ue));
+        }
+        std::vector<double> dfds = heav ? hfilter.GetFilteredSensitivitis(s, dfdrho) : dfilter.GetFilteredSensitivitis(s, dfdrho);
+        std::vector<double> dgds = heav ? hfilter.GetFilteredSensitivitis(s, dgdrho) : dfilter.GetFilteredSensitivitis(s, dgdrho);
+
+        f_hist.push_back(f); g_hist.push_back(g);
+        rho_hist.insert(rho_hist.end(), rho.begin(), rho.end());
+        dfdrho_hist.insert(dfdrho_hist.end(), dfdrho.begin(), dfdrho.end());
+        dfds_hist.insert(dfds_hist.end(), dfds.begin(), dfds.end());
+        for (auto& ui : u) for (int d = 0; d < ndof; d++) u_hist.push_back(ui(d));
+        if (k == 0) for (auto& ri : r) for (int d = 0; d < ndof; d++) r_hist.push_back(ri(d));
+
+        if (optimizer == 1) {
+            mma.UpdateVariables(s, f, dfds, {g}, {dgds});
+        } else {
+            oc.UpdateVariables(s, f, dfds, g, dgds, [&](std::vector<double> _xkp1) {
+                double gg = 0.0;
+                std::vector<double> rr = heav ? hfilter.GetFilteredVariables(_xkp1) : dfilter.GetFilteredVariables(_xkp1);
+                for (size_t i = 0; i < elements.size(); i++) gg += scale1 * rr[i] / (vf * elements.size());
+                return gg - 1.0 * scale1;
+            });
+        }
+        s_hist.insert(s_hist.end(), s.begin(), s.end());
+    }
+    out.d("f", f_hist); out.d("g", g_hist); out.d("rho", rho_hist); out.d("dfdrho", dfdrho_hist);
+    out.d("dfds", dfds_hist); out.d("s_after", s_hist); out.d("u", u_hist); out.d("r0", r_hist);
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 2) { fprintf(stderr, "usage: ref_driver <simp|...> key=value ...\n"); return 2; }
+    for (int i = 2; i < argc; i++) {
+        std::string a = argv[i];
+        size_t eq = a.find('=');
+        if (eq != std::string::npos) g_args[a.substr(0, eq)] = a.substr(eq + 1);
+    }
+    std::string mode = argv[1];
+    if (mode == "simp") return run_simp();
+    fprintf(stderr, "unknown mode %s\n", mode.c_str());
+    return 2;
+}

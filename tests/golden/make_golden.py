@@ -1,0 +1,69 @@
+"""Generates the golden fixtures in tests/golden/ from the PANSFEM2 reference.
+
+Runs oracle/_ref/ref_driver (the reference headers compiled by
+oracle/build_ref.sh) on small SIMP problems and the reference's own test mains
+(src/LinearAlgebra/Solvers/test_CG.cpp, src/Optimize/Solver/test_MMA*.cpp), and
+stores their outputs as compressed .npz / .txt fixtures.  Needs the reference
+source tree, so it runs only where that tree exists; the fixtures it writes
+are committed and used everywhere else.
+
+    python tests/golden/make_golden.py [path-to-PANSFEM2]
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle import build as obuild  # noqa: E402
+from oracle.pyoracle import read_dump  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+# name -> (ref_driver args, iterations, fields to keep (None = all))
+CASES = {
+    "cantilever_12x6_oc": (["kind=0", "nx=12", "ny=6", "bc=cantilever", "solvers=1"], 5, None),
+    "cantilever_60x30_oc": (["kind=0", "nx=60", "ny=30", "bc=cantilever", "move=0.2"], 10,
+                            ["f", "g", "rho", "s_after", "n2g", "indptr", "indices", "data", "F0",
+                             "result0", "Ke0", "nb_ptr", "nb_idx", "nb_w"]),
+    "mbb_16x8_mma": (["kind=0", "nx=16", "ny=8", "bc=mbb", "opt=1", "vf=0.4", "R=3"], 6, None),
+    "mbb_48x24_mma": (["kind=0", "nx=48", "ny=24", "bc=mbb", "opt=1", "vf=0.4", "R=3"], 10,
+                      ["f", "g", "rho", "s_after", "dfds", "n2g", "nb_ptr", "nb_idx", "nb_w"]),
+    "heatsink_10x10_oc": (["kind=1", "nx=10", "ny=10", "bc=heatsink", "E0=1e-3", "patch_w=1",
+                           "patch_i0=4"], 4, None),
+    "cantilever_h8_6x3x3_oc": (["kind=2", "nx=6", "ny=3", "nz=3", "vf=0.3", "R=1.5"], 3, None),
+    "cantilever_12x6_heaviside": (["kind=0", "nx=12", "ny=6", "bc=cantilever", "heaviside=1"], 4,
+                                  None),
+}
+TEST_MAINS = ["test_CG", "test_MMA", "test_MMA_3", "test_MMA_TOY2"]
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    obuild.build()
+    if not obuild.build_reference(ref_root):
+        raise SystemExit(f"reference tree not found at {ref_root}")
+    tmp = os.path.join(ROOT, "oracle", "_ref", "dump.bin")
+    for name, (args, iters, keep) in CASES.items():
+        subprocess.run([os.path.join(REF, "ref_driver"), "simp", f"out={tmp}", f"iters={iters}"] + args,
+                       check=True, stdout=subprocess.DEVNULL)
+        d = read_dump(tmp)
+        if keep is not None:
+            d = {k: v for k, v in d.items() if k in keep or k in ("fix_node", "fix_dof", "load_node",
+                                                                   "load_dof", "load_val")}
+        d["iters"] = np.array([iters], np.int32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(f"{name}: {sorted(d)}")
+    os.remove(tmp)
+    for t in TEST_MAINS:
+        out = subprocess.run([os.path.join(REF, t)], check=True, capture_output=True, text=True).stdout
+        with open(os.path.join(HERE, f"ref_{t}.txt"), "w") as fh:
+            fh.write(out)
+        print(f"ref_{t}.txt: {len(out)} bytes")
+
+
+if __name__ == "__main__":
+    main()
