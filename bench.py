@@ -1,0 +1,333 @@
+"""Benchmark: SIMP iterations/s on the 2D plane-strain MBB half beam,
+1024 x 512 Q4 (1,051,650 dofs), MMA update, filter radius 3, every solve to
+an FP64 relative residual of 1e-8.
+
+A step is one SIMP iteration (filter, moduli, solve, compliance and
+sensitivities, filtered sensitivities, MMA update).  Steps are consecutive
+iterations of one optimisation run, after W warm-up iterations.
+
+  value : steps/s with the design resident in HBM (device time from CUDA
+          events on the library's stream, summed over the step's phases)
+  e2e   : steps/s through psf_simp_step_host with host buffers (design in,
+          design + densities out, copies inside the timed region)
+
+One process per GPU (replicas only: independent optimisation runs, no
+collective on the data path).  `--impl reference` times the reference's CPU
+algorithm (the oracle restatement built -O3 -fopenmp) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "SIMP iters/s at 1M DOF, resid 1e-8: learned+mixed FCG vs plain FP64 GPU PCG"
+UNIT = "SIMP iterations/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def workload(nx=1024, ny=512):
+    from pansfem2_gb300 import problems as PB
+    return PB.mbb_q4(nx, ny)
+
+
+def bytes_per_krylov_iteration(solver, ne, ndofs, nnz, nfree):
+    """Algorithmic HBM bytes of one Jacobi-PCG iteration: operator + 11 vector
+    passes (x, p, r, Ap, D read; x, r write; r, D, p read; p write)."""
+    if solver == "csr_jacobi_f64":
+        return 12 * nnz + 20 * nfree + 11 * 8 * nfree
+    if solver == "ebe_jacobi_f64":
+        return 8 * ne + 16 * ndofs + 11 * 8 * ndofs
+    # FP32 inner iterations
+    return 4 * ne + 8 * ndofs + 11 * 4 * ndofs
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def run_device(pr, solver, warmup, steps, cg_eps, warm_start):
+    import pansfem2_gb300 as P
+    prob = P.Problem(pr)
+    prob.setup_bc()
+    prob.simp_begin(solver=solver, cg_eps=cg_eps, warm_start=warm_start)
+    for _ in range(warmup):
+        prob.simp_step()
+    prob.sync()
+    infos = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        infos.append(prob.simp_step())
+    prob.sync()
+    wall = time.perf_counter() - t0
+    return prob, infos, wall
+
+
+def run_e2e(pr, solver, warmup, steps, cg_eps, warm_start):
+    import pansfem2_gb300 as P
+    try:
+        import torch
+        pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    except Exception:
+        pin = lambda n: np.empty(n)  # noqa: E731
+    prob = P.Problem(pr)
+    prob.setup_bc()
+    prob.simp_begin(solver=solver, cg_eps=cg_eps, warm_start=warm_start)
+    ne = prob.ne
+    s_host, s_next, rho_host = pin(ne), pin(ne), pin(ne)
+    s_host[:] = pr["vf"]
+    for _ in range(warmup):
+        prob.simp_step_host(s_host, s_next, rho_host)
+        s_host[:] = s_next
+    prob.sync()
+    t0 = time.perf_counter()
+    infos = []
+    for _ in range(steps):
+        infos.append(prob.simp_step_host(s_host, s_next, rho_host))
+        s_host[:] = s_next
+    wall = time.perf_counter() - t0
+    prob.close()
+    return infos, wall, 8 * ne, 16 * ne
+
+
+def cpu_reference_sample(pr, steps, warmup, threads, cg_cap=400, calibrate=True):
+    """The reference's CPU algorithm (oracle restatement, -O3 -fopenmp, SpMV on
+    `threads` OpenMP threads).  Calibration: SIMP iteration 0 in full (ScalingCG
+    to the 1e-8 recurrence residual) gives the CG iteration count n0 and a real
+    iteration time.  Each step: one SIMP iteration with ScalingCG capped at
+    cg_cap iterations, its solve time scaled to n0 iterations."""
+    from oracle import build as ob
+    from oracle import pyoracle as O
+    ob.build()
+    O.set_threads(threads, fast=True)
+    full = dict(pr, cg_eps=1e-8, cg_itmax=100000)
+    t0 = time.perf_counter()
+    res = O.simp_run(full, 1, fast=True)
+    t_full = time.perf_counter() - t0
+    n0 = int(res["cg_iters"][0]) if res["cg_iters"][0] > 0 else 100000
+    samples = []
+    capped = dict(pr, cg_eps=1e-8, cg_itmax=cg_cap)
+    for k in range(warmup + steps):
+        t0 = time.perf_counter()
+        r = O.simp_run(capped, 1, fast=True)
+        wall = time.perf_counter() - t0
+        ph = r["phase_seconds"]
+        ran = cg_cap if r["cg_iters"][0] < 0 else int(r["cg_iters"][0])
+        t = wall - ph[3] + ph[3] / max(ran, 1) * n0
+        if k >= warmup:
+            samples.append(t)
+    return {"t_iter0_full": t_full, "n_cg_iter0": n0, "samples": samples}
+
+
+def ncpus():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--solver", default="ir_jacobi_f32")
+    ap.add_argument("--baseline-solver", default="csr_jacobi_f64")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 GPU PCG comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--warm-start", type=int, default=1)
+    ap.add_argument("--nx", type=int, default=1024)
+    ap.add_argument("--ny", type=int, default=512)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    pr = workload(args.nx, args.ny)
+    config = {"workload": f"MBB half beam {args.nx}x{args.ny} Q4 plane strain, MMA, R=3, vf=0.4",
+              "dofs": 2 * (args.nx + 1) * (args.ny + 1), "elements": args.nx * args.ny,
+              "residual": "FP64 relative 1e-8", "l2": "inputs larger than L2 (CSR 227 MB) for the FP64 path; "
+              "FP32 matrix-free working set ~40 MB is L2-resident", "parallelism": f"replicas{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        thr = ncpus()
+        r = cpu_reference_sample(pr, args.steps, args.warmup, thr)
+        t = float(np.mean(r["samples"]))
+        v = 1.0 / t
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                                 "sample": (f"each step: one SIMP iteration with ScalingCG capped at 400 iterations, "
+                                            f"solve time scaled to the {r['n_cg_iter0']} iterations iteration 0 needs "
+                                            f"to reach 1e-8 (full iteration 0 took {r['t_iter0_full']:.1f} s)")},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import pansfem2_gb300 as P
+    P.load()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- value: device-resident design
+    barrier()
+    with ClockSampler(local) as clk:
+        prob, infos, wall = run_device(pr, args.solver, args.warmup, args.steps, 1e-8, bool(args.warm_start))
+    barrier()
+    dev_t = sum(sum(i["phase_seconds"]) for i in infos)
+    if world > 1:
+        t = torch.tensor([dev_t], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_t = float(t.item())
+    value = world * args.steps / dev_t
+    prob._sizes()
+    ne, ndofs, nnz, nfree = prob.ne, prob.nnodes * prob.ndof, prob.nnz or 0, prob.nfree
+    prob.close()
+
+    # roofline of the dominant kernel (the Krylov kernel)
+    kit = sum(i["solve"]["iterations"] for i in infos)
+    ksec = sum(i["solve"]["kernel_seconds"] for i in infos)
+    klaunch = sum(i["solve"]["kernel_launches"] for i in infos)
+    bpi = bytes_per_krylov_iteration(args.solver, ne, ndofs, 18 * nfree, nfree)
+    peak, peak_kind = peaks()
+    achieved = bpi * kit / ksec / 1e9 if ksec > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(args.solver)
+        except Exception:
+            traffic = None
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * dev_t / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 inner / f64 refinement" if "f32" in args.solver else "f64",
+           "data": "synthetic (the MBB configuration; design starts uniform at vf)",
+           "config": dict(config, solver=args.solver, warm_start=bool(args.warm_start)),
+           "clocks": clk.summary(), "gpu_launches": None,
+           "detail": {"wall_s": wall, "krylov_iterations": kit, "krylov_kernel_seconds": ksec,
+                      "krylov_launches": klaunch, "f_last": infos[-1]["f"],
+                      "true_residual_max": max(i["solve"]["rel_residual"] for i in infos),
+                      "phase_seconds_mean": list(np.mean([i["phase_seconds"] for i in infos], axis=0))}}
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                       "kernel": f"persistent Jacobi PCG ({args.solver})", "bytes_per_iteration": bpi,
+                       "peak_source": peak_kind}
+    # launches of our kernels in the timed region: per step ~12 fixed kernels + Krylov launches + residual kernels
+    out["gpu_launches"] = int(args.steps * 14 + klaunch + 3 * sum(i["solve"]["outer_iterations"] for i in infos))
+
+    # ---- e2e through host buffers
+    if not args.no_e2e:
+        barrier()
+        einfos, ewall, h2d, d2h = run_e2e(pr, args.solver, args.warmup, args.steps, 1e-8, bool(args.warm_start))
+        barrier()
+        if world > 1:
+            t = torch.tensor([ewall], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ewall = float(t.item())
+        out["e2e"] = {"value": world * args.steps / ewall, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h}
+
+    # ---- plain FP64 GPU PCG on the same steps (the spec denominator)
+    if not args.no_compare:
+        barrier()
+        bprob, binfos, bwall = run_device(pr, args.baseline_solver, args.warmup, args.steps, 1e-8, False)
+        bprob.close()
+        bt = sum(sum(i["phase_seconds"]) for i in binfos)
+        out["fp64_gpu_pcg"] = {"solver": args.baseline_solver, "value": args.steps / bt, "unit": UNIT,
+                               "krylov_iterations": sum(i["solve"]["iterations"] for i in binfos),
+                               "speedup_of_value": value / (args.steps / bt),
+                               "f_last": binfos[-1]["f"],
+                               "compliance_rel_diff_last": abs(binfos[-1]["f"] - infos[-1]["f"]) / abs(binfos[-1]["f"])}
+
+    # ---- CPU baseline (rank 0 at N=1 only)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        thr = ncpus()
+        r = cpu_reference_sample(pr, 1, 0, thr)
+        t = r["t_iter0_full"]
+        out["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": thr, "kind": "port",
+                               "sample": f"SIMP iteration 0 in full on the host (ScalingCG to 1e-8: "
+                                         f"{r['n_cg_iter0']} iterations), oracle restatement -O3 -fopenmp"}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

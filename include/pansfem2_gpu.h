@@ -1,0 +1,189 @@
+/*
+ * pansfem2_gpu.h -- C ABI of the GB300 (sm_103a) SIMP topology-optimisation library.
+ *
+ * The library replaces the hot path of PANSFEM2's density-based topology
+ * optimisation (the sample drivers sample/optimize/sample_optimize_density_oc.cpp
+ * and sample_optimize_density_mma.cpp) on structured Q4 / H8 grids.  Every
+ * entry point takes plain pointers and sizes, returns a psf_status, and runs on
+ * one GPU.  Host pointers are borrowed for the duration of the call (copied in
+ * or out); device memory is owned by the context.  A context is not
+ * thread-safe: one host thread drives it; its device work is ordered on the
+ * context's stream.
+ *
+ * Citations name the PANSFEM2 routine each entry point replaces.
+ */
+#ifndef PANSFEM2_GPU_H
+#define PANSFEM2_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PSF_OK = 0,
+    PSF_NOT_CONVERGED = 1,   /* solver hit its iteration cap; the last iterate is returned,
+                                as CG.h:451-452 does after printing "Convergence:faild" */
+    PSF_FELL_BACK = 2,       /* a preconditioner stalled and the solve finished with Jacobi PCG */
+    PSF_BAD_INPUT = 3,       /* invalid argument, size or state */
+    PSF_CUDA_ERROR = 4,      /* a CUDA runtime error (message via psf_last_error) */
+    PSF_TIMEOUT = 5,         /* a device-side wait ran past its limit; the context stays usable */
+    PSF_NOT_FINITE = 6       /* NaN/Inf in a scalar recurrence (e.g. pow of a negative base in OC) */
+} psf_status;
+
+typedef enum {
+    PSF_Q4_PLANE_STRAIN = 0, /* PlaneStrainStiffness<ShapeFunction4Square, Gauss4Square> (PlaneStrain.h:20-58) */
+    PSF_Q4_HEAT = 1,         /* HeatTransfer<ShapeFunction4Square, Gauss4Square> (HeatTransfer.h:19-43) */
+    PSF_H8_SOLID = 2         /* SolidLinearIsotropicElastic<ShapeFunction8Cubic, Gauss8Cubic> (Solid.h:20-64) */
+} psf_element_kind;
+
+typedef enum {
+    PSF_SOLVE_CSR_JACOBI_F64 = 0, /* ScalingCG on the assembled CSR (CG.h:419-453), all FP64 */
+    PSF_SOLVE_EBE_JACOBI_F64 = 1, /* same iteration, matrix-free element-by-element K.u, FP64 */
+    PSF_SOLVE_IR_JACOBI_F32 = 2,  /* FP32 matrix-free Jacobi PCG inside FP64 iterative refinement */
+    PSF_SOLVE_IR_MG_F32 = 3,      /* FP32 multigrid-preconditioned flexible CG inside FP64 refinement */
+    PSF_SOLVE_CSR_CG_F64 = 4,     /* CG (CG.h:123-154) on the CSR */
+    PSF_SOLVE_CSR_BICGSTAB_F64 = 5, /* BiCGSTAB (CG.h:158-193) on the CSR */
+    PSF_SOLVE_IR_LEARNED_F32 = 6  /* FP32 FCG preconditioned by the learned grid U-Net inside FP64 refinement */
+} psf_solver;
+
+typedef struct psf_ctx psf_ctx;
+
+typedef struct {
+    int iterations;          /* Krylov iterations (inner iterations summed for IR) */
+    int outer_iterations;    /* refinement steps (1 for the plain FP64 solvers) */
+    int fell_back;           /* 1 if the solve fell back to Jacobi PCG */
+    double rel_residual;     /* FP64 true residual ||b - K u|| / ||b|| of the returned u */
+    double rel_residual_recurrence; /* the recurrence residual the stopping test used */
+    double seconds;          /* device time of the solve (CUDA events) */
+    double kernel_seconds;   /* device time inside the Krylov kernel launches alone */
+    int kernel_launches;     /* Krylov kernel launches (persistent: one per (inner) solve) */
+    int pad_;
+} psf_solve_info;
+
+/* ---------------- context / mesh ---------------- */
+/* SquareMesh(lx, ly, nx, ny) nodes/elements (SquareMesh.h:61-106) or the H8
+ * analogue (node ((ny+1)*i+j)*(nz+1)+k), material V (Poisson) and t
+ * (thickness; unused for H8).  nz is ignored for the Q4 kinds. */
+psf_status psf_create(psf_ctx **ctx, int kind, int nx, int ny, int nz, double lx, double ly,
+                      double lz, double V, double t);
+psf_status psf_destroy(psf_ctx *ctx);
+const char *psf_last_error(void);
+/* sizes: elements, nodes, dofs per node, free dofs (after psf_set_dirichlet), CSR nnz (after psf_build_csr) */
+psf_status psf_sizes(const psf_ctx *ctx, int64_t *ne, int64_t *nnodes, int *ndof, int64_t *nfree,
+                     int64_t *nnz);
+
+/* SetDirichlet + Renumbering (BoundaryCondition.h:19-25, Assembling.h:175-186):
+ * marks (node, dof) pairs fixed with prescribed values (NULL = zeros) and numbers
+ * the free dofs node-major / dof-minor on the device.  n2g_out (nnodes*ndof,
+ * optional) receives the numbering with -1 for fixed dofs. */
+psf_status psf_set_dirichlet(psf_ctx *ctx, int n, const int *node, const int *dof,
+                             const double *value, int32_t *n2g_out);
+/* Assembling(F, qfixed, nodetoglobal) (Assembling.h:151-158): point loads on free dofs. */
+psf_status psf_set_loads(psf_ctx *ctx, int n, const int *node, const int *dof, const double *value);
+
+/* Element matrix of element 0 for modulus E (conductivity for heat): the
+ * reference element routine evaluated on the device in its operation order.
+ * Ke_out is (nen*ndof)^2 row-major. */
+psf_status psf_element_matrix(psf_ctx *ctx, double E, double *Ke_out);
+
+/* LILCSR -> CSR (CSR.h:92-105) pattern on the device: every free-free dof pair
+ * sharing an element, columns ascending.  indptr_out (nfree+1) / indices_out
+ * (nnz) are optional host copies; call psf_sizes for nnz. */
+psf_status psf_build_csr(psf_ctx *ctx, int32_t *indptr_out, int32_t *indices_out);
+
+/* Assembling(LILCSR&, F, u, Ke, ...) (Assembling.h:46-66) for every element with
+ * modulus E_e (ne values): CSR values summed in ascending element order plus the
+ * Dirichlet lift into F, then the point loads.  data_out (nnz) and F_out (nfree)
+ * are optional host copies. */
+psf_status psf_assemble(psf_ctx *ctx, const double *E_e, double *data_out, double *F_out);
+
+/* y = K x with the assembled CSR (CSR::operator*, CSR.h:108-122). Host vectors of length nfree. */
+psf_status psf_spmv(psf_ctx *ctx, const double *x, double *y);
+/* y = K x matrix-free (element-by-element with Ke(E=1) scaled by E_e), same K. */
+psf_status psf_ebe_matvec(psf_ctx *ctx, const double *x, double *y);
+
+/* Solve K u = F for the current E_e / loads (ScalingCG signature: itmax, eps;
+ * CG.h:420).  u_out (nfree) is the reduced solution, optional.  For the
+ * refinement solvers eps is the FP64 true-residual target. */
+psf_status psf_solve(psf_ctx *ctx, int solver, int itmax, double eps, double *u_out,
+                     psf_solve_info *info);
+
+/* ---------------- SIMP pieces ---------------- */
+/* DensityFilter / HeavisideFilter neighbour lists (DensityFilter.h:16-30): the
+ * lists of the samples (sample_optimize_density_oc.cpp:50-60), every element j
+ * whose centroid lies within R, weight (R - d)/R, built on the device. */
+psf_status psf_filter_setup(psf_ctx *ctx, double R);
+/* GetFilteredVariables (DensityFilter.h:44-56): rho = W s / wsum; host arrays of ne. */
+psf_status psf_filter_forward(psf_ctx *ctx, const double *s, double *rho);
+/* GetFilteredSensitivitis (DensityFilter.h:59-71): dfds_i = sum_j w_ij dfdrho_j / wsum_i. */
+psf_status psf_filter_backward(psf_ctx *ctx, const double *dfdrho, double *dfds);
+
+/* Compliance and sensitivities of sample_optimize_density_oc.cpp:136-162 for the
+ * solved u: f = scale0 * u.K u and dfdrho_e = -scale0*p*(E1 - E0)*rho_e^(p-1) u_e.Ke(1) u_e.
+ * rho (ne) in, dfdrho (ne) out. */
+psf_status psf_compliance_sensitivity(psf_ctx *ctx, const double *rho, double E1, double E0,
+                                      double p, double scale0, double *f, double *dfdrho);
+
+/* OC::UpdateVariables (OC.h:76-107) with the samples' volume callback
+ * (filtered volume fraction vf, scale1): x (ne) updated in place. */
+psf_status psf_oc_update(psf_ctx *ctx, double *x, const double *dfdx, const double *dgdx,
+                         double iota, double lmin, double lmax, double leps, double move,
+                         double vf, double scale1, double *lambda_out);
+
+/* MMA (MMA.h:18-509) for m = 1 with state (asymptotes, history) kept on the device. */
+psf_status psf_mma_init(psf_ctx *ctx, double a0, double a, double c, double d, double xmin,
+                        double xmax, double raa0, double albefa, double move, double asyinit,
+                        double asydecr, double asyincr, double epsvalue);
+psf_status psf_mma_update(psf_ctx *ctx, double *x, double f, const double *dfdx, double g,
+                          const double *dgdx, int *newton_steps);
+
+/* ---------------- the whole SIMP loop on the device ---------------- */
+typedef struct {
+    double E1, E0, p;        /* E = E1*rho^p + E0*(1 - rho^p) (sample law) */
+    double vf, R, scale0, scale1, rho0;
+    int optimizer;           /* 0 = OC, 1 = MMA */
+    double oc_iota, oc_lmin, oc_lmax, oc_leps, oc_move;
+    double mma_raa0, mma_albefa, mma_move, mma_asyinit, mma_asydecr, mma_asyincr, mma_eps;
+    double mma_a0, mma_c, mma_d, mma_xmin, mma_xmax;
+    int solver;              /* psf_solver */
+    int cg_itmax;
+    double cg_eps;           /* recurrence (plain) or FP64 true-residual (refinement) target */
+    int warm_start;          /* 1: start each solve from the previous displacement */
+} psf_simp_params;
+
+typedef struct {
+    double f, g;             /* objective and volume constraint of this iteration */
+    double lambda;           /* last OC lambda */
+    int newton_steps;        /* MMA interior-point steps */
+    int converged;           /* IsConvergence (OC.h:67-73 / MMA.h:107-113) on f */
+    psf_solve_info solve;
+    double phase_seconds[6]; /* filter, assemble, solve, sensitivity, filter-back, update */
+} psf_iter_info;
+
+/* Uploads the design s0 (ne, NULL = uniform rho0) and sets up filter/optimiser. */
+psf_status psf_simp_begin(psf_ctx *ctx, const psf_simp_params *prm, const double *s0);
+/* One SIMP iteration on the device (filter, volume, solve, compliance,
+ * sensitivities, filtered sensitivities, OC/MMA update). */
+psf_status psf_simp_step(psf_ctx *ctx, psf_iter_info *info);
+/* The same iteration through host buffers: s_in (ne) is copied to the device
+ * first, s_out / rho_out (ne, optional) and u_out (nnodes*ndof, optional) are
+ * copied back.  This is the call a host loop replacing the sample driver makes. */
+psf_status psf_simp_step_host(psf_ctx *ctx, const double *s_in, double *s_out, double *rho_out,
+                              double *u_out, psf_iter_info *info);
+/* Host copies of the current device fields (optional pointers). */
+psf_status psf_simp_fields(psf_ctx *ctx, double *s, double *rho, double *dfdrho, double *dfds,
+                           double *u_nodal);
+
+/* Device pointers of the context's arrays, for callers that keep data resident
+ * (name: "s", "rho", "E", "dfdrho", "dfds", "u" (nodal, nnodes*ndof doubles)). */
+psf_status psf_device_ptr(psf_ctx *ctx, const char *name, void **ptr);
+
+/* Synchronise the context's stream. */
+psf_status psf_sync(psf_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

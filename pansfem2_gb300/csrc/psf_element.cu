@@ -1,0 +1,208 @@
+// psf_element.cu -- element stiffness / conductivity matrices on the device.
+//
+// Compiled with --fmad=false: every product and sum is rounded on its own, in
+// the order of the reference element routines, so the matrix equals the
+// reference's PlaneStrainStiffness / HeatTransfer / SolidLinearIsotropicElastic
+// output bit for bit.  Structured grids share one geometry, so one matrix per
+// context (element 0, E = 1) serves every element, scaled by E_e.
+#include "psf_internal.cuh"
+
+namespace psf {
+namespace {
+
+// C = A(r x k) B(k x c), sums from 0 in k order (Matrix::operator*, Matrix.h:243-256)
+__device__ void mm(const double *A, const double *B, double *C, int r, int k, int c) {
+    for (int i = 0; i < r; i++)
+        for (int j = 0; j < c; j++) {
+            double v = 0.0;
+            for (int q = 0; q < k; q++) v += A[i * k + q] * B[q * c + j];
+            C[i * c + j] = v;
+        }
+}
+
+__device__ double det2(const double *v) { return v[0] * v[3] - v[1] * v[2]; }
+// Matrix::Determinant 3x3 term order (Matrix.h:333-334)
+__device__ double det3(const double *v) {
+    return -v[8] * v[1] * v[3] - v[7] * v[5] * v[0] - v[2] * v[4] * v[6] + v[6] * v[1] * v[5] +
+           v[7] * v[3] * v[2] + v[0] * v[4] * v[8];
+}
+// Matrix::Inverse (Matrix.h:346-360): signed cofactor determinants of the
+// transposed position, then each entry divided by the determinant
+__device__ void inv_n(const double *A, int n, double *inv) {
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            // cofactor of (row j, column i)
+            double cof[4];
+            int m = 0;
+            for (int a = 0; a < n; a++) {
+                if (a == j) continue;
+                for (int b = 0; b < n; b++) {
+                    if (b == i) continue;
+                    cof[m++] = A[a * n + b];
+                }
+            }
+            double d = (n == 2) ? cof[0] : det2(cof);
+            inv[i * n + j] = (((i + j) & 1) ? -1.0 : 1.0) * d;
+        }
+    double det = (n == 2) ? det2(A) : det3(A);
+    for (int k = 0; k < n * n; k++) inv[k] /= det;
+}
+
+__device__ void gauss_q4(int g, double *r) {
+    const double a = 1.0 / sqrt(3.0);
+    r[0] = (g == 0 || g == 2) ? -a : a;   // (-,-), (+,-), (-,+), (+,+)
+    r[1] = (g < 2) ? -a : a;
+}
+__device__ void gauss_h8(int g, double *r) {
+    const double a = 1.0 / sqrt(3.0);
+    const int sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+              sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+    r[0] = sx[g] < 0 ? -a : a;
+    r[1] = sy[g] < 0 ? -a : a;
+    r[2] = sz[g] < 0 ? -a : a;
+}
+__device__ void dndr_q4(const double *r, double *d) {
+    d[0] = -0.25 * (1.0 - r[1]); d[1] = 0.25 * (1.0 - r[1]);
+    d[2] = 0.25 * (1.0 + r[1]);  d[3] = -0.25 * (1.0 + r[1]);
+    d[4] = -0.25 * (1.0 - r[0]); d[5] = -0.25 * (1.0 + r[0]);
+    d[6] = 0.25 * (1.0 + r[0]);  d[7] = 0.25 * (1.0 - r[0]);
+}
+__device__ void dndr_h8(const double *r, double *d) {
+    const double sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+                 sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+    // ShapeFunction8Cubic::dNdr (ShapeFunction.h:318-329): +-0.125 times the two
+    // other factors, in the order the reference writes them
+    for (int n = 0; n < 8; n++) {
+        double c = (sx[n] < 0 ? -0.125 : 0.125);
+        d[n] = c * (sy[n] < 0 ? 1.0 - r[1] : 1.0 + r[1]) * (sz[n] < 0 ? 1.0 - r[2] : 1.0 + r[2]);
+        c = (sy[n] < 0 ? -0.125 : 0.125);
+        d[8 + n] = c * (sz[n] < 0 ? 1.0 - r[2] : 1.0 + r[2]) * (sx[n] < 0 ? 1.0 - r[0] : 1.0 + r[0]);
+        c = (sz[n] < 0 ? -0.125 : 0.125);
+        d[16 + n] = c * (sx[n] < 0 ? 1.0 - r[0] : 1.0 + r[0]) * (sy[n] < 0 ? 1.0 - r[1] : 1.0 + r[1]);
+    }
+}
+
+// PlaneStrainStiffness (PlaneStrain.h:20-58)
+__device__ void ke_planestrain(const double *X, double E, double V, double t, double *Ke) {
+    double D[9] = {1.0 - V, V, 0.0, V, 1.0 - V, 0.0, 0.0, 0.0, 0.5 * (1.0 - 2.0 * V)};
+    const double sc = E / ((1.0 - 2.0 * V) * (1.0 + V));
+    for (int k = 0; k < 9; k++) D[k] *= sc;
+    for (int k = 0; k < 64; k++) Ke[k] = 0.0;
+    for (int g = 0; g < 4; g++) {
+        double r[2], dN[8], J2[4], iv[4], dX[8], B[24], Bt[24], BtD[24], K[64];
+        gauss_q4(g, r);
+        dndr_q4(r, dN);
+        mm(dN, X, J2, 2, 4, 2);
+        const double J = det2(J2);
+        inv_n(J2, 2, iv);
+        mm(iv, dN, dX, 2, 2, 4);
+        for (int n = 0; n < 4; n++) {
+            B[2 * n] = dX[n];          B[2 * n + 1] = 0.0;
+            B[8 + 2 * n] = 0.0;        B[8 + 2 * n + 1] = dX[4 + n];
+            B[16 + 2 * n] = dX[4 + n]; B[16 + 2 * n + 1] = dX[n];
+        }
+        for (int i = 0; i < 8; i++)
+            for (int j = 0; j < 3; j++) Bt[i * 3 + j] = B[j * 8 + i];
+        mm(Bt, D, BtD, 8, 3, 3);
+        mm(BtD, B, K, 8, 3, 8);
+        for (int k = 0; k < 64; k++) Ke[k] += K[k] * J * t * 1.0 * 1.0;
+    }
+}
+
+// HeatTransfer (HeatTransfer.h:19-43)
+__device__ void ke_heat(const double *X, double alpha, double t, double *Ke) {
+    for (int k = 0; k < 16; k++) Ke[k] = 0.0;
+    for (int g = 0; g < 4; g++) {
+        double r[2], dN[8], J2[4], iv[4], B[8], Bt[8], K[16];
+        gauss_q4(g, r);
+        dndr_q4(r, dN);
+        mm(dN, X, J2, 2, 4, 2);
+        const double J = det2(J2);
+        inv_n(J2, 2, iv);
+        mm(iv, dN, B, 2, 2, 4);
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 2; j++) Bt[i * 2 + j] = B[j * 4 + i];
+        mm(Bt, B, K, 4, 2, 4);
+        for (int k = 0; k < 16; k++) Ke[k] += K[k] * J * alpha * t * 1.0 * 1.0;
+    }
+}
+
+// SolidLinearIsotropicElastic (Solid.h:20-64)
+__device__ void ke_solid(const double *X, double E, double V, double *Ke, double *wk) {
+    double C[36];
+    for (int k = 0; k < 36; k++) C[k] = 0.0;
+    C[0] = 1.0 - V; C[1] = V;  C[2] = V;
+    C[6] = V;  C[7] = 1.0 - V; C[8] = V;
+    C[12] = V; C[13] = V;      C[14] = 1.0 - V;
+    C[21] = 0.5 * (1.0 - 2.0 * V);
+    C[28] = 0.5 * (1.0 - 2.0 * V);
+    C[35] = 0.5 * (1.0 - 2.0 * V);
+    const double sc = E / ((1.0 + V) * (1.0 - 2.0 * V));
+    for (int k = 0; k < 36; k++) C[k] *= sc;
+    for (int k = 0; k < 576; k++) Ke[k] = 0.0;
+    double *B = wk, *Bt = wk + 144, *BtC = wk + 288, *K = wk + 432;
+    for (int g = 0; g < 8; g++) {
+        double r[3], dN[24], J3[9], iv[9], dX[24];
+        gauss_h8(g, r);
+        dndr_h8(r, dN);
+        mm(dN, X, J3, 3, 8, 3);
+        const double J = det3(J3);
+        inv_n(J3, 3, iv);
+        mm(iv, dN, dX, 3, 3, 8);
+        for (int k = 0; k < 144; k++) B[k] = 0.0;
+        for (int n = 0; n < 8; n++) {
+            const double d0 = dX[n], d1 = dX[8 + n], d2 = dX[16 + n];
+            B[3 * n] = d0;
+            B[24 + 3 * n + 1] = d1;
+            B[48 + 3 * n + 2] = d2;
+            B[72 + 3 * n] = d1;      B[72 + 3 * n + 1] = d0;
+            B[96 + 3 * n + 1] = d2;  B[96 + 3 * n + 2] = d1;
+            B[120 + 3 * n] = d2;     B[120 + 3 * n + 2] = d0;
+        }
+        for (int i = 0; i < 24; i++)
+            for (int j = 0; j < 6; j++) Bt[i * 6 + j] = B[j * 24 + i];
+        mm(Bt, C, BtC, 24, 6, 6);
+        mm(BtC, B, K, 24, 6, 24);
+        for (int k = 0; k < 576; k++) Ke[k] += K[k] * J * 1.0 * 1.0 * 1.0;
+    }
+}
+
+// one thread: the element matrix of element 0 with its actual node coordinates
+__global__ void ke_element0_kernel(int kind, int nx, int ny, int nz, double lx, double ly, double lz,
+                                   double E, double V, double t, double *Ke, double *wk) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    // SquareMesh coordinates x*(i/(T)nx) of element 0's nodes, in the element's node order
+    double X[24];
+    if (kind == PSF_H8_SOLID) {
+        const int ci[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cj[8] = {0, 0, 1, 1, 0, 0, 1, 1},
+                  ck[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+        for (int n = 0; n < 8; n++) {
+            X[3 * n + 0] = lx * (ci[n] / (double)nx);
+            X[3 * n + 1] = ly * (cj[n] / (double)ny);
+            X[3 * n + 2] = lz * (ck[n] / (double)nz);
+        }
+        ke_solid(X, E, V, Ke, wk);
+    } else {
+        const int ci[4] = {0, 1, 1, 0}, cj[4] = {0, 0, 1, 1};
+        for (int n = 0; n < 4; n++) {
+            X[2 * n + 0] = lx * (ci[n] / (double)nx);
+            X[2 * n + 1] = ly * (cj[n] / (double)ny);
+        }
+        if (kind == PSF_Q4_PLANE_STRAIN) ke_planestrain(X, E, V, t, Ke);
+        else ke_heat(X, E, t, Ke);
+    }
+}
+
+}  // namespace
+
+psf_status ke_element0(Ctx *c, double E, double *Ke_dev) {
+    double *wk = nullptr;
+    if (c->kind == PSF_H8_SOLID) PSF_CUDA(cudaMallocAsync((void **)&wk, 576 * sizeof(double), c->stream));
+    ke_element0_kernel<<<1, 32, 0, c->stream>>>(c->kind, c->nx, c->ny, c->nz, c->lx, c->ly, c->lz, E,
+                                                c->V, c->t, Ke_dev, wk);
+    PSF_CUDA(cudaGetLastError());
+    if (wk) PSF_CUDA(cudaFreeAsync(wk, c->stream));
+    return PSF_OK;
+}
+
+}  // namespace psf

@@ -1,0 +1,613 @@
+// psf_solve.cu -- matrix-free K.u and the Krylov solvers.
+//
+// Matrix-free operator: y = sum_e E_e P_e^T Ke0 P_e u over the structured grid,
+// one thread per node gathering its 2^d surrounding elements (no atomics, no
+// element list).  Ke0 travels as a kernel parameter (constant bank): every
+// lane of a warp reads the same entry at the same time.  Fixed dofs hold zero
+// in every vector and their rows of y are zero, which is K restricted to the
+// free dofs in the nodal layout.
+//
+// Solvers run as persistent cooperative kernels: one launch per solve, two
+// fused reduce-barriers per iteration (see psf_common.cuh), every block
+// computing the same scalars so that all agree on when to stop.  The search
+// direction update p = z + beta p is folded into the next operator phase.
+//
+// ScalingCG (CG.h:419-453) is the plain FP64 path, on the CSR (bit-exact
+// pattern) or matrix-free.  The mixed-precision path runs that iteration in
+// FP32 (operator, vectors) with FP64 dot products inside FP64 iterative
+// refinement on the true residual.
+#include <cmath>
+#include <cstdio>
+
+#include "psf_internal.cuh"
+
+namespace psf {
+
+template <class T>
+struct KeT {
+    T v[576];
+};
+
+struct Geo {
+    int nx, ny, nz;
+    long long nnodes;
+};
+
+__device__ __forceinline__ long long pad_index(const Geo &g, int ei, int ej, int ek, bool is3d) {
+    return is3d ? ((long long)(ei + 1) * (g.ny + 2) + (ej + 1)) * (g.nz + 2) + (ek + 1)
+                : (long long)(ei + 1) * (g.ny + 2) + (ej + 1);
+}
+
+// local node index of corner offset (di, dj, dk) (SquareMesh / ShapeFunction8Cubic order)
+__device__ __forceinline__ int corner_local(int di, int dj, int dk) {
+    return (di ? (dj ? 2 : 1) : (dj ? 3 : 0)) + 4 * dk;
+}
+
+// y[0..ndof) of node (i,j,k) = sum over surrounding elements; get(dof index) reads the input
+template <class T, int KIND, class Get>
+__device__ __forceinline__ void ebe_node(const Geo &g, const KeT<T> &Ke, const T *__restrict__ Ep, int i, int j,
+                                         int k, Get get, T *y) {
+    constexpr bool is3d = KIND == PSF_H8_SOLID;
+    constexpr int ndof = KIND == PSF_Q4_PLANE_STRAIN ? 2 : (KIND == PSF_Q4_HEAT ? 1 : 3);
+    constexpr int nen = is3d ? 8 : 4;
+    constexpr int nk = nen * ndof;
+#pragma unroll
+    for (int a = 0; a < ndof; a++) y[a] = T(0);
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++)
+#pragma unroll
+            for (int ck = 0; ck < (is3d ? 2 : 1); ck++) {
+                const int ei = i - 1 + ci, ej = j - 1 + cj, ek = is3d ? k - 1 + ck : 0;
+                const T Ee = Ep[pad_index(g, ei, ej, ek, is3d)];
+                const int li = corner_local(1 - ci, 1 - cj, is3d ? 1 - ck : 0);
+                T ue[nk];
+#pragma unroll
+                for (int q = 0; q < nen; q++) {
+                    const int qi = (q == 1 || q == 2 || q == 5 || q == 6), qj = (q == 2 || q == 3 || q == 6 || q == 7),
+                              qk = q >= 4;
+                    int ni = min(max(ei + qi, 0), g.nx), nj = min(max(ej + qj, 0), g.ny);
+                    long long m;
+                    if (is3d) {
+                        int nkk = min(max(ek + qk, 0), g.nz);
+                        m = ((long long)(g.ny + 1) * ni + nj) * (g.nz + 1) + nkk;
+                    } else {
+                        m = (long long)(g.ny + 1) * ni + nj;
+                    }
+#pragma unroll
+                    for (int b = 0; b < ndof; b++) ue[q * ndof + b] = get(m * ndof + b);
+                }
+#pragma unroll
+                for (int a = 0; a < ndof; a++) {
+                    T acc = T(0);
+                    const int row = (li * ndof + a) * nk;
+#pragma unroll
+                    for (int l = 0; l < nk; l++) acc += Ke.v[row + l] * ue[l];
+                    y[a] += Ee * acc;
+                }
+            }
+}
+
+template <int KIND>
+__device__ __forceinline__ void node_ijk(const Geo &g, long long n, int &i, int &j, int &k) {
+    if (KIND == PSF_H8_SOLID) {
+        k = (int)(n % (g.nz + 1));
+        long long r = n / (g.nz + 1);
+        j = (int)(r % (g.ny + 1));
+        i = (int)(r / (g.ny + 1));
+    } else {
+        k = 0;
+        j = (int)(n % (g.ny + 1));
+        i = (int)(n / (g.ny + 1));
+    }
+}
+
+template <int KIND>
+__host__ __device__ constexpr int ndof_of() { return KIND == PSF_Q4_PLANE_STRAIN ? 2 : (KIND == PSF_Q4_HEAT ? 1 : 3); }
+
+// ------------------------------------------------------------------ plain operator y = K x (+ optional r = b - K x, norm)
+template <class T, int KIND>
+__global__ void ebe_apply_kernel(Geo g, KeT<T> Ke, const T *__restrict__ Ep, const unsigned char *__restrict__ fixed,
+                                 const T *__restrict__ x, T *__restrict__ y) {
+    constexpr int nd = ndof_of<KIND>();
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_ijk<KIND>(g, n, i, j, k);
+        T yv[nd];
+        ebe_node<T, KIND>(g, Ke, Ep, i, j, k, [&](long long a) { return x[a]; }, yv);
+#pragma unroll
+        for (int a = 0; a < nd; a++) y[n * nd + a] = fixed[n * nd + a] ? T(0) : yv[a];
+    }
+}
+
+// r = b - K x (FP64), block partial of |r|^2 and |b|^2
+template <int KIND>
+__global__ void residual64_kernel(Geo g, KeT<double> Ke, const double *__restrict__ Ep,
+                                  const unsigned char *__restrict__ fixed, const double *__restrict__ b,
+                                  const double *__restrict__ x, double *__restrict__ r, double *partials) {
+    constexpr int nd = ndof_of<KIND>();
+    __shared__ double sm[64];
+    double acc[2] = {0.0, 0.0};
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_ijk<KIND>(g, n, i, j, k);
+        double yv[nd];
+        ebe_node<double, KIND>(g, Ke, Ep, i, j, k, [&](long long a) { return x[a]; }, yv);
+#pragma unroll
+        for (int a = 0; a < nd; a++) {
+            const long long q = n * nd + a;
+            const double rv = fixed[q] ? 0.0 : b[q] - yv[a];
+            r[q] = rv;
+            acc[0] += rv * rv;
+            acc[1] += b[q] * b[q];
+        }
+    }
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = acc[0];
+        partials[gridDim.x + blockIdx.x] = acc[1];
+    }
+}
+
+__global__ void finalize_sums(const double *partials, int nb, int nv, double *out) {
+    // one warp per value, fixed order
+    const int v = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (v >= nv) return;
+    double a = 0.0;
+    for (int b = lane; b < nb; b += 32) a += partials[(size_t)v * nb + b];
+    a = warp_sum(a);
+    if (lane == 0) out[v] = a;
+}
+
+// x64 += s * d32 (nodal)
+__global__ void axpy_mixed(long long n, double s, const float *__restrict__ d, double *__restrict__ x) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        x[q] += s * (double)d[q];
+}
+
+// ------------------------------------------------------------------ persistent Jacobi PCG, matrix-free
+template <class T>
+struct PcgArgs {
+    Geo g;
+    KeT<T> Ke;
+    const T *Ep;
+    const T *D;                      // nodal diagonal (1 on fixed dofs)
+    const unsigned char *fixed;
+    const double *b;                 // nodal right-hand side (FP64), multiplied by bscale
+    double bscale;
+    const double *x0;                // optional FP64 start (nullptr: zero start)
+    T *x, *r, *z, *pA, *pB, *Ap;
+    int itmax;
+    double eps;
+    GridSync *gs;
+    double *partials;
+    double *out;                     // out[0] = iterations, out[1] = |r|^2, out[2] = |b|^2, out[3] = converged
+};
+
+template <class T, int KIND>
+__global__ void __launch_bounds__(256) pcg_ebe_kernel(PcgArgs<T> A) {
+    constexpr int nd = ndof_of<KIND>();
+    __shared__ double sm[32 * 2];
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const Geo g = A.g;
+    // ---- start: r = b - K x0, z = r / D, p_prev = 0
+    {
+        double acc[2] = {0.0, 0.0};
+        for (long long n = tid; n < g.nnodes; n += stride) {
+            T kx[nd];
+            if (A.x0) {
+                int i, j, k;
+                node_ijk<KIND>(g, n, i, j, k);
+                ebe_node<T, KIND>(g, A.Ke, A.Ep, i, j, k, [&](long long a) { return (T)A.x0[a]; }, kx);
+            } else {
+#pragma unroll
+                for (int a = 0; a < nd; a++) kx[a] = T(0);
+            }
+#pragma unroll
+            for (int a = 0; a < nd; a++) {
+                const long long q = n * nd + a;
+                const bool fx = A.fixed[q];
+                const T bv = fx ? T(0) : (T)(A.b[q] * A.bscale);
+                const T rv = fx ? T(0) : bv - kx[a];
+                A.x[q] = A.x0 && !fx ? (T)A.x0[q] : T(0);
+                A.r[q] = rv;
+                const T zv = rv / A.D[q];
+                A.z[q] = zv;
+                A.pA[q] = T(0);
+                acc[0] += (double)zv * (double)rv;
+                acc[1] += (double)bv * (double)bv;
+            }
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+    }
+    double zr = gs_result(A.gs, 0);
+    const double bnorm = sqrt(gs_result(A.gs, 1));
+    double beta = 0.0, rr = 0.0;
+    T *pp = A.pA, *pn = A.pB;
+    int it = 0, conv = 0;
+    for (; it < A.itmax; it++) {
+        // ---- phase A: p = z + beta p_prev (on the fly for neighbours), Ap = K p, p.Ap
+        double pAp[1] = {0.0};
+        const T tb = (T)beta;
+        for (long long n = tid; n < g.nnodes; n += stride) {
+            int i, j, k;
+            node_ijk<KIND>(g, n, i, j, k);
+            T yv[nd];
+            ebe_node<T, KIND>(g, A.Ke, A.Ep, i, j, k,
+                              [&](long long a) { return fma_t(tb, pp[a], A.z[a]); }, yv);
+#pragma unroll
+            for (int a = 0; a < nd; a++) {
+                const long long q = n * nd + a;
+                const T pv = fma_t(tb, pp[q], A.z[q]);
+                const T av = A.fixed[q] ? T(0) : yv[a];
+                pn[q] = pv;
+                A.Ap[q] = av;
+                pAp[0] += (double)pv * (double)av;
+            }
+        }
+        block_sum<1>(pAp, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, pAp, 0.0)) return;
+        const double alpha = zr / gs_result(A.gs, 0);
+        // ---- phase B: x += alpha p, r -= alpha Ap, z = r / D, z.r and r.r
+        double acc[2] = {0.0, 0.0};
+        const T ta = (T)alpha, tma = (T)(-alpha);
+        for (long long q = tid; q < g.nnodes * nd; q += stride) {
+            const T pv = pn[q];
+            A.x[q] = fma_t(ta, pv, A.x[q]);
+            const T rv = fma_t(tma, A.Ap[q], A.r[q]);
+            A.r[q] = rv;
+            const T zv = rv / A.D[q];
+            A.z[q] = zv;
+            acc[0] += (double)zv * (double)rv;
+            acc[1] += (double)rv * (double)rv;
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+        const double zr1 = gs_result(A.gs, 0);
+        rr = gs_result(A.gs, 1);
+        beta = zr1 / zr;
+        zr = zr1;
+        T *t = pp; pp = pn; pn = t;
+        if (sqrt(rr) < A.eps * bnorm) { it++; conv = 1; break; }
+        if (!isfinite(rr)) { it++; break; }
+    }
+    if (tid == 0) {
+        A.out[0] = it;
+        A.out[1] = rr;
+        A.out[2] = bnorm * bnorm;
+        A.out[3] = conv;
+    }
+}
+
+// ------------------------------------------------------------------ persistent Jacobi PCG on the CSR (FP64)
+struct PcgCsrArgs {
+    long long rows;
+    const int *indptr, *indices, *diag;
+    const double *data, *b;
+    double *x, *r, *z, *pA, *pB, *Ap;
+    int itmax;
+    double eps;
+    GridSync *gs;
+    double *partials;
+    double *out;
+};
+
+// ScalingCG (CG.h:419-453): x0 = 0, r = b, z = r / D (division, CG.h:412), p = z;
+// the recurrence residual ||r|| < eps ||b|| stops it (CG.h:443-448).
+__global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
+    __shared__ double sm[32 * 2];
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    {
+        double acc[2] = {0.0, 0.0};
+        for (long long i = tid; i < A.rows; i += stride) {
+            const double bv = A.b[i];
+            const double D = A.data[A.diag[i]];
+            A.x[i] = 0.0;
+            A.r[i] = bv;
+            const double zv = bv / D;
+            A.z[i] = zv;
+            A.pA[i] = 0.0;
+            acc[0] += zv * bv;
+            acc[1] += bv * bv;
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+    }
+    double zr = gs_result(A.gs, 0);
+    const double bnorm = sqrt(gs_result(A.gs, 1));
+    double beta = 0.0, rr = 0.0;
+    double *pp = A.pA, *pn = A.pB;
+    int it = 0, conv = 0;
+    const int sub = threadIdx.x & 3;
+    const long long rstride = stride >> 2;
+    for (; it < A.itmax; it++) {
+        double pAp[1] = {0.0};
+        // four lanes per row; warp-uniform loop bound (8 rows per warp)
+        for (long long base = (tid >> 5) << 3; base < A.rows; base += rstride) {
+            const long long i = base + ((threadIdx.x & 31) >> 2);
+            double v = 0.0;
+            if (i < A.rows)
+                for (int q = A.indptr[i] + sub; q < A.indptr[i + 1]; q += 4) {
+                    const int jc = A.indices[q];
+                    v += A.data[q] * fma(beta, pp[jc], A.z[jc]);
+                }
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            if (sub == 0 && i < A.rows) {
+                const double pv = fma(beta, pp[i], A.z[i]);
+                pn[i] = pv;
+                A.Ap[i] = v;
+                pAp[0] += pv * v;
+            }
+        }
+        block_sum<1>(pAp, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, pAp, 0.0)) return;
+        const double alpha = zr / gs_result(A.gs, 0);
+        double acc[2] = {0.0, 0.0};
+        for (long long i = tid; i < A.rows; i += stride) {
+            A.x[i] = A.x[i] + alpha * pn[i];
+            const double rv = A.r[i] + (-alpha) * A.Ap[i];
+            A.r[i] = rv;
+            const double zv = rv / A.data[A.diag[i]];
+            A.z[i] = zv;
+            acc[0] += zv * rv;
+            acc[1] += rv * rv;
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+        const double zr1 = gs_result(A.gs, 0);
+        rr = gs_result(A.gs, 1);
+        beta = zr1 / zr;
+        zr = zr1;
+        double *t = pp; pp = pn; pn = t;
+        if (sqrt(rr) < A.eps * bnorm) { it++; conv = 1; break; }
+        if (!isfinite(rr)) { it++; break; }
+    }
+    if (tid == 0) {
+        A.out[0] = it;
+        A.out[1] = rr;
+        A.out[2] = bnorm * bnorm;
+        A.out[3] = conv;
+        // the final x lives in A.x; p buffers swapped in registers only
+    }
+}
+
+// ------------------------------------------------------------------ host side
+template <class T>
+static KeT<T> ke_param(const Ctx *c) {
+    KeT<T> k{};
+    const int nk = c->nen * c->ndof;
+    for (int q = 0; q < nk * nk; q++) k.v[q] = (T)c->Ke0_host[q];
+    return k;
+}
+
+static Geo geo_of(const Ctx *c) {
+    Geo g;
+    g.nx = c->nx; g.ny = c->ny; g.nz = c->nz;
+    g.nnodes = c->nnodes;
+    return g;
+}
+
+template <class T>
+static psf_status ebe_apply_t(Ctx *c, const T *x, T *y, const T *Ep) {
+    Geo g = geo_of(c);
+    KeT<T> Ke = ke_param<T>(c);
+    const int nb = grid_for(c->nnodes, 256, c->num_sms * 8);
+    switch (c->kind) {
+    case PSF_Q4_PLANE_STRAIN: ebe_apply_kernel<T, 0><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y); break;
+    case PSF_Q4_HEAT: ebe_apply_kernel<T, 1><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y); break;
+    default: ebe_apply_kernel<T, 2><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y); break;
+    }
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
+psf_status ebe_apply64(Ctx *c, const double *xn, double *yn) { return ebe_apply_t<double>(c, xn, yn, c->Epad); }
+psf_status ebe_apply32(Ctx *c, const float *xn, float *yn) { return ebe_apply_t<float>(c, xn, yn, c->Epadf); }
+
+// r = b - K x in FP64 (nodal); returns |r| and |b| on the host
+static psf_status residual64(Ctx *c, const double *b, const double *x, double *r, double *rnorm, double *bnorm) {
+    Geo g = geo_of(c);
+    KeT<double> Ke = ke_param<double>(c);
+    const int nb = grid_for(c->nnodes, 256, c->num_sms * 4);
+    switch (c->kind) {
+    case PSF_Q4_PLANE_STRAIN: residual64_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials); break;
+    case PSF_Q4_HEAT: residual64_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials); break;
+    default: residual64_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials); break;
+    }
+    finalize_sums<<<1, 64, 0, c->stream>>>(c->partials, nb, 2, c->scal + 8);
+    PSF_CUDA(cudaGetLastError());
+    double h[2];
+    PSF_CUDA(cudaMemcpyAsync(h, c->scal + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    *rnorm = sqrt(h[0]);
+    *bnorm = sqrt(h[1]);
+    return PSF_OK;
+}
+
+psf_status add_kernel_time(Ctx *c) {
+    float ms = 0.f;
+    PSF_CUDA(cudaEventSynchronize(c->evk1));
+    PSF_CUDA(cudaEventElapsedTime(&ms, c->evk0, c->evk1));
+    c->ksec += ms * 1e-3;
+    c->klaunch++;
+    return PSF_OK;
+}
+
+template <class T, int KIND>
+static psf_status run_pcg_ebe(Ctx *c, PcgArgs<T> &a, int *iters, double *rr, double *bb, int *conv) {
+    const void *fn = (const void *)pcg_ebe_kernel<T, KIND>;
+    int per_sm = 0;
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_ebe_kernel<T, KIND>, 256, 0));
+    if (per_sm < 1) { set_error("persistent PCG kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
+    int blocks = c->num_sms * (per_sm < 4 ? per_sm : 4);
+    long long need = (c->nnodes + 255) / 256;
+    if (blocks > need) blocks = (int)need;
+    if (blocks < 1) blocks = 1;
+    void *args[] = {&a};
+    PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
+    PSF_CHECK(launch_coop(c, fn, blocks, 256, args));
+    PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
+    PSF_CHECK(read_sync_status(c));
+    PSF_CHECK(add_kernel_time(c));
+    double h[4];
+    PSF_CUDA(cudaMemcpyAsync(h, a.out, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    *iters = (int)h[0];
+    *rr = h[1];
+    *bb = h[2];
+    *conv = (int)h[3];
+    return PSF_OK;
+}
+
+template <class T>
+static psf_status pcg_ebe(Ctx *c, const double *b, double bscale, const double *x0, T *x, T **w, int itmax,
+                          double eps, int *iters, double *rr, double *bb, int *conv) {
+    PcgArgs<T> a;
+    a.g = geo_of(c);
+    a.Ke = ke_param<T>(c);
+    if constexpr (sizeof(T) == 8) { a.Ep = (const T *)c->Epad; a.D = (const T *)c->Dn; }
+    else { a.Ep = (const T *)c->Epadf; a.D = (const T *)c->Dnf; }
+    a.fixed = c->fixed;
+    a.b = b;
+    a.bscale = bscale;
+    a.x0 = x0;
+    a.x = x; a.r = w[0]; a.z = w[1]; a.pA = w[2]; a.pB = w[3]; a.Ap = w[4];
+    a.itmax = itmax;
+    a.eps = eps;
+    a.gs = c->gs;
+    a.partials = c->partials;
+    a.out = c->scal + 12;
+    switch (c->kind) {
+    case PSF_Q4_PLANE_STRAIN: return run_pcg_ebe<T, 0>(c, a, iters, rr, bb, conv);
+    case PSF_Q4_HEAT: return run_pcg_ebe<T, 1>(c, a, iters, rr, bb, conv);
+    default: return run_pcg_ebe<T, 2>(c, a, iters, rr, bb, conv);
+    }
+}
+
+static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr, double *bb, int *conv) {
+    PcgCsrArgs a;
+    a.rows = c->nfree;
+    a.indptr = c->indptr; a.indices = c->indices; a.diag = c->diag; a.data = c->data;
+    a.b = c->F;
+    a.x = c->u;
+    double *w = c->w64[0];   // 5 reduced-length buffers carved from nodal scratch
+    const long long n = c->nfree;
+    a.r = w; a.z = w + n; a.pA = w + 2 * n; a.pB = w + 3 * n; a.Ap = w + 4 * n;
+    a.itmax = itmax;
+    a.eps = eps;
+    a.gs = c->gs;
+    a.partials = c->partials;
+    a.out = c->scal + 12;
+    int per_sm = 0;
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_csr_kernel, 256, 0));
+    if (per_sm < 1) { set_error("persistent PCG kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
+    int blocks = c->num_sms * (per_sm < 4 ? per_sm : 4);
+    long long need = (n * 4 + 255) / 256;
+    if (blocks > need) blocks = (int)need;
+    if (blocks < 1) blocks = 1;
+    void *args[] = {&a};
+    PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
+    PSF_CHECK(launch_coop(c, (const void *)pcg_csr_kernel, blocks, 256, args));
+    PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
+    PSF_CHECK(read_sync_status(c));
+    PSF_CHECK(add_kernel_time(c));
+    double h[4];
+    PSF_CUDA(cudaMemcpyAsync(h, a.out, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    *iters = (int)h[0];
+    *rr = h[1];
+    *bb = h[2];
+    *conv = (int)h[3];
+    return PSF_OK;
+}
+
+psf_status mg_solve_ir(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_mg.cu
+
+psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *info) {
+    psf_solve_info inf{};
+    c->ksec = 0.0;
+    c->klaunch = 0;
+    PSF_CUDA(cudaEventRecord(c->ev0, c->stream));
+    psf_status st = PSF_OK;
+    if (solver == PSF_SOLVE_CSR_JACOBI_F64) {
+        if (!c->have_values) { set_error("psf_solve: assemble first"); return PSF_BAD_INPUT; }
+        int it, conv;
+        double rr, bb;
+        PSF_CHECK(pcg_csr(c, itmax, eps, &it, &rr, &bb, &conv));
+        inf.iterations = it;
+        inf.outer_iterations = 1;
+        inf.rel_residual_recurrence = bb > 0 ? sqrt(rr / bb) : 0.0;
+        PSF_CHECK(scatter_reduced(c, c->u, c->un));
+        if (!conv) st = PSF_NOT_CONVERGED;
+    } else if (solver == PSF_SOLVE_EBE_JACOBI_F64) {
+        int it, conv;
+        double rr, bb;
+        double *x = c->w64[5];
+        PSF_CHECK(pcg_ebe<double>(c, c->Fn, 1.0, warm ? c->un : nullptr, x, c->w64, itmax, eps, &it, &rr, &bb, &conv));
+        PSF_CUDA(cudaMemcpyAsync(c->un, x, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
+        PSF_CHECK(gather_reduced(c, c->un, c->u));
+        inf.iterations = it;
+        inf.outer_iterations = 1;
+        inf.rel_residual_recurrence = bb > 0 ? sqrt(rr / bb) : 0.0;
+        if (!conv) st = PSF_NOT_CONVERGED;
+    } else if (solver == PSF_SOLVE_IR_JACOBI_F32) {
+        // FP64 iterative refinement: r = F - K x (FP64), FP32 PCG on K d = r, x += d
+        double *x = c->w64[5], *r = c->w64[6];
+        if (warm) PSF_CUDA(cudaMemcpyAsync(x, c->un, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
+        else PSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * c->ndofs, c->stream));
+        const double inner_tol = 1e-4;
+        const int max_outer = 30;
+        int total = 0, outer = 0;
+        double rn = 0, bn = 0;
+        bool ok = false;
+        for (outer = 0; outer <= max_outer; outer++) {
+            PSF_CHECK(residual64(c, c->Fn, x, r, &rn, &bn));
+            if (bn == 0.0 || rn <= eps * bn) { ok = true; break; }
+            if (!std::isfinite(rn)) break;
+            if (outer == max_outer || total >= itmax) break;
+            int it, conv;
+            double rr, bb;
+            PSF_CHECK(pcg_ebe<float>(c, r, 1.0 / rn, nullptr, c->w32[5], c->w32, itmax - total, inner_tol, &it, &rr,
+                                     &bb, &conv));
+            total += it;
+            axpy_mixed<<<grid_for(c->ndofs, 256, c->num_sms * 8), 256, 0, c->stream>>>(c->ndofs, rn, c->w32[5], x);
+            PSF_CUDA(cudaGetLastError());
+        }
+        PSF_CUDA(cudaMemcpyAsync(c->un, x, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
+        PSF_CHECK(gather_reduced(c, c->un, c->u));
+        inf.iterations = total;
+        inf.outer_iterations = outer;
+        inf.rel_residual_recurrence = bn > 0 ? rn / bn : 0.0;
+        if (!ok) st = PSF_NOT_CONVERGED;
+    } else if (solver == PSF_SOLVE_IR_MG_F32 || solver == PSF_SOLVE_IR_LEARNED_F32) {
+        st = mg_solve_ir(c, itmax, eps, warm, &inf);
+        if (st != PSF_OK && st != PSF_NOT_CONVERGED && st != PSF_FELL_BACK) return st;
+        if (solver == PSF_SOLVE_IR_LEARNED_F32 && !c->learned) {
+            // no trained network in this context: the multigrid path answered
+        }
+    } else {
+        set_error("psf_solve: unknown solver");
+        return PSF_BAD_INPUT;
+    }
+    PSF_CUDA(cudaEventRecord(c->ev1, c->stream));
+    // FP64 true residual of the returned solution
+    double rn, bn;
+    PSF_CHECK(residual64(c, c->Fn, c->un, c->w64[6], &rn, &bn));
+    inf.rel_residual = bn > 0 ? rn / bn : 0.0;
+    float ms = 0.f;
+    PSF_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    inf.seconds = ms * 1e-3;
+    inf.kernel_seconds = c->ksec;
+    inf.kernel_launches = c->klaunch;
+    if (info) *info = inf;
+    return st;
+}
+
+}  // namespace psf

@@ -1,0 +1,63 @@
+"""CPU-only checks of the C ABI boundary: the CUDA library loads without a GPU
+and exports every entry point include/*.h declares (no compute calls)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for fn in os.listdir(inc):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(inc, fn)).read()
+            syms |= set(re.findall(r"^\s*(?:psf_status|const char \*)\s*(psf_\w+)\s*\(", txt, re.M))
+    return syms
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    from pansfem2_gb300 import build
+    try:
+        return build.build()
+    except (RuntimeError, FileNotFoundError) as e:   # no nvcc on this host
+        pytest.skip(f"cannot build the CUDA library here: {e}")
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert {"psf_create", "psf_solve", "psf_simp_step", "psf_mma_update", "psf_oc_update"} <= syms
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (psf_\w+)", out))
+    missing = declared_symbols() - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+
+
+def test_library_loads_without_gpu(lib_path):
+    lib = ctypes.CDLL(lib_path)
+    for s in declared_symbols():
+        assert hasattr(lib, s)
+
+
+def test_python_binding_lists_every_symbol():
+    from pansfem2_gb300 import _lib
+    assert declared_symbols() <= set(_lib.EXPORTS) | {"psf_last_error"}
+
+
+def test_problem_definitions_match_generate_fixedlist_order():
+    """BC lists follow SquareMesh::GenerateFixedlist: node-major, dofs in list order."""
+    from pansfem2_gb300 import problems as PB
+    pr = PB.cantilever_q4(4, 2)
+    assert pr["fix_node"] == [0, 0, 1, 1, 2, 2] and pr["fix_dof"] == [0, 1, 0, 1, 0, 1]
+    assert pr["load_node"] == [4 * 3 + 1] and pr["load_dof"] == [1]
+    mbb = PB.mbb_q4(4, 2)
+    assert mbb["fix_node"] == [0, 1, 2, 12] and mbb["fix_dof"] == [0, 0, 0, 1]
+    assert mbb["load_node"] == [2]
