@@ -192,7 +192,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--solver", default="ir_jacobi_f32")
+    ap.add_argument("--solver", default="ir_mg_f32")
     ap.add_argument("--baseline-solver", default="csr_jacobi_f64")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 GPU PCG comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

@@ -1,0 +1,326 @@
+// pansfem2_gb300.hpp -- the reference's C++ template API for the SIMP path,
+// backed by the GB300 library through its C ABI (pansfem2_gpu.h).
+//
+// A driver written against PANSFEM2's headers (sample/optimize/
+// sample_optimize_density_{oc,mma}.cpp) switches to the GPU by including this
+// header instead and using namespace PANSFEM2_GB300: the class and function
+// names, argument order and meaning, and the error behaviour (return the last
+// iterate when a solver hits itrmax) are the reference's.  Differences, all
+// forced by the device boundary, are listed where they occur:
+//   * OC::UpdateVariables takes the samples' volume constraint as a
+//     VolumeConstraint value instead of a host callable, because the
+//     bisection runs on the device (a host callable cannot run there).
+//   * Structured grids: Problem owns the device context of a SquareMesh-style
+//     grid (or its 3D analogue); the matrix-free and multigrid solvers and the
+//     whole-iteration driver SimpLoop work on it.
+// Every call throws std::runtime_error with psf_last_error() on a device or
+// input error; nothing falls back to the CPU.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "pansfem2_gpu.h"
+
+namespace PANSFEM2_GB300 {
+
+inline psf_status check(psf_status s, bool allow_not_converged = true) {
+    if (s == PSF_OK || (allow_not_converged && (s == PSF_NOT_CONVERGED || s == PSF_FELL_BACK))) return s;
+    throw std::runtime_error(std::string("pansfem2_gb300: ") + psf_last_error());
+}
+
+// ------------------------------------------------------------------ LILCSR / CSR (LILCSR.h, CSR.h)
+template <class T>
+class CSR;
+
+// LILCSR<T> (LILCSR.h:24-63): rows of (column, value) pairs in first-touch order
+template <class T>
+class LILCSR {
+public:
+    LILCSR(int rows, int cols) : ROWS(rows), COLS(cols), data(rows) {}
+    const int ROWS;
+    const int COLS;
+    bool set(int row, int col, T v) {
+        for (auto &d : data[row])
+            if (d.first == col) { d.second = v; return true; }
+        data[row].push_back({col, v});
+        return false;
+    }
+    T get(int row, int col) const {
+        for (const auto &d : data[row])
+            if (d.first == col) return d.second;
+        return T();
+    }
+    template <class F>
+    friend class CSR;
+
+private:
+    std::vector<std::vector<std::pair<int, T> > > data;
+};
+
+// CSR<T> (CSR.h:25-75): host arrays; operator* runs on the GPU
+template <class T>
+class CSR {
+public:
+    CSR(int rows, int cols) : ROWS(rows), COLS(cols), indptr(rows + 1, 0) {}
+    // CSR(LILCSR&) (CSR.h:92-105): row sizes, per-row column sort, concatenation
+    explicit CSR(LILCSR<T> &m) : ROWS(m.ROWS), COLS(m.COLS), indptr(m.ROWS + 1, 0) {
+        for (int i = 0; i < ROWS; i++) {
+            auto row = m.data[i];
+            std::sort(row.begin(), row.end());
+            indptr[i + 1] = indptr[i] + (int)row.size();
+            for (auto &e : row) { indices.push_back(e.first); values.push_back(e.second); }
+        }
+    }
+    CSR(int rows, int cols, std::vector<int32_t> p, std::vector<int32_t> idx, std::vector<T> v)
+        : ROWS(rows), COLS(cols), indptr(std::move(p)), indices(std::move(idx)), values(std::move(v)) {}
+    const int ROWS;
+    const int COLS;
+    const std::vector<T> operator*(const std::vector<T> &x) {
+        std::vector<T> y(ROWS);
+        check(psf_csr_spmv(ROWS, indptr.data(), indices.data(), values.data(), x.data(), y.data()), false);
+        return y;
+    }
+    T get(int row, int col) const {
+        auto b = indices.begin() + indptr[row], e = indices.begin() + indptr[row + 1];
+        auto it = std::lower_bound(b, e, col);
+        return (it != e && *it == col) ? values[it - indices.begin()] : T();
+    }
+    const std::vector<int32_t> &Indptr() const { return indptr; }
+    const std::vector<int32_t> &Indices() const { return indices; }
+    const std::vector<T> &Data() const { return values; }
+
+private:
+    std::vector<int32_t> indptr, indices;
+    std::vector<T> values;
+};
+
+namespace detail {
+template <class T>
+std::vector<T> csr_solve(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps, int solver) {
+    static_assert(sizeof(T) == sizeof(double), "the GPU solvers take double");
+    std::vector<T> x(b.size());
+    psf_solve_info info;
+    psf_status s = psf_csr_solve(A.ROWS, A.Indptr().data(), A.Indices().data(), A.Data().data(), b.data(), solver,
+                                 itrmax, eps, x.data(), &info);
+    check(s);
+    return x;   // last iterate on PSF_NOT_CONVERGED, as CG.h:451-452
+}
+}  // namespace detail
+
+// ScalingCG (CG.h:419-453)
+template <class T>
+std::vector<T> ScalingCG(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps) {
+    return detail::csr_solve(A, b, itrmax, eps, PSF_SOLVE_CSR_JACOBI_F64);
+}
+// CG (CG.h:123-154)
+template <class T>
+std::vector<T> CG(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps) {
+    return detail::csr_solve(A, b, itrmax, eps, PSF_SOLVE_CSR_CG_F64);
+}
+
+// ------------------------------------------------------------------ structured-grid problem
+// SquareMesh<T>(lx, ly, nx, ny) (SquareMesh.h:19-45) or its 3D analogue, with
+// the element routine of `kind` (psf_element_kind); owns the device context.
+class Problem {
+public:
+    Problem(int kind, int nx, int ny, int nz, double lx, double ly, double lz, double V = 0.3, double t = 1.0) {
+        check(psf_create(&ctx_, kind, nx, ny, nz, lx, ly, lz, V, t), false);
+        int64_t ne, nn, nf, nz2;
+        int nd;
+        check(psf_sizes(ctx_, &ne, &nn, &nd, &nf, &nz2), false);
+        ne_ = ne; nnodes_ = nn; ndof_ = nd;
+    }
+    ~Problem() { psf_destroy(ctx_); }
+    Problem(const Problem &) = delete;
+    Problem &operator=(const Problem &) = delete;
+    psf_ctx *ctx() const { return ctx_; }
+    long long ne() const { return ne_; }
+    long long nnodes() const { return nnodes_; }
+    int ndof() const { return ndof_; }
+
+    // SetDirichlet + Renumbering (BoundaryCondition.h:19-25, Assembling.h:175-186): the
+    // samples' ufixed list of ((node, dof), value); returns KDEGREE
+    int SetDirichlet(const std::vector<std::pair<std::pair<int, int>, double> > &ufixed) {
+        std::vector<int> n, d;
+        std::vector<double> v;
+        for (auto &u : ufixed) { n.push_back(u.first.first); d.push_back(u.first.second); v.push_back(u.second); }
+        check(psf_set_dirichlet(ctx_, (int)n.size(), n.data(), d.data(), v.data(), nullptr), false);
+        int64_t nf;
+        check(psf_sizes(ctx_, nullptr, nullptr, nullptr, &nf, nullptr), false);
+        return (int)nf;
+    }
+    // Assembling(F, qfixed, nodetoglobal) (Assembling.h:151-158)
+    void SetLoads(const std::vector<std::pair<std::pair<int, int>, double> > &qfixed) {
+        std::vector<int> n, d;
+        std::vector<double> v;
+        for (auto &q : qfixed) { n.push_back(q.first.first); d.push_back(q.first.second); v.push_back(q.second); }
+        check(psf_set_loads(ctx_, (int)n.size(), n.data(), d.data(), v.data()), false);
+    }
+    // the element loop of the samples (PlaneStrainStiffness + Assembling for every
+    // element with modulus E_e, then CSR(LILCSR&)), assembled on the device
+    void Assemble(const std::vector<double> &E) { check(psf_assemble(ctx_, E.data(), nullptr, nullptr), false); }
+    // ScalingCG(Kmod, F, itrmax, eps) on the assembled system (solver
+    // PSF_SOLVE_CSR_JACOBI_F64), or any other psf_solver; returns the reduced u
+    std::vector<double> Solve(int solver, int itrmax, double eps, psf_solve_info *info = nullptr) {
+        int64_t nf;
+        check(psf_sizes(ctx_, nullptr, nullptr, nullptr, &nf, nullptr), false);
+        std::vector<double> u(nf);
+        psf_solve_info tmp;
+        check(psf_solve(ctx_, solver, itrmax, eps, u.data(), info ? info : &tmp));
+        return u;
+    }
+    // compliance and dfdrho of the samples' reaction/sensitivity loops
+    // (sample_optimize_density_oc.cpp:136-162) for the last solution
+    double ComplianceSensitivity(const std::vector<double> &rho, double E1, double E0, double p, double scale0,
+                                 std::vector<double> &dfdrho) {
+        double f = 0.0;
+        dfdrho.resize(rho.size());
+        check(psf_compliance_sensitivity(ctx_, rho.data(), E1, E0, p, scale0, &f, dfdrho.data()), false);
+        return f;
+    }
+
+private:
+    psf_ctx *ctx_ = nullptr;
+    long long ne_ = 0, nnodes_ = 0;
+    int ndof_ = 0;
+};
+
+// ------------------------------------------------------------------ DensityFilter (DensityFilter.h:16-71)
+template <class T>
+class DensityFilter {
+public:
+    // the reference's constructor: explicit neighbour lists and weights
+    DensityFilter(int n, std::vector<std::vector<int> > neighbors, std::vector<std::vector<T> > w) : n_(n) {
+        ptr_.push_back(0);
+        for (int i = 0; i < n; i++) {
+            for (size_t k = 0; k < neighbors[i].size(); k++) { idx_.push_back(neighbors[i][k]); w_.push_back(w[i][k]); }
+            ptr_.push_back((int32_t)idx_.size());
+        }
+    }
+    // structured grid: the lists of radius R are the clipped stencil, built on the device
+    DensityFilter(Problem &p, double R) : n_((int)p.ne()), prob_(&p) { check(psf_filter_setup(p.ctx(), R), false); }
+    std::vector<T> GetFilteredVariables(std::vector<T> s) {
+        std::vector<T> out(n_);
+        if (prob_) check(psf_filter_forward(prob_->ctx(), s.data(), out.data()), false);
+        else check(psf_list_filter(n_, ptr_.data(), idx_.data(), w_.data(), s.data(), out.data()), false);
+        return out;
+    }
+    // normalised by wsum_i, as DensityFilter.h:68 does
+    std::vector<T> GetFilteredSensitivitis(std::vector<T> s, std::vector<T> dfdrho) {
+        (void)s;
+        std::vector<T> out(n_);
+        if (prob_) check(psf_filter_backward(prob_->ctx(), dfdrho.data(), out.data()), false);
+        else check(psf_list_filter(n_, ptr_.data(), idx_.data(), w_.data(), dfdrho.data(), out.data()), false);
+        return out;
+    }
+
+private:
+    int n_;
+    Problem *prob_ = nullptr;
+    std::vector<int32_t> ptr_, idx_;
+    std::vector<T> w_;
+};
+
+// ------------------------------------------------------------------ OC (OC.h:16-107)
+// The samples' constraint callback (sample_optimize_density_oc.cpp:198-207):
+// filtered volume fraction g(x) = sum_i scale1*rho_i(x)/(vf*n) - scale1.
+struct VolumeConstraint {
+    double vf;
+    double scale1;
+};
+
+template <class T>
+class OC {
+public:
+    OC(Problem &p, int n, T iota, T lambdamin, T lambdamax, T lambdaeps, T movelimit, const std::vector<T> &xmin,
+       const std::vector<T> &xmax)
+        : p_(p), n_(n), iota_(iota), lmin_(lambdamin), lmax_(lambdamax), leps_(lambdaeps), move_(movelimit) {
+        (void)xmin; (void)xmax;   // stored but unused by the reference's update (OC.h:86-91)
+    }
+    bool IsConvergence(T f) { return std::fabs(f - prev_) / (f + prev_) < 1.0e-5; }
+    // UpdateVariables (OC.h:76-107) with the filtered-volume constraint on the
+    // device; the filter is the Problem's (DensityFilter(Problem&, R)).
+    void UpdateVariables(std::vector<T> &xk, T f, std::vector<T> dfdx, T g, std::vector<T> dgdx,
+                         const VolumeConstraint &c) {
+        (void)g;
+        double lambda;
+        check(psf_oc_update(p_.ctx(), xk.data(), dfdx.data(), dgdx.data(), iota_, lmin_, lmax_, leps_, move_, c.vf,
+                            c.scale1, &lambda), false);
+        prev_ = f;
+    }
+
+private:
+    Problem &p_;
+    int n_;
+    T iota_, lmin_, lmax_, leps_, move_, prev_ = T();
+};
+
+// ------------------------------------------------------------------ MMA (MMA.h:18-509), m = 1
+template <class T>
+class MMA {
+public:
+    MMA(Problem &p, int n, int m, T a0, std::vector<T> a, std::vector<T> c, std::vector<T> d,
+        const std::vector<T> &xmin, const std::vector<T> &xmax)
+        : p_(p), n_(n), a0_(a0), a_(a.at(0)), c_(c.at(0)), d_(d.at(0)), xmin_(xmin.at(0)), xmax_(xmax.at(0)) {
+        if (m != 1) throw std::runtime_error("pansfem2_gb300: the device MMA solves m = 1 (one constraint)");
+        init();
+    }
+    void SetParameters(T raa0, T albefa, T move, T asyinit, T asydecr, T asyincr, T epsvalue) {
+        raa0_ = raa0; albefa_ = albefa; move_ = move; asyinit_ = asyinit; asydecr_ = asydecr; asyincr_ = asyincr;
+        eps_ = epsvalue;
+        init();
+    }
+    bool IsConvergence(T f) { return std::fabs(f - prev_) / (f + prev_) < eps_; }
+    void UpdateVariables(std::vector<T> &xk, T f, std::vector<T> dfdx, std::vector<T> g,
+                         std::vector<std::vector<T> > dgdx) {
+        int newton = 0;
+        check(psf_mma_update(p_.ctx(), xk.data(), f, dfdx.data(), g.at(0), dgdx.at(0).data(), &newton));
+        prev_ = f;
+    }
+
+private:
+    void init() {
+        check(psf_mma_init(p_.ctx(), a0_, a_, c_, d_, xmin_, xmax_, raa0_, albefa_, move_, asyinit_, asydecr_,
+                           asyincr_, eps_), false);
+    }
+    Problem &p_;
+    int n_;
+    T a0_, a_, c_, d_, xmin_, xmax_;
+    T raa0_ = 1.0e-5, albefa_ = 0.1, move_ = 0.5, asyinit_ = 0.5, asydecr_ = 0.7, asyincr_ = 1.2, eps_ = 1.0e-5;
+    T prev_ = T();
+};
+
+// ------------------------------------------------------------------ the whole iteration on the device
+// One call per iteration of the samples' loop body (filter, volume, solve,
+// compliance, sensitivities, filtered sensitivities, OC/MMA update).
+class SimpLoop {
+public:
+    SimpLoop(Problem &p, const psf_simp_params &prm, const std::vector<double> *s0 = nullptr) : p_(p) {
+        check(psf_simp_begin(p.ctx(), &prm, s0 ? s0->data() : nullptr), false);
+    }
+    psf_iter_info Step() {
+        psf_iter_info info;
+        check(psf_simp_step(p_.ctx(), &info));
+        return info;
+    }
+    std::vector<double> Densities() {
+        std::vector<double> rho(p_.ne());
+        check(psf_simp_fields(p_.ctx(), nullptr, rho.data(), nullptr, nullptr, nullptr), false);
+        return rho;
+    }
+    std::vector<double> Design() {
+        std::vector<double> s(p_.ne());
+        check(psf_simp_fields(p_.ctx(), s.data(), nullptr, nullptr, nullptr, nullptr), false);
+        return s;
+    }
+
+private:
+    Problem &p_;
+};
+
+}  // namespace PANSFEM2_GB300

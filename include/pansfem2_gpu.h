@@ -183,6 +183,24 @@ psf_status psf_device_ptr(psf_ctx *ctx, const char *name, void **ptr);
 /* Synchronise the context's stream. */
 psf_status psf_sync(psf_ctx *ctx);
 
+/* ---------------- entry points on the reference's general data structures ---------------- */
+/* CSR<T>::operator* (CSR.h:108-122) on host CSR arrays: indptr (n+1), indices and
+ * data (indptr[n] entries, columns ascending per row). */
+psf_status psf_csr_spmv(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                        const double *x, double *y);
+/* ScalingCG (CG.h:419-453; solver PSF_SOLVE_CSR_JACOBI_F64) or CG (CG.h:123-154;
+ * PSF_SOLVE_CSR_CG_F64) on host CSR arrays: x0 = 0, stop when the recurrence
+ * residual drops below eps*||b||, last iterate returned with PSF_NOT_CONVERGED
+ * after itmax iterations.  x has n entries. */
+psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                         const double *b, int solver, int itmax, double eps, double *x,
+                         psf_solve_info *info);
+/* DensityFilter::GetFilteredVariables / GetFilteredSensitivitis (DensityFilter.h:44-71)
+ * with explicit neighbour lists: out_i = sum_k w[k]*in[idx[k]] / sum_k w[k] over
+ * k in [ptr[i], ptr[i+1]), summed in list order. */
+psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const double *w,
+                           const double *in, double *out);
+
 #ifdef __cplusplus
 }
 #endif

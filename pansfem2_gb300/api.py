@@ -89,14 +89,14 @@ class Problem:
 
     def assemble(self, E_e):
         E_e = f64(E_e)
-        data = np.zeros(max(self.nnz or 1, 1))
+        if not self.nnz:
+            # the pattern fixes the size of the value array the library writes
+            check(self.L.psf_build_csr(self.h, None, None))
+            self._sizes()
+        data = np.zeros(max(self.nnz, 1))
         F = np.zeros(self.nfree)
         check(self.L.psf_assemble(self.h, ptr(E_e), ptr(data), ptr(F)))
-        self._sizes()
-        if len(data) != self.nnz:
-            data = np.zeros(self.nnz)
-            check(self.L.psf_assemble(self.h, ptr(E_e), ptr(data), ptr(F)))
-        return data, F
+        return data[: self.nnz], F
 
     def spmv(self, x):
         x = f64(x)

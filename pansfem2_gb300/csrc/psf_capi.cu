@@ -84,6 +84,7 @@ psf_status psf_create(psf_ctx **out, int kind, int nx, int ny, int nz, double lx
     A(dzalloc(c, &c->Epadf, padn));
     A(dzalloc(c, &c->Dn, c->ndofs));
     A(dzalloc(c, &c->Dnf, c->ndofs));
+    A(dzalloc(c, &c->Dl1f, c->ndofs));
     A(dzalloc(c, &c->w64[0], 5 * c->ndofs));
     for (int k = 1; k < 8; k++) A(dzalloc(c, &c->w64[k], c->ndofs));
     for (int k = 0; k < 8; k++) A(dzalloc(c, &c->w32[k], c->ndofs));

@@ -99,6 +99,7 @@ __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV >
     __shared__ int s_last;
     __shared__ unsigned int s_gen;
     __shared__ int s_ok;
+    __shared__ double s_red[32 * (NV > 0 ? NV : 1)];
     const unsigned int nb = gridDim.x;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -113,25 +114,30 @@ __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV >
     }
     __syncthreads();
     if (s_last) {
-        // last block: fold the partials in block order, publish, release
+        // last block: every thread loads a strided share of the partials (one
+        // L2 round trip instead of nb/32 dependent ones), fixed-order tree sum,
+        // publish, release
         __threadfence();
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
+        if (NV > 0) {
+            double acc[NV > 0 ? NV : 1];
 #pragma unroll
             for (int k = 0; k < NV; k++) {
-                double acc = 0.0;
-                for (unsigned int b = lane; b < nb; b += 32)
-                    acc += *(volatile double *)&partials[(size_t)k * nb + b];
-                acc = warp_sum(acc);
-                if (lane == 0) gs->result[k] = acc;
+                acc[k] = 0.0;
+                for (unsigned int b = threadIdx.x; b < nb; b += blockDim.x)
+                    acc[k] += __ldcg(&partials[(size_t)k * nb + b]);
             }
-            if (NMAX) {
-                double m = -INFINITY;
-                for (unsigned int b = lane; b < nb; b += 32)
-                    m = fmax(m, *(volatile double *)&partials[(size_t)NV * nb + b]);
-                m = warp_max(m);
-                if (lane == 0) gs->result_max = m;
+            block_sum<(NV > 0 ? NV : 1)>(acc, s_red);
+            if (threadIdx.x == 0) {
+#pragma unroll
+                for (int k = 0; k < NV; k++) gs->result[k] = acc[k];
             }
+        }
+        if (NMAX) {
+            double m = -INFINITY;
+            for (unsigned int b = threadIdx.x; b < nb; b += blockDim.x)
+                m = fmax(m, __ldcg(&partials[(size_t)NV * nb + b]));
+            m = block_max(m, s_red);
+            if (threadIdx.x == 0) gs->result_max = m;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -145,7 +151,7 @@ __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV >
         long long spins = 0;
         int ok = 1;
         while (ld_acquire(&gs->gen) == g) {
-            __nanosleep(64);
+            if (spins > 256) __nanosleep(32);   // tight polling first, then back off
             if (++spins > kSpinLimit || ld_volatile_int(&gs->status) != 0) {
                 atomicCAS(&gs->status, 0, (int)PSF_TIMEOUT);
                 ok = 0;

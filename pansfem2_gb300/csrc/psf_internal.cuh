@@ -69,6 +69,7 @@ struct Ctx {
     float *Epadf = nullptr;
     double *Dn = nullptr;        // nodal diagonal of K (1 on fixed dofs)
     float *Dnf = nullptr;
+    float *Dl1f = nullptr;       // nodal l1 row sums sum_j |K_ij| (the multigrid smoother's diagonal)
 
     // Krylov work vectors (nodal length, FP64 and FP32)
     double *w64[8] = {nullptr};

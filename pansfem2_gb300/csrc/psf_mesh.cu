@@ -379,15 +379,17 @@ __global__ void moduli_pad(Grid g, long long ne, const double *E, float *Ef, dou
 }
 
 // nodal diagonal of K: sum over the node's elements of E_e*Ke0[l,l]; 1 on fixed dofs
+// nodal diagonal of K and its l1 row sums sum_j |K_ij| (the smoother's diagonal);
+// 1 on fixed dofs
 __global__ void nodal_diag(Grid g, long long nnodes, const double *Ep, const Ke64 *Ke0, const int *n2g,
-                           double *D, float *Df) {
+                           double *D, float *Df, float *Dl1) {
     const int nk = (g.is3d ? 8 : 4) * g.ndof;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
          n += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         g.node_ijk(n, i, j, k);
         for (int d = 0; d < g.ndof; d++) {
-            double s = 0.0;
+            double s = 0.0, s1 = 0.0;
             for (int ei = i - 1; ei <= i; ei++)
                 for (int ej = j - 1; ej <= j; ej++)
                     for (int ek = g.is3d ? k - 1 : 0; ek <= (g.is3d ? k : 0); ek++) {
@@ -395,11 +397,15 @@ __global__ void nodal_diag(Grid g, long long nnodes, const double *Ep, const Ke6
                                              : (long long)(ei + 1) * (g.ny + 2) + (ej + 1);
                         const int l = Grid::local(i - ei, j - ej, g.is3d ? k - ek : 0) * g.ndof + d;
                         s += Ep[p] * Ke0->v[l * nk + l];
+                        double rs = 0.0;
+                        for (int q = 0; q < nk; q++) rs += fabs(Ke0->v[l * nk + q]);
+                        s1 += Ep[p] * rs;
                     }
             long long a = n * g.ndof + d;
-            if (n2g[a] < 0) s = 1.0;
+            if (n2g[a] < 0) { s = 1.0; s1 = 1.0; }
             D[a] = s;
             Df[a] = (float)s;
+            Dl1[a] = (float)s1;
         }
     }
 }
@@ -478,6 +484,7 @@ psf_status set_dirichlet(Ctx *c, int n, const int *node, const int *dof, const d
     c->have_bc = true;
     c->have_csr = false;
     c->have_values = false;
+    c->nnz = 0;   // the pattern depends on the fixed set: rebuilt on demand
     PSF_CUDA(cudaStreamSynchronize(c->stream));
     return PSF_OK;
 }
@@ -540,7 +547,7 @@ psf_status set_moduli(Ctx *c, const double *E_dev) {
     Grid g = grid_of(c);
     moduli_pad<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(g, c->ne, c->E, c->Ef, c->Epad, c->Epadf);
     nodal_diag<<<grid_for(c->nnodes, 256, 65536), 256, 0, c->stream>>>(g, c->nnodes, c->Epad, (const Ke64 *)c->Ke0,
-                                                                         c->n2g, c->Dn, c->Dnf);
+                                                                         c->n2g, c->Dn, c->Dnf, c->Dl1f);
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }

@@ -1,12 +1,833 @@
-// psf_mg.cu -- multigrid-preconditioned mixed-precision solver (placeholder until built).
+// psf_mg.cu -- geometric multigrid preconditioned CG in FP32 inside FP64
+// iterative refinement (PSF_SOLVE_IR_MG_F32).
+//
+// Hierarchy: the structured grid is halved per axis while every axis stays
+// even and the level has more than kCoarseDofs dofs.  Coarse operators are
+// Galerkin products built element by element: bilinear (trilinear)
+// prolongation restricted to one coarse element depends only on that
+// element's nodes, so A_c = P^T A_f P is the sum over coarse elements of
+// K_c = sum_children P_c^T K_child P_c.  Element matrices are stored per coarse
+// element (FP32), with the rows / columns of fixed dofs zeroed at every level;
+// a coarse node is fixed where its coincident fine node is.
+//
+// Cycle: V(2,2) with l1-Jacobi smoothing, full restriction R = P^T, and an
+// exact coarsest solve by a dense FP64 inverse (Gauss-Jordan on the device),
+// all in FP32 on the normalised residual.  The Krylov method around it is
+// flexible CG in FP64 (operator, dot products, recurrences), so FP32 rounding
+// only perturbs the preconditioner.  The whole solve is one persistent
+// cooperative kernel; a final FP64 true residual confirms convergence.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
 #include "psf_internal.cuh"
 
 namespace psf {
-psf_status mg_solve_ir(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info) {
-    (void)c; (void)itmax; (void)eps; (void)warm; (void)info;
-    set_error("multigrid solver not available in this build");
-    return PSF_BAD_INPUT;
+
+constexpr int kMaxLev = 14;
+constexpr long long kCoarseDofs = 400;
+
+struct KeF {
+    float v[576];
+};
+struct KeT64 {
+    double v[576];
+};
+
+psf_status residual64_pub(Ctx *c, const double *b, const double *x, double *r, double *rnorm, double *bnorm);  // psf_solve.cu
+static inline psf_status residual64_check(Ctx *c, const double *b, const double *x, double *r, double *rn, double *bn) {
+    return residual64_pub(c, b, x, r, rn, bn);
 }
-psf_status mg_free(Ctx *c) { (void)c; return PSF_OK; }
+
+struct MgLev {
+    int nx, ny, nz;              // elements
+    long long nnodes, ndofs, ne;
+    float *K;                    // element matrices (levels >= 1), ne * nk * nk
+    float *Ep;                   // padded moduli (level 0)
+    float *D;                    // nodal diagonal, 1 on fixed dofs
+    unsigned char *fixed;
+    float *x, *xt, *b, *r;
+};
+
+struct MgHier {
+    int nlev = 0;
+    MgLev L[kMaxLev];
+    int nc = 0;                  // coarsest dofs
+    double *Ac = nullptr;        // coarsest dense matrix / inverse (nc x nc)
+    std::vector<void *> allocs;
+    bool built_for_current_E = false;
+};
+
+// ------------------------------------------------------------------ geometry helpers
+template <int KIND>
+struct KT {
+    static constexpr bool is3d = KIND == PSF_H8_SOLID;
+    static constexpr int nd = KIND == PSF_Q4_PLANE_STRAIN ? 2 : (KIND == PSF_Q4_HEAT ? 1 : 3);
+    static constexpr int nen = is3d ? 8 : 4;
+    static constexpr int nk = nen * nd;
+};
+
+__device__ __forceinline__ int corner_q(int di, int dj, int dk) { return (di ? (dj ? 2 : 1) : (dj ? 3 : 0)) + 4 * dk; }
+__device__ __forceinline__ void corner_of(int q, int &qi, int &qj, int &qk) {
+    qi = (q == 1 || q == 2 || q == 5 || q == 6);
+    qj = (q == 2 || q == 3 || q == 6 || q == 7);
+    qk = q >= 4;
+}
+
+template <int KIND>
+__device__ __forceinline__ long long lnode(const MgLev &L, int i, int j, int k) {
+    return KT<KIND>::is3d ? ((long long)(L.ny + 1) * i + j) * (L.nz + 1) + k : (long long)(L.ny + 1) * i + j;
+}
+template <int KIND>
+__device__ __forceinline__ void lnode_ijk(const MgLev &L, long long n, int &i, int &j, int &k) {
+    if (KT<KIND>::is3d) {
+        k = (int)(n % (L.nz + 1));
+        long long r = n / (L.nz + 1);
+        j = (int)(r % (L.ny + 1));
+        i = (int)(r / (L.ny + 1));
+    } else {
+        k = 0;
+        j = (int)(n % (L.ny + 1));
+        i = (int)(n / (L.ny + 1));
+    }
+}
+template <int KIND>
+__device__ __forceinline__ long long lelem(const MgLev &L, int i, int j, int k) {
+    return KT<KIND>::is3d ? ((long long)L.ny * i + j) * L.nz + k : (long long)L.ny * i + j;
+}
+
+// y = (A_l v)(node) for the ndof dofs of node (i,j,k); level 0 uses E*Ke0, coarse levels their element matrices
+template <int KIND>
+__device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &Ke, const float *__restrict__ v, int i,
+                                           int j, int k, float *y) {
+    using T = KT<KIND>;
+#pragma unroll
+    for (int a = 0; a < T::nd; a++) y[a] = 0.f;
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++)
+#pragma unroll
+            for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
+                const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
+                const bool inside = ei >= 0 && ei < L.nx && ej >= 0 && ej < L.ny && (!T::is3d || (ek >= 0 && ek < L.nz));
+                const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0);
+                float ue[T::nk];
+#pragma unroll
+                for (int q = 0; q < T::nen; q++) {
+                    int qi, qj, qk;
+                    corner_of(q, qi, qj, qk);
+                    const int ni = min(max(ei + qi, 0), L.nx), nj = min(max(ej + qj, 0), L.ny),
+                              nk2 = T::is3d ? min(max(ek + qk, 0), L.nz) : 0;
+                    const long long m = lnode<KIND>(L, ni, nj, nk2);
+#pragma unroll
+                    for (int b = 0; b < T::nd; b++) ue[q * T::nd + b] = v[m * T::nd + b];
+                }
+                if (lev == 0) {
+                    const float Ee = L.Ep[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
+                                                  : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
+#pragma unroll
+                    for (int a = 0; a < T::nd; a++) {
+                        float acc = 0.f;
+                        const int row = (li * T::nd + a) * T::nk;
+#pragma unroll
+                        for (int l = 0; l < T::nk; l++) acc += Ke.v[row + l] * ue[l];
+                        y[a] += Ee * acc;
+                    }
+                } else if (inside) {
+                    const float *Kel = L.K + lelem<KIND>(L, ei, ej, ek) * (T::nk * T::nk);
+#pragma unroll
+                    for (int a = 0; a < T::nd; a++) {
+                        float acc = 0.f;
+                        const float *row = Kel + (li * T::nd + a) * T::nk;
+#pragma unroll
+                        for (int l = 0; l < T::nk; l++) acc += row[l] * ue[l];
+                        y[a] += acc;
+                    }
+                }
+            }
+}
+
+// interpolation weight of coarse corner q at fine position (fx, fy, fz) in {0, 1/2, 1}
+__device__ __forceinline__ float interp_w(int q, int hx, int hy, int hz, bool is3d) {
+    // hx, hy, hz in {0, 1, 2} = fine offsets in halves of the coarse element
+    int qi, qj, qk;
+    corner_of(q, qi, qj, qk);
+    const float wx = qi ? hx * 0.5f : (2 - hx) * 0.5f;
+    const float wy = qj ? hy * 0.5f : (2 - hy) * 0.5f;
+    const float wz = is3d ? (qk ? hz * 0.5f : (2 - hz) * 0.5f) : 1.f;
+    return wx * wy * wz;
+}
+
+// ------------------------------------------------------------------ hierarchy set-up kernels
+// coarse element matrices: K_c = sum_children P_c^T K_child P_c, then masked by the coarse fixed set
+template <int KIND>
+__global__ void galerkin_kernel(MgLev F, MgLev Cc, int fine_lev, KeF Ke) {
+    using T = KT<KIND>;
+    constexpr int nk = T::nk, nen = T::nen, nd = T::nd;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < Cc.ne; e += (long long)gridDim.x * blockDim.x) {
+        int ci, cj, ck = 0;
+        if (T::is3d) {
+            ck = (int)(e % Cc.nz);
+            long long r = e / Cc.nz;
+            cj = (int)(r % Cc.ny);
+            ci = (int)(r / Cc.ny);
+        } else {
+            cj = (int)(e % Cc.ny);
+            ci = (int)(e / Cc.ny);
+        }
+        float Kc[nk * nk];
+        for (int q = 0; q < nk * nk; q++) Kc[q] = 0.f;
+        for (int ch = 0; ch < (T::is3d ? 8 : 4); ch++) {
+            int a, b, c;
+            corner_of(ch, a, b, c);
+            const int fi = 2 * ci + a, fj = 2 * cj + b, fk = T::is3d ? 2 * ck + c : 0;
+            // child matrix (masked at the fine level)
+            float Kf[nk * nk];
+            const long long fe = lelem<KIND>(F, fi, fj, fk);
+            if (fine_lev == 0) {
+                const float E = F.Ep[T::is3d ? ((long long)(fi + 1) * (F.ny + 2) + (fj + 1)) * (F.nz + 2) + (fk + 1)
+                                             : (long long)(fi + 1) * (F.ny + 2) + (fj + 1)];
+                for (int q = 0; q < nk * nk; q++) Kf[q] = E * Ke.v[q];
+                bool fx[nk];
+                for (int f = 0; f < nen; f++) {
+                    int qi, qj, qk;
+                    corner_of(f, qi, qj, qk);
+                    const long long m = lnode<KIND>(F, fi + qi, fj + qj, fk + qk);
+                    for (int s = 0; s < nd; s++) fx[f * nd + s] = F.fixed[m * nd + s] != 0;
+                }
+                for (int r = 0; r < nk; r++)
+                    for (int s = 0; s < nk; s++)
+                        if (fx[r] || fx[s]) Kf[r * nk + s] = 0.f;
+            } else {
+                const float *src = F.K + fe * (nk * nk);
+                for (int q = 0; q < nk * nk; q++) Kf[q] = src[q];
+            }
+            // W[f][q]: fine local node f of this child from coarse corner q
+            float W[nen * nen];
+            for (int f = 0; f < nen; f++) {
+                int qi, qj, qk;
+                corner_of(f, qi, qj, qk);
+                for (int q = 0; q < nen; q++) W[f * nen + q] = interp_w(q, a + qi, b + qj, c + qk, T::is3d);
+            }
+            // Kc += (W x I)^T Kf (W x I)
+            for (int fr = 0; fr < nen; fr++)
+                for (int s = 0; s < nd; s++) {
+                    // t[q'][s'] = sum_f' Kf[fr s][f' s'] W[f'][q']
+                    float t[nk];
+                    for (int q2 = 0; q2 < nen; q2++)
+                        for (int s2 = 0; s2 < nd; s2++) {
+                            float acc = 0.f;
+                            for (int f2 = 0; f2 < nen; f2++) acc += Kf[(fr * nd + s) * nk + f2 * nd + s2] * W[f2 * nen + q2];
+                            t[q2 * nd + s2] = acc;
+                        }
+                    for (int q = 0; q < nen; q++) {
+                        const float w = W[fr * nen + q];
+                        if (w == 0.f) continue;
+                        for (int l = 0; l < nk; l++) Kc[(q * nd + s) * nk + l] += w * t[l];
+                    }
+                }
+        }
+        // mask by the coarse fixed set
+        bool cx[nk];
+        for (int f = 0; f < nen; f++) {
+            int qi, qj, qk;
+            corner_of(f, qi, qj, qk);
+            const long long m = lnode<KIND>(Cc, ci + qi, cj + qj, ck + qk);
+            for (int s = 0; s < nd; s++) cx[f * nd + s] = Cc.fixed[m * nd + s] != 0;
+        }
+        float *dst = Cc.K + e * (nk * nk);
+        for (int r = 0; r < nk; r++)
+            for (int s = 0; s < nk; s++) dst[r * nk + s] = (cx[r] || cx[s]) ? 0.f : Kc[r * nk + s];
+    }
+}
+
+// coarse fixed set from the coincident fine nodes
+template <int KIND>
+__global__ void coarse_fixed_kernel(MgLev F, MgLev Cc) {
+    using T = KT<KIND>;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < Cc.nnodes; n += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        lnode_ijk<KIND>(Cc, n, i, j, k);
+        const long long m = lnode<KIND>(F, 2 * i, 2 * j, 2 * k);
+        for (int s = 0; s < T::nd; s++) Cc.fixed[n * T::nd + s] = F.fixed[m * T::nd + s];
+    }
+}
+
+// l1 row sums sum_j |A_ij| of a coarse level from its element matrices (the
+// smoother's diagonal: l1-Jacobi converges for any SPD operator)
+template <int KIND>
+__global__ void coarse_diag_kernel(MgLev L) {
+    using T = KT<KIND>;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < L.nnodes; n += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        lnode_ijk<KIND>(L, n, i, j, k);
+        for (int s = 0; s < T::nd; s++) {
+            float d = 0.f;
+            for (int ci = 0; ci < 2; ci++)
+                for (int cj = 0; cj < 2; cj++)
+                    for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
+                        const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
+                        if (ei < 0 || ei >= L.nx || ej < 0 || ej >= L.ny || (T::is3d && (ek < 0 || ek >= L.nz))) continue;
+                        const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0) * T::nd + s;
+                        const float *row = L.K + lelem<KIND>(L, ei, ej, ek) * (T::nk * T::nk) + li * T::nk;
+                        for (int q = 0; q < T::nk; q++) d += fabsf(row[q]);
+                    }
+            const long long a = n * T::nd + s;
+            L.D[a] = (L.fixed[a] || !(d > 0.f)) ? 1.f : d;
+        }
+    }
+}
+
+// dense coarsest matrix (FP64) from its element matrices; fixed dofs -> identity
+template <int KIND>
+__global__ void coarse_dense_kernel(MgLev L, double *A, int n) {
+    using T = KT<KIND>;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.ne; e += (long long)gridDim.x * blockDim.x) {
+        int i, j, k = 0;
+        if (T::is3d) {
+            k = (int)(e % L.nz);
+            long long r = e / L.nz;
+            j = (int)(r % L.ny);
+            i = (int)(r / L.ny);
+        } else {
+            j = (int)(e % L.ny);
+            i = (int)(e / L.ny);
+        }
+        long long dof[T::nk];
+        for (int q = 0; q < T::nen; q++) {
+            int qi, qj, qk;
+            corner_of(q, qi, qj, qk);
+            const long long m = lnode<KIND>(L, i + qi, j + qj, k + qk);
+            for (int s = 0; s < T::nd; s++) dof[q * T::nd + s] = m * T::nd + s;
+        }
+        const float *Kel = L.K + e * (T::nk * T::nk);
+        for (int r = 0; r < T::nk; r++)
+            for (int s = 0; s < T::nk; s++) {
+                const float v = Kel[r * T::nk + s];
+                if (v != 0.f) atomicAdd(&A[dof[r] * n + dof[s]], (double)v);
+            }
+    }
+}
+
+__global__ void dense_fix_identity(double *A, const unsigned char *fixed, int n) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+        if (fixed[q] || A[(long long)q * n + q] == 0.0) {
+            for (int t = 0; t < n; t++) { A[(long long)q * n + t] = 0.0; A[(long long)t * n + q] = 0.0; }
+            A[(long long)q * n + q] = 1.0;
+        }
+}
+
+// in-place Gauss-Jordan inverse of an SPD matrix (no pivoting), one block
+__global__ void gauss_jordan_kernel(double *A, int n) {
+    for (int k = 0; k < n; k++) {
+        const double piv = 1.0 / A[(long long)k * n + k];
+        __syncthreads();
+        for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
+            const int i = (int)(q / n), j = (int)(q % n);
+            if (i != k && j != k) A[q] -= A[(long long)i * n + k] * A[(long long)k * n + j] * piv;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            if (t != k) {
+                A[(long long)k * n + t] *= piv;
+                A[(long long)t * n + k] *= -piv;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) A[(long long)k * n + k] = piv;
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ the persistent solver kernel
+// FP64 flexible CG, preconditioned by one FP32 V-cycle per iteration:
+//   z = rn * V(r / rn);  beta = z.q_prev / p_prev.q_prev;  p = z - beta p_prev;
+//   q = K p (FP64 matrix-free);  alpha = p.r / p.q;  x += alpha p;  r -= alpha q.
+// The recurrences, dot products and operator stay in FP64; the cycle works on
+// the normalised residual in FP32, so rounding in it perturbs the
+// preconditioner only (no cond(K) amplification as in an FP32 inner solve).
+struct MgFcgArgs {
+    int nlev;
+    MgLev L[kMaxLev];
+    KeF Ke;                   // level-0 element matrix (FP32, cycle)
+    KeT64 Ke64;               // level-0 element matrix (FP64, operator)
+    const double *Ainv;
+    int nc;
+    float omega;
+    const double *Ep64;       // padded FP64 moduli
+    const double *b;          // nodal right-hand side
+    double *x, *r, *z, *p, *q;
+    int warm;                 // x holds the start vector
+    int itmax;
+    double eps;
+    GridSync *gs;
+    double *partials;
+    double *out;              // iterations, |r|^2, |b|^2, converged, V-cycles
+};
+
+// one damped (l1-)Jacobi sweep xout = xin + w (b - A xin) / D on level l
+template <int KIND>
+__device__ __forceinline__ void jacobi_sweep(const MgFcgArgs &A, int l, const float *xin, float *xout, long long tid,
+                                             long long stride) {
+    using T = KT<KIND>;
+    const MgLev &L = A.L[l];
+    for (long long n = tid; n < L.nnodes; n += stride) {
+        int i, j, k;
+        lnode_ijk<KIND>(L, n, i, j, k);
+        float y[T::nd];
+        apply_node<KIND>(L, l, A.Ke, xin, i, j, k, y);
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) {
+            const long long q = n * T::nd + s;
+            xout[q] = L.fixed[q] ? 0.f : xin[q] + A.omega * (L.b[q] - y[s]) / L.D[q];
+        }
+    }
+}
+
+// V(2,2)-cycle; on entry L[0].b holds the level-0 right-hand side and L[0].x its
+// first sweep from zero (w b / D), both written by the caller before a barrier.
+// On exit L[0].x holds the result, written by the node loop of the last sweep
+// (same node -> thread mapping as the caller's next node loop, no barrier).
+template <int KIND>
+__device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride) {
+    using T = KT<KIND>;
+    const int nl = A.nlev;
+    for (int l = 0; l < nl - 1; l++) {
+        const MgLev &L = A.L[l];
+        jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                 // second pre-smoothing sweep
+        if (!grid_barrier(A.gs, A.partials)) return false;
+        for (long long n = tid; n < L.nnodes; n += stride) {              // residual r = b - A xt
+            int i, j, k;
+            lnode_ijk<KIND>(L, n, i, j, k);
+            float y[T::nd];
+            apply_node<KIND>(L, l, A.Ke, L.xt, i, j, k, y);
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long q = n * T::nd + s;
+                L.r[q] = L.fixed[q] ? 0.f : L.b[q] - y[s];
+            }
+        }
+        if (!grid_barrier(A.gs, A.partials)) return false;
+        const MgLev &Cc = A.L[l + 1];
+        for (long long n = tid; n < Cc.nnodes; n += stride) {             // restriction b_c = P^T r
+            int i, j, k;
+            lnode_ijk<KIND>(Cc, n, i, j, k);
+            float acc[T::nd];
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) acc[s] = 0.f;
+            for (int di = -1; di <= 1; di++)
+                for (int dj = -1; dj <= 1; dj++)
+                    for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++) {
+                        const int fi = 2 * i + di, fj = 2 * j + dj, fk = 2 * k + dk;
+                        if (fi < 0 || fi > L.nx || fj < 0 || fj > L.ny || (T::is3d && (fk < 0 || fk > L.nz))) continue;
+                        const float w = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * (dk ? 0.5f : 1.f);
+                        const long long m = lnode<KIND>(L, fi, fj, fk);
+#pragma unroll
+                        for (int s = 0; s < T::nd; s++) acc[s] += w * L.r[m * T::nd + s];
+                    }
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long q = n * T::nd + s;
+                const float bv = Cc.fixed[q] ? 0.f : acc[s];
+                Cc.b[q] = bv;
+                Cc.x[q] = (l + 1 < nl - 1) ? A.omega * bv / Cc.D[q] : 0.f;   // first sweep from zero
+            }
+        }
+        if (!grid_barrier(A.gs, A.partials)) return false;
+    }
+    {   // coarsest: x = Ainv b (dense, FP64)
+        const MgLev &Cc = A.L[nl - 1];
+        const int n = A.nc;
+        for (long long q = tid; q < n; q += stride) {
+            double acc = 0.0;
+            const double *row = A.Ainv + q * n;
+            for (int t = 0; t < n; t++) acc += row[t] * (double)Cc.b[t];
+            Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
+        }
+        if (!grid_barrier(A.gs, A.partials)) return false;
+    }
+    for (int l = nl - 2; l >= 0; l--) {
+        const MgLev &L = A.L[l];
+        const MgLev &Cc = A.L[l + 1];
+        for (long long n = tid; n < L.nnodes; n += stride) {              // x = xt + P x_c
+            int i, j, k;
+            lnode_ijk<KIND>(L, n, i, j, k);
+            const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+            const int hi = i & 1, hj = j & 1, hk = k & 1;
+            float acc[T::nd];
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) acc[s] = 0.f;
+            for (int a = 0; a <= hi; a++)
+                for (int b = 0; b <= hj; b++)
+                    for (int c = 0; c <= (T::is3d ? hk : 0); c++) {
+                        const float w = (hi ? 0.5f : 1.f) * (hj ? 0.5f : 1.f) * ((T::is3d && hk) ? 0.5f : 1.f);
+                        const long long m = lnode<KIND>(Cc, ci + a, cj + b, ck + c);
+#pragma unroll
+                        for (int s = 0; s < T::nd; s++) acc[s] += w * Cc.x[m * T::nd + s];
+                    }
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long q = n * T::nd + s;
+                L.x[q] = L.fixed[q] ? 0.f : L.xt[q] + acc[s];
+            }
+        }
+        if (!grid_barrier(A.gs, A.partials)) return false;
+        jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                  // post-smoothing, sweep 1
+        if (!grid_barrier(A.gs, A.partials)) return false;
+        jacobi_sweep<KIND>(A, l, L.xt, L.x, tid, stride);                  // sweep 2 -> x
+        if (l > 0) {
+            if (!grid_barrier(A.gs, A.partials)) return false;
+        }
+    }
+    return true;
+}
+
+// q = K v (FP64 matrix-free) for node n; partial v.q returned
+template <int KIND>
+__device__ __forceinline__ double apply64_node(const MgFcgArgs &A, const double *__restrict__ v, long long n,
+                                               double *__restrict__ out) {
+    using T = KT<KIND>;
+    const MgLev &L = A.L[0];
+    int i, j, k;
+    lnode_ijk<KIND>(L, n, i, j, k);
+    double y[T::nd];
+#pragma unroll
+    for (int a = 0; a < T::nd; a++) y[a] = 0.0;
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++)
+#pragma unroll
+            for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
+                const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
+                const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0);
+                const double Ee = A.Ep64[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
+                                                 : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
+                if (Ee == 0.0) continue;
+                double ue[T::nk];
+#pragma unroll
+                for (int q = 0; q < T::nen; q++) {
+                    int qi, qj, qk;
+                    corner_of(q, qi, qj, qk);
+                    const long long m = lnode<KIND>(L, min(max(ei + qi, 0), L.nx), min(max(ej + qj, 0), L.ny),
+                                                    T::is3d ? min(max(ek + qk, 0), L.nz) : 0);
+#pragma unroll
+                    for (int b = 0; b < T::nd; b++) ue[q * T::nd + b] = v[m * T::nd + b];
+                }
+#pragma unroll
+                for (int a = 0; a < T::nd; a++) {
+                    double acc = 0.0;
+                    const int row = (li * T::nd + a) * T::nk;
+#pragma unroll
+                    for (int l = 0; l < T::nk; l++) acc += A.Ke64.v[row + l] * ue[l];
+                    y[a] += Ee * acc;
+                }
+            }
+    double d = 0.0;
+#pragma unroll
+    for (int a = 0; a < T::nd; a++) {
+        const long long t = n * T::nd + a;
+        const double qv = L.fixed[t] ? 0.0 : y[a];
+        out[t] = qv;
+        d += v[t] * qv;
+    }
+    return d;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) mg_fcg_kernel(MgFcgArgs A) {
+    using T = KT<KIND>;
+    __shared__ double sm[32 * 4];
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const MgLev &L0 = A.L[0];
+    // ---- start: r = b - K x0 (x0 = 0 unless warm)
+    {
+        double acc[2] = {0.0, 0.0};
+        if (A.warm) {
+            for (long long n = tid; n < L0.nnodes; n += stride) {
+                apply64_node<KIND>(A, A.x, n, A.r);   // r = K x (own dofs)
+#pragma unroll
+                for (int s = 0; s < T::nd; s++) {
+                    const long long t = n * T::nd + s;
+                    const double bv = L0.fixed[t] ? 0.0 : A.b[t];
+                    const double rv = L0.fixed[t] ? 0.0 : bv - A.r[t];
+                    A.r[t] = rv;
+                    A.p[t] = 0.0;
+                    A.q[t] = 0.0;
+                    acc[0] += bv * bv;
+                    acc[1] += rv * rv;
+                }
+            }
+        } else {
+            for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+                for (int s = 0; s < T::nd; s++) {
+                    const long long t = n * T::nd + s;
+                    const double bv = L0.fixed[t] ? 0.0 : A.b[t];
+                    A.x[t] = 0.0;
+                    A.r[t] = bv;
+                    A.p[t] = 0.0;
+                    A.q[t] = 0.0;
+                    acc[0] += bv * bv;
+                    acc[1] += bv * bv;
+                }
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+    }
+    const double bnorm = sqrt(gs_result(A.gs, 0));
+    double rr = gs_result(A.gs, 1);
+    double rn = sqrt(rr), pq_prev = 1.0;
+    int it = 0, conv = (rn <= A.eps * bnorm) ? 1 : 0, cycles = 0;
+    for (; !conv && it < A.itmax; it++) {
+        // ---- preconditioner: one FP32 V-cycle on r / |r|
+        const float sc = (float)(1.0 / rn);
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                const float bv = L0.fixed[t] ? 0.f : (float)A.r[t] * sc;
+                L0.b[t] = bv;
+                L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
+            }
+        if (!grid_barrier(A.gs, A.partials)) return;
+        if (!vcycle<KIND>(A, tid, stride)) return;
+        cycles++;
+        // ---- z = |r| V(r/|r|); z.q_prev, z.r, p_prev.r
+        double a3[3] = {0.0, 0.0, 0.0};
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                const double zv = rn * (double)L0.x[t];
+                A.z[t] = zv;
+                a3[0] += zv * A.q[t];
+                a3[1] += zv * A.r[t];
+                a3[2] += A.p[t] * A.r[t];
+            }
+        block_sum<3>(a3, sm);
+        if (!grid_sync<3, 0>(A.gs, A.partials, a3, 0.0)) return;
+        const double beta = it > 0 ? gs_result(A.gs, 0) / pq_prev : 0.0;
+        const double pr = gs_result(A.gs, 1) - beta * gs_result(A.gs, 2);
+        // ---- p = z - beta p_prev (own dofs, node mapping)
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                A.p[t] = A.z[t] - beta * A.p[t];
+            }
+        if (!grid_barrier(A.gs, A.partials)) return;
+        // ---- q = K p, p.q
+        double pq[1] = {0.0};
+        for (long long n = tid; n < L0.nnodes; n += stride) pq[0] += apply64_node<KIND>(A, A.p, n, A.q);
+        block_sum<1>(pq, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, pq, 0.0)) return;
+        const double pqv = gs_result(A.gs, 0);
+        if (!(pqv > 0.0)) { it++; break; }
+        const double alpha = pr / pqv;
+        // ---- x += alpha p, r -= alpha q, |r|^2
+        double ra[1] = {0.0};
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                A.x[t] += alpha * A.p[t];
+                const double rv = A.r[t] - alpha * A.q[t];
+                A.r[t] = rv;
+                ra[0] += rv * rv;
+            }
+        block_sum<1>(ra, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, ra, 0.0)) return;
+        rr = gs_result(A.gs, 0);
+        rn = sqrt(rr);
+        pq_prev = pqv;
+        if (rn <= A.eps * bnorm) { it++; conv = 1; break; }
+        if (!isfinite(rr)) { it++; break; }
+    }
+    if (tid == 0) {
+        A.out[0] = it;
+        A.out[1] = rr;
+        A.out[2] = bnorm * bnorm;
+        A.out[3] = conv;
+        A.out[4] = cycles;
+    }
+}
+
+// ------------------------------------------------------------------ host side
+static psf_status mg_alloc(MgHier *H, Ctx *c, void **p, size_t bytes) {
+    PSF_CUDA(cudaMalloc(p, bytes ? bytes : 1));
+    PSF_CUDA(cudaMemsetAsync(*p, 0, bytes ? bytes : 1, c->stream));
+    H->allocs.push_back(*p);
+    return PSF_OK;
+}
+
+static KeF kef_of(const Ctx *c) {
+    KeF k{};
+    const int nk = c->nen * c->ndof;
+    for (int q = 0; q < nk * nk; q++) k.v[q] = (float)c->Ke0_host[q];
+    return k;
+}
+
+static psf_status mg_build_hierarchy(Ctx *c) {
+    MgHier *H = new MgHier;
+    c->mg = H;
+    const bool is3d = c->kind == PSF_H8_SOLID;
+    const int nd = c->ndof, nk = c->nen * c->ndof;
+    MgLev &L0 = H->L[0];
+    L0.nx = c->nx; L0.ny = c->ny; L0.nz = c->nz;
+    L0.nnodes = c->nnodes; L0.ndofs = c->ndofs; L0.ne = c->ne;
+    L0.K = nullptr; L0.Ep = c->Epadf; L0.D = c->Dl1f; L0.fixed = c->fixed;
+    int nl = 1;
+    while (nl < kMaxLev) {
+        const MgLev &F = H->L[nl - 1];
+        if (nl > 1 && F.ndofs <= kCoarseDofs) break;
+        if ((F.nx & 1) || (F.ny & 1) || (is3d && (F.nz & 1)) || F.nx < 2 || F.ny < 2 || (is3d && F.nz < 2)) break;
+        MgLev &Cc = H->L[nl];
+        Cc.nx = F.nx / 2; Cc.ny = F.ny / 2; Cc.nz = is3d ? F.nz / 2 : 0;
+        Cc.nnodes = is3d ? (long long)(Cc.nx + 1) * (Cc.ny + 1) * (Cc.nz + 1) : (long long)(Cc.nx + 1) * (Cc.ny + 1);
+        Cc.ndofs = Cc.nnodes * nd;
+        Cc.ne = is3d ? (long long)Cc.nx * Cc.ny * Cc.nz : (long long)Cc.nx * Cc.ny;
+        PSF_CHECK(mg_alloc(H, c, (void **)&Cc.K, sizeof(float) * Cc.ne * nk * nk));
+        PSF_CHECK(mg_alloc(H, c, (void **)&Cc.D, sizeof(float) * Cc.ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&Cc.fixed, Cc.ndofs));
+        Cc.Ep = nullptr;
+        nl++;
+    }
+    H->nlev = nl;
+    for (int l = 0; l < nl; l++) {
+        MgLev &L = H->L[l];
+        PSF_CHECK(mg_alloc(H, c, (void **)&L.x, sizeof(float) * L.ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&L.xt, sizeof(float) * L.ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&L.r, sizeof(float) * L.ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&L.b, sizeof(float) * L.ndofs));
+    }
+    if (nl < 2) { set_error("multigrid needs at least one even coarsening of the grid"); return PSF_BAD_INPUT; }
+    H->nc = (int)H->L[nl - 1].ndofs;
+    if (H->nc > 4096) { set_error("multigrid coarsest level too large for the dense solve (grid not divisible enough)"); return PSF_BAD_INPUT; }
+    PSF_CHECK(mg_alloc(H, c, (void **)&H->Ac, sizeof(double) * (size_t)H->nc * H->nc));
+    return PSF_OK;
+}
+
+template <int KIND>
+static psf_status mg_setup_t(Ctx *c, MgHier *H) {
+    KeF Ke = kef_of(c);
+    for (int l = 1; l < H->nlev; l++) {
+        MgLev &F = H->L[l - 1], &Cc = H->L[l];
+        coarse_fixed_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(F, Cc);
+        galerkin_kernel<KIND><<<grid_for(Cc.ne, 64, 65536), 64, 0, c->stream>>>(F, Cc, l - 1, Ke);
+        coarse_diag_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(Cc);
+        PSF_CUDA(cudaGetLastError());
+    }
+    MgLev &Lc = H->L[H->nlev - 1];
+    const int n = H->nc;
+    PSF_CUDA(cudaMemsetAsync(H->Ac, 0, sizeof(double) * (size_t)n * n, c->stream));
+    coarse_dense_kernel<KIND><<<grid_for(Lc.ne, 128, 4096), 128, 0, c->stream>>>(Lc, H->Ac, n);
+    dense_fix_identity<<<grid_for(n, 128), 128, 0, c->stream>>>(H->Ac, Lc.fixed, n);
+    gauss_jordan_kernel<<<1, 1024, 0, c->stream>>>(H->Ac, n);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
+static psf_status mg_setup(Ctx *c) {
+    if (!c->mg) PSF_CHECK(mg_build_hierarchy(c));
+    MgHier *H = (MgHier *)c->mg;
+    H->L[0].Ep = c->Epadf;
+    H->L[0].D = c->Dl1f;
+    switch (c->kind) {
+    case PSF_Q4_PLANE_STRAIN: return mg_setup_t<0>(c, H);
+    case PSF_Q4_HEAT: return mg_setup_t<1>(c, H);
+    default: return mg_setup_t<2>(c, H);
+    }
+}
+
+template <int KIND>
+static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h) {
+    const void *fn = (const void *)mg_fcg_kernel<KIND>;
+    int per_sm = 0;
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_fcg_kernel<KIND>, 256, 0));
+    if (per_sm < 1) { set_error("multigrid kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
+    int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
+    long long need = (c->nnodes + 255) / 256;
+    if (blocks > need) blocks = (int)need;
+    if (blocks < 1) blocks = 1;
+    void *args[] = {&a};
+    PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
+    PSF_CHECK(launch_coop(c, fn, blocks, 256, args));
+    PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
+    PSF_CHECK(read_sync_status(c));
+    PSF_CHECK(add_kernel_time(c));
+    PSF_CUDA(cudaMemcpyAsync(h, a.out, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    return PSF_OK;
+}
+
+// PSF_SOLVE_IR_MG_F32: the whole solve in one persistent launch (a second one
+// only if the FP64 true residual disagrees with the recurrence)
+psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info) {
+    PSF_CHECK(mg_setup(c));
+    MgHier *H = (MgHier *)c->mg;
+    MgFcgArgs *a = new MgFcgArgs;
+    a->nlev = H->nlev;
+    for (int l = 0; l < H->nlev; l++) a->L[l] = H->L[l];
+    a->Ke = kef_of(c);
+    const int nk = c->nen * c->ndof;
+    for (int q = 0; q < nk * nk; q++) a->Ke64.v[q] = c->Ke0_host[q];
+    a->Ainv = H->Ac;
+    a->nc = H->nc;
+    a->omega = 1.0f;   // l1-Jacobi: convergent for any SPD operator
+    a->Ep64 = c->Epad;
+    a->b = c->Fn;
+    a->x = c->w64[5]; a->r = c->w64[6]; a->z = c->w64[7]; a->p = c->w64[1]; a->q = c->w64[2];
+    a->itmax = itmax;
+    a->eps = eps;
+    a->gs = c->gs;
+    a->partials = c->partials;
+    a->out = c->scal + 12;
+    if (warm) PSF_CUDA(cudaMemcpyAsync(a->x, c->un, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
+    a->warm = warm ? 1 : 0;
+    int total = 0, cycles = 0, launches = 0;
+    bool ok = false;
+    double h[5] = {0, 0, 0, 0, 0};
+    psf_status st = PSF_OK;
+    for (int pass = 0; pass < 3 && total < itmax; pass++) {
+        a->itmax = itmax - total;
+        switch (c->kind) {
+        case PSF_Q4_PLANE_STRAIN: st = mg_fcg_t<0>(c, *a, h); break;
+        case PSF_Q4_HEAT: st = mg_fcg_t<1>(c, *a, h); break;
+        default: st = mg_fcg_t<2>(c, *a, h); break;
+        }
+        if (st != PSF_OK) break;
+        launches++;
+        total += (int)h[0];
+        cycles += (int)h[4];
+        if (h[3] == 0.0) break;
+        // confirm on the FP64 true residual; restart from x if the recurrence drifted
+        double rn, bn;
+        PSF_CHECK(residual64_check(c, c->Fn, a->x, c->w64[3], &rn, &bn));
+        if (bn == 0.0 || rn <= eps * bn) { ok = true; break; }
+        a->warm = 1;
+    }
+    delete a;
+    if (st != PSF_OK) return st;
+    PSF_CUDA(cudaMemcpyAsync(c->un, c->w64[5], sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
+    PSF_CHECK(gather_reduced(c, c->un, c->u));
+    info->iterations = total;
+    info->outer_iterations = launches;
+    info->rel_residual_recurrence = h[2] > 0 ? sqrt(h[1] / h[2]) : 0.0;
+    return ok ? PSF_OK : PSF_NOT_CONVERGED;
+}
+
+psf_status mg_free(Ctx *c) {
+    MgHier *H = (MgHier *)c->mg;
+    if (!H) return PSF_OK;
+    for (void *p : H->allocs) cudaFree(p);
+    delete H;
+    c->mg = nullptr;
+    return PSF_OK;
+}
+
 psf_status learned_free(Ctx *c) { (void)c; return PSF_OK; }
+
 }  // namespace psf

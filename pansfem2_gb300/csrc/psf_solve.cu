@@ -168,6 +168,72 @@ __global__ void axpy_mixed(long long n, double s, const float *__restrict__ d, d
         x[q] += s * (double)d[q];
 }
 
+// ---- outer FP64 flexible CG around an FP32 inner solve (see outer_fcg64)
+// z = s * d32; partial z.q_prev
+__global__ void fcg_z_kernel(long long n, double s, const float *__restrict__ d, const double *__restrict__ qprev,
+                             double *__restrict__ z, double *partials) {
+    __shared__ double sm[32];
+    double acc[1] = {0.0};
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const double zv = s * (double)d[q];
+        z[q] = zv;
+        acc[0] += zv * qprev[q];
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+// p = z - beta p_prev (p_prev -> p in place); partial p.r
+__global__ void fcg_p_kernel(long long n, double beta, const double *__restrict__ z, const double *__restrict__ r,
+                             double *__restrict__ p, double *partials) {
+    __shared__ double sm[32];
+    double acc[1] = {0.0};
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const double pv = z[q] - beta * p[q];
+        p[q] = pv;
+        acc[0] += pv * r[q];
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+// q = K p (FP64, matrix-free); partial p.q
+template <int KIND>
+__global__ void fcg_q_kernel(Geo g, KeT<double> Ke, const double *__restrict__ Ep, const unsigned char *__restrict__ fixed,
+                             const double *__restrict__ p, double *__restrict__ q, double *partials) {
+    constexpr int nd = ndof_of<KIND>();
+    __shared__ double sm[32];
+    double acc[1] = {0.0};
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_ijk<KIND>(g, n, i, j, k);
+        double yv[nd];
+        ebe_node<double, KIND>(g, Ke, Ep, i, j, k, [&](long long a) { return p[a]; }, yv);
+#pragma unroll
+        for (int a = 0; a < nd; a++) {
+            const long long t = n * nd + a;
+            const double qv = fixed[t] ? 0.0 : yv[a];
+            q[t] = qv;
+            acc[0] += p[t] * qv;
+        }
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+// x += alpha p; r -= alpha q; partial |r|^2
+__global__ void fcg_update_kernel(long long n, double alpha, const double *__restrict__ p, const double *__restrict__ qv,
+                                  double *__restrict__ x, double *__restrict__ r, double *partials) {
+    __shared__ double sm[32];
+    double acc[1] = {0.0};
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        x[q] += alpha * p[q];
+        const double rv = r[q] - alpha * qv[q];
+        r[q] = rv;
+        acc[0] += rv * rv;
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+
 // ------------------------------------------------------------------ persistent Jacobi PCG, matrix-free
 template <class T>
 struct PcgArgs {
@@ -287,7 +353,8 @@ __global__ void __launch_bounds__(256) pcg_ebe_kernel(PcgArgs<T> A) {
 // ------------------------------------------------------------------ persistent Jacobi PCG on the CSR (FP64)
 struct PcgCsrArgs {
     long long rows;
-    const int *indptr, *indices, *diag;
+    int jacobi;                      // 1: ScalingCG (z = r / D), 0: CG (CG.h:123-154, z = r)
+    const int *indptr, *indices, *diag;   // diag[i] = position of (i, i), -1 when absent
     const double *data, *b;
     double *x, *r, *z, *pA, *pB, *Ap;
     int itmax;
@@ -296,6 +363,13 @@ struct PcgCsrArgs {
     double *partials;
     double *out;
 };
+
+// GetDiagonal (CG.h:397-404): CSR::get(i, i), zero when the entry is absent
+__device__ __forceinline__ double csr_diag(const PcgCsrArgs &A, long long i) {
+    if (!A.jacobi) return 1.0;
+    const int d = A.diag[i];
+    return d >= 0 ? A.data[d] : 0.0;
+}
 
 // ScalingCG (CG.h:419-453): x0 = 0, r = b, z = r / D (division, CG.h:412), p = z;
 // the recurrence residual ||r|| < eps ||b|| stops it (CG.h:443-448).
@@ -307,7 +381,7 @@ __global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
         double acc[2] = {0.0, 0.0};
         for (long long i = tid; i < A.rows; i += stride) {
             const double bv = A.b[i];
-            const double D = A.data[A.diag[i]];
+            const double D = csr_diag(A, i);
             A.x[i] = 0.0;
             A.r[i] = bv;
             const double zv = bv / D;
@@ -354,7 +428,7 @@ __global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
             A.x[i] = A.x[i] + alpha * pn[i];
             const double rv = A.r[i] + (-alpha) * A.Ap[i];
             A.r[i] = rv;
-            const double zv = rv / A.data[A.diag[i]];
+            const double zv = rv / csr_diag(A, i);
             A.z[i] = zv;
             acc[0] += zv * rv;
             acc[1] += rv * rv;
@@ -440,6 +514,10 @@ psf_status add_kernel_time(Ctx *c) {
     return PSF_OK;
 }
 
+psf_status residual64_pub(Ctx *c, const double *b, const double *x, double *r, double *rnorm, double *bnorm) {
+    return residual64(c, b, x, r, rnorm, bnorm);
+}
+
 template <class T, int KIND>
 static psf_status run_pcg_ebe(Ctx *c, PcgArgs<T> &a, int *iters, double *rr, double *bb, int *conv) {
     const void *fn = (const void *)pcg_ebe_kernel<T, KIND>;
@@ -491,14 +569,17 @@ static psf_status pcg_ebe(Ctx *c, const double *b, double bscale, const double *
     }
 }
 
-static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr, double *bb, int *conv) {
+// Jacobi PCG (jacobi = 1) or CG (jacobi = 0) on any device CSR; w holds 5*rows doubles
+psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *indices, const int *diag,
+                       const double *data, const double *b, double *x, double *w, int jacobi, int itmax, double eps,
+                       int *iters, double *rr, double *bb, int *conv) {
     PcgCsrArgs a;
-    a.rows = c->nfree;
-    a.indptr = c->indptr; a.indices = c->indices; a.diag = c->diag; a.data = c->data;
-    a.b = c->F;
-    a.x = c->u;
-    double *w = c->w64[0];   // 5 reduced-length buffers carved from nodal scratch
-    const long long n = c->nfree;
+    a.jacobi = jacobi;
+    a.rows = rows;
+    a.indptr = indptr; a.indices = indices; a.diag = diag; a.data = data;
+    a.b = b;
+    a.x = x;
+    const long long n = rows;
     a.r = w; a.z = w + n; a.pA = w + 2 * n; a.pB = w + 3 * n; a.Ap = w + 4 * n;
     a.itmax = itmax;
     a.eps = eps;
@@ -528,7 +609,87 @@ static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr,
     return PSF_OK;
 }
 
-psf_status mg_solve_ir(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_mg.cu
+static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr, double *bb, int *conv) {
+    // 5 reduced-length buffers carved from the nodal scratch
+    return pcg_csr_any(c, c->nfree, c->indptr, c->indices, c->diag, c->data, c->F, c->u, c->w64[0], 1, itmax, eps,
+                       iters, rr, bb, conv);
+}
+
+psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_mg.cu
+
+static psf_status sum_partials_host(Ctx *c, int nb, double *out) {
+    finalize_sums<<<1, 32, 0, c->stream>>>(c->partials, nb, 1, c->scal + 8);
+    PSF_CUDA(cudaGetLastError());
+    PSF_CUDA(cudaMemcpyAsync(out, c->scal + 8, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    return PSF_OK;
+}
+
+// FP32 Jacobi-PCG inner solve of K d = r / |r| into c->w32[5]
+static psf_status inner_solve(Ctx *c, int solver, const double *r, double bscale, int itmax, double tol, int *iters) {
+    (void)solver;
+    int conv;
+    double rr, bb;
+    return pcg_ebe<float>(c, r, bscale, nullptr, c->w32[5], c->w32, itmax, tol, iters, &rr, &bb, &conv);
+}
+
+// Mixed-precision solve: flexible CG in FP64 (true FP64 operator, dot products,
+// recurrences) whose preconditioner is an FP32 inner solve.  Stationary
+// refinement x += K32^-1 r stalls once eps32 * cond(K) approaches one (the
+// 1M-dof SIMP operators reach that); the K-orthogonalised outer directions
+// keep converging.  FCG(1): p = z - (z.Kp_prev / p_prev.Kp_prev) p_prev.
+static psf_status outer_fcg64(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *inf) {
+    double *x = c->w64[5], *r = c->w64[6], *z = c->w64[7], *p = c->w64[1], *q = c->w64[2];
+    const long long n = c->ndofs;
+    if (warm) PSF_CUDA(cudaMemcpyAsync(x, c->un, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    else PSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, c->stream));
+    PSF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, c->stream));
+    PSF_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
+    const double inner_tol = 1e-3;
+    const int inner_cap = 20000;
+    const int max_outer = 200;
+    double rn = 0, bn = 0, pq_prev = 1.0;
+    PSF_CHECK(residual64(c, c->Fn, x, r, &rn, &bn));
+    int total = 0, outer = 0;
+    bool ok = bn == 0.0 || rn <= eps * bn;
+    const int nb = grid_for(n, 256, c->num_sms * 4);
+    Geo g = geo_of(c);
+    KeT<double> Ke = ke_param<double>(c);
+    for (outer = 0; !ok && outer < max_outer && total < itmax && std::isfinite(rn); outer++) {
+        int it = 0;
+        PSF_CHECK(inner_solve(c, solver, r, 1.0 / rn, std::min(inner_cap, itmax - total), inner_tol, &it));
+        total += it;
+        double zq = 0, pr = 0, pq = 0, rr = 0;
+        fcg_z_kernel<<<nb, 256, 0, c->stream>>>(n, rn, c->w32[5], q, z, c->partials);
+        PSF_CHECK(sum_partials_host(c, nb, &zq));
+        const double beta = outer > 0 ? zq / pq_prev : 0.0;
+        fcg_p_kernel<<<nb, 256, 0, c->stream>>>(n, beta, z, r, p, c->partials);
+        PSF_CHECK(sum_partials_host(c, nb, &pr));
+        switch (c->kind) {
+        case PSF_Q4_PLANE_STRAIN: fcg_q_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials); break;
+        case PSF_Q4_HEAT: fcg_q_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials); break;
+        default: fcg_q_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials); break;
+        }
+        PSF_CHECK(sum_partials_host(c, nb, &pq));
+        if (!(pq > 0.0)) break;   // direction of no energy: nothing more to gain
+        const double alpha = pr / pq;
+        fcg_update_kernel<<<nb, 256, 0, c->stream>>>(n, alpha, p, q, x, r, c->partials);
+        PSF_CHECK(sum_partials_host(c, nb, &rr));
+        rn = sqrt(rr);
+        pq_prev = pq;
+        if (rn <= eps * bn) {
+            // confirm on the true residual before stopping
+            PSF_CHECK(residual64(c, c->Fn, x, r, &rn, &bn));
+            ok = rn <= eps * bn;
+        }
+    }
+    PSF_CUDA(cudaMemcpyAsync(c->un, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    PSF_CHECK(gather_reduced(c, c->un, c->u));
+    inf->iterations = total;
+    inf->outer_iterations = outer;
+    inf->rel_residual_recurrence = bn > 0 ? rn / bn : 0.0;
+    return ok ? PSF_OK : PSF_NOT_CONVERGED;
+}
 
 psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *info) {
     psf_solve_info inf{};
@@ -558,40 +719,11 @@ psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve
         inf.rel_residual_recurrence = bb > 0 ? sqrt(rr / bb) : 0.0;
         if (!conv) st = PSF_NOT_CONVERGED;
     } else if (solver == PSF_SOLVE_IR_JACOBI_F32) {
-        // FP64 iterative refinement: r = F - K x (FP64), FP32 PCG on K d = r, x += d
-        double *x = c->w64[5], *r = c->w64[6];
-        if (warm) PSF_CUDA(cudaMemcpyAsync(x, c->un, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
-        else PSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * c->ndofs, c->stream));
-        const double inner_tol = 1e-4;
-        const int max_outer = 30;
-        int total = 0, outer = 0;
-        double rn = 0, bn = 0;
-        bool ok = false;
-        for (outer = 0; outer <= max_outer; outer++) {
-            PSF_CHECK(residual64(c, c->Fn, x, r, &rn, &bn));
-            if (bn == 0.0 || rn <= eps * bn) { ok = true; break; }
-            if (!std::isfinite(rn)) break;
-            if (outer == max_outer || total >= itmax) break;
-            int it, conv;
-            double rr, bb;
-            PSF_CHECK(pcg_ebe<float>(c, r, 1.0 / rn, nullptr, c->w32[5], c->w32, itmax - total, inner_tol, &it, &rr,
-                                     &bb, &conv));
-            total += it;
-            axpy_mixed<<<grid_for(c->ndofs, 256, c->num_sms * 8), 256, 0, c->stream>>>(c->ndofs, rn, c->w32[5], x);
-            PSF_CUDA(cudaGetLastError());
-        }
-        PSF_CUDA(cudaMemcpyAsync(c->un, x, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
-        PSF_CHECK(gather_reduced(c, c->un, c->u));
-        inf.iterations = total;
-        inf.outer_iterations = outer;
-        inf.rel_residual_recurrence = bn > 0 ? rn / bn : 0.0;
-        if (!ok) st = PSF_NOT_CONVERGED;
-    } else if (solver == PSF_SOLVE_IR_MG_F32 || solver == PSF_SOLVE_IR_LEARNED_F32) {
-        st = mg_solve_ir(c, itmax, eps, warm, &inf);
-        if (st != PSF_OK && st != PSF_NOT_CONVERGED && st != PSF_FELL_BACK) return st;
-        if (solver == PSF_SOLVE_IR_LEARNED_F32 && !c->learned) {
-            // no trained network in this context: the multigrid path answered
-        }
+        st = outer_fcg64(c, solver, itmax, eps, warm, &inf);
+        if (st != PSF_OK && st != PSF_NOT_CONVERGED) return st;
+    } else if (solver == PSF_SOLVE_IR_MG_F32) {
+        st = mg_solve(c, itmax, eps, warm, &inf);
+        if (st != PSF_OK && st != PSF_NOT_CONVERGED) return st;
     } else {
         set_error("psf_solve: unknown solver");
         return PSF_BAD_INPUT;
