@@ -32,6 +32,7 @@ EXPORTS = [
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_compliance_sensitivity",
     "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_simp_begin", "psf_simp_step",
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
+    "psf_csr_spmv", "psf_csr_solve", "psf_list_filter",
 ]
 
 
@@ -116,6 +117,10 @@ def load(path=LIB_PATH):
         "psf_simp_fields": [vp, dp, dp, dp, dp, dp],
         "psf_device_ptr": [vp, C.c_char_p, C.POINTER(C.c_void_p)],
         "psf_sync": [vp],
+        "psf_csr_spmv": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, dp],
+        "psf_csr_solve": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, C.c_int, C.c_int,
+                          C.c_double, dp, C.POINTER(SolveInfo)],
+        "psf_list_filter": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, dp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
