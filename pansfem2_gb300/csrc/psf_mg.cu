@@ -56,6 +56,7 @@ struct MgHier {
     double *Ac = nullptr;        // coarsest dense matrix / inverse (nc x nc)
     std::vector<void *> allocs;
     bool built_for_current_E = false;
+    unsigned long long *trace = nullptr;   // phase timestamps (PSF_MG_TRACE)
 };
 
 // ------------------------------------------------------------------ geometry helpers
@@ -364,7 +365,22 @@ struct MgFcgArgs {
     GridSync *gs;
     double *partials;
     double *out;              // iterations, |r|^2, |b|^2, converged, V-cycles
+    unsigned long long *trace;   // optional: [0] = count, then %globaltimer after each sync of one iteration
+    int trace_iter;
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// block 0 / thread 0 stamps the time after a grid sync of the traced iteration
+__device__ __forceinline__ void stamp(const MgFcgArgs &A, bool on) {
+    if (on && A.trace && blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long n = A.trace[0];
+        if (n < 1000) { A.trace[1 + n] = global_ns(); A.trace[0] = n + 1; }
+    }
+}
 
 // one damped (l1-)Jacobi sweep xout = xin + w (b - A xin) / D on level l
 template <int KIND>
@@ -390,13 +406,14 @@ __device__ __forceinline__ void jacobi_sweep(const MgFcgArgs &A, int l, const fl
 // On exit L[0].x holds the result, written by the node loop of the last sweep
 // (same node -> thread mapping as the caller's next node loop, no barrier).
 template <int KIND>
-__device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride) {
+__device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride, bool tr) {
     using T = KT<KIND>;
     const int nl = A.nlev;
     for (int l = 0; l < nl - 1; l++) {
         const MgLev &L = A.L[l];
         jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                 // second pre-smoothing sweep
         if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
         for (long long n = tid; n < L.nnodes; n += stride) {              // residual r = b - A xt
             int i, j, k;
             lnode_ijk<KIND>(L, n, i, j, k);
@@ -409,6 +426,7 @@ __device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride) {
             }
         }
         if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
         const MgLev &Cc = A.L[l + 1];
         for (long long n = tid; n < Cc.nnodes; n += stride) {             // restriction b_c = P^T r
             int i, j, k;
@@ -435,6 +453,7 @@ __device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride) {
             }
         }
         if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
     }
     {   // coarsest: x = Ainv b (dense, FP64)
         const MgLev &Cc = A.L[nl - 1];
@@ -446,6 +465,7 @@ __device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride) {
             Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
         }
         if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
     }
     for (int l = nl - 2; l >= 0; l--) {
         const MgLev &L = A.L[l];
@@ -473,11 +493,14 @@ __device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride) {
             }
         }
         if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
         jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                  // post-smoothing, sweep 1
         if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
         jacobi_sweep<KIND>(A, l, L.xt, L.x, tid, stride);                  // sweep 2 -> x
         if (l > 0) {
             if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
         }
     }
     return true;
@@ -592,8 +615,11 @@ __global__ void __launch_bounds__(256) mg_fcg_kernel(MgFcgArgs A) {
                 L0.b[t] = bv;
                 L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
             }
+        const bool tr = it == A.trace_iter;
+        stamp(A, tr);
         if (!grid_barrier(A.gs, A.partials)) return;
-        if (!vcycle<KIND>(A, tid, stride)) return;
+        stamp(A, tr);
+        if (!vcycle<KIND>(A, tid, stride, tr)) return;
         cycles++;
         // ---- z = |r| V(r/|r|); z.q_prev, z.r, p_prev.r
         double a3[3] = {0.0, 0.0, 0.0};
@@ -609,6 +635,7 @@ __global__ void __launch_bounds__(256) mg_fcg_kernel(MgFcgArgs A) {
             }
         block_sum<3>(a3, sm);
         if (!grid_sync<3, 0>(A.gs, A.partials, a3, 0.0)) return;
+        stamp(A, tr);
         const double beta = it > 0 ? gs_result(A.gs, 0) / pq_prev : 0.0;
         const double pr = gs_result(A.gs, 1) - beta * gs_result(A.gs, 2);
         // ---- p = z - beta p_prev (own dofs, node mapping)
@@ -619,11 +646,13 @@ __global__ void __launch_bounds__(256) mg_fcg_kernel(MgFcgArgs A) {
                 A.p[t] = A.z[t] - beta * A.p[t];
             }
         if (!grid_barrier(A.gs, A.partials)) return;
+        stamp(A, tr);
         // ---- q = K p, p.q
         double pq[1] = {0.0};
         for (long long n = tid; n < L0.nnodes; n += stride) pq[0] += apply64_node<KIND>(A, A.p, n, A.q);
         block_sum<1>(pq, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, pq, 0.0)) return;
+        stamp(A, tr);
         const double pqv = gs_result(A.gs, 0);
         if (!(pqv > 0.0)) { it++; break; }
         const double alpha = pr / pqv;
@@ -640,6 +669,7 @@ __global__ void __launch_bounds__(256) mg_fcg_kernel(MgFcgArgs A) {
             }
         block_sum<1>(ra, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, ra, 0.0)) return;
+        stamp(A, tr);
         rr = gs_result(A.gs, 0);
         rn = sqrt(rr);
         pq_prev = pqv;
@@ -785,6 +815,15 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     a->gs = c->gs;
     a->partials = c->partials;
     a->out = c->scal + 12;
+    // optional per-phase trace of the third iteration (PSF_MG_TRACE=<file>)
+    const char *trace_path = getenv("PSF_MG_TRACE");
+    a->trace = nullptr;
+    a->trace_iter = 2;
+    if (trace_path && *trace_path) {
+        if (!H->trace) PSF_CHECK(mg_alloc(H, c, (void **)&H->trace, sizeof(unsigned long long) * 1001));
+        PSF_CUDA(cudaMemsetAsync(H->trace, 0, sizeof(unsigned long long) * 1001, c->stream));
+        a->trace = H->trace;
+    }
     if (warm) PSF_CUDA(cudaMemcpyAsync(a->x, c->un, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
     a->warm = warm ? 1 : 0;
     int total = 0, cycles = 0, launches = 0;
@@ -811,6 +850,17 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     }
     delete a;
     if (st != PSF_OK) return st;
+    if (trace_path && *trace_path && H->trace) {
+        std::vector<unsigned long long> t(1001);
+        PSF_CUDA(cudaMemcpy(t.data(), H->trace, sizeof(unsigned long long) * 1001, cudaMemcpyDeviceToHost));
+        FILE *fh = fopen(trace_path, "a");
+        if (fh) {
+            fprintf(fh, "levels %d phases %llu ns:", H->nlev, t[0]);
+            for (unsigned long long k = 1; k < t[0] && k < 1001; k++) fprintf(fh, " %llu", t[k + 1] - t[k]);
+            fprintf(fh, "\n");
+            fclose(fh);
+        }
+    }
     PSF_CUDA(cudaMemcpyAsync(c->un, c->w64[5], sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
     PSF_CHECK(gather_reduced(c, c->un, c->u));
     info->iterations = total;
