@@ -201,6 +201,28 @@ psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, c
 psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const double *w,
                            const double *in, double *out);
 
+/* ---------------- allocation-free solve ---------------- */
+/* No counterpart in the reference.  The ScalingCG iteration of psf_csr_solve
+ * (PSF_SOLVE_CSR_JACOBI_F64) for callers that cannot allocate device memory
+ * when they solve: a host whose pool allocator owns the device heap, a
+ * real-time or embedded loop that forbids allocation after start-up, a host
+ * whose allocator belongs to another framework.  Inputs and outputs are DEVICE
+ * pointers (CSR arrays of n rows, b, x); the call makes no cudaMalloc /
+ * cudaFree and calls no allocating library routine.  Its scratch lives in one
+ * fixed file-scope device array sized for PSF_NOALLOC_MAX_ROWS rows (about
+ * 11.6 MB, held by every GPU that loads the library until the process exits);
+ * larger n is rejected with PSF_BAD_INPUT.  The first call on a device looks
+ * up that array's device address (once per device, with the device current):
+ * make that first call before any stream capture.  Every call reuses the same
+ * array, so calls that overlap on the GPU (other streams, other host threads)
+ * race: order them on one stream or synchronise between them.  stream may be
+ * NULL (the default stream).  Returns PSF_NOT_CONVERGED with the last iterate
+ * after itmax iterations. */
+#define PSF_NOALLOC_MAX_ROWS 262144
+psf_status psf_csr_solve_noalloc(int n, const int32_t *d_indptr, const int32_t *d_indices,
+                                 const double *d_data, const double *d_b, double *d_x, int itmax,
+                                 double eps, void *stream, psf_solve_info *info);
+
 #ifdef __cplusplus
 }
 #endif

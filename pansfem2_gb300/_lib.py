@@ -32,7 +32,7 @@ EXPORTS = [
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_compliance_sensitivity",
     "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_simp_begin", "psf_simp_step",
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
-    "psf_csr_spmv", "psf_csr_solve", "psf_list_filter",
+    "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
 ]
 
 
@@ -121,6 +121,8 @@ def load(path=LIB_PATH):
         "psf_csr_solve": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, C.c_int, C.c_int,
                           C.c_double, dp, C.POINTER(SolveInfo)],
         "psf_list_filter": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, dp],
+        # device pointers and a stream handle
+        "psf_csr_solve_noalloc": [C.c_int, vp, vp, vp, vp, vp, C.c_int, C.c_double, vp, C.POINTER(SolveInfo)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

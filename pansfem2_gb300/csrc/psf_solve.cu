@@ -609,6 +609,41 @@ psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *ind
     return PSF_OK;
 }
 
+// Cooperative launch of pcg_csr_kernel (ScalingCG) on caller-owned device
+// buffers and the caller's stream, without a context and without allocating:
+// w holds 5*rows doubles, gs is zeroed here, partials holds (kMaxRed+2)*blocks
+// doubles, out receives iterations, |r|^2, |b|^2, converged.
+psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr, const int *indices, const int *diag,
+                              const double *data, const double *b, double *x, double *w, int itmax, double eps,
+                              GridSync *gs, double *partials, int max_blocks, double *out) {
+    PcgCsrArgs a;
+    a.jacobi = 1;
+    a.rows = rows;
+    a.indptr = indptr; a.indices = indices; a.diag = diag; a.data = data;
+    a.b = b;
+    a.x = x;
+    a.r = w; a.z = w + rows; a.pA = w + 2 * rows; a.pB = w + 3 * rows; a.Ap = w + 4 * rows;
+    a.itmax = itmax;
+    a.eps = eps;
+    a.gs = gs;
+    a.partials = partials;
+    a.out = out;
+    int dev = 0, sms = 0, per_sm = 0;
+    PSF_CUDA(cudaGetDevice(&dev));
+    PSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_csr_kernel, 256, 0));
+    if (per_sm < 1) { set_error("persistent PCG kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
+    int blocks = sms * (per_sm < 4 ? per_sm : 4);
+    const long long need = (rows * 4 + 255) / 256;
+    if (blocks > need) blocks = (int)need;
+    if (blocks > max_blocks) blocks = max_blocks;
+    if (blocks < 1) blocks = 1;
+    PSF_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), s));
+    void *args[] = {&a};
+    PSF_CUDA(cudaLaunchCooperativeKernel((const void *)pcg_csr_kernel, dim3(blocks), dim3(256), args, 0, s));
+    return PSF_OK;
+}
+
 static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr, double *bb, int *conv) {
     // 5 reduced-length buffers carved from the nodal scratch
     return pcg_csr_any(c, c->nfree, c->indptr, c->indices, c->diag, c->data, c->F, c->u, c->w64[0], 1, itmax, eps,
