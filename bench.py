@@ -38,14 +38,40 @@ def workload(nx=1024, ny=512):
     return PB.mbb_q4(nx, ny)
 
 
-def bytes_per_krylov_iteration(solver, ne, ndofs, nnz, nfree):
-    """Algorithmic HBM bytes of one Jacobi-PCG iteration: operator + 11 vector
-    passes (x, p, r, Ap, D read; x, r write; r, D, p read; p write)."""
+def mg_levels(nx, ny, nd=2, coarse_dofs=100):
+    """Node counts of the multigrid hierarchy (halving while even, until the
+    level has <= coarse_dofs dofs), as psf_mg.cu builds it."""
+    levels = [(nx + 1) * (ny + 1)]
+    while True:
+        if len(levels) > 1 and levels[-1] * nd <= coarse_dofs:
+            break
+        if nx % 2 or ny % 2 or nx < 2 or ny < 2:
+            break
+        nx, ny = nx // 2, ny // 2
+        levels.append((nx + 1) * (ny + 1))
+    return levels
+
+
+def bytes_per_krylov_iteration(solver, ne, ndofs, nnz, nfree, nx=1024, ny=512):
+    """Algorithmic HBM bytes of one Krylov iteration (every array a phase
+    touches counted once per phase).
+    Jacobi PCG: operator + 11 vector passes (x, p, r, Ap, D read; x, r write;
+    r, D, p read; p write).
+    Multigrid FCG (ir_mg_f32): FP64 outer phases 144 B/dof + 8 B/element
+    (V-cycle input 20, z 36, p 24, q = K p 16 + E, x/r update 48), the FP32
+    level-0 V(2,2) work 72 B/dof + 16 B/element, and per coarse level four
+    stencil applications (9 blocks of 2x2 floats per node) plus 72 B/dof of
+    level vectors."""
     if solver == "csr_jacobi_f64":
         return 12 * nnz + 20 * nfree + 11 * 8 * nfree
     if solver == "ebe_jacobi_f64":
         return 8 * ne + 16 * ndofs + 11 * 8 * ndofs
-    # FP32 inner iterations
+    if solver == "ir_mg_f32":
+        outer = 144 * ndofs + 8 * ne
+        level0 = 72 * ndofs + 16 * ne
+        coarse = sum(4 * 9 * 4 * 4 * n + 72 * 2 * n for n in mg_levels(nx, ny)[1:-1])
+        return outer + level0 + coarse
+    # FP32 inner Jacobi iterations
     return 4 * ne + 8 * ndofs + 11 * 4 * ndofs
 
 
@@ -262,7 +288,7 @@ def main():
     kit = sum(i["solve"]["iterations"] for i in infos)
     ksec = sum(i["solve"]["kernel_seconds"] for i in infos)
     klaunch = sum(i["solve"]["kernel_launches"] for i in infos)
-    bpi = bytes_per_krylov_iteration(args.solver, ne, ndofs, 18 * nfree, nfree)
+    bpi = bytes_per_krylov_iteration(args.solver, ne, ndofs, 18 * nfree, nfree, args.nx, args.ny)
     peak, peak_kind = peaks()
     achieved = bpi * kit / ksec / 1e9 if ksec > 0 else None
     traffic = None

@@ -25,7 +25,9 @@
 namespace psf {
 
 constexpr int kMaxLev = 14;
-constexpr long long kCoarseDofs = 400;
+// coarsen while the level has more dofs than this: the dense FP64 inverse of the
+// coarsest level costs O(n^3) on one block, so keep n at about a hundred
+constexpr long long kCoarseDofs = 100;
 
 struct KeF {
     float v[576];
@@ -42,7 +44,8 @@ static inline psf_status residual64_check(Ctx *c, const double *b, const double 
 struct MgLev {
     int nx, ny, nz;              // elements
     long long nnodes, ndofs, ne;
-    float *K;                    // element matrices (levels >= 1), ne * nk * nk
+    float *K;                    // element matrices (levels >= 1), ne * nk * nk (Galerkin build)
+    float *S;                    // node stencil (levels >= 1): [slot][a][b][node], 3^d slots of nd x nd
     float *Ep;                   // padded moduli (level 0)
     float *D;                    // nodal diagonal, 1 on fixed dofs
     unsigned char *fixed;
@@ -104,6 +107,30 @@ __device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &K
     using T = KT<KIND>;
 #pragma unroll
     for (int a = 0; a < T::nd; a++) y[a] = 0.f;
+    if (lev > 0) {
+        // coarse levels: assembled node stencil, structure of arrays (coalesced
+        // across the warp's consecutive nodes); out-of-grid slots hold zeros
+        const long long n = lnode<KIND>(L, i, j, k);
+        int slot = 0;
+#pragma unroll
+        for (int di = -1; di <= 1; di++)
+#pragma unroll
+            for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+                for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++, slot++) {
+                    const long long m = lnode<KIND>(L, min(max(i + di, 0), L.nx), min(max(j + dj, 0), L.ny),
+                                                    T::is3d ? min(max(k + dk, 0), L.nz) : 0);
+                    float vb[T::nd];
+#pragma unroll
+                    for (int b = 0; b < T::nd; b++) vb[b] = v[m * T::nd + b];
+#pragma unroll
+                    for (int a = 0; a < T::nd; a++)
+#pragma unroll
+                        for (int b = 0; b < T::nd; b++)
+                            y[a] += L.S[((long long)(slot * T::nd + a) * T::nd + b) * L.nnodes + n] * vb[b];
+                }
+        return;
+    }
 #pragma unroll
     for (int ci = 0; ci < 2; ci++)
 #pragma unroll
@@ -255,27 +282,49 @@ __global__ void coarse_fixed_kernel(MgLev F, MgLev Cc) {
     }
 }
 
-// l1 row sums sum_j |A_ij| of a coarse level from its element matrices (the
-// smoother's diagonal: l1-Jacobi converges for any SPD operator)
+// Node stencil of a coarse level from its (masked) element matrices: the block
+// coupling node n to neighbour m sums, over the elements holding both, the
+// element matrix block (local n, local m).  Also the l1 row sums sum_j |A_ij|
+// (the smoother's diagonal: l1-Jacobi converges for any SPD operator).
 template <int KIND>
-__global__ void coarse_diag_kernel(MgLev L) {
+__global__ void coarse_stencil_kernel(MgLev L) {
     using T = KT<KIND>;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < L.nnodes; n += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         lnode_ijk<KIND>(L, n, i, j, k);
-        for (int s = 0; s < T::nd; s++) {
-            float d = 0.f;
-            for (int ci = 0; ci < 2; ci++)
-                for (int cj = 0; cj < 2; cj++)
-                    for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
-                        const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
-                        if (ei < 0 || ei >= L.nx || ej < 0 || ej >= L.ny || (T::is3d && (ek < 0 || ek >= L.nz))) continue;
-                        const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0) * T::nd + s;
-                        const float *row = L.K + lelem<KIND>(L, ei, ej, ek) * (T::nk * T::nk) + li * T::nk;
-                        for (int q = 0; q < T::nk; q++) d += fabsf(row[q]);
+        float d1[T::nd];
+        for (int a = 0; a < T::nd; a++) d1[a] = 0.f;
+        int slot = 0;
+        for (int di = -1; di <= 1; di++)
+            for (int dj = -1; dj <= 1; dj++)
+                for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++, slot++) {
+                    float blk[T::nd * T::nd];
+                    for (int q = 0; q < T::nd * T::nd; q++) blk[q] = 0.f;
+                    const int mi = i + di, mj = j + dj, mk = k + dk;
+                    const bool mok = mi >= 0 && mi <= L.nx && mj >= 0 && mj <= L.ny && (!T::is3d || (mk >= 0 && mk <= L.nz));
+                    if (mok) {
+                        for (int ei = max(i, mi) - 1; ei <= min(i, mi); ei++)
+                            for (int ej = max(j, mj) - 1; ej <= min(j, mj); ej++)
+                                for (int ek = (T::is3d ? max(k, mk) - 1 : 0); ek <= (T::is3d ? min(k, mk) : 0); ek++) {
+                                    if (ei < 0 || ei >= L.nx || ej < 0 || ej >= L.ny) continue;
+                                    if (T::is3d && (ek < 0 || ek >= L.nz)) continue;
+                                    const float *Ke = L.K + lelem<KIND>(L, ei, ej, ek) * (T::nk * T::nk);
+                                    const int ln = corner_q(i - ei, j - ej, T::is3d ? k - ek : 0);
+                                    const int lm = corner_q(mi - ei, mj - ej, T::is3d ? mk - ek : 0);
+                                    for (int a = 0; a < T::nd; a++)
+                                        for (int b = 0; b < T::nd; b++)
+                                            blk[a * T::nd + b] += Ke[(ln * T::nd + a) * T::nk + lm * T::nd + b];
+                                }
                     }
-            const long long a = n * T::nd + s;
-            L.D[a] = (L.fixed[a] || !(d > 0.f)) ? 1.f : d;
+                    for (int a = 0; a < T::nd; a++)
+                        for (int b = 0; b < T::nd; b++) {
+                            L.S[((long long)(slot * T::nd + a) * T::nd + b) * L.nnodes + n] = blk[a * T::nd + b];
+                            d1[a] += fabsf(blk[a * T::nd + b]);
+                        }
+                }
+        for (int a = 0; a < T::nd; a++) {
+            const long long q = n * T::nd + a;
+            L.D[q] = (L.fixed[q] || !(d1[a] > 0.f)) ? 1.f : d1[a];
         }
     }
 }
@@ -456,13 +505,16 @@ __device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride, bool
         stamp(A, tr);
     }
     {   // coarsest: x = Ainv b (dense, FP64)
+        // one warp per row: the lanes read the row contiguously (coalesced)
         const MgLev &Cc = A.L[nl - 1];
         const int n = A.nc;
-        for (long long q = tid; q < n; q += stride) {
+        const int lane = threadIdx.x & 31;
+        for (long long q = tid >> 5; q < n; q += stride >> 5) {
             double acc = 0.0;
             const double *row = A.Ainv + q * n;
-            for (int t = 0; t < n; t++) acc += row[t] * (double)Cc.b[t];
-            Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
+            for (int t = lane; t < n; t += 32) acc += row[t] * (double)Cc.b[t];
+            acc = warp_sum(acc);
+            if (lane == 0) Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
         }
         if (!grid_barrier(A.gs, A.partials)) return false;
         stamp(A, tr);
@@ -558,8 +610,10 @@ __device__ __forceinline__ double apply64_node(const MgFcgArgs &A, const double 
     return d;
 }
 
+constexpr int kMgThreads = 512;   // one block per SM: half the barrier arrivals of 2 x 256
+
 template <int KIND>
-__global__ void __launch_bounds__(256) mg_fcg_kernel(MgFcgArgs A) {
+__global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
     using T = KT<KIND>;
     __shared__ double sm[32 * 4];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -720,6 +774,7 @@ static psf_status mg_build_hierarchy(Ctx *c) {
         Cc.ndofs = Cc.nnodes * nd;
         Cc.ne = is3d ? (long long)Cc.nx * Cc.ny * Cc.nz : (long long)Cc.nx * Cc.ny;
         PSF_CHECK(mg_alloc(H, c, (void **)&Cc.K, sizeof(float) * Cc.ne * nk * nk));
+        PSF_CHECK(mg_alloc(H, c, (void **)&Cc.S, sizeof(float) * Cc.nnodes * (is3d ? 27 : 9) * nd * nd));
         PSF_CHECK(mg_alloc(H, c, (void **)&Cc.D, sizeof(float) * Cc.ndofs));
         PSF_CHECK(mg_alloc(H, c, (void **)&Cc.fixed, Cc.ndofs));
         Cc.Ep = nullptr;
@@ -747,7 +802,7 @@ static psf_status mg_setup_t(Ctx *c, MgHier *H) {
         MgLev &F = H->L[l - 1], &Cc = H->L[l];
         coarse_fixed_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(F, Cc);
         galerkin_kernel<KIND><<<grid_for(Cc.ne, 64, 65536), 64, 0, c->stream>>>(F, Cc, l - 1, Ke);
-        coarse_diag_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(Cc);
+        coarse_stencil_kernel<KIND><<<grid_for(Cc.nnodes, 128, 65536), 128, 0, c->stream>>>(Cc);
         PSF_CUDA(cudaGetLastError());
     }
     MgLev &Lc = H->L[H->nlev - 1];
@@ -776,15 +831,15 @@ template <int KIND>
 static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h) {
     const void *fn = (const void *)mg_fcg_kernel<KIND>;
     int per_sm = 0;
-    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_fcg_kernel<KIND>, 256, 0));
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_fcg_kernel<KIND>, kMgThreads, 0));
     if (per_sm < 1) { set_error("multigrid kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
     int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
-    long long need = (c->nnodes + 255) / 256;
+    long long need = (c->nnodes + kMgThreads - 1) / kMgThreads;
     if (blocks > need) blocks = (int)need;
     if (blocks < 1) blocks = 1;
     void *args[] = {&a};
     PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
-    PSF_CHECK(launch_coop(c, fn, blocks, 256, args));
+    PSF_CHECK(launch_coop(c, fn, blocks, kMgThreads, args));
     PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
     PSF_CHECK(read_sync_status(c));
     PSF_CHECK(add_kernel_time(c));
