@@ -31,6 +31,10 @@ import numpy as np  # noqa: E402
 METRIC = "SIMP iters/s at 1M DOF, resid 1e-8: learned+mixed FCG vs plain FP64 GPU PCG"
 UNIT = "SIMP iterations/s"
 L2_BYTES = 129 * 1024 * 1024
+KERNEL_NAME = {"ir_mg_f32": "mg_fcg_kernel (persistent FP64 flexible CG, FP32 V(2,2) multigrid)",
+               "csr_jacobi_f64": "pcg_csr_kernel (persistent FP64 Jacobi PCG on CSR)",
+               "ebe_jacobi_f64": "pcg_ebe_kernel<double> (persistent matrix-free FP64 Jacobi PCG)",
+               "ir_jacobi_f32": "pcg_ebe_kernel<float> (FP32 Jacobi inner iterations)"}
 
 
 def workload(nx=1024, ny=512):
@@ -312,7 +316,7 @@ def main():
                       "phase_seconds_mean": list(np.mean([i["phase_seconds"] for i in infos], axis=0))}}
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                       "kernel": f"persistent Jacobi PCG ({args.solver})", "bytes_per_iteration": bpi,
+                       "kernel": KERNEL_NAME.get(args.solver, args.solver), "bytes_per_iteration": bpi,
                        "peak_source": peak_kind}
     # launches of our kernels in the timed region: per step ~12 fixed kernels + Krylov launches + residual kernels
     out["gpu_launches"] = int(args.steps * 14 + klaunch + 3 * sum(i["solve"]["outer_iterations"] for i in infos))

@@ -223,6 +223,35 @@ psf_status psf_csr_solve_noalloc(int n, const int32_t *d_indptr, const int32_t *
                                  const double *d_data, const double *d_b, double *d_x, int itmax,
                                  double eps, void *stream, psf_solve_info *info);
 
+/* ---------------- learned preconditioner: the network ---------------- */
+/* No counterpart in the reference (its solvers have no learned part).  A
+ * 4-level U-Net on the node grid (H x W nodes, H and W odd so that the levels
+ * nest: H = 8k+1, W = 8m+1), base width c0 (16: channels 16, 32, 64, 128), bf16 weights and
+ * activations with fp32 accumulation on the tensor cores, trained with Adam on
+ * the GPU.  Inputs are [B][H][W][8] (density, the two residual components,
+ * five zero channels), outputs [B][H][W][2].  The parameter vector is laid out
+ * per layer as W[co][tap][ci] then b[co] (oracle/unet_oracle.c restates the
+ * network on the CPU). */
+typedef struct psf_unet psf_unet;
+psf_status psf_unet_create(int c0, int H, int W, int batch, uint64_t seed, psf_unet **net);
+psf_status psf_unet_destroy(psf_unet *net);
+int psf_unet_nparams(const psf_unet *net);
+psf_status psf_unet_set_params(psf_unet *net, const float *host, int n);
+psf_status psf_unet_get_params(const psf_unet *net, float *host, int n);
+/* forward of B host samples (B <= batch of psf_unet_create) */
+psf_status psf_unet_forward_host(psf_unet *net, int B, const float *in, float *out);
+/* forward, masked mean squared error against tgt, backward: loss, output and
+ * parameter gradient (any output pointer may be NULL; mask may be NULL) */
+psf_status psf_unet_loss_grad_host(psf_unet *net, int B, const float *in, const float *tgt,
+                                   const float *mask, double *loss, float *out, float *grad);
+/* one tensor-core convolution on host arrays (test and tuning hook):
+ * y[b][o][n] = act(bias[n] + sum_tap sum_ci w[n][tap][ci] x[b][src(o, tap)][ci]) with
+ * src by mode: 0 stride 1, 1 stride 2, 2 transposed stride 1, 3 transposed stride 2;
+ * x [B][hin][win][cin] (cin a multiple of 8), y [B][hout][wout][N], N in
+ * {16, 32, 48, 64, 96, 128, 192}; inputs and weights are rounded to bf16 */
+psf_status psf_unet_conv(int mode, int N, int cin, int hin, int win, int hout, int wout, int B,
+                         const float *x, const float *w, const float *bias, int relu, float *y);
+
 #ifdef __cplusplus
 }
 #endif

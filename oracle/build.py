@@ -5,6 +5,8 @@ Two builds of the same source:
                          with the reference's operation order on any host)
   libpsf_oracle_fast.so  -O3 -fopenmp          : the CPU baseline, the
                          reference's own stock flags (README: g++ -O3 -fopenmp)
+and the network oracle of the learned preconditioner:
+  libunet_oracle.so      -O2                   : U-Net forward/backward checker
 """
 import os
 import subprocess
@@ -13,6 +15,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "psf_oracle.c")
+USRC = os.path.join(HERE, "unet_oracle.c")
 
 
 def build(verbose=False):
@@ -23,6 +26,8 @@ def build(verbose=False):
          SRC, "-o", os.path.join(OUT, "libpsf_oracle.so"), "-lm"],
         [cc, "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11",
          SRC, "-o", os.path.join(OUT, "libpsf_oracle_fast.so"), "-lm"],
+        [cc, "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11",
+         USRC, "-o", os.path.join(OUT, "libunet_oracle.so"), "-lm"],
     ]
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
     for j, p in zip(jobs, procs):

@@ -379,3 +379,43 @@ def read_dump(path):
         n = cnt * np.dtype(dt).itemsize
         out[name] = np.frombuffer(buf[o:o + n], dtype=dt).copy(); o += n
     return out
+
+
+# ---------------------------------------------------------------- U-Net oracle
+_unet = None
+
+
+def _unet_lib():
+    global _unet
+    if _unet is None:
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libunet_oracle.so")
+        if not os.path.exists(path):
+            from oracle import build as _b
+            _b.build()
+        lib = C.CDLL(path)
+        lib.uo_nparams.restype = C.c_int
+        lib.uo_loss_grad.restype = C.c_double
+        lib.uo_loss_grad.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        _unet = lib
+    return _unet
+
+
+def unet_nparams(c0=16):
+    return int(_unet_lib().uo_nparams(c0))
+
+
+def unet_loss_grad(params, inp, target, mask=None, c0=16, bf16=True, want_grad=True):
+    """Loss, output [B,H,W,2] and parameter gradient of the U-Net oracle.
+    inp: float32 [B,H,W,8]; target, mask: float32 [B,H,W,2]."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    inp = np.ascontiguousarray(inp, dtype=np.float32)
+    target = np.ascontiguousarray(target, dtype=np.float32)
+    B, H, W, _ = inp.shape
+    out = np.zeros((B, H, W, 2), np.float32)
+    grad = np.zeros(params.size, np.float32) if want_grad else None
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+    loss = _unet_lib().uo_loss_grad(params.ctypes.data, c0, B, H, W, inp.ctypes.data, target.ctypes.data,
+                                    None if m is None else m.ctypes.data, int(bf16), out.ctypes.data,
+                                    None if grad is None else grad.ctypes.data)
+    return loss, out, grad

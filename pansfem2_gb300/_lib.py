@@ -33,6 +33,8 @@ EXPORTS = [
     "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_simp_begin", "psf_simp_step",
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
+    "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
+    "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv",
 ]
 
 
@@ -89,6 +91,7 @@ def load(path=LIB_PATH):
         raise RuntimeError(f"CUDA library not built: {path} (run pansfem2_gb300/build.py)")
     lib = C.CDLL(path)
     vp, dp, ip, i64p = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int64)
+    fp = C.POINTER(C.c_float)
     lib.psf_last_error.restype = C.c_char_p
     sig = {
         "psf_create": [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
@@ -123,6 +126,15 @@ def load(path=LIB_PATH):
         "psf_list_filter": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, dp],
         # device pointers and a stream handle
         "psf_csr_solve_noalloc": [C.c_int, vp, vp, vp, vp, vp, C.c_int, C.c_double, vp, C.POINTER(SolveInfo)],
+        # learned preconditioner network
+        "psf_unet_create": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)],
+        "psf_unet_destroy": [vp],
+        "psf_unet_nparams": [vp],
+        "psf_unet_set_params": [vp, fp, C.c_int],
+        "psf_unet_get_params": [vp, fp, C.c_int],
+        "psf_unet_forward_host": [vp, C.c_int, fp, fp],
+        "psf_unet_loss_grad_host": [vp, C.c_int, fp, fp, fp, dp, fp, fp],
+        "psf_unet_conv": [C.c_int] * 8 + [fp, fp, fp, C.c_int, fp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
