@@ -295,11 +295,13 @@ def main():
     bpi = bytes_per_krylov_iteration(args.solver, ne, ndofs, 18 * nfree, nfree, args.nx, args.ny)
     peak, peak_kind = peaks()
     achieved = bpi * kit / ksec / 1e9 if ksec > 0 else None
+    # DRAM bytes per Krylov iteration from one ncu capture of the same kernel and workload
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and klaunch > 0:
         try:
-            traffic = json.load(open(tpath)).get(args.solver)
+            t_it = json.load(open(tpath))[args.solver]["dram_bytes_per_iteration"]
+            traffic = t_it * kit / klaunch
         except Exception:
             traffic = None
 
@@ -317,6 +319,8 @@ def main():
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                        "kernel": KERNEL_NAME.get(args.solver, args.solver), "bytes_per_iteration": bpi,
+                       "algorithmic_bytes_per_launch": bpi * kit / max(klaunch, 1),
+                       "traffic_unit": "DRAM bytes per launch (read + write)",
                        "peak_source": peak_kind}
     # launches of our kernels in the timed region: per step ~12 fixed kernels + Krylov launches + residual kernels
     out["gpu_launches"] = int(args.steps * 14 + klaunch + 3 * sum(i["solve"]["outer_iterations"] for i in infos))

@@ -252,6 +252,34 @@ psf_status psf_unet_loss_grad_host(psf_unet *net, int B, const float *in, const 
 psf_status psf_unet_conv(int mode, int N, int cin, int hin, int win, int hout, int wout, int B,
                          const float *x, const float *w, const float *bias, int relu, float *y);
 
+/* ---------------- learned preconditioner: training and use ---------------- */
+/* No counterpart in the reference.  PSF_SOLVE_IR_LEARNED_F32 runs flexible CG
+ * in FP64 whose preconditioner is nu_pre l1-Jacobi sweeps (FP32), a U-Net
+ * correction of the smoothed residual (bf16), and nu_post sweeps; the FP64 true
+ * residual decides convergence; after a stall (fallback_after iterations, 0:
+ * twice the previous converged solve) it falls back to FP64 Jacobi PCG and
+ * reports fell_back.  use_net = 0 keeps the same cycle without the network (the
+ * ablation).  The network's grid must be (nx+1) x (ny+1) nodes of a 2D problem
+ * and must outlive the context's use of it. */
+psf_status psf_learned_attach(psf_ctx *ctx, psf_unet *net, int nu_pre, int nu_post, int use_net,
+                              int fallback_after);
+
+/* Training pairs on the device, grid H x W nodes: input (density, D^-1/2 r1 / s),
+ * target D^1/2 K^-1 r1 / s, per-pair weighted mask. */
+typedef struct psf_trainset psf_trainset;
+psf_status psf_trainset_create(int H, int W, int capacity, psf_trainset **ts);
+psf_status psf_trainset_destroy(psf_trainset *ts);
+int psf_trainset_size(const psf_trainset *ts);
+/* npairs pairs from the context's current design: residuals of the multigrid
+ * FCG after iters[k % niters] iterations from zero (NULL: 0, 2, 4, 6), smoothed
+ * by the preconditioner's pre-sweeps, and their FP64 solutions (multigrid FCG
+ * to 1e-8).  The context's displacement is left unchanged. */
+psf_status psf_learned_harvest(psf_ctx *ctx, psf_trainset *ts, int npairs, const int *iters, int niters);
+/* steps of Adam (batch samples drawn with a seeded generator, warm-up then
+ * cosine decay from lr); loss_hist (may be NULL) receives the loss per step */
+psf_status psf_learned_train(psf_unet *net, psf_trainset *ts, int steps, int batch, float lr, uint64_t seed,
+                             double *loss_hist);
+
 #ifdef __cplusplus
 }
 #endif

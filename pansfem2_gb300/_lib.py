@@ -35,6 +35,8 @@ EXPORTS = [
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
     "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
     "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv",
+    "psf_learned_attach", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
+    "psf_learned_harvest", "psf_learned_train",
 ]
 
 
@@ -135,6 +137,12 @@ def load(path=LIB_PATH):
         "psf_unet_forward_host": [vp, C.c_int, fp, fp],
         "psf_unet_loss_grad_host": [vp, C.c_int, fp, fp, fp, dp, fp, fp],
         "psf_unet_conv": [C.c_int] * 8 + [fp, fp, fp, C.c_int, fp],
+        "psf_learned_attach": [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int],
+        "psf_trainset_create": [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
+        "psf_trainset_destroy": [vp],
+        "psf_trainset_size": [vp],
+        "psf_learned_harvest": [vp, vp, C.c_int, ip, C.c_int],
+        "psf_learned_train": [vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, dp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -15,6 +15,7 @@ static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
 const char *last_error() { return g_last_error.c_str(); }
 psf_status cuda_status(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return PSF_OK;
     g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
     return PSF_CUDA_ERROR;
 }

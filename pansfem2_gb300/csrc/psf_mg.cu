@@ -36,7 +36,6 @@ struct KeT64 {
     double v[576];
 };
 
-psf_status residual64_pub(Ctx *c, const double *b, const double *x, double *r, double *rnorm, double *bnorm);  // psf_solve.cu
 static inline psf_status residual64_check(Ctx *c, const double *b, const double *x, double *r, double *rn, double *bn) {
     return residual64_pub(c, b, x, r, rn, bn);
 }
@@ -933,6 +932,5 @@ psf_status mg_free(Ctx *c) {
     return PSF_OK;
 }
 
-psf_status learned_free(Ctx *c) { (void)c; return PSF_OK; }
 
 }  // namespace psf

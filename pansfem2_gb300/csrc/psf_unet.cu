@@ -187,6 +187,7 @@ template <int N>
 __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ ConvArgs a) {
     using S = ConvSmem<N>;
     extern __shared__ __align__(128) uint8_t smem[];
+    if (a.skip && *a.skip) return;
     const int tid = threadIdx.x, warp = tid >> 5;
     uint8_t *meta = smem + 2 * S::STAGE;
     const uint32_t sbase = s_addr(smem);
@@ -359,7 +360,8 @@ __global__ void pack_kernel(const float *__restrict__ W, int cout, int cin, int 
 // ------------------------------------------------------------------ elementwise pieces
 // bilinear vertex prolongation: fine channels [dc0, dc0 + C) of dst from the coarse tensor src (C channels)
 __global__ void upsample_kernel(const bf16 *__restrict__ src, int C, int hc, int wc, bf16 *__restrict__ dst, int dcs,
-                                int dc0, int hf, int wf, int batch) {
+                                int dc0, int hf, int wf, int batch, const int *skip) {
+    if (skip && *skip) return;
     const int groups = C / 8;
     const long long total = (long long)batch * hf * wf * groups;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
@@ -728,7 +730,7 @@ psf_status Net::forward(int B, const bf16 *input) {
             const int lc = lev[src], lf = lev[dst];
             const long long n = (long long)B * H[lf] * W[lf] * (C[src] / 8);
             upsample_kernel<<<gsz(n), 256, 0, stream>>>(tin[src], C[src], H[lc], W[lc], t[dst], C[dst],
-                                                        C[dst] - C[src], H[lf], W[lf], B);
+                                                        C[dst] - C[src], H[lf], W[lf], B, skip);
         }
         ConvArgs a{};
         a.x = tin[y.in];
@@ -746,6 +748,7 @@ psf_status Net::forward(int B, const bf16 *input) {
         a.relu = y.relu;
         a.mode = y.stride == 1 ? kFwdS1 : kFwdS2;
         a.err = err;
+        a.skip = skip;
         if (l == kLayers - 1) {
             a.y32 = out32;
             a.y_cs = 2;
@@ -890,7 +893,6 @@ psf_status Net::upload_input(int B, const float *host_in) {
 }  // namespace psf
 
 // ------------------------------------------------------------------ C ABI
-using psf::unet::Net;
 using psf::unet::bf16;
 using psf::unet::ConvArgs;
 using psf::unet::f32_to_bf16_kernel;
@@ -898,16 +900,13 @@ using psf::unet::gsz;
 using psf::unet::launch_conv;
 using psf::unet::pack_kernel;
 
-struct psf_unet {
-    Net net;
-};
-
 extern "C" {
 
 psf_status psf_unet_create(int c0, int H, int W, int batch, uint64_t seed, psf_unet **out) {
     if (!out) return PSF_BAD_INPUT;
     *out = nullptr;
     psf_unet *u = new psf_unet();
+    using psf::unet::Net;
     psf_status s = u->net.init(c0, H, W, batch, seed);
     if (s == PSF_OK) s = psf::cuda_status(cudaStreamSynchronize(u->net.stream), "network init");
     if (s != PSF_OK) {
@@ -947,7 +946,7 @@ psf_status psf_unet_get_params(const psf_unet *u, float *host, int n) {
 
 psf_status psf_unet_forward_host(psf_unet *u, int B, const float *in, float *out) {
     if (!u || !in || !out) return PSF_BAD_INPUT;
-    Net &n = u->net;
+    psf::unet::Net &n = u->net;
     if (B < 1 || B > n.cap) return PSF_BAD_INPUT;
     PSF_CHECK(n.upload_input(B, in));
     PSF_CHECK(n.forward(B, nullptr));
@@ -959,7 +958,7 @@ psf_status psf_unet_forward_host(psf_unet *u, int B, const float *in, float *out
 psf_status psf_unet_loss_grad_host(psf_unet *u, int B, const float *in, const float *tgt, const float *mask,
                                    double *loss, float *out, float *grad) {
     if (!u || !in || !tgt) return PSF_BAD_INPUT;
-    Net &n = u->net;
+    psf::unet::Net &n = u->net;
     if (B < 1 || B > n.cap) return PSF_BAD_INPUT;
     const size_t no = n.npix_b(B, 0) * 2;
     float *dt = nullptr, *dm = nullptr;

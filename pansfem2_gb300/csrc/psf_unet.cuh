@@ -42,6 +42,7 @@ struct ConvArgs {
     const float *bias;    // may be null
     int nchunks, relu, mode;
     int *err;
+    const int *skip;      // when non-null and *skip != 0 the launch does nothing
 };
 
 struct DwArgs {
@@ -73,6 +74,7 @@ struct Net {
     int *err = nullptr;
     long long step_count = 0;
     cudaStream_t stream = nullptr;
+    const int *skip = nullptr;   // forward() launches do nothing while *skip != 0 (graph replays after convergence)
     std::vector<void *> allocs;
 
     ~Net();
@@ -93,3 +95,7 @@ struct Net {
 
 }  // namespace unet
 }  // namespace psf
+
+struct psf_unet {
+    psf::unet::Net net;
+};
