@@ -238,6 +238,10 @@ psf_status psf_unet_destroy(psf_unet *net);
 int psf_unet_nparams(const psf_unet *net);
 psf_status psf_unet_set_params(psf_unet *net, const float *host, int n);
 psf_status psf_unet_get_params(const psf_unet *net, float *host, int n);
+/* the factor the preconditioner applies to the network output (the rms of the
+ * training targets, set by psf_learned_train); saved beside the parameters */
+psf_status psf_unet_get_out_scale(const psf_unet *net, float *scale);
+psf_status psf_unet_set_out_scale(psf_unet *net, float scale);
 /* forward of B host samples (B <= batch of psf_unet_create) */
 psf_status psf_unet_forward_host(psf_unet *net, int B, const float *in, float *out);
 /* forward, masked mean squared error against tgt, backward: loss, output and

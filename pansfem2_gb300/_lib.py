@@ -34,7 +34,8 @@ EXPORTS = [
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
     "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
-    "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv",
+    "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv", "psf_unet_get_out_scale",
+    "psf_unet_set_out_scale",
     "psf_learned_attach", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
     "psf_learned_harvest", "psf_learned_train",
 ]
@@ -137,6 +138,8 @@ def load(path=LIB_PATH):
         "psf_unet_forward_host": [vp, C.c_int, fp, fp],
         "psf_unet_loss_grad_host": [vp, C.c_int, fp, fp, fp, dp, fp, fp],
         "psf_unet_conv": [C.c_int] * 8 + [fp, fp, fp, C.c_int, fp],
+        "psf_unet_get_out_scale": [vp, fp],
+        "psf_unet_set_out_scale": [vp, C.c_float],
         "psf_learned_attach": [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int],
         "psf_trainset_create": [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
         "psf_trainset_destroy": [vp],

@@ -207,6 +207,19 @@ class Problem:
     def sync(self):
         check(self.L.psf_sync(self.h))
 
+    # ---------------------------------------------------------------- learned preconditioner
+    def attach_learned(self, net=None, nu_pre=2, nu_post=2, use_net=True, fallback_after=0):
+        """Preconditioner of the ir_learned_f32 solver: nu_pre / nu_post l1-Jacobi sweeps around
+        the U-Net correction (use_net=False: the same cycle without the network)."""
+        check(self.L.psf_learned_attach(self.h, None if net is None else net._h, int(nu_pre), int(nu_post),
+                                        int(bool(use_net) and net is not None), int(fallback_after)))
+
+    def harvest(self, trainset, npairs, iters=None):
+        """Adds npairs training pairs from the current design (see psf_learned_harvest)."""
+        it = None if iters is None else np.ascontiguousarray(iters, dtype=np.int32)
+        check(self.L.psf_learned_harvest(self.h, trainset._h, int(npairs), ptr(it, C.c_int),
+                                         0 if it is None else len(it)))
+
 
 def run_simp(pr, iters, solver="csr_jacobi_f64", **kw):
     """Runs `iters` SIMP iterations on the device; returns per-iteration infos and final fields."""

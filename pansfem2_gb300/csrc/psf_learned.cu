@@ -54,7 +54,7 @@ struct Learned {
     double *hsc = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int graph_key[4] = {-1, -1, -1, -1};
+    float graph_scale = 0.0f;
     std::vector<void *> allocs;
 };
 
@@ -184,10 +184,10 @@ __global__ void __launch_bounds__(kLpThreads) nn_prep_kernel(long long nnodes, l
 // x += D^-1/2 * s * out on the free dofs
 template <int KIND>
 __global__ void nn_apply_kernel(long long nnodes, const float *__restrict__ out, const float *__restrict__ isd,
-                                const double *sc, float *__restrict__ x, const int *flags) {
+                                const double *sc, float oscale, float *__restrict__ x, const int *flags) {
     if (lp_done(flags)) return;
     constexpr int nd = ndof_of<KIND>();
-    const float s = (float)sc[S_SCALE];
+    const float s = (float)sc[S_SCALE] * oscale;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
          n += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
@@ -511,7 +511,8 @@ static psf_status lp_iteration(Ctx *c, Learned *L, double *x, double *r, double 
         L->net->stream = st;
         L->net->skip = fl;
         PSF_CHECK(L->net->forward(1, L->nnin));
-        nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc, cur, fl);
+        nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc,
+                                                               L->net->out_scale, cur, fl);
     }
     for (int s = 1; s < L->nu_post; s++) {
         lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl);
@@ -567,6 +568,14 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
         PSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * c->ndofs, st));
     PSF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * c->ndofs, st));
     PSF_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * c->ndofs, st));
+    // the output scale is a kernel parameter of the captured graph: recapture when it changed
+    if (L->exec && L->net && L->graph_scale != L->net->out_scale) {
+        cudaGraphExecDestroy(L->exec);
+        cudaGraphDestroy(L->graph);
+        L->exec = nullptr;
+        L->graph = nullptr;
+    }
+    if (L->net) L->graph_scale = L->net->out_scale;
     PSF_CHECK(lp_build_graph<KIND>(c, L, x, r, z, p, q));
     // automatic stall limit: twice the iterations of the last converged learned solve (at least 100)
     int limit = L->fallback_after > 0 ? L->fallback_after : std::max(100, 2 * L->ref_iters);
@@ -673,6 +682,23 @@ __global__ void mask_scale_kernel(long long n, const double *part, float *__rest
         mask[i] *= w;
 }
 
+// rms of the targets over the masked entries (partials per block; folded by the host)
+__global__ void __launch_bounds__(kLpThreads) tgt_rms_kernel(long long n, const float *__restrict__ tgt,
+                                                             const float *__restrict__ mask, double *part) {
+    double v[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        if (mask[i] > 0.0f) {
+            v[0] += (double)tgt[i] * tgt[i];
+            v[1] += 1.0;
+        }
+    write_parts<2>(v, part);
+}
+
+__global__ void scale_copy_kernel(long long n, const float *__restrict__ a, float s, float *__restrict__ b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = a[i] * s;
+}
+
 __global__ void f32_to_f64_kernel(long long n, const float *__restrict__ a, double *__restrict__ b) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         b[i] = (double)a[i];
@@ -721,6 +747,8 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
 // ------------------------------------------------------------------ C ABI: training set, harvest, training
 struct psf_trainset {
     int H = 0, W = 0, cap = 0, n = 0;
+    double out_scale = 0.0;   // rms of the stored targets (0: not computed for the current pairs)
+    int scale_n = 0;          // pair count out_scale was computed over
     psf::unet::bf16 *in = nullptr;   // cap x H x W x 8
     float *tgt = nullptr;            // cap x H x W x 2
     float *mask = nullptr;           // cap x H x W x 2
@@ -833,6 +861,26 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
     mask = tgt + P * 2 * batch;
     PSF_CUDA(cudaMalloc(&dl, sizeof(double) * (size_t)steps));
     cudaStream_t st = net.stream;
+    // global target scale: the network learns targets of unit rms, the preconditioner scales back
+    if (ts->scale_n != ts->n || !(ts->out_scale > 0.0)) {
+        double *part = nullptr;
+        PSF_CUDA(cudaMalloc(&part, sizeof(double) * 2 * psf::kLpBlocks));
+        psf::tgt_rms_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>((long long)ts->n * P * 2, ts->tgt, ts->mask,
+                                                                        part);
+        std::vector<double> h(2 * psf::kLpBlocks);
+        cudaError_t e = cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(part);
+        if (e != cudaSuccess) return psf::cuda_status(e, "target scale");
+        double a = 0.0, m = 0.0;
+        for (int b = 0; b < psf::kLpBlocks; b++) {
+            a += h[2 * b];
+            m += h[2 * b + 1];
+        }
+        ts->out_scale = (m > 0.0 && a > 0.0) ? sqrt(a / m) : 1.0;
+        ts->scale_n = ts->n;
+    }
+    net.out_scale = (float)ts->out_scale;
     uint64_t rs = seed ? seed : 1;
     auto rnd = [&rs]() {
         rs ^= rs << 13;
@@ -847,9 +895,11 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
             const size_t i = (size_t)(rnd() % (uint64_t)ts->n);
             s = psf::cuda_status(cudaMemcpyAsync(net.t[0] + b * P * 8, ts->in + i * P * 8, sizeof(psf::unet::bf16) * P * 8,
                                                  cudaMemcpyDeviceToDevice, st), "copy");
-            if (s == PSF_OK)
-                s = psf::cuda_status(cudaMemcpyAsync(tgt + b * P * 2, ts->tgt + i * P * 2, sizeof(float) * P * 2,
-                                                     cudaMemcpyDeviceToDevice, st), "copy");
+            if (s == PSF_OK) {
+                psf::scale_copy_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (long long)P * 2, ts->tgt + i * P * 2, (float)(1.0 / ts->out_scale), tgt + b * P * 2);
+                s = psf::cuda_status(cudaGetLastError(), "scale_copy_kernel");
+            }
             if (s == PSF_OK)
                 s = psf::cuda_status(cudaMemcpyAsync(mask + b * P * 2, ts->mask + i * P * 2, sizeof(float) * P * 2,
                                                      cudaMemcpyDeviceToDevice, st), "copy");

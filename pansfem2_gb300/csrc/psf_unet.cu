@@ -317,6 +317,27 @@ static cudaError_t launch_conv_n(const ConvArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// the dynamic shared-memory opt-in of every instantiation (called before any stream capture)
+cudaError_t conv_init_attrs() {
+    const int Ns[7] = {16, 32, 48, 64, 96, 128, 192};
+    for (int N : Ns) {
+        ConvArgs a{};
+        a.batch = 0;   // empty launch: only sets the attribute
+        cudaError_t e = cudaSuccess;
+        switch (N) {
+            case 16: e = launch_conv_n<16>(a, 0); break;
+            case 32: e = launch_conv_n<32>(a, 0); break;
+            case 48: e = launch_conv_n<48>(a, 0); break;
+            case 64: e = launch_conv_n<64>(a, 0); break;
+            case 96: e = launch_conv_n<96>(a, 0); break;
+            case 128: e = launch_conv_n<128>(a, 0); break;
+            default: e = launch_conv_n<192>(a, 0); break;
+        }
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_conv(int N, const ConvArgs &a, cudaStream_t st) {
     switch (N) {
         case 16: return launch_conv_n<16>(a, st);
@@ -631,6 +652,7 @@ psf_status Net::init(int c0_, int H_, int W_, int batch_, uint64_t seed) {
         set_error("network grid must be (8k+1) x (8m+1) nodes, at least 9 x 9, with batch >= 1");
         return PSF_BAD_INPUT;
     }
+    PSF_CUDA(conv_init_attrs());
     c0 = c0_;
     H[0] = H_;
     W[0] = W_;
@@ -941,6 +963,18 @@ psf_status psf_unet_get_params(const psf_unet *u, float *host, int n) {
         return PSF_BAD_INPUT;
     }
     PSF_CUDA(cudaMemcpy(host, u->net.params, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    return PSF_OK;
+}
+
+psf_status psf_unet_get_out_scale(const psf_unet *u, float *scale) {
+    if (!u || !scale) return PSF_BAD_INPUT;
+    *scale = u->net.out_scale;
+    return PSF_OK;
+}
+
+psf_status psf_unet_set_out_scale(psf_unet *u, float scale) {
+    if (!u || !(scale > 0.0f)) return PSF_BAD_INPUT;
+    u->net.out_scale = scale;
     return PSF_OK;
 }
 

@@ -73,6 +73,7 @@ struct Net {
     double *dloss = nullptr;
     int *err = nullptr;
     long long step_count = 0;
+    float out_scale = 1.0f;      // the preconditioner multiplies the output by this (set by training)
     cudaStream_t stream = nullptr;
     const int *skip = nullptr;   // forward() launches do nothing while *skip != 0 (graph replays after convergence)
     std::vector<void *> allocs;

@@ -49,6 +49,26 @@ class UNet:
         p = self._f32(p)
         L.check(L.load().psf_unet_set_params(self._h, L.ptr(p, C.c_float), p.size))
 
+    @property
+    def out_scale(self):
+        v = C.c_float()
+        L.check(L.load().psf_unet_get_out_scale(self._h, C.byref(v)))
+        return v.value
+
+    @out_scale.setter
+    def out_scale(self, v):
+        L.check(L.load().psf_unet_set_out_scale(self._h, float(v)))
+
+    def save(self, path):
+        """Parameters and output scale to an .npz file."""
+        np.savez(path, params=self.get_params(), out_scale=np.float32(self.out_scale), H=self.H, W=self.W,
+                 c0=self.c0)
+
+    def load(self, path):
+        d = np.load(path)
+        self.set_params(d["params"])
+        self.out_scale = float(d["out_scale"])
+
     def forward(self, inp):
         inp = self._f32(inp)
         B = inp.shape[0]
@@ -127,3 +147,35 @@ def conv_reference(mode, x, w, bias=None, relu=False, out_hw=None):
     if relu:
         y = np.maximum(y, 0.0)
     return y
+
+
+class TrainSet:
+    """Training pairs resident on the GPU (psf_trainset_*), grid H x W nodes."""
+
+    def __init__(self, H, W, capacity):
+        lib = L.load()
+        h = C.c_void_p()
+        L.check(lib.psf_trainset_create(H, W, capacity, C.byref(h)))
+        self._h, self.H, self.W, self.capacity = h, H, W, capacity
+
+    def __len__(self):
+        return int(L.load().psf_trainset_size(self._h))
+
+    def close(self):
+        if self._h:
+            L.load().psf_trainset_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def train(net, trainset, steps, batch=8, lr=1e-3, seed=1):
+    """Adam on the GPU (psf_learned_train); returns the loss per step."""
+    hist = np.zeros(steps)
+    L.check(L.load().psf_learned_train(net._h, trainset._h, int(steps), int(batch), float(lr), int(seed),
+                                       L.ptr(hist)))
+    return hist
