@@ -258,15 +258,19 @@ psf_status psf_unet_conv(int mode, int N, int cin, int hin, int win, int hout, i
 
 /* ---------------- learned preconditioner: training and use ---------------- */
 /* No counterpart in the reference.  PSF_SOLVE_IR_LEARNED_F32 runs flexible CG
- * in FP64 whose preconditioner is nu_pre l1-Jacobi sweeps (FP32), a U-Net
- * correction of the smoothed residual (bf16), and nu_post sweeps; the FP64 true
+ * in FP64 whose preconditioner is a pre-stage in FP32 (pre_mg = 1: one
+ * multigrid V-cycle; 0: nu_pre l1-Jacobi sweeps), a U-Net correction of the
+ * remaining residual (bf16), and nu_post l1-Jacobi sweeps; the FP64 true
  * residual decides convergence; after a stall (fallback_after iterations, 0:
- * twice the previous converged solve) it falls back to FP64 Jacobi PCG and
- * reports fell_back.  use_net = 0 keeps the same cycle without the network (the
- * ablation).  The network's grid must be (nx+1) x (ny+1) nodes of a 2D problem
- * and must outlive the context's use of it. */
-psf_status psf_learned_attach(psf_ctx *ctx, psf_unet *net, int nu_pre, int nu_post, int use_net,
+ * twice the previous converged solve, < 0: never) it falls back to FP64 Jacobi
+ * PCG and reports fell_back.  use_net = 0 keeps the same cycle without the
+ * network (the ablation).  The network's grid must be (nx+1) x (ny+1) nodes of a
+ * 2D problem and must outlive the context's use of it. */
+psf_status psf_learned_attach(psf_ctx *ctx, psf_unet *net, int pre_mg, int nu_pre, int nu_post, int use_net,
                               int fallback_after);
+/* one application z = M(r) of the attached preconditioner to a host vector of
+ * free dofs (diagnostics and tests; fallback_after < 0 disables the fallback) */
+psf_status psf_learned_apply(psf_ctx *ctx, const double *r, double *z);
 
 /* Training pairs on the device, grid H x W nodes: input (density, D^-1/2 r1 / s),
  * target D^1/2 K^-1 r1 / s, per-pair weighted mask. */
@@ -276,13 +280,28 @@ psf_status psf_trainset_destroy(psf_trainset *ts);
 int psf_trainset_size(const psf_trainset *ts);
 /* npairs pairs from the context's current design: residuals of the multigrid
  * FCG after iters[k % niters] iterations from zero (NULL: 0, 2, 4, 6), smoothed
- * by the preconditioner's pre-sweeps, and their FP64 solutions (multigrid FCG
+ * by the attached preconditioner's pre-stage (default: one V-cycle), and the
+ * FP64 solutions of what remains (multigrid FCG
  * to 1e-8).  The context's displacement is left unchanged. */
 psf_status psf_learned_harvest(psf_ctx *ctx, psf_trainset *ts, int npairs, const int *iters, int niters);
 /* steps of Adam (batch samples drawn with a seeded generator, warm-up then
- * cosine decay from lr); loss_hist (may be NULL) receives the loss per step */
+ * cosine decay from lr).  loss_mode 0: mean squared error of the target
+ * D^1/2 K^-1 r1 / s; 1: energy norm of the correction's error,
+ * (y - t) . K^ (y - t) / t . K^ t with K^ = D^-1/2 K D^-1/2 (the norm flexible
+ * CG minimises).  loss_hist (may be NULL) receives per step the loss relative
+ * to that of a zero output (1 = nothing learned) */
 psf_status psf_learned_train(psf_unet *net, psf_trainset *ts, int steps, int batch, float lr, uint64_t seed,
-                             double *loss_hist);
+                             int loss_mode, double *loss_hist);
+
+/* ---------------- VTK output ---------------- */
+/* Replaces the per-iteration dump of sample_optimize_density_oc.cpp:173-181
+ * (ExportToVTK.h:19-141): writes the current iteration (points, cells, cell
+ * types, point vectors "u" and "r" = K u over all dofs, cell scalars "s" = the
+ * filtered density) as a legacy ASCII VTK file with the reference writer's
+ * formatting.  async = 1 returns after queueing the device->host copy; a host
+ * thread writes the file (psf_export_wait, or the next export, joins it). */
+psf_status psf_export_vtk(psf_ctx *ctx, const char *path, int async);
+psf_status psf_export_wait(psf_ctx *ctx);
 
 #ifdef __cplusplus
 }

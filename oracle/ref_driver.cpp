@@ -10,8 +10,8 @@
 // sample/optimize/sample_optimize_density_oc.cpp:93-207 (OC) and
 // sample/optimize/sample_optimize_density_mma.cpp:98-203 (MMA), with the
 // configuration's parameters in place of the sample's literals, the linear
-// DensityFilter (or the sample's HeavisideFilter with heaviside=1) and no VTK
-// output.  Usage:  ref_driver <mode> out=<file> key=value ...
+// DensityFilter (or the sample's HeavisideFilter with heaviside=1); with
+// vtk=<file> iteration 0 is also written by the reference's VTK writer.  Usage:  ref_driver <mode> out=<file> key=value ...
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -39,6 +39,7 @@
 #include "src/FEM/Controller/Assembling.h"
 #include "src/LinearAlgebra/Solvers/CG.h"
 #include "src/Optimize/Solver/OC.h"
+#include "src/PrePost/Export/ExportToVTK.h"
 #include "src/Optimize/Solver/MMA.h"
 #include "src/Optimize/Filter/DensityFilter.h"
 #include "src/Optimize/Filter/HeavisideFilter.h"
@@ -279,6 +280,18 @@ static int run_simp() {
         dfds_hist.insert(dfds_hist.end(), dfds.begin(), dfds.end());
         for (auto& ui : u) for (int d = 0; d < ndof; d++) u_hist.push_back(ui(d));
         if (k == 0) for (auto& ri : r) for (int d = 0; d < ndof; d++) r_hist.push_back(ri(d));
+        // vtk=<path>: iteration 0 written by the reference's own writer in the sample's order
+        if (k == 0 && !args("vtk", "").empty()) {
+            std::ofstream fout(args("vtk", ""));
+            MakeHeadderToVTK(fout);
+            AddPointsToVTK(x, fout);
+            AddElementToVTK(elements, fout);
+            AddElementTypes(std::vector<int>(elements.size(), kind == 2 ? 12 : 9), fout);
+            AddPointVectors(u, "u", fout, true);
+            AddPointVectors(r, "r", fout, false);
+            AddElementScalers(rho, "s", fout, true);
+            fout.close();
+        }
 
         if (optimizer == 1) {
             mma.UpdateVariables(s, f, dfds, {g}, {dgds});

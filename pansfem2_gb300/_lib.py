@@ -36,8 +36,8 @@ EXPORTS = [
     "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
     "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv", "psf_unet_get_out_scale",
     "psf_unet_set_out_scale",
-    "psf_learned_attach", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
-    "psf_learned_harvest", "psf_learned_train",
+    "psf_learned_attach", "psf_learned_apply", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
+    "psf_learned_harvest", "psf_learned_train", "psf_export_vtk", "psf_export_wait",
 ]
 
 
@@ -140,12 +140,15 @@ def load(path=LIB_PATH):
         "psf_unet_conv": [C.c_int] * 8 + [fp, fp, fp, C.c_int, fp],
         "psf_unet_get_out_scale": [vp, fp],
         "psf_unet_set_out_scale": [vp, C.c_float],
-        "psf_learned_attach": [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int],
+        "psf_learned_attach": [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int],
+        "psf_learned_apply": [vp, dp, dp],
         "psf_trainset_create": [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
         "psf_trainset_destroy": [vp],
         "psf_trainset_size": [vp],
         "psf_learned_harvest": [vp, vp, C.c_int, ip, C.c_int],
-        "psf_learned_train": [vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, dp],
+        "psf_learned_train": [vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_int, dp],
+        "psf_export_vtk": [vp, C.c_char_p, C.c_int],
+        "psf_export_wait": [vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -207,12 +207,28 @@ class Problem:
     def sync(self):
         check(self.L.psf_sync(self.h))
 
+    def export_vtk(self, path, async_=False):
+        """Legacy VTK file of the current iteration (u, r, s), as the samples write it."""
+        check(self.L.psf_export_vtk(self.h, str(path).encode(), int(bool(async_))))
+
+    def export_wait(self):
+        check(self.L.psf_export_wait(self.h))
+
     # ---------------------------------------------------------------- learned preconditioner
-    def attach_learned(self, net=None, nu_pre=2, nu_post=2, use_net=True, fallback_after=0):
-        """Preconditioner of the ir_learned_f32 solver: nu_pre / nu_post l1-Jacobi sweeps around
-        the U-Net correction (use_net=False: the same cycle without the network)."""
-        check(self.L.psf_learned_attach(self.h, None if net is None else net._h, int(nu_pre), int(nu_post),
-                                        int(bool(use_net) and net is not None), int(fallback_after)))
+    def attach_learned(self, net=None, pre_mg=True, nu_pre=2, nu_post=1, use_net=True, fallback_after=0):
+        """Preconditioner of the ir_learned_f32 solver: a pre-stage (one multigrid V-cycle, or
+        nu_pre l1-Jacobi sweeps), the U-Net correction of the remaining residual, nu_post
+        sweeps (use_net=False: the same cycle without the network)."""
+        check(self.L.psf_learned_attach(self.h, None if net is None else net._h, int(bool(pre_mg)), int(nu_pre),
+                                        int(nu_post), int(bool(use_net) and net is not None),
+                                        int(fallback_after)))
+
+    def learned_apply(self, r):
+        """z = M(r) of the attached learned preconditioner (free-dof vectors)."""
+        r = f64(r)
+        z = np.zeros(self.nfree)
+        check(self.L.psf_learned_apply(self.h, ptr(r), ptr(z)))
+        return z
 
     def harvest(self, trainset, npairs, iters=None):
         """Adds npairs training pairs from the current design (see psf_learned_harvest)."""

@@ -112,6 +112,7 @@ psf_status psf_destroy(psf_ctx *h) {
     if (!h) return PSF_OK;
     Ctx *c = &h->c;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    vtk_free(c);
     mg_free(c);
     learned_free(c);
     for (void *p : c->allocs) cudaFree(p);

@@ -110,6 +110,8 @@ struct Ctx {
     void *mg = nullptr;
     // learned preconditioner
     void *learned = nullptr;
+    // VTK export (pinned buffers, writer thread)
+    void *vtk = nullptr;
 
     std::vector<void *> allocs;
 };
@@ -167,6 +169,7 @@ psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g,
 psf_status moduli_from_rho(Ctx *c, const double *rho, double E1, double E0, double p, double *E_dev);
 psf_status mg_free(Ctx *c);
 psf_status learned_free(Ctx *c);                                                       // psf_learned.cu
+void vtk_free(Ctx *c);                                                                 // psf_vtk.cu
 psf_status learned_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_learned.cu
 psf_status residual64_pub(Ctx *c, const double *b, const double *x, double *r, double *rnorm, double *bnorm);  // psf_solve.cu
 

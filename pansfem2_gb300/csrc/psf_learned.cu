@@ -29,6 +29,22 @@
 #include "psf_internal.cuh"
 #include "psf_unet.cuh"
 
+// training pairs on the device (one slot per pair)
+struct psf_trainset {
+    int H = 0, W = 0, cap = 0, n = 0;
+    double out_scale = 0.0;   // rms of the stored targets (0: not computed for the current pairs)
+    int scale_n = 0;          // pair count out_scale was computed over
+    int kind = -1, nd = 0;    // problem kind of the harvested pairs (Q4 only)
+    float Ke[64];             // element matrix (E = 1) of the grid, for the energy loss
+    psf::unet::bf16 *in = nullptr;   // cap x H x W x 8: network input (density, rhat, zeros)
+    float *tgt = nullptr;            // cap x H x W x 2: D^1/2 K^-1 r1 / s
+    float *mask = nullptr;           // cap x H x W x 2: free dofs, weighted 1 / mean(tgt^2) per pair
+    float *rhat = nullptr;           // cap x H x W x 2: D^-1/2 r1 / s in fp32
+    float *isd = nullptr;            // cap x H x W x 2: D^-1/2 (0 on fixed dofs)
+    float *epad = nullptr;           // cap x (H+1)(W+1): zero-padded element moduli
+    double *cden = nullptr;          // cap: tgt . rhat, the energy of the exact correction
+};
+
 namespace psf {
 
 using unet::bf16;
@@ -44,6 +60,7 @@ enum { F_DONE = 0, F_ITERS, F_NONFINITE, F_LIMIT, F_ITMAX, F_N = 8 };
 
 struct Learned {
     unet::Net *net = nullptr;
+    int pre_mg = 0;   // pre-stage: 0 = nu_pre l1-Jacobi sweeps, 1 = one multigrid V-cycle
     int nu_pre = 2, nu_post = 2, use_net = 1;
     int fallback_after = 0;
     int ref_iters = 0;   // iterations of the last converged learned solve (the stall reference)
@@ -428,7 +445,8 @@ static KeT<T> lp_ke(const Ctx *c) {
     return k;
 }
 
-psf_status learned_attach(Ctx *c, unet::Net *net, int nu_pre, int nu_post, int use_net, int fallback_after) {
+psf_status learned_attach(Ctx *c, unet::Net *net, int pre_mg, int nu_pre, int nu_post, int use_net,
+                          int fallback_after) {
     if (c->kind == PSF_H8_SOLID) {
         set_error("learned preconditioner: 2D grids only (Q4 plane strain, Q4 heat)");
         return PSF_BAD_INPUT;
@@ -439,6 +457,10 @@ psf_status learned_attach(Ctx *c, unet::Net *net, int nu_pre, int nu_post, int u
     }
     if (nu_pre < 1 || nu_pre > 8 || nu_post < 0 || nu_post > 8) {
         set_error("learned preconditioner: 1 <= nu_pre <= 8, 0 <= nu_post <= 8");
+        return PSF_BAD_INPUT;
+    }
+    if (pre_mg && c->kind == PSF_H8_SOLID) {
+        set_error("learned preconditioner: 2D grids only");
         return PSF_BAD_INPUT;
     }
     if (!c->learned) {
@@ -464,13 +486,15 @@ psf_status learned_attach(Ctx *c, unet::Net *net, int nu_pre, int nu_post, int u
         }
     }
     Learned *L = (Learned *)c->learned;
-    if (L->net != net || L->nu_pre != nu_pre || L->nu_post != nu_post || L->use_net != use_net) {
+    if (L->net != net || L->nu_pre != nu_pre || L->nu_post != nu_post || L->use_net != use_net ||
+        L->pre_mg != pre_mg) {
         if (L->exec) cudaGraphExecDestroy(L->exec);
         if (L->graph) cudaGraphDestroy(L->graph);
         L->exec = nullptr;
         L->graph = nullptr;
     }
     L->net = net;
+    L->pre_mg = pre_mg ? 1 : 0;
     L->nu_pre = nu_pre;
     L->nu_post = nu_post;
     L->use_net = use_net;
@@ -488,21 +512,36 @@ static psf_status lp_refresh(Ctx *c, Learned *L) {
     return PSF_OK;
 }
 
-// preconditioner z = M(r) followed by the FCG step; recorded into the capture stream
+psf_status mg_prepare(Ctx *c);                                                        // psf_mg.cu
+psf_status mg_apply(Ctx *c, const double *r, float *r32, float *xo, const int *flags);  // psf_mg.cu
+
+// pre-stage of M: r32 = r and x (returned in *cur; *oth is the other buffer)
 template <int KIND>
-static psf_status lp_iteration(Ctx *c, Learned *L, double *x, double *r, double *z, double *p, double *q) {
+static psf_status lp_pre(Ctx *c, Learned *L, const double *r, const int *fl, float **cur, float **oth) {
+    cudaStream_t st = c->stream;
+    *cur = L->xa;
+    *oth = L->xb;
+    if (L->pre_mg) return mg_apply(c, r, L->r32, L->xa, fl);
+    const Geo g = lp_geo(c);
+    const KeT<float> Kf = lp_ke<float>(c);
+    lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, r, c->Dl1f, c->fixed, L->r32, L->xa, fl);
+    for (int k = 1; k < L->nu_pre; k++) {
+        lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, *cur,
+                                                               *oth, fl);
+        std::swap(*cur, *oth);
+    }
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
+// z = M(r) and the partial sums of z . qprev
+template <int KIND>
+static psf_status lp_precond(Ctx *c, Learned *L, const double *r, double *z, const double *qprev, const int *fl) {
     cudaStream_t st = c->stream;
     const Geo g = lp_geo(c);
     const KeT<float> Kf = lp_ke<float>(c);
-    const KeT<double> Kd = lp_ke<double>(c);
-    const long long nd = c->ndofs;
-    const int *fl = L->flags;
-    lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, r, c->Dl1f, c->fixed, L->r32, L->xa, fl);
-    float *cur = L->xa, *oth = L->xb;
-    for (int s = 1; s < L->nu_pre; s++) {
-        lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl);
-        std::swap(cur, oth);
-    }
+    float *cur, *oth;
+    PSF_CHECK(lp_pre<KIND>(c, L, r, fl, &cur, &oth));
     if (L->use_net) {
         lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
                                                                L->part, fl);
@@ -514,12 +553,25 @@ static psf_status lp_iteration(Ctx *c, Learned *L, double *x, double *r, double 
         nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc,
                                                                L->net->out_scale, cur, fl);
     }
-    for (int s = 1; s < L->nu_post; s++) {
+    for (int k = 1; k < L->nu_post; k++) {
         lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl);
         std::swap(cur, oth);
     }
     lp_last_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur,
-                                                          L->nu_post > 0 ? 1 : 0, z, q, L->part, fl);
+                                                          L->nu_post > 0 ? 1 : 0, z, qprev, L->part, fl);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
+// preconditioner z = M(r) followed by the FCG step; recorded into the capture stream
+template <int KIND>
+static psf_status lp_iteration(Ctx *c, Learned *L, double *x, double *r, double *z, double *p, double *q) {
+    cudaStream_t st = c->stream;
+    const Geo g = lp_geo(c);
+    const KeT<double> Kd = lp_ke<double>(c);
+    const long long nd = c->ndofs;
+    const int *fl = L->flags;
+    PSF_CHECK(lp_precond<KIND>(c, L, r, z, q, fl));
     fcg_dir_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, z, p, L->sc, fl);
     fcg_op_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, p, q, r, L->part, fl);
     // the step writes |r|^2 partials into the upper half so that the (p.q, r.p) partials stay readable
@@ -562,6 +614,7 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     const Geo g = lp_geo(c);
     const KeT<double> Kd = lp_ke<double>(c);
     PSF_CHECK(lp_refresh(c, L));
+    if (L->pre_mg) PSF_CHECK(mg_prepare(c));
     if (warm)
         PSF_CUDA(cudaMemcpyAsync(x, c->un, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, st));
     else
@@ -579,8 +632,10 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     PSF_CHECK(lp_build_graph<KIND>(c, L, x, r, z, p, q));
     // automatic stall limit: twice the iterations of the last converged learned solve (at least 100)
     int limit = L->fallback_after > 0 ? L->fallback_after : std::max(100, 2 * L->ref_iters);
-    if (L->ref_iters == 0 && L->fallback_after <= 0) limit = std::max(limit, 400);
+    if (L->ref_iters == 0 && L->fallback_after == 0) limit = std::max(limit, 400);
+    if (L->fallback_after < 0) limit = itmax;
     limit = std::min(limit, itmax);
+    const bool allow_fallback = L->fallback_after >= 0;
     int total = 0, passes = 0;
     bool ok = false, stalled = false;
     double rn = 0.0, bn = 0.0;
@@ -619,7 +674,7 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     c->ksec += ms * 1e-3;
     c->klaunch += passes * (int)((total + kGraphIters - 1) / kGraphIters);
     int fb_iters = 0;
-    if (!ok && (stalled || total >= limit)) {
+    if (!ok && allow_fallback && (stalled || total >= limit)) {
         // fallback: FP64 Jacobi PCG from the current iterate (zero start if the iterate is not finite)
         if (L->hflags[F_NONFINITE]) PSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * c->ndofs, st));
         bool conv = false;
@@ -706,22 +761,108 @@ __global__ void f32_to_f64_kernel(long long n, const float *__restrict__ a, doub
 
 psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_mg.cu
 
+// energy-loss data of a pair: rhat = D^-1/2 r1 / s, isd in [P][2] layout, partial sums of tgt . rhat
+__global__ void __launch_bounds__(kLpThreads) pair_extra_kernel(long long nnodes, int nd, const float *__restrict__ r1,
+                                                                const float *__restrict__ isd, const double *sc,
+                                                                const float *__restrict__ tgt,
+                                                                float *__restrict__ rhat, float *__restrict__ isd2,
+                                                                double *part) {
+    const double is = 1.0 / sc[S_SCALE];
+    double v[1] = {0.0};
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
+         n += (long long)gridDim.x * blockDim.x)
+        for (int a = 0; a < 2; a++) {
+            float rh = 0.0f, id = 0.0f;
+            if (a < nd) {
+                id = isd[n * nd + a];
+                rh = (float)(id * r1[n * nd + a] * is);
+            }
+            rhat[n * 2 + a] = rh;
+            isd2[n * 2 + a] = id;
+            v[0] += (double)tgt[n * 2 + a] * rh;
+        }
+    write_parts<1>(v, part);
+}
+
+// energy loss of a batch (the norm flexible CG minimises): per sample
+//   L_b = 1 + (y . K^ y - 2 y . rhat) / c_b,   y = oscale * out,  K^ = D^-1/2 K D^-1/2,
+// which is the K-norm error of the correction relative to that of the exact one
+// (c_b = t . rhat = t . K^ t); gradient d(mean_b L_b)/d out = 2 oscale (K^ y - rhat) / (c_b B).
+template <int KIND>
+__global__ void __launch_bounds__(kLpThreads) energy_kernel(int nx, int ny, KeT<float> Ke, int B,
+                                                            const float *__restrict__ out,
+                                                            const float *__restrict__ rhat,
+                                                            const float *__restrict__ isd,
+                                                            const float *__restrict__ epad,
+                                                            const double *__restrict__ cden, float oscale,
+                                                            float *__restrict__ gout, double *part) {
+    constexpr int nd = ndof_of<KIND>();
+    const long long P = (long long)(nx + 1) * (ny + 1), Pe = (long long)(nx + 2) * (ny + 2);
+    Geo g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = 0;
+    g.nnodes = P;
+    double v[1] = {0.0};
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < (long long)B * P;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(idx / P);
+        const long long n = idx - (long long)b * P;
+        const float *yb = out + (size_t)b * P * 2, *ib = isd + (size_t)b * P * 2, *rb = rhat + (size_t)b * P * 2;
+        int i, j, k;
+        node_ijk<KIND>(g, n, i, j, k);
+        float kv[nd];
+        ebe_node<float, KIND>(g, Ke, epad + (size_t)b * Pe, i, j, k,
+                              [&](long long a) {
+                                  const long long m = a / nd;
+                                  const int d = (int)(a - m * nd);
+                                  return ib[m * 2 + d] * oscale * yb[m * 2 + d];
+                              },
+                              kv);
+        const double ic = 1.0 / cden[b];
+#pragma unroll
+        for (int a = 0; a < 2; a++) {
+            float gr = 0.0f;
+            if (a < nd && ib[n * 2 + a] > 0.0f) {
+                const float yh = oscale * yb[n * 2 + a];
+                const float kh = ib[n * 2 + a] * kv[a < nd ? a : 0];
+                const float rh = rb[n * 2 + a];
+                gr = (float)(2.0 * ((double)kh - rh) * ic * oscale / B);
+                v[0] += ((double)yh * kh - 2.0 * (double)yh * rh) * ic;
+            }
+            gout[(size_t)b * P * 2 + n * 2 + a] = gr;
+        }
+    }
+    write_parts<1>(v, part);
+}
+
+__global__ void energy_loss_kernel(const double *part, int B, double *out) {
+    double v[1];
+    fold_parts<1>(part, v);
+    if (threadIdx.x == 0) *out = 1.0 + v[0] / B;
+}
+
+__global__ void fold_to_kernel(const double *part, double *out) {
+    double v[1];
+    fold_parts<1>(part, v);
+    if (threadIdx.x == 0) *out = v[0];
+}
+
 // one training pair from residual r (FP64 nodal): input (density, scaled r1), target D^1/2 K^-1 r1 / s
 template <int KIND>
-static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs64, double *e64, bf16 *in_out,
-                               float *tgt_out, float *mask_out) {
+static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs64, double *e64, psf_trainset *ts,
+                               size_t slot) {
+    const size_t P = (size_t)ts->H * ts->W, Pe = (size_t)(ts->H + 1) * (ts->W + 1);
+    bf16 *in_out = ts->in + slot * P * 8;
+    float *tgt_out = ts->tgt + slot * P * 2, *mask_out = ts->mask + slot * P * 2;
     cudaStream_t st = c->stream;
     const Geo g = lp_geo(c);
     const KeT<float> Kf = lp_ke<float>(c);
     const long long nd = c->ndofs;
     PSF_CUDA(cudaMemsetAsync(L->flags, 0, sizeof(int) * F_N, st));
-    lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, r, c->Dl1f, c->fixed, L->r32, L->xa, L->flags);
-    float *cur = L->xa, *oth = L->xb;
-    for (int s = 1; s < L->nu_pre; s++) {
-        lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth,
-                                                               L->flags);
-        std::swap(cur, oth);
-    }
+    float *cur, *oth;
+    if (L->pre_mg) PSF_CHECK(mg_prepare(c));
+    PSF_CHECK(lp_pre<KIND>(c, L, r, L->flags, &cur, &oth));
     lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
                                                            L->part, L->flags);
     nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho, in_out,
@@ -738,6 +879,10 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     PSF_CUDA(cudaMemcpyAsync(e64, c->un, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st));
     tgt_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, e64, L->isd, L->sc, tgt_out, mask_out, L->part);
     mask_scale_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes * 2, L->part, mask_out);
+    pair_extra_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, L->r1, L->isd, L->sc, tgt_out,
+                                                        ts->rhat + slot * P * 2, ts->isd + slot * P * 2, L->part);
+    fold_to_kernel<<<1, 32, 0, st>>>(L->part, ts->cden + slot);
+    PSF_CUDA(cudaMemcpyAsync(ts->epad + slot * Pe, c->Epadf, sizeof(float) * Pe, cudaMemcpyDeviceToDevice, st));
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -745,16 +890,10 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
 }  // namespace psf
 
 // ------------------------------------------------------------------ C ABI: training set, harvest, training
-struct psf_trainset {
-    int H = 0, W = 0, cap = 0, n = 0;
-    double out_scale = 0.0;   // rms of the stored targets (0: not computed for the current pairs)
-    int scale_n = 0;          // pair count out_scale was computed over
-    psf::unet::bf16 *in = nullptr;   // cap x H x W x 8
-    float *tgt = nullptr;            // cap x H x W x 2
-    float *mask = nullptr;           // cap x H x W x 2
-};
 
 extern "C" {
+
+psf_status psf_trainset_destroy(psf_trainset *t);
 
 psf_status psf_trainset_create(int H, int W, int capacity, psf_trainset **out) {
     if (!out || H < 9 || W < 9 || capacity < 1) return PSF_BAD_INPUT;
@@ -764,14 +903,16 @@ psf_status psf_trainset_create(int H, int W, int capacity, psf_trainset **out) {
     t->W = W;
     t->cap = capacity;
     const size_t P = (size_t)H * W;
+    const size_t Pe = (size_t)(H + 1) * (W + 1);
     cudaError_t e = cudaMalloc(&t->in, sizeof(psf::unet::bf16) * P * 8 * capacity);
     if (e == cudaSuccess) e = cudaMalloc(&t->tgt, sizeof(float) * P * 2 * capacity);
     if (e == cudaSuccess) e = cudaMalloc(&t->mask, sizeof(float) * P * 2 * capacity);
+    if (e == cudaSuccess) e = cudaMalloc(&t->rhat, sizeof(float) * P * 2 * capacity);
+    if (e == cudaSuccess) e = cudaMalloc(&t->isd, sizeof(float) * P * 2 * capacity);
+    if (e == cudaSuccess) e = cudaMalloc(&t->epad, sizeof(float) * Pe * capacity);
+    if (e == cudaSuccess) e = cudaMalloc(&t->cden, sizeof(double) * capacity);
     if (e != cudaSuccess) {
-        cudaFree(t->in);
-        cudaFree(t->tgt);
-        cudaFree(t->mask);
-        delete t;
+        psf_trainset_destroy(t);
         return psf::cuda_status(e, "psf_trainset_create");
     }
     *out = t;
@@ -780,9 +921,9 @@ psf_status psf_trainset_create(int H, int W, int capacity, psf_trainset **out) {
 
 psf_status psf_trainset_destroy(psf_trainset *t) {
     if (t) {
-        cudaFree(t->in);
-        cudaFree(t->tgt);
-        cudaFree(t->mask);
+        for (void *p : {(void *)t->in, (void *)t->tgt, (void *)t->mask, (void *)t->rhat, (void *)t->isd,
+                        (void *)t->epad, (void *)t->cden})
+            if (p) cudaFree(p);
         delete t;
     }
     return PSF_OK;
@@ -798,7 +939,14 @@ psf_status learned_harvest(Ctx *c, psf_trainset *ts, int npairs, const int *iter
         set_error("psf_learned_harvest: the training set grid must be (nx+1) x (ny+1) nodes of a 2D problem");
         return PSF_BAD_INPUT;
     }
-    if (!c->learned) PSF_CHECK(learned_attach(c, nullptr, 2, 2, 0, 0));
+    if (ts->kind >= 0 && ts->kind != c->kind) {
+        set_error("psf_learned_harvest: the training set holds pairs of another problem kind");
+        return PSF_BAD_INPUT;
+    }
+    ts->kind = c->kind;
+    ts->nd = c->ndof;
+    for (int q = 0; q < 64; q++) ts->Ke[q] = q < (int)c->Ke0_host.size() ? (float)c->Ke0_host[q] : 0.0f;
+    if (!c->learned) PSF_CHECK(learned_attach(c, nullptr, 1, 2, 1, 0, 0));
     Learned *L = (Learned *)c->learned;
     PSF_CHECK(lp_refresh(c, L));
     cudaStream_t st = c->stream;
@@ -825,13 +973,8 @@ psf_status learned_harvest(Ctx *c, psf_trainset *ts, int npairs, const int *iter
         if (s != PSF_OK) break;
         const size_t slot = (size_t)ts->n;
         switch (c->kind) {
-            case PSF_Q4_PLANE_STRAIN:
-                s = harvest_pair<PSF_Q4_PLANE_STRAIN>(c, L, rbuf, rhs, ebuf, ts->in + slot * P * 8,
-                                                      ts->tgt + slot * P * 2, ts->mask + slot * P * 2);
-                break;
-            default:
-                s = harvest_pair<PSF_Q4_HEAT>(c, L, rbuf, rhs, ebuf, ts->in + slot * P * 8, ts->tgt + slot * P * 2,
-                                              ts->mask + slot * P * 2);
+            case PSF_Q4_PLANE_STRAIN: s = harvest_pair<PSF_Q4_PLANE_STRAIN>(c, L, rbuf, rhs, ebuf, ts, slot); break;
+            default: s = harvest_pair<PSF_Q4_HEAT>(c, L, rbuf, rhs, ebuf, ts, slot);
         }
         if (s == PSF_OK) ts->n++;
     }
@@ -847,19 +990,26 @@ psf_status learned_harvest(Ctx *c, psf_trainset *ts, int npairs, const int *iter
 extern "C" {
 
 psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch, float lr, uint64_t seed,
-                             double *loss_hist) {
-    if (!u || !ts || steps < 1 || batch < 1 || ts->n < 1) return PSF_BAD_INPUT;
+                             int loss_mode, double *loss_hist) {
+    if (!u || !ts || steps < 1 || batch < 1 || ts->n < 1 || loss_mode < 0 || loss_mode > 1) return PSF_BAD_INPUT;
     psf::unet::Net &net = u->net;
     if (net.H[0] != ts->H || net.W[0] != ts->W || batch > net.cap) {
         psf::set_error("psf_learned_train: network grid or batch capacity does not match the training set");
         return PSF_BAD_INPUT;
     }
-    const size_t P = (size_t)ts->H * ts->W;
-    float *tgt = nullptr, *mask = nullptr;
-    double *dl = nullptr;
-    PSF_CUDA(cudaMalloc(&tgt, sizeof(float) * P * 2 * batch * 2));
+    const size_t P = (size_t)ts->H * ts->W, Pe = (size_t)(ts->H + 1) * (ts->W + 1);
+    float *tgt = nullptr, *mask = nullptr, *rhat = nullptr, *isdb = nullptr, *epad = nullptr;
+    double *dl = nullptr, *cden = nullptr, *epart = nullptr;
+    PSF_CUDA(cudaMalloc(&tgt, sizeof(float) * (P * 2 * batch * 4 + Pe * batch)));
     mask = tgt + P * 2 * batch;
-    PSF_CUDA(cudaMalloc(&dl, sizeof(double) * (size_t)steps));
+    rhat = mask + P * 2 * batch;
+    isdb = rhat + P * 2 * batch;
+    epad = isdb + P * 2 * batch;
+    PSF_CUDA(cudaMalloc(&cden, sizeof(double) * (batch + 2 * psf::kLpBlocks)));
+    epart = cden + batch;
+    psf::KeT<float> Kf{};
+    for (int q = 0; q < 64; q++) Kf.v[q] = ts->Ke[q];
+    PSF_CUDA(cudaMalloc(&dl, sizeof(double) * (size_t)steps * 2));
     cudaStream_t st = net.stream;
     // global target scale: the network learns targets of unit rms, the preconditioner scales back
     if (ts->scale_n != ts->n || !(ts->out_scale > 0.0)) {
@@ -903,13 +1053,39 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
             if (s == PSF_OK)
                 s = psf::cuda_status(cudaMemcpyAsync(mask + b * P * 2, ts->mask + i * P * 2, sizeof(float) * P * 2,
                                                      cudaMemcpyDeviceToDevice, st), "copy");
+            if (s == PSF_OK && loss_mode == 1) {
+                s = psf::cuda_status(cudaMemcpyAsync(rhat + b * P * 2, ts->rhat + i * P * 2, sizeof(float) * P * 2,
+                                                     cudaMemcpyDeviceToDevice, st), "copy");
+                if (s == PSF_OK)
+                    s = psf::cuda_status(cudaMemcpyAsync(isdb + b * P * 2, ts->isd + i * P * 2, sizeof(float) * P * 2,
+                                                         cudaMemcpyDeviceToDevice, st), "copy");
+                if (s == PSF_OK)
+                    s = psf::cuda_status(cudaMemcpyAsync(epad + b * Pe, ts->epad + i * Pe, sizeof(float) * Pe,
+                                                         cudaMemcpyDeviceToDevice, st), "copy");
+                if (s == PSF_OK)
+                    s = psf::cuda_status(cudaMemcpyAsync(cden + b, ts->cden + i, sizeof(double),
+                                                         cudaMemcpyDeviceToDevice, st), "copy");
+            }
         }
         // linear warm-up, then cosine decay to 5% of lr
         const double fr = (double)k / steps;
         double lrk = lr * (0.05 + 0.95 * 0.5 * (1.0 + cos(3.141592653589793 * fr)));
         if (k < warm) lrk = lr * (k + 1) / (double)warm;
         if (s == PSF_OK) s = net.forward(batch, nullptr);
-        if (s == PSF_OK) s = net.loss_grad(batch, tgt, mask, dl + k);
+        if (s == PSF_OK && loss_mode == 0) s = net.loss_grad(batch, tgt, mask, dl + steps + k, dl + k);
+        if (s == PSF_OK && loss_mode == 1) {
+            const int nx = ts->H - 1, ny = ts->W - 1;
+            if (ts->kind == PSF_Q4_HEAT)
+                psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, cden, net.out_scale, net.g[psf::unet::kTensors - 1],
+                    epart);
+            else
+                psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, cden, net.out_scale, net.g[psf::unet::kTensors - 1],
+                    epart);
+            psf::energy_loss_kernel<<<1, 32, 0, st>>>(epart, batch, dl + k);
+            s = psf::cuda_status(cudaGetLastError(), "energy loss");
+        }
         if (s == PSF_OK) s = net.backward(batch, nullptr);
         if (s == PSF_OK) s = net.adam((float)lrk);
     }
@@ -918,16 +1094,74 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
         s = psf::cuda_status(cudaMemcpy(loss_hist, dl, sizeof(double) * steps, cudaMemcpyDeviceToHost), "copy");
     cudaFree(tgt);
     cudaFree(dl);
+    cudaFree(cden);
     return s;
 }
 
 }  // extern "C"
 
+namespace psf {
+// z = M(r) once, outside any graph (reduced vectors in, reduced out)
+template <int KIND>
+static psf_status learned_apply_t(Ctx *c, const double *r_red, double *z_red) {
+    Learned *L = (Learned *)c->learned;
+    cudaStream_t st = c->stream;
+    PSF_CHECK(lp_refresh(c, L));
+    double *r = c->w64[3], *z = c->w64[4], *q0 = c->w64[0];
+    double *red = nullptr;
+    PSF_CUDA(cudaMalloc(&red, sizeof(double) * std::max<long long>(c->nfree, 1)));
+    psf_status s0 = cuda_status(cudaMemcpyAsync(red, r_red, sizeof(double) * c->nfree, cudaMemcpyHostToDevice, st),
+                                "copy");
+    if (s0 == PSF_OK) s0 = scatter_reduced(c, red, r);
+    if (s0 != PSF_OK) {
+        cudaFree(red);
+        return s0;
+    }
+    PSF_CUDA(cudaMemsetAsync(q0, 0, sizeof(double) * c->ndofs, st));
+    PSF_CUDA(cudaMemsetAsync(L->flags, 0, sizeof(int) * F_N, st));
+    if (L->pre_mg) {
+        psf_status sp = mg_prepare(c);
+        if (sp != PSF_OK) {
+            cudaFree(red);
+            return sp;
+        }
+    }
+    psf_status sq = lp_precond<KIND>(c, L, r, z, q0, L->flags);
+    if (sq != PSF_OK) {
+        cudaFree(red);
+        return sq;
+    }
+    psf_status s = cuda_status(cudaGetLastError(), "learned apply");
+    if (s == PSF_OK) s = gather_reduced(c, z, red);
+    if (s == PSF_OK)
+        s = cuda_status(cudaMemcpyAsync(z_red, red, sizeof(double) * c->nfree, cudaMemcpyDeviceToHost, st), "copy");
+    if (s == PSF_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+    cudaFree(red);
+    if (s == PSF_OK && L->use_net) s = L->net->check_err();
+    return s;
+}
+}  // namespace psf
+
 extern "C" {
 
-psf_status psf_learned_attach(psf_ctx *h, psf_unet *net, int nu_pre, int nu_post, int use_net, int fallback_after) {
+psf_status psf_learned_apply(psf_ctx *h, const double *r, double *z) {
+    if (!h || !r || !z) return PSF_BAD_INPUT;
+    psf::Ctx *c = &h->c;
+    if (!c->learned) {
+        psf::set_error("psf_learned_apply: no learned preconditioner attached");
+        return PSF_BAD_INPUT;
+    }
+    switch (c->kind) {
+        case PSF_Q4_PLANE_STRAIN: return psf::learned_apply_t<PSF_Q4_PLANE_STRAIN>(c, r, z);
+        case PSF_Q4_HEAT: return psf::learned_apply_t<PSF_Q4_HEAT>(c, r, z);
+        default: return PSF_BAD_INPUT;
+    }
+}
+
+psf_status psf_learned_attach(psf_ctx *h, psf_unet *net, int pre_mg, int nu_pre, int nu_post, int use_net,
+                              int fallback_after) {
     if (!h) return PSF_BAD_INPUT;
-    return psf::learned_attach(&h->c, net ? &net->net : nullptr, nu_pre, nu_post, use_net, fallback_after);
+    return psf::learned_attach(&h->c, net ? &net->net : nullptr, pre_mg, nu_pre, nu_post, use_net, fallback_after);
 }
 
 psf_status psf_learned_harvest(psf_ctx *h, psf_trainset *ts, int npairs, const int *iters, int niters) {

@@ -738,6 +738,46 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
     }
 }
 
+// One V-cycle as a standalone preconditioner application (the learned
+// solver's global stage): r32 = r, x = |r| V(r / |r|) in FP32.  Returns at
+// once (every block) when *flags != 0.
+template <int KIND>
+__global__ void __launch_bounds__(kMgThreads, 1) mg_apply_kernel(MgFcgArgs A, const double *__restrict__ r,
+                                                                 float *__restrict__ r32, float *__restrict__ xo,
+                                                                 const int *flags) {
+    using T = KT<KIND>;
+    if (flags && *(volatile const int *)flags) return;
+    __shared__ double sm[32 * 4];
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const MgLev &L0 = A.L[0];
+    double acc[1] = {0.0};
+    for (long long t = tid; t < L0.ndofs; t += stride) {
+        const double rv = L0.fixed[t] ? 0.0 : r[t];
+        r32[t] = (float)rv;
+        acc[0] += rv * rv;
+    }
+    block_sum<1>(acc, sm);
+    if (!grid_sync<1, 0>(A.gs, A.partials, acc, 0.0)) return;
+    const double rn = sqrt(gs_result(A.gs, 0));
+    if (!(rn > 0.0)) {
+        for (long long t = tid; t < L0.ndofs; t += stride) xo[t] = 0.0f;
+        return;
+    }
+    const float sc = (float)(1.0 / rn);
+    for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) {
+            const long long t = n * T::nd + s;
+            const float bv = L0.fixed[t] ? 0.f : (float)r[t] * sc;
+            L0.b[t] = bv;
+            L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
+        }
+    if (!grid_barrier(A.gs, A.partials)) return;
+    if (!vcycle<KIND>(A, tid, stride, false)) return;
+    for (long long t = tid; t < L0.ndofs; t += stride) xo[t] = L0.fixed[t] ? 0.0f : (float)(rn * (double)L0.x[t]);
+}
+
 // ------------------------------------------------------------------ host side
 static psf_status mg_alloc(MgHier *H, Ctx *c, void **p, size_t bytes) {
     PSF_CUDA(cudaMalloc(p, bytes ? bytes : 1));
@@ -933,4 +973,57 @@ psf_status mg_free(Ctx *c) {
 }
 
 
+}  // namespace psf
+
+namespace psf {
+// the Galerkin hierarchy of the current design (once per design, before mg_apply)
+psf_status mg_prepare(Ctx *c) { return mg_setup(c); }
+
+template <int KIND>
+static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, const int *flags) {
+    MgHier *H = (MgHier *)c->mg;
+    MgFcgArgs *a = new MgFcgArgs;
+    a->nlev = H->nlev;
+    for (int l = 0; l < H->nlev; l++) a->L[l] = H->L[l];
+    a->Ke = kef_of(c);
+    const int nk = c->nen * c->ndof;
+    for (int q = 0; q < nk * nk; q++) a->Ke64.v[q] = c->Ke0_host[q];
+    a->Ainv = H->Ac;
+    a->nc = H->nc;
+    a->omega = 1.0f;
+    a->Ep64 = c->Epad;
+    a->gs = c->gs;
+    a->partials = c->partials;
+    a->trace = nullptr;
+    a->trace_iter = -1;
+    int per_sm = 0;
+    psf_status st = cuda_status(
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_apply_kernel<KIND>, kMgThreads, 0), "occupancy");
+    if (st == PSF_OK && per_sm < 1) {
+        set_error("multigrid apply kernel does not fit on an SM");
+        st = PSF_CUDA_ERROR;
+    }
+    if (st == PSF_OK) {
+        int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
+        const long long need = (c->nnodes + kMgThreads - 1) / kMgThreads;
+        if (blocks > need) blocks = (int)need;
+        if (blocks < 1) blocks = 1;
+        void *args[] = {a, (void *)&r, (void *)&r32, (void *)&xo, (void *)&flags};
+        st = launch_coop(c, (const void *)mg_apply_kernel<KIND>, blocks, kMgThreads, args);
+    }
+    delete a;
+    return st;
+}
+
+psf_status mg_apply(Ctx *c, const double *r, float *r32, float *xo, const int *flags) {
+    if (!c->mg) {
+        set_error("mg_apply: hierarchy not prepared");
+        return PSF_BAD_INPUT;
+    }
+    switch (c->kind) {
+        case PSF_Q4_PLANE_STRAIN: return mg_apply_t<0>(c, r, r32, xo, flags);
+        case PSF_Q4_HEAT: return mg_apply_t<1>(c, r, r32, xo, flags);
+        default: return mg_apply_t<2>(c, r, r32, xo, flags);
+    }
+}
 }  // namespace psf

@@ -566,33 +566,39 @@ __global__ void reduce_parts_kernel(const float *__restrict__ part, int nsplit, 
 constexpr int kLossBlocks = 256;
 __global__ void loss_partial_kernel(const float *__restrict__ out, const float *__restrict__ tgt,
                                     const float *__restrict__ mask, long long n, double *__restrict__ part) {
-    __shared__ double sm[64];
-    double v[2] = {0.0, 0.0};
+    __shared__ double sm[96];
+    double v[3] = {0.0, 0.0, 0.0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double m = mask ? (double)mask[i] : 1.0, d = (double)out[i] - (double)tgt[i];
         v[0] += m;
         v[1] += m * d * d;
+        v[2] += m * (double)tgt[i] * (double)tgt[i];
     }
-    block_sum<2>(v, sm);
+    block_sum<3>(v, sm);
     if (threadIdx.x == 0) {
-        part[blockIdx.x * 2] = v[0];
-        part[blockIdx.x * 2 + 1] = v[1];
+        part[blockIdx.x * 3] = v[0];
+        part[blockIdx.x * 3 + 1] = v[1];
+        part[blockIdx.x * 3 + 2] = v[2];
     }
 }
 // sums the partials (every block redundantly, fixed order) and writes the output gradient 2 m (o - t) / sum(m)
 __global__ void loss_grad_kernel(const float *__restrict__ out, const float *__restrict__ tgt,
                                  const float *__restrict__ mask, long long n, const double *__restrict__ part,
-                                 float *__restrict__ gout, double *__restrict__ loss) {
+                                 float *__restrict__ gout, double *__restrict__ loss, double *__restrict__ rel) {
     __shared__ double s_m;
     if (threadIdx.x == 0) {
-        double m = 0.0, l = 0.0;
+        double m = 0.0, l = 0.0, t = 0.0;
         for (int b = 0; b < kLossBlocks; b++) {
-            m += part[2 * b];
-            l += part[2 * b + 1];
+            m += part[3 * b];
+            l += part[3 * b + 1];
+            t += part[3 * b + 2];
         }
         if (m <= 0.0) m = 1.0;
         s_m = m;
-        if (blockIdx.x == 0 && loss) *loss = l / m;
+        if (blockIdx.x == 0 && loss) {
+            loss[0] = l / m;
+            if (rel) rel[0] = t > 0.0 ? l / t : 0.0;
+        }
     }
     __syncthreads();
     const float sc = (float)(2.0 / s_m);
@@ -671,7 +677,7 @@ psf_status Net::init(int c0_, int H_, int W_, int batch_, uint64_t seed) {
     PSF_CUDA(cudaMemset(adam_v, 0, sizeof(float) * nparams));
     PSF_CHECK(net_alloc(this, &err, 4));
     PSF_CUDA(cudaMemset(err, 0, sizeof(int) * 4));
-    PSF_CHECK(net_alloc(this, &dloss, 2 * kLossBlocks + 2));
+    PSF_CHECK(net_alloc(this, &dloss, 3 * kLossBlocks + 2));
     size_t part_max = 0;
     for (int l = 0; l < kLayers; l++) {
         const LayerDesc &y = L[l];
@@ -867,11 +873,11 @@ psf_status Net::backward(int B, const bf16 *input) {
     return PSF_OK;
 }
 
-psf_status Net::loss_grad(int B, const float *tgt, const float *mask, double *d_loss) {
+psf_status Net::loss_grad(int B, const float *tgt, const float *mask, double *d_loss, double *d_rel) {
     const long long n = npix_b(B, 0) * 2;
     loss_partial_kernel<<<kLossBlocks, 256, 0, stream>>>(out32, tgt, mask, n, dloss);
     loss_grad_kernel<<<gsz(n), 256, 0, stream>>>(out32, tgt, mask, n, dloss, g[kTensors - 1],
-                                                  d_loss ? d_loss : dloss + 2 * kLossBlocks);
+                                                  d_loss ? d_loss : dloss + 3 * kLossBlocks, d_rel);
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -1005,7 +1011,7 @@ psf_status psf_unet_loss_grad_host(psf_unet *u, int B, const float *in, const fl
     if (s == PSF_OK && mask)
         s = psf::cuda_status(cudaMemcpy(dm, mask, sizeof(float) * no, cudaMemcpyHostToDevice), "copy");
     if (s == PSF_OK) s = n.forward(B, nullptr);
-    if (s == PSF_OK) s = n.loss_grad(B, dt, mask ? dm : nullptr, dl);
+    if (s == PSF_OK) s = n.loss_grad(B, dt, mask ? dm : nullptr, dl, nullptr);
     if (s == PSF_OK) s = n.backward(B, nullptr);
     if (s == PSF_OK) s = n.check_err();
     if (s == PSF_OK && loss) s = psf::cuda_status(cudaMemcpy(loss, dl, sizeof(double), cudaMemcpyDeviceToHost), "copy");

@@ -85,7 +85,8 @@ struct Net {
     // forward of B samples; input [B][H][W][8] bf16 (null: t[0])
     psf_status forward(int B, const bf16 *input);
     // output gradient from the masked squared error against tgt (fp32 [B][H][W][2])
-    psf_status loss_grad(int B, const float *tgt, const float *mask, double *d_loss);
+    // d_rel (may be null) receives the loss relative to that of a zero output
+    psf_status loss_grad(int B, const float *tgt, const float *mask, double *d_loss, double *d_rel);
     psf_status backward(int B, const bf16 *input);
     psf_status adam(float lr);
     psf_status check_err();

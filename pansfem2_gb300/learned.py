@@ -173,9 +173,13 @@ class TrainSet:
             pass
 
 
-def train(net, trainset, steps, batch=8, lr=1e-3, seed=1):
-    """Adam on the GPU (psf_learned_train); returns the loss per step."""
+LOSS_MODES = {"mse": 0, "energy": 1}
+
+
+def train(net, trainset, steps, batch=8, lr=1e-3, seed=1, loss="energy"):
+    """Adam on the GPU (psf_learned_train); returns the loss per step relative to
+    that of a zero output (loss: "energy" = K-norm error, "mse" = squared error)."""
     hist = np.zeros(steps)
     L.check(L.load().psf_learned_train(net._h, trainset._h, int(steps), int(batch), float(lr), int(seed),
-                                       L.ptr(hist)))
+                                       LOSS_MODES[loss], L.ptr(hist)))
     return hist

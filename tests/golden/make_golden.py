@@ -57,6 +57,11 @@ def main():
         d["iters"] = np.array([iters], np.int32)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(f"{name}: {sorted(d)}")
+    # iteration 0 of the 12x6 cantilever written by the reference's own VTK writer
+    vtk = os.path.join(HERE, "ref_cantilever_12x6_it0.vtk")
+    subprocess.run([os.path.join(REF, "ref_driver"), "simp", f"out={tmp}", "iters=1", "kind=0", "nx=12", "ny=6",
+                    "bc=cantilever", f"vtk={vtk}"], check=True, stdout=subprocess.DEVNULL)
+    print(f"{os.path.basename(vtk)}: {os.path.getsize(vtk)} bytes")
     os.remove(tmp)
     for t in TEST_MAINS:
         out = subprocess.run([os.path.join(REF, t)], check=True, capture_output=True, text=True).stdout
