@@ -151,6 +151,13 @@ typedef struct {
     int cg_itmax;
     double cg_eps;           /* recurrence (plain) or FP64 true-residual (refinement) target */
     int warm_start;          /* 1: start each solve from the previous displacement */
+    /* HeavisideFilter (HeavisideFilter.h:16-98) in place of DensityFilter, with the
+     * samples' beta continuation (sample_optimize_density_oc.cpp:85-88): at every
+     * iteration k with k % beta_every == 0, beta *= beta_mult */
+    int heaviside;           /* 0: DensityFilter, 1: HeavisideFilter */
+    double beta;             /* beta before the first continuation step (the samples: 0.5) */
+    int beta_every;          /* continuation period (the samples: 40; 0: never) */
+    double beta_mult;        /* continuation factor (the samples: 2) */
 } psf_simp_params;
 
 typedef struct {

@@ -67,7 +67,8 @@ class SimpParams(C.Structure):
                 ("mma_asyinit", C.c_double), ("mma_asydecr", C.c_double), ("mma_asyincr", C.c_double),
                 ("mma_eps", C.c_double), ("mma_a0", C.c_double), ("mma_c", C.c_double), ("mma_d", C.c_double),
                 ("mma_xmin", C.c_double), ("mma_xmax", C.c_double),
-                ("solver", C.c_int), ("cg_itmax", C.c_int), ("cg_eps", C.c_double), ("warm_start", C.c_int)]
+                ("solver", C.c_int), ("cg_itmax", C.c_int), ("cg_eps", C.c_double), ("warm_start", C.c_int),
+                ("heaviside", C.c_int), ("beta", C.c_double), ("beta_every", C.c_int), ("beta_mult", C.c_double)]
 
 
 class IterInfo(C.Structure):

@@ -171,7 +171,8 @@ class Problem:
         pr = self.pr
         P = SimpParams()
         for name, _ in SimpParams._fields_:
-            if name in pr and name not in ("optimizer", "cg_itmax", "solver", "warm_start"):
+            if name in pr and name not in ("optimizer", "cg_itmax", "solver", "warm_start", "heaviside",
+                                            "beta_every"):
                 setattr(P, name, float(pr[name]))
         P.rho0 = float(pr.get("rho0", pr["vf"]))
         P.optimizer = int(pr["optimizer"])
@@ -179,6 +180,10 @@ class Problem:
         P.cg_itmax = int(pr["cg_itmax"] if cg_itmax is None else cg_itmax)
         P.cg_eps = float(pr["cg_eps"] if cg_eps is None else cg_eps)
         P.warm_start = int(bool(warm_start))
+        P.heaviside = int(pr.get("heaviside", 0))
+        P.beta = float(pr.get("beta", 0.5))
+        P.beta_every = int(pr.get("beta_every", 40))
+        P.beta_mult = float(pr.get("beta_mult", 2.0))
         self._params = P
         s0 = None if s0 is None else f64(s0)
         check(self.L.psf_simp_begin(self.h, C.byref(P), ptr(s0)))

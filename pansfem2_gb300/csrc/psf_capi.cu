@@ -346,6 +346,12 @@ psf_status psf_simp_begin(psf_ctx *h, const psf_simp_params *prm, const double *
         PSF_CHECK(psf_mma_init(h, prm->mma_a0, 0.0, prm->mma_c, prm->mma_d, prm->mma_xmin, prm->mma_xmax,
                                prm->mma_raa0, prm->mma_albefa, prm->mma_move, prm->mma_asyinit, prm->mma_asydecr,
                                prm->mma_asyincr, prm->mma_eps));
+    c->heav = prm->heaviside ? 1 : 0;
+    c->beta = prm->beta;
+    if (c->heav && !c->dH) {
+        PSF_CHECK(dalloc(c, &c->dH, c->ne));
+        PSF_CHECK(dalloc(c, &c->tmp_ne, c->ne));
+    }
     c->oc_prev = 0.0;
     c->iter = 0;
     c->simp_ready = true;
@@ -362,6 +368,8 @@ psf_status psf_simp_step(psf_ctx *h, psf_iter_info *info) {
     cudaEvent_t ev[7];
     for (auto &e : ev) PSF_CUDA(cudaEventCreate(&e));
     PSF_CUDA(cudaEventRecord(ev[0], c->stream));
+    // beta continuation of the Heaviside projection (sample_optimize_density_oc.cpp:85-88)
+    if (c->heav && P.beta_every > 0 && c->iter % P.beta_every == 0) c->beta *= P.beta_mult;
     // filtered densities, moduli, volume constraint (sample :93-105, :123)
     PSF_CHECK(filter_moduli(c, c->s, c->rho, c->E, P.E1, P.E0, P.p, P.vf, P.scale1, c->scal + 1));
     PSF_CUDA(cudaEventRecord(ev[1], c->stream));
@@ -377,8 +385,13 @@ psf_status psf_simp_step(psf_ctx *h, psf_iter_info *info) {
     PSF_CHECK(compliance_sens(c, c->rho, P.E1, P.E0, P.p, P.scale0, c->scal + 0, c->dfdrho));
     PSF_CUDA(cudaEventRecord(ev[4], c->stream));
     // filtered sensitivities (sample :168-169)
-    PSF_CHECK(filter_apply(c, c->dfdrho, c->dfds, true));
-    PSF_CHECK(filter_apply(c, c->dgdrho, c->dgds, true));
+    if (c->heav) {
+        PSF_CHECK(heaviside_back(c, c->dfdrho, c->dfds));
+        PSF_CHECK(heaviside_back(c, c->dgdrho, c->dgds));
+    } else {
+        PSF_CHECK(filter_apply(c, c->dfdrho, c->dfds, true));
+        PSF_CHECK(filter_apply(c, c->dgdrho, c->dgds, true));
+    }
     PSF_CUDA(cudaEventRecord(ev[5], c->stream));
     double fg[2];
     PSF_CHECK(d2h_sync(c, fg, c->scal, 2 * sizeof(double)));

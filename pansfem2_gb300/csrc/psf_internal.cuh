@@ -91,6 +91,9 @@ struct Ctx {
     double *s = nullptr, *rho = nullptr, *dfdrho = nullptr, *dgdrho = nullptr, *dfds = nullptr,
            *dgds = nullptr, *snew = nullptr;
     double *scal = nullptr;      // device scalars (f, g, ...), 16 doubles
+    int heav = 0;                // Heaviside projection after the density filter
+    double beta = 1.0;           // its current beta
+    double *dH = nullptr, *tmp_ne = nullptr;   // d rho / d rho~ per element; scratch
     psf_simp_params prm{};
     bool simp_ready = false;
     double oc_prev = 0.0;
@@ -160,6 +163,7 @@ psf_status scatter_reduced(Ctx *c, const double *red, double *nodal);  // psf_me
 psf_status gather_reduced(Ctx *c, const double *nodal, double *red);   // psf_mesh.cu
 psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_solve.cu
 psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward);               // psf_opt.cu
+psf_status heaviside_back(Ctx *c, const double *d, double *out);                            // psf_opt.cu
 psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, double p, double scale0,
                            double *f_dev, double *dfdrho);                                 // psf_opt.cu
 psf_status oc_update(Ctx *c, double *x, const double *dfdx, const double *dgdx, double iota, double lmin,

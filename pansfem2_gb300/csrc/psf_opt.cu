@@ -82,15 +82,29 @@ __global__ void filter_kernel(const __grid_constant__ Stencil S, long long ne, c
 
 // filtered density, moduli E = E1 rho^p + E0 (1 - rho^p) (sample :123) and the
 // volume sum sum_i scale1*rho_i/(vf*ne) (sample :99-105) in one pass
+// HeavisideFilter.h:74 and :88 (the projection of the filtered density and its derivative)
+__device__ __forceinline__ double heav_rho(double rt, double beta) {
+    return 0.5 * (tanh(0.5 * beta) + tanh(beta * (rt - 0.5))) / tanh(0.5 * beta);
+}
+__device__ __forceinline__ double heav_drho(double rt, double beta) {
+    const double t = tanh(beta * (rt - 0.5));
+    return 0.5 * beta * (1.0 - t * t) / tanh(0.5 * beta);
+}
+
 __global__ void filter_moduli_kernel(const __grid_constant__ Stencil S, long long ne, const double *__restrict__ s,
                                      const double *__restrict__ wsum, double E1, double E0, double p, double vscale,
-                                     double *__restrict__ rho, double *__restrict__ E, double *partials) {
+                                     double *__restrict__ rho, double *__restrict__ E, double *partials, int heav,
+                                     double beta, double *__restrict__ dH) {
     __shared__ double sm[32];
     double acc[1] = {0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         elem_ijk(S, e, i, j, k);
-        const double r = stencil_sum(S, s, i, j, k) / wsum[e];
+        double r = stencil_sum(S, s, i, j, k) / wsum[e];
+        if (heav) {
+            dH[e] = heav_drho(r, beta);
+            r = heav_rho(r, beta);
+        }
         rho[e] = r;
         const double rp = pow(r, p);
         E[e] = E1 * rp + E0 * (1.0 - rp);
@@ -178,6 +192,8 @@ struct OcArgs {
     double *x, *xnew, *rho;
     const double *dfdx, *dgdx, *wsum;
     double iota, lmin, lmax, leps, move, vscale, scale1;
+    int heav;
+    double beta;
     GridSync *gs;
     double *partials;
     double *out;   // out[0] = lambda, out[1] = bisection steps
@@ -208,7 +224,8 @@ __global__ void __launch_bounds__(256) oc_kernel(const __grid_constant__ Stencil
         for (long long e = tid; e < A.n; e += stride) {
             int i, j, k;
             elem_ijk(S, e, i, j, k);
-            const double r = stencil_sum(S, A.xnew, i, j, k) / A.wsum[e];
+            double r = stencil_sum(S, A.xnew, i, j, k) / A.wsum[e];
+            if (A.heav) r = heav_rho(r, A.beta);
             acc[0] += A.vscale * r;
         }
         block_sum<1>(acc, sm);
@@ -483,6 +500,20 @@ psf_status filter_setup(Ctx *c, double R) {
     return PSF_OK;
 }
 
+__global__ void mul_kernel(long long n, const double *__restrict__ a, const double *__restrict__ b,
+                           double *__restrict__ out) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        out[e] = a[e] * b[e];
+}
+
+// filtered sensitivity through the projection (HeavisideFilter.h:81-97):
+// out_i = sum_j w_ij d_j dH_j / wsum_i
+psf_status heaviside_back(Ctx *c, const double *d, double *out) {
+    mul_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, d, c->dH, c->tmp_ne);
+    PSF_CUDA(cudaGetLastError());
+    return filter_apply(c, c->tmp_ne, out, true);
+}
+
 psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward) {
     (void)backward;   // both directions are the same stencil sum normalised by wsum_i
     Stencil *S = new Stencil;
@@ -503,7 +534,8 @@ psf_status filter_moduli(Ctx *c, const double *s, double *rho, double *E, double
     if (st != PSF_OK) { delete S; return st; }
     const int nb = grid_for(c->ne, 256, c->num_sms * 8);
     const double vscale = scale1 / (vf * (double)c->ne);
-    filter_moduli_kernel<<<nb, 256, 0, c->stream>>>(*S, c->ne, s, c->filt_wsum, E1, E0, p, vscale, rho, E, c->partials);
+    filter_moduli_kernel<<<nb, 256, 0, c->stream>>>(*S, c->ne, s, c->filt_wsum, E1, E0, p, vscale, rho, E, c->partials,
+                                                    c->heav, c->beta, c->dH);
     delete S;
     sum_partials<<<1, 32, 0, c->stream>>>(c->partials, nb, 1.0, -1.0 * scale1, g_dev);
     PSF_CUDA(cudaGetLastError());
@@ -572,6 +604,8 @@ psf_status oc_update(Ctx *c, double *x, const double *dfdx, const double *dgdx, 
     A.iota = iota; A.lmin = lmin; A.lmax = lmax; A.leps = leps; A.move = move;
     A.vscale = scale1 / (vf * (double)c->ne);
     A.scale1 = scale1;
+    A.heav = c->heav;
+    A.beta = c->beta;
     A.gs = c->gs;
     A.partials = c->partials;
     A.out = c->scal + 4;
