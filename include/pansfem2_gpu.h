@@ -236,7 +236,7 @@ psf_status psf_csr_solve_noalloc(int n, const int32_t *d_indptr, const int32_t *
  * nest: H = 8k+1, W = 8m+1), base width c0 (16: channels 16, 32, 64, 128), bf16 weights and
  * activations with fp32 accumulation on the tensor cores, trained with Adam on
  * the GPU.  Inputs are [B][H][W][8] (density, the two residual components,
- * five zero channels), outputs [B][H][W][2].  The parameter vector is laid out
+ * the moduli of the four surrounding elements, one zero channel), outputs [B][H][W][2].  The parameter vector is laid out
  * per layer as W[co][tap][ci] then b[co] (oracle/unet_oracle.c restates the
  * network on the CPU). */
 typedef struct psf_unet psf_unet;
@@ -299,6 +299,9 @@ psf_status psf_learned_harvest(psf_ctx *ctx, psf_trainset *ts, int npairs, const
  * to that of a zero output (1 = nothing learned) */
 psf_status psf_learned_train(psf_unet *net, psf_trainset *ts, int steps, int batch, float lr, uint64_t seed,
                              int loss_mode, double *loss_hist);
+/* mean over pairs [first, first + count) of the energy-norm error of the
+ * network's correction relative to that of no correction (1 = no gain) */
+psf_status psf_learned_eval(psf_unet *net, psf_trainset *ts, int first, int count, double *mean_rel_energy);
 
 /* ---------------- VTK output ---------------- */
 /* Replaces the per-iteration dump of sample_optimize_density_oc.cpp:173-181

@@ -13,7 +13,7 @@
  * 3x3 convolutions, ReLU, stride-2 3x3 convolutions down, bilinear vertex
  * prolongation up, skip connections by channel concatenation, a final 3x3
  * convolution to 2 channels.  Inputs have 8 channels (density, 2 residual
- * components, 5 zero).  Parameter layout per layer: W[co][tap][ci] then
+ * components, the four surrounding element moduli, 1 zero).  Parameter layout per layer: W[co][tap][ci] then
  * b[co], tap = 3*dy + dx for offsets (dy-1, dx-1).  Loss: masked mean squared
  * error of the 2-channel output.
  */

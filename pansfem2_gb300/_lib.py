@@ -37,7 +37,7 @@ EXPORTS = [
     "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv", "psf_unet_get_out_scale",
     "psf_unet_set_out_scale",
     "psf_learned_attach", "psf_learned_apply", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
-    "psf_learned_harvest", "psf_learned_train", "psf_export_vtk", "psf_export_wait",
+    "psf_learned_harvest", "psf_learned_train", "psf_learned_eval", "psf_export_vtk", "psf_export_wait",
 ]
 
 
@@ -148,6 +148,7 @@ def load(path=LIB_PATH):
         "psf_trainset_size": [vp],
         "psf_learned_harvest": [vp, vp, C.c_int, ip, C.c_int],
         "psf_learned_train": [vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_int, dp],
+        "psf_learned_eval": [vp, vp, C.c_int, C.c_int, dp],
         "psf_export_vtk": [vp, C.c_char_p, C.c_int],
         "psf_export_wait": [vp],
     }

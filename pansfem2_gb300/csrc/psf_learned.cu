@@ -54,7 +54,7 @@ constexpr int kLpThreads = 256;
 constexpr int kGraphIters = 4;   // FCG iterations per host check
 
 // scalar slots
-enum { S_SCALE = 0, S_ZQ, S_PQPREV, S_PQ, S_RP, S_RR, S_BB, S_EPS2, S_FIRST, S_NSC = 16 };
+enum { S_SCALE = 0, S_ZQ, S_PQPREV, S_PQ, S_RP, S_RR, S_BB, S_EPS2, S_FIRST, S_OMEGA, S_NSC = 16 };
 // flag slots
 enum { F_DONE = 0, F_ITERS, F_NONFINITE, F_LIMIT, F_ITMAX, F_N = 8 };
 
@@ -72,6 +72,8 @@ struct Learned {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     float graph_scale = 0.0f;
+    float inv_e1 = 1.0f;   // 1 / E1 of the design (density features)
+    float *dcorr = nullptr;   // the network's correction in x space (before its step length)
     std::vector<void *> allocs;
 };
 
@@ -170,13 +172,16 @@ __global__ void __launch_bounds__(kLpThreads) lp_resid_kernel(Geo g, KeT<float> 
 }
 
 // network input: density, D^-1/2 r1 / s per dof, zeros; s = rms over the free dofs
+// channels: 0 node density, 1-2 D^-1/2 r1 / s per dof, 3-6 (E / E1)^(1/3) of the four
+// surrounding elements (the local operator; 0 outside the grid), 7 zero
 template <int KIND>
 __global__ void __launch_bounds__(kLpThreads) nn_prep_kernel(long long nnodes, long long nfree,
                                                              const double *__restrict__ part,
                                                              const float *__restrict__ r1,
                                                              const float *__restrict__ isd,
                                                              const float *__restrict__ rho, bf16 *__restrict__ nnin,
-                                                             double *sc, const int *flags) {
+                                                             double *sc, const int *flags, int ny,
+                                                             const float *__restrict__ epad, float inv_e1) {
     if (lp_done(flags)) return;
     constexpr int nd = ndof_of<KIND>();
     double ss[1];
@@ -188,6 +193,13 @@ __global__ void __launch_bounds__(kLpThreads) nn_prep_kernel(long long nnodes, l
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
          n += (long long)gridDim.x * blockDim.x) {
         float c[8] = {rho[n], 0, 0, 0, 0, 0, 0, 0};
+        const int i = (int)(n / (ny + 1)), j = (int)(n % (ny + 1));
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int ei = i - 1 + (q >> 1), ej = j - 1 + (q & 1);
+            const float e = epad[(long long)(ei + 1) * (ny + 2) + (ej + 1)];
+            c[3 + q] = e > 0.0f ? cbrtf(e * inv_e1) : 0.0f;
+        }
 #pragma unroll
         for (int a = 0; a < nd && a < 2; a++) c[1 + a] = isd[n * nd + a] * r1[n * nd + a] * is;
         uint4 o;
@@ -198,18 +210,59 @@ __global__ void __launch_bounds__(kLpThreads) nn_prep_kernel(long long nnodes, l
     }
 }
 
-// x += D^-1/2 * s * out on the free dofs
+// the correction d = D^-1/2 * s * out on the free dofs
 template <int KIND>
 __global__ void nn_apply_kernel(long long nnodes, const float *__restrict__ out, const float *__restrict__ isd,
-                                const double *sc, float oscale, float *__restrict__ x, const int *flags) {
+                                const double *sc, float oscale, float *__restrict__ d, const int *flags) {
     if (lp_done(flags)) return;
     constexpr int nd = ndof_of<KIND>();
     const float s = (float)sc[S_SCALE] * oscale;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
          n += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
-        for (int a = 0; a < nd && a < 2; a++) x[n * nd + a] += isd[n * nd + a] * s * out[n * 2 + a];
+        for (int a = 0; a < nd; a++) d[n * nd + a] = a < 2 ? isd[n * nd + a] * s * out[n * 2 + a] : 0.0f;
     }
+}
+
+// partial sums of d . r1 and d . K d (the energy-optimal step length of the correction)
+template <int KIND>
+__global__ void __launch_bounds__(kLpThreads) nn_step_kernel(Geo g, KeT<float> Ke, const float *__restrict__ Ep,
+                                                             const unsigned char *__restrict__ fixed,
+                                                             const float *__restrict__ d,
+                                                             const float *__restrict__ r1, double *part,
+                                                             const int *flags) {
+    if (lp_done(flags)) return;
+    constexpr int nd = ndof_of<KIND>();
+    double v[2] = {0.0, 0.0};
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_ijk<KIND>(g, n, i, j, k);
+        float y[nd];
+        ebe_node<float, KIND>(g, Ke, Ep, i, j, k, [&](long long a) { return d[a]; }, y);
+#pragma unroll
+        for (int a = 0; a < nd; a++) {
+            const long long t = n * nd + a;
+            if (fixed[t]) continue;
+            v[0] += (double)d[t] * r1[t];
+            v[1] += (double)d[t] * y[a];
+        }
+    }
+    write_parts<2>(v, part);
+}
+
+// x += omega d with omega = (d . r1) / (d . K d), 0 when the correction has no energy
+__global__ void __launch_bounds__(kLpThreads) nn_add_kernel(long long nd, const double *part,
+                                                            const float *__restrict__ d, float *__restrict__ x,
+                                                            double *sc, const int *flags) {
+    if (lp_done(flags)) return;
+    double v[2];
+    fold_parts<2>(part, v);
+    const double om = (v[1] > 0.0 && isfinite(v[0] / v[1])) ? v[0] / v[1] : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc[S_OMEGA] = om;
+    const float w = (float)om;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nd; t += (long long)gridDim.x * blockDim.x)
+        x[t] += w * d[t];
 }
 
 // last step of the preconditioner: optional sweep, z = x in FP64, partial z . q_prev
@@ -472,6 +525,7 @@ psf_status learned_attach(Ctx *c, unet::Net *net, int pre_mg, int nu_pre, int nu
         if (s == PSF_OK) s = lp_alloc(L, &L->xa, nd);
         if (s == PSF_OK) s = lp_alloc(L, &L->xb, nd);
         if (s == PSF_OK) s = lp_alloc(L, &L->r1, nd);
+        if (s == PSF_OK) s = lp_alloc(L, &L->dcorr, nd);
         if (s == PSF_OK) s = lp_alloc(L, &L->isd, nd);
         if (s == PSF_OK) s = lp_alloc(L, &L->rho, c->nnodes);
         if (s == PSF_OK) s = lp_alloc(L, &L->nnin, (size_t)c->nnodes * 8);
@@ -507,6 +561,7 @@ static psf_status lp_refresh(Ctx *c, Learned *L) {
     const int gb = 4 * std::max(c->num_sms, 1);
     isd_kernel<<<gb, 256, 0, c->stream>>>(c->ndofs, c->Dl1f, c->fixed, L->isd);
     const double E1 = c->simp_ready && c->prm.E1 > 0 ? c->prm.E1 : 1.0;
+    L->inv_e1 = (float)(1.0 / E1);
     rho_node_kernel<<<gb, 256, 0, c->stream>>>(c->nx, c->ny, c->Epad, E1, L->rho);
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -546,12 +601,14 @@ static psf_status lp_precond(Ctx *c, Learned *L, const double *r, double *z, con
         lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
                                                                L->part, fl);
         nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho,
-                                                              L->nnin, L->sc, fl);
+                                                              L->nnin, L->sc, fl, c->ny, c->Epadf, L->inv_e1);
         L->net->stream = st;
         L->net->skip = fl;
         PSF_CHECK(L->net->forward(1, L->nnin));
         nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc,
-                                                               L->net->out_scale, cur, fl);
+                                                               L->net->out_scale, L->dcorr, fl);
+        nn_step_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->dcorr, L->r1, L->part, fl);
+        nn_add_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, L->part, L->dcorr, cur, L->sc, fl);
     }
     for (int k = 1; k < L->nu_post; k++) {
         lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl);
@@ -866,7 +923,7 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
                                                            L->part, L->flags);
     nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho, in_out,
-                                                          L->sc, L->flags);
+                                                          L->sc, L->flags, c->ny, c->Epadf, L->inv_e1);
     f32_to_f64_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->r1, rhs64);
     PSF_CUDA(cudaGetLastError());
     // e = K^-1 r1 with the multigrid FCG to 1e-8 (its right-hand side is the context's nodal load vector)
@@ -1167,6 +1224,59 @@ psf_status psf_learned_attach(psf_ctx *h, psf_unet *net, int pre_mg, int nu_pre,
 psf_status psf_learned_harvest(psf_ctx *h, psf_trainset *ts, int npairs, const int *iters, int niters) {
     if (!h) return PSF_BAD_INPUT;
     return psf::learned_harvest(&h->c, ts, npairs, iters, niters);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+psf_status psf_learned_eval(psf_unet *u, psf_trainset *ts, int first, int count, double *mean_rel_energy) {
+    if (!u || !ts || !mean_rel_energy || first < 0 || count < 1 || first + count > ts->n) return PSF_BAD_INPUT;
+    psf::unet::Net &net = u->net;
+    if (net.H[0] != ts->H || net.W[0] != ts->W) {
+        psf::set_error("psf_learned_eval: network grid does not match the training set");
+        return PSF_BAD_INPUT;
+    }
+    const size_t P = (size_t)ts->H * ts->W, Pe = (size_t)(ts->H + 1) * (ts->W + 1);
+    const int B = net.cap;
+    double *dl = nullptr, *part = nullptr;
+    PSF_CUDA(cudaMalloc(&dl, sizeof(double) * ((size_t)count + 2 * psf::kLpBlocks)));
+    part = dl + count;
+    psf::KeT<float> Kf{};
+    for (int q = 0; q < 64; q++) Kf.v[q] = ts->Ke[q];
+    cudaStream_t st = net.stream;
+    psf_status s = PSF_OK;
+    const int nx = ts->H - 1, ny = ts->W - 1;
+    std::vector<double> h(count);
+    for (int i0 = 0; i0 < count && s == PSF_OK; i0 += B) {
+        const int nb = std::min(B, count - i0);
+        const size_t i = (size_t)(first + i0);
+        // consecutive pairs: the trainset slots are already laid out as a batch
+        s = psf::cuda_status(cudaMemcpyAsync(net.t[0], ts->in + i * P * 8, sizeof(psf::unet::bf16) * P * 8 * nb,
+                                             cudaMemcpyDeviceToDevice, st), "copy");
+        if (s == PSF_OK) s = net.forward(nb, nullptr);
+        for (int b = 0; b < nb && s == PSF_OK; b++) {
+            const size_t j = i + b;
+            if (ts->kind == PSF_Q4_HEAT)
+                psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2, ts->epad + j * Pe,
+                    ts->cden + j, net.out_scale, net.g[psf::unet::kTensors - 1], part);
+            else
+                psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2, ts->epad + j * Pe,
+                    ts->cden + j, net.out_scale, net.g[psf::unet::kTensors - 1], part);
+            psf::energy_loss_kernel<<<1, 32, 0, st>>>(part, 1, dl + i0 + b);
+            s = psf::cuda_status(cudaGetLastError(), "energy loss");
+        }
+    }
+    if (s == PSF_OK) s = net.check_err();
+    if (s == PSF_OK) s = psf::cuda_status(cudaMemcpy(h.data(), dl, sizeof(double) * count, cudaMemcpyDeviceToHost), "copy");
+    cudaFree(dl);
+    if (s != PSF_OK) return s;
+    double m = 0.0;
+    for (double v : h) m += v;
+    *mean_rel_energy = m / count;
+    return PSF_OK;
 }
 
 }  // extern "C"

@@ -19,7 +19,7 @@
 // inputs, fp32 accumulation, fixed-order partial sums: deterministic).
 //
 // Network layout (the CPU oracle oracle/unet_oracle.c restates it):
-//   tensors  0 input(8: density, residual x, residual y, 5 zero)  1 e0a  2 cat0 = [e0 | up(d1)]
+//   tensors  0 input(8: density, residual x/y, 4 element moduli, 1 zero)  1 e0a  2 cat0 = [e0 | up(d1)]
 //            3 e1a  4 cat1 = [e1 | up(d2)]  5 e2a  6 cat2 = [e2 | up(e3)]  7 e3a  8 e3
 //            9 d2a 10 d2 11 d1a 12 d1 13 d0a 14 d0 15 output (2, fp32)
 //   channels c0, 2c0, 4c0, 8c0 on levels 0..3; level sizes H_l = (H_{l-1} + 1) / 2
@@ -712,15 +712,14 @@ psf_status Net::init(int c0_, int H_, int W_, int batch_, uint64_t seed) {
         return ((z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
     };
     for (int l = 0; l < kLayers; l++) {
-        const double sd = sqrt(2.0 / (9.0 * (l == 0 ? 3 : L[l].cin)));
+        const double sd = sqrt(2.0 / (9.0 * (l == 0 ? 7 : L[l].cin)));
         for (int i = L[l].woff; i < L[l].boff; i++) {
             const double u1 = next(), u2 = next();
             h[i] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
         }
-        if (l == 0)  // the padded input channels 3..7 carry nothing
+        if (l == 0)  // the padded input channel 7 carries nothing
             for (int co = 0; co < L[0].cout; co++)
-                for (int tp = 0; tp < 9; tp++)
-                    for (int ci = 3; ci < 8; ci++) h[L[0].woff + ((size_t)co * 9 + tp) * 8 + ci] = 0.0f;
+                for (int tp = 0; tp < 9; tp++) h[L[0].woff + ((size_t)co * 9 + tp) * 8 + 7] = 0.0f;
         if (l == kLayers - 1)
             for (int i = L[l].woff; i < L[l].boff; i++) h[i] *= 0.1f;
     }

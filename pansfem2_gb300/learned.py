@@ -183,3 +183,12 @@ def train(net, trainset, steps, batch=8, lr=1e-3, seed=1, loss="energy"):
     L.check(L.load().psf_learned_train(net._h, trainset._h, int(steps), int(batch), float(lr), int(seed),
                                        LOSS_MODES[loss], L.ptr(hist)))
     return hist
+
+
+def evaluate(net, trainset, first=0, count=None):
+    """Mean energy-norm error of the network's correction over pairs
+    [first, first + count), relative to no correction (1 = no gain)."""
+    count = len(trainset) - first if count is None else count
+    v = C.c_double()
+    L.check(L.load().psf_learned_eval(net._h, trainset._h, int(first), int(count), C.byref(v)))
+    return v.value

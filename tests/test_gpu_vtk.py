@@ -32,7 +32,7 @@ def sections(path):
             t = line.split()
             if not t:
                 continue
-            if t[0].isalpha() or t[0].startswith("#"):
+            if t[0][0].isalpha() or t[0].startswith("#"):
                 cur = (line.strip(), [])
                 out.append(cur)
             else:
