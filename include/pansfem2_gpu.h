@@ -313,6 +313,30 @@ psf_status psf_learned_eval(psf_unet *net, psf_trainset *ts, int first, int coun
 psf_status psf_export_vtk(psf_ctx *ctx, const char *path, int async);
 psf_status psf_export_wait(psf_ctx *ctx);
 
+/* ---------------- batched heat-conduction SIMP ---------------- */
+/* No counterpart in the reference (its samples run one problem per process).
+ * ninst independent 2D heat-sink problems (HeatTransfer Q4, unit elements,
+ * uniform unit source lumped to the nodes, zero-temperature patch of nodes
+ * patch_i0 .. patch_i0 + patch_w on edge 0: j = 0, 1: j = side, 2: i = 0,
+ * 3: i = side; even sides whose halving reaches <= 64 nodes), each with its own
+ * volume fraction.  One CTA of `threads` threads owns an instance in each
+ * phase; one SIMP iteration of all instances (filter + conductivities,
+ * multigrid-preconditioned FCG to the FP64 true residual cg_eps, compliance +
+ * sensitivities, OC) is captured as one CUDA graph by psf_batch_begin. */
+typedef struct psf_batch psf_batch;
+psf_status psf_batch_create(int ninst, const int *side, const int *edge, const int *patch_w, const int *patch_i0,
+                            const double *vf, int threads, psf_batch **batch);
+psf_status psf_batch_destroy(psf_batch *batch);
+/* shared parameters: E1 = k0, E0 = kmin, p, R, OC parameters, cg_eps, cg_itmax,
+ * warm_start (optimizer must be 0); starts every instance at s = vf */
+psf_status psf_batch_begin(psf_batch *batch, const psf_simp_params *prm);
+/* iters SIMP iterations of every instance (graph replays); device seconds */
+psf_status psf_batch_step(psf_batch *batch, int iters, double *seconds);
+/* per instance 8 values: f, g, OC lambda, solver iterations, FP64 relative
+ * residual, converged, refinement passes, bisection steps */
+psf_status psf_batch_results(psf_batch *batch, double *out);
+psf_status psf_batch_fields(psf_batch *batch, int instance, double *s, double *rho, double *T);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,8 @@ EXPORTS = [
     "psf_unet_set_out_scale",
     "psf_learned_attach", "psf_learned_apply", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
     "psf_learned_harvest", "psf_learned_train", "psf_learned_eval", "psf_export_vtk", "psf_export_wait",
+    "psf_batch_create", "psf_batch_destroy", "psf_batch_begin", "psf_batch_step", "psf_batch_results",
+    "psf_batch_fields",
 ]
 
 
@@ -150,6 +152,12 @@ def load(path=LIB_PATH):
         "psf_learned_train": [vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_int, dp],
         "psf_learned_eval": [vp, vp, C.c_int, C.c_int, dp],
         "psf_export_vtk": [vp, C.c_char_p, C.c_int],
+        "psf_batch_create": [C.c_int, ip, ip, ip, ip, dp, C.c_int, C.POINTER(C.c_void_p)],
+        "psf_batch_destroy": [vp],
+        "psf_batch_begin": [vp, C.POINTER(SimpParams)],
+        "psf_batch_step": [vp, C.c_int, dp],
+        "psf_batch_results": [vp, dp],
+        "psf_batch_fields": [vp, C.c_int, dp, dp, dp],
         "psf_export_wait": [vp],
     }
     for name, args in sig.items():

@@ -1,0 +1,944 @@
+// psf_batch.cu -- many independent 2D heat-conduction SIMP problems (square Q4
+// grids of uneven size, one temperature dof per node, OC update) advanced
+// together: each SIMP iteration is four launches over all instances
+// (filter + moduli + volume; solve; compliance + sensitivities + filtered
+// sensitivities; OC), captured once as a CUDA graph and replayed.
+//
+// One CTA owns one instance for the whole phase, so every reduction and every
+// barrier of an instance is block-local (__syncthreads, shared memory): no grid
+// barrier, no atomics, deterministic.  Instances are launched largest first.
+// The solve is flexible CG in FP64 (operator, dot products, recurrences) whose
+// preconditioner is one FP32 V(2,2) multigrid cycle per iteration: l1-Jacobi
+// smoothing, Galerkin coarse operators built element by element inside the
+// block (P^T K P with bilinear P, fixed nodes masked), 9-point coarse stencils,
+// and a dense inverse of the coarsest level (<= 64 nodes) in shared memory.
+// The FP64 true residual decides convergence.
+//
+// Each instance follows the single-problem path of this library for the
+// heat-sink configuration (the reference's HeatTransfer element, DensityFilter,
+// OC with the filtered-volume callback), so its trajectory matches a psf_ctx run
+// of the same problem to the solver tolerance.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "psf_internal.cuh"
+
+namespace psf {
+namespace batch {
+
+constexpr int kLev = 10;
+constexpr int kCoarseNodes = 64;
+constexpr int kMaxStencilB = 49;   // filter stencil entries (radius < 3.5 elements)
+
+struct Inst {
+    int n, nlev, nc;
+    int pad_;
+    long long e0, v0;        // level-0 element / node offsets
+    long long me[kLev];      // per-level element offsets (coarse element matrices, levels >= 1)
+    long long mv[kLev];      // per-level node offsets (multigrid vectors, all levels)
+    long long ainv;          // offset of the coarsest dense inverse
+    double vf;
+};
+
+struct Args {
+    int ninst;
+    const Inst *inst;
+    const int *order;        // block b processes instance order[b]
+    // level-0 element arrays
+    double *s, *rho, *E, *dfdrho, *dfds, *dgds, *snew, *wsum;
+    float *Ef;
+    // level-0 node arrays (FP64 Krylov vectors, loads, fixed flags)
+    double *x, *r, *z, *p, *q, *F;
+    const unsigned char *fixed;
+    // multigrid arrays
+    float *Kel;              // 16 floats per coarse element
+    float *St;               // 9 floats per coarse node
+    float *D, *mx, *mb, *mr; // per node, all levels
+    unsigned char *mfix;     // per node, all levels (level 0 copies the Dirichlet flags)
+    float *Ainv;
+    double *out;             // per instance, kOut values
+    // parameters
+    double k0, kmin, pexp, iota, lmin, lmax, leps, move, eps;
+    int itmax, warm;
+    double Ke0[16];
+    float Ke0f[16];
+    int nst;                 // filter stencil
+    int sdi[kMaxStencilB], sdj[kMaxStencilB];
+    double sw[kMaxStencilB];
+};
+
+// per-instance outputs
+enum { O_F = 0, O_G, O_LAMBDA, O_ITERS, O_RES, O_CONV, O_PASSES, O_BISECT, kOut = 8 };
+
+constexpr int kThreads = 512;
+
+// ------------------------------------------------------------------ block helpers
+// block-wide sum, every thread gets the result (fixed tree order)
+__device__ __forceinline__ double bsum(double v, double *sm) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    double t = lane < nw ? sm[lane] : 0.0;
+    t = warp_sum(t);
+    return t;
+}
+
+__device__ __forceinline__ int corner(int di, int dj) { return di ? (dj ? 2 : 1) : (dj ? 3 : 0); }
+
+// FP64 operator row of node (i, j) of level 0: y = sum over the 4 surrounding elements of E_e Ke0 x_e
+__device__ __forceinline__ double op64(const Args &A, const Inst &I, const double *xv, int i, int j) {
+    const int n = I.n;
+    double y = 0.0;
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++) {
+            const int ei = i - 1 + ci, ej = j - 1 + cj;
+            if (ei < 0 || ej < 0 || ei >= n || ej >= n) continue;
+            const double Ee = A.E[I.e0 + (long long)n * ei + ej];
+            const int li = corner(1 - ci, 1 - cj);
+            double acc = 0.0;
+#pragma unroll
+            for (int lb = 0; lb < 4; lb++) {
+                const int bi = ei + (lb == 1 || lb == 2), bj = ej + (lb == 2 || lb == 3);
+                acc += A.Ke0[li * 4 + lb] * xv[(long long)(n + 1) * bi + bj];
+            }
+            y += Ee * acc;
+        }
+    return y;
+}
+
+// FP32 operator row of node (i, j) at level l (level 0: element by element, else the 9-point stencil)
+__device__ __forceinline__ float opl(const Args &A, const Inst &I, int l, const float *xv, int i, int j) {
+    const int m = I.n >> l;
+    if (l == 0) {
+        float y = 0.0f;
+#pragma unroll
+        for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+            for (int cj = 0; cj < 2; cj++) {
+                const int ei = i - 1 + ci, ej = j - 1 + cj;
+                if (ei < 0 || ej < 0 || ei >= m || ej >= m) continue;
+                const float Ee = A.Ef[I.e0 + (long long)m * ei + ej];
+                const int li = corner(1 - ci, 1 - cj);
+                float acc = 0.0f;
+#pragma unroll
+                for (int lb = 0; lb < 4; lb++) {
+                    const int bi = ei + (lb == 1 || lb == 2), bj = ej + (lb == 2 || lb == 3);
+                    acc += A.Ke0f[li * 4 + lb] * xv[(long long)(m + 1) * bi + bj];
+                }
+                y += Ee * acc;
+            }
+        return y;
+    }
+    const float *st = A.St + (I.mv[l] + (long long)(m + 1) * i + j) * 9;
+    float y = 0.0f;
+#pragma unroll
+    for (int di = -1; di <= 1; di++)
+#pragma unroll
+        for (int dj = -1; dj <= 1; dj++) {
+            const int a = i + di, b = j + dj;
+            if (a < 0 || b < 0 || a > m || b > m) continue;
+            y += st[(di + 1) * 3 + (dj + 1)] * xv[(long long)(m + 1) * a + b];
+        }
+    return y;
+}
+
+// ------------------------------------------------------------------ multigrid setup (inside the block)
+__device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // level 0: l1 row sums (E >= 0) and the fixed flags
+    {
+        const int m = I.n;
+        const long long nn = (long long)(m + 1) * (m + 1);
+        for (long long v = tid; v < nn; v += nt) {
+            const int i = (int)(v / (m + 1)), j = (int)(v % (m + 1));
+            const bool fx = A.fixed[I.v0 + v];
+            A.mfix[I.mv[0] + v] = fx;
+            float d = 0.0f;
+            for (int ci = 0; ci < 2; ci++)
+                for (int cj = 0; cj < 2; cj++) {
+                    const int ei = i - 1 + ci, ej = j - 1 + cj;
+                    if (ei < 0 || ej < 0 || ei >= m || ej >= m) continue;
+                    const int li = corner(1 - ci, 1 - cj);
+                    float a = 0.0f;
+                    for (int lb = 0; lb < 4; lb++) a += fabsf(A.Ke0f[li * 4 + lb]);
+                    d += A.Ef[I.e0 + (long long)m * ei + ej] * a;
+                }
+            A.D[I.mv[0] + v] = fx ? 1.0f : d;
+        }
+    }
+    __syncthreads();
+    for (int l = 1; l < I.nlev; l++) {
+        const int mf = I.n >> (l - 1), mc = I.n >> l;
+        const long long nnc = (long long)(mc + 1) * (mc + 1);
+        // coarse fixed flags: a coarse node is fixed when the coincident fine node is
+        for (long long v = tid; v < nnc; v += nt) {
+            const int i = (int)(v / (mc + 1)), j = (int)(v % (mc + 1));
+            A.mfix[I.mv[l] + v] = A.mfix[I.mv[l - 1] + (long long)(mf + 1) * (2 * i) + 2 * j];
+        }
+        __syncthreads();
+        // Galerkin element matrices: Kc = sum over the 4 fine children of P_f^T K_f P_f
+        const long long nec = (long long)mc * mc;
+        for (long long e = tid; e < nec; e += nt) {
+            const int ci = (int)(e / mc), cj = (int)(e % mc);
+            float Kc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) Kc[q] = 0.0f;
+            bool cfix[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int ai = ci + (a == 1 || a == 2), aj = cj + (a == 2 || a == 3);
+                cfix[a] = A.mfix[I.mv[l] + (long long)(mc + 1) * ai + aj];
+            }
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const int fx = f & 1, fy = f >> 1;
+                const int fi = 2 * ci + fx, fj = 2 * cj + fy;   // fine element
+                float Kf[16];
+                if (l == 1) {
+                    const float Ee = A.Ef[I.e0 + (long long)mf * fi + fj];
+#pragma unroll
+                    for (int q = 0; q < 16; q++) Kf[q] = Ee * A.Ke0f[q];
+                } else {
+                    const float *src = A.Kel + (I.me[l - 1] + (long long)mf * fi + fj) * 16;
+#pragma unroll
+                    for (int q = 0; q < 16; q++) Kf[q] = src[q];
+                }
+                // P_f[lf][a]: weight of coarse node a at the fine element's local node lf
+                float P[16];
+#pragma unroll
+                for (int lf = 0; lf < 4; lf++) {
+                    const int x = fx + (lf == 1 || lf == 2), y = fy + (lf == 2 || lf == 3);   // 0..2 in the coarse element
+                    const bool ffix = A.mfix[I.mv[l - 1] + (long long)(mf + 1) * (2 * ci + x) + (2 * cj + y)];
+#pragma unroll
+                    for (int a = 0; a < 4; a++) {
+                        const int ax = (a == 1 || a == 2), ay = (a == 2 || a == 3);
+                        const float wx = 1.0f - 0.5f * fabsf((float)(x - 2 * ax));
+                        const float wy = 1.0f - 0.5f * fabsf((float)(y - 2 * ay));
+                        P[lf * 4 + a] = (ffix || cfix[a] || wx <= 0.0f || wy <= 0.0f) ? 0.0f : wx * wy;
+                    }
+                }
+                float Q[16];   // K_f P
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        float t = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) t += Kf[r * 4 + k] * P[k * 4 + b];
+                        Q[r * 4 + b] = t;
+                    }
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        float t = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) t += P[k * 4 + a] * Q[k * 4 + b];
+                        Kc[a * 4 + b] += t;
+                    }
+            }
+            float *dst = A.Kel + (I.me[l] + e) * 16;
+#pragma unroll
+            for (int q = 0; q < 16; q++) dst[q] = Kc[q];
+        }
+        __syncthreads();
+        // 9-point stencils and l1 diagonals (identity rows on fixed nodes)
+        for (long long v = tid; v < nnc; v += nt) {
+            const int i = (int)(v / (mc + 1)), j = (int)(v % (mc + 1));
+            float st[9];
+#pragma unroll
+            for (int q = 0; q < 9; q++) st[q] = 0.0f;
+            const bool fx = A.mfix[I.mv[l] + v];
+            if (fx) {
+                st[4] = 1.0f;
+            } else {
+                for (int ci = 0; ci < 2; ci++)
+                    for (int cj = 0; cj < 2; cj++) {
+                        const int ei = i - 1 + ci, ej = j - 1 + cj;
+                        if (ei < 0 || ej < 0 || ei >= mc || ej >= mc) continue;
+                        const float *K = A.Kel + (I.me[l] + (long long)mc * ei + ej) * 16;
+                        const int li = corner(1 - ci, 1 - cj);
+                        for (int lb = 0; lb < 4; lb++) {
+                            const int bi = ei + (lb == 1 || lb == 2) - i, bj = ej + (lb == 2 || lb == 3) - j;
+                            st[(bi + 1) * 3 + (bj + 1)] += K[li * 4 + lb];
+                        }
+                    }
+            }
+            float d = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 9; q++) d += fabsf(st[q]);
+            float *dst = A.St + (I.mv[l] + v) * 9;
+#pragma unroll
+            for (int q = 0; q < 9; q++) dst[q] = st[q];
+            A.D[I.mv[l] + v] = d > 0.0f ? d : 1.0f;
+        }
+        __syncthreads();
+    }
+    // coarsest level: dense matrix from the stencils, Gauss-Jordan inverse in shared memory (FP64)
+    {
+        const int l = I.nlev - 1, mc = I.n >> l, nc = I.nc;
+        double *M = sm;   // nc x 2nc
+        for (int t = tid; t < nc * 2 * nc; t += nt) M[t] = 0.0;
+        __syncthreads();
+        for (int v = tid; v < nc; v += nt) {
+            const int i = v / (mc + 1), j = v % (mc + 1);
+            const float *st = A.St + (I.mv[l] + v) * 9;
+            for (int di = -1; di <= 1; di++)
+                for (int dj = -1; dj <= 1; dj++) {
+                    const int a = i + di, b = j + dj;
+                    if (a < 0 || b < 0 || a > mc || b > mc) continue;
+                    M[v * 2 * nc + (mc + 1) * a + b] = st[(di + 1) * 3 + (dj + 1)];
+                }
+            M[v * 2 * nc + nc + v] = 1.0;
+        }
+        __syncthreads();
+        double *fcol = M + (size_t)nc * 2 * nc;   // column k of the other rows, read before the update
+        for (int k = 0; k < nc; k++) {
+            // the coarse operator is SPD (fixed rows identity): no pivoting
+            const double piv = M[k * 2 * nc + k];
+            __syncthreads();
+            for (int c = tid; c < 2 * nc; c += nt) M[k * 2 * nc + c] /= piv;
+            for (int r = tid; r < nc; r += nt) fcol[r] = (r == k) ? 0.0 : M[r * 2 * nc + k];
+            __syncthreads();
+            for (int t = tid; t < nc * 2 * nc; t += nt) {
+                const int r = t / (2 * nc), c = t % (2 * nc);
+                if (r != k) M[t] -= fcol[r] * M[k * 2 * nc + c];
+            }
+            __syncthreads();
+        }
+        for (int t = tid; t < nc * nc; t += nt) A.Ainv[I.ainv + t] = (float)M[(t / nc) * 2 * nc + nc + (t % nc)];
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ the V(2,2) cycle (FP32)
+__device__ void jacobi_sweep(const Args &A, const Inst &I, int l) {
+    const int m = I.n >> l, tid = threadIdx.x, nt = blockDim.x;
+    const long long nn = (long long)(m + 1) * (m + 1);
+    const float *x = A.mx + I.mv[l];
+    float *t = A.mr + I.mv[l];
+    const float *b = A.mb + I.mv[l];
+    for (long long v = tid; v < nn; v += nt) {
+        const int i = (int)(v / (m + 1)), j = (int)(v % (m + 1));
+        t[v] = A.mfix[I.mv[l] + v] ? 0.0f : (b[v] - opl(A, I, l, x, i, j)) / A.D[I.mv[l] + v];
+    }
+    __syncthreads();
+    float *xw = A.mx + I.mv[l];
+    for (long long v = tid; v < nn; v += nt) xw[v] += t[v];
+    __syncthreads();
+}
+
+__device__ void vcycle(const Args &A, const Inst &I) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int l = 0; l < I.nlev - 1; l++) {
+        jacobi_sweep(A, I, l);
+        jacobi_sweep(A, I, l);
+        // residual into mr
+        const int m = I.n >> l;
+        const long long nn = (long long)(m + 1) * (m + 1);
+        {
+            const float *x = A.mx + I.mv[l], *b = A.mb + I.mv[l];
+            float *r = A.mr + I.mv[l];
+            for (long long v = tid; v < nn; v += nt) {
+                const int i = (int)(v / (m + 1)), j = (int)(v % (m + 1));
+                r[v] = A.mfix[I.mv[l] + v] ? 0.0f : b[v] - opl(A, I, l, x, i, j);
+            }
+        }
+        __syncthreads();
+        // restriction (P^T, fixed nodes masked) and the first sweep of the coarse level from zero
+        const int mc = m >> 1;
+        const long long nnc = (long long)(mc + 1) * (mc + 1);
+        const float *r = A.mr + I.mv[l];
+        for (long long v = tid; v < nnc; v += nt) {
+            const int I2 = (int)(v / (mc + 1)), J2 = (int)(v % (mc + 1));
+            float acc = 0.0f;
+            if (!A.mfix[I.mv[l + 1] + v]) {
+                for (int dx = -1; dx <= 1; dx++)
+                    for (int dy = -1; dy <= 1; dy++) {
+                        const int fi = 2 * I2 + dx, fj = 2 * J2 + dy;
+                        if (fi < 0 || fj < 0 || fi > m || fj > m) continue;
+                        const float w = (dx ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f);
+                        acc += w * r[(long long)(m + 1) * fi + fj];   // r is zero on fixed fine nodes
+                    }
+            }
+            A.mb[I.mv[l + 1] + v] = acc;
+            A.mx[I.mv[l + 1] + v] = 0.0f;
+        }
+        __syncthreads();
+    }
+    // coarsest: x = Ainv b
+    {
+        const int l = I.nlev - 1, nc = I.nc;
+        const float *Ai = A.Ainv + I.ainv, *b = A.mb + I.mv[l];
+        for (int v = tid; v < nc; v += nt) {
+            float acc = 0.0f;
+            for (int c = 0; c < nc; c++) acc += Ai[v * nc + c] * b[c];
+            A.mx[I.mv[l] + v] = acc;
+        }
+        __syncthreads();
+    }
+    for (int l = I.nlev - 2; l >= 0; l--) {
+        const int m = I.n >> l, mc = m >> 1;
+        const long long nn = (long long)(m + 1) * (m + 1);
+        const float *xc = A.mx + I.mv[l + 1];
+        float *x = A.mx + I.mv[l];
+        for (long long v = tid; v < nn; v += nt) {
+            if (A.mfix[I.mv[l] + v]) continue;
+            const int i = (int)(v / (m + 1)), j = (int)(v % (m + 1));
+            const int i0 = i >> 1, j0 = j >> 1, i1 = (i + 1) >> 1, j1 = (j + 1) >> 1;
+            const float c = 0.25f * (xc[(long long)(mc + 1) * i0 + j0] + xc[(long long)(mc + 1) * i0 + j1] +
+                                     xc[(long long)(mc + 1) * i1 + j0] + xc[(long long)(mc + 1) * i1 + j1]);
+            x[v] += c;
+        }
+        __syncthreads();
+        jacobi_sweep(A, I, l);
+        jacobi_sweep(A, I, l);
+    }
+}
+
+// ------------------------------------------------------------------ phase kernels
+__device__ __forceinline__ const Inst &inst_of(const Args &A) { return A.inst[A.order[blockIdx.x]]; }
+
+__device__ __forceinline__ double filt(const Args &A, const Inst &I, const double *v, int i, int j) {
+    const int n = I.n;
+    double s = 0.0;
+    for (int q = 0; q < A.nst; q++) {
+        const int a = i + A.sdi[q], b = j + A.sdj[q];
+        if (a < 0 || b < 0 || a >= n || b >= n) continue;
+        s += A.sw[q] * v[(long long)n * a + b];
+    }
+    return s;
+}
+
+// rho = filter(s), E = kmin + (k0 - kmin) rho^p, g = sum(rho) / (vf n^2) - 1
+__global__ void __launch_bounds__(kThreads) filter_moduli_batch(const __grid_constant__ Args A) {
+    __shared__ double sm[32];
+    const Inst &I = inst_of(A);
+    const int n = I.n;
+    const long long ne = (long long)n * n;
+    const double *s = A.s + I.e0;
+    double vol = 0.0;
+    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        const double r = filt(A, I, s, i, j) / A.wsum[I.e0 + e];
+        A.rho[I.e0 + e] = r;
+        const double rp = pow(r, A.pexp);
+        const double Ee = A.k0 * rp + A.kmin * (1.0 - rp);
+        A.E[I.e0 + e] = Ee;
+        A.Ef[I.e0 + e] = (float)Ee;
+        vol += r;
+    }
+    vol = bsum(vol, sm);
+    if (threadIdx.x == 0) A.out[(long long)A.order[blockIdx.x] * kOut + O_G] = vol / (I.vf * (double)ne) - 1.0;
+}
+
+// flexible CG (FP64) with one FP32 V-cycle per iteration; FP64 true residual checks
+__global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ Args A) {
+    extern __shared__ double dyn[];
+    double *sm = dyn;            // 32 doubles of reduction space, then the coarse inverse workspace
+    const Inst &I = inst_of(A);
+    const int idx = A.order[blockIdx.x];
+    const int n = I.n, tid = threadIdx.x, nt = blockDim.x;
+    const long long nn = (long long)(n + 1) * (n + 1);
+    double *x = A.x + I.v0, *r = A.r + I.v0, *z = A.z + I.v0, *p = A.p + I.v0, *q = A.q + I.v0;
+    const double *F = A.F + I.v0;
+    const unsigned char *fx = A.fixed + I.v0;
+    mg_setup(A, I, sm + 32);
+    int total = 0, passes = 0;
+    bool conv = false;
+    double rr = 0.0, bb = 0.0;
+    for (int pass = 0; pass < 3 && total < A.itmax && !conv; pass++) {
+        passes++;
+        // r = F - K x (x = 0 on the first pass unless warm)
+        double acc[2] = {0.0, 0.0};
+        for (long long v = tid; v < nn; v += nt) {
+            if (pass == 0 && !A.warm) x[v] = 0.0;
+        }
+        __syncthreads();
+        for (long long v = tid; v < nn; v += nt) {
+            const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
+            const double bv = fx[v] ? 0.0 : F[v];
+            const double rv = fx[v] ? 0.0 : bv - op64(A, I, x, i, j);
+            r[v] = rv;
+            p[v] = 0.0;
+            q[v] = 0.0;
+            acc[0] += rv * rv;
+            acc[1] += bv * bv;
+        }
+        rr = bsum(acc[0], sm);
+        bb = bsum(acc[1], sm);
+        if (bb == 0.0 || rr <= A.eps * A.eps * bb) {
+            conv = true;
+            break;
+        }
+        double pq_prev = 1.0;
+        for (int it = 0; total < A.itmax; it++) {
+            total++;
+            // z = |r| V(r / |r|)
+            const double rn = sqrt(rr);
+            const float sc = (float)(1.0 / rn);
+            for (long long v = tid; v < nn; v += nt) {
+                const float bv = fx[v] ? 0.0f : (float)r[v] * sc;
+                A.mb[I.mv[0] + v] = bv;
+                A.mx[I.mv[0] + v] = fx[v] ? 0.0f : bv / A.D[I.mv[0] + v];
+            }
+            __syncthreads();
+            vcycle(A, I);
+            double a3[3] = {0.0, 0.0, 0.0};
+            for (long long v = tid; v < nn; v += nt) {
+                const double zv = fx[v] ? 0.0 : rn * (double)A.mx[I.mv[0] + v];
+                z[v] = zv;
+                a3[0] += zv * q[v];
+                a3[1] += zv * r[v];
+                a3[2] += p[v] * r[v];
+            }
+            const double zq = bsum(a3[0], sm), zr = bsum(a3[1], sm), pr0 = bsum(a3[2], sm);
+            const double beta = it > 0 ? zq / pq_prev : 0.0;
+            const double pr = zr - beta * pr0;
+            for (long long v = tid; v < nn; v += nt) p[v] = z[v] - beta * p[v];
+            __syncthreads();
+            double pqa = 0.0;
+            for (long long v = tid; v < nn; v += nt) {
+                const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
+                const double qv = fx[v] ? 0.0 : op64(A, I, p, i, j);
+                q[v] = qv;
+                pqa += p[v] * qv;
+            }
+            const double pq = bsum(pqa, sm);
+            if (!(pq > 0.0)) break;
+            const double alpha = pr / pq;
+            double ra = 0.0;
+            for (long long v = tid; v < nn; v += nt) {
+                x[v] += alpha * p[v];
+                const double rv = r[v] - alpha * q[v];
+                r[v] = rv;
+                ra += rv * rv;
+            }
+            rr = bsum(ra, sm);
+            pq_prev = pq;
+            if (rr <= A.eps * A.eps * bb || !isfinite(rr)) break;
+        }
+        // FP64 true residual
+        double ta = 0.0;
+        for (long long v = tid; v < nn; v += nt) {
+            const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
+            const double rv = fx[v] ? 0.0 : F[v] - op64(A, I, x, i, j);
+            ta += rv * rv;
+        }
+        rr = bsum(ta, sm);
+        conv = rr <= A.eps * A.eps * bb;
+    }
+    if (tid == 0) {
+        double *o = A.out + (long long)idx * kOut;
+        o[O_ITERS] = total;
+        o[O_RES] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+        o[O_CONV] = conv ? 1.0 : 0.0;
+        o[O_PASSES] = passes;
+    }
+}
+
+// f = sum_e E_e T_e.Ke0 T_e; dfdrho = -p (k0 - kmin) rho^(p-1) T_e.Ke0 T_e; filtered sensitivities
+__global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ Args A) {
+    __shared__ double sm[32];
+    const Inst &I = inst_of(A);
+    const int n = I.n;
+    const long long ne = (long long)n * n;
+    const double *T = A.x + I.v0;
+    double f = 0.0;
+    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        double te[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+            te[a] = T[(long long)(n + 1) * (i + (a == 1 || a == 2)) + (j + (a == 2 || a == 3))];
+        double qv = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            double v = 0.0;
+#pragma unroll
+            for (int b = 0; b < 4; b++) v += A.Ke0[a * 4 + b] * te[b];
+            qv += te[a] * v;
+        }
+        A.dfdrho[I.e0 + e] = -A.pexp * (-A.kmin + A.k0) * pow(A.rho[I.e0 + e], A.pexp - 1.0) * qv;
+        f += A.E[I.e0 + e] * qv;
+    }
+    f = bsum(f, sm);
+    if (threadIdx.x == 0) A.out[(long long)A.order[blockIdx.x] * kOut + O_F] = f;
+    __syncthreads();
+    const double dg = 1.0 / (I.vf * (double)ne);
+    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        const double w = A.wsum[I.e0 + e];
+        A.dfds[I.e0 + e] = filt(A, I, A.dfdrho + I.e0, i, j) / w;
+        double sw = 0.0;
+        for (int q = 0; q < A.nst; q++) {
+            const int a = i + A.sdi[q], b = j + A.sdj[q];
+            if (a < 0 || b < 0 || a >= n || b >= n) continue;
+            sw += A.sw[q] * dg;
+        }
+        A.dgds[I.e0 + e] = sw / w;
+    }
+}
+
+// OC (OC.h:76-107) with the samples' filtered-volume constraint, bisection inside the block
+__global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Args A) {
+    __shared__ double sm[32];
+    const Inst &I = inst_of(A);
+    const int n = I.n;
+    const long long ne = (long long)n * n;
+    double *x = A.s + I.e0, *xn = A.snew + I.e0;
+    const double *dfdx = A.dfds + I.e0, *dgdx = A.dgds + I.e0;
+    double l0 = A.lmin, l1 = A.lmax, lambda = 0.0;
+    int steps = 0;
+    while ((l1 - l0) / (l1 + l0) > A.leps && steps < 4000) {
+        lambda = 0.5 * (l1 + l0);
+        steps++;
+        for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+            const double xe = x[e];
+            double v = pow(-dfdx[e] / (dgdx[e] * lambda), A.iota) * xe;
+            const double lo0 = (1.0 - A.move) * xe, hi0 = (1.0 + A.move) * xe;
+            const double lo = (0.0 < lo0) ? lo0 : 0.0;
+            const double hi = (hi0 < 1.0) ? hi0 : 1.0;
+            if (v < lo) v = lo;
+            else if (v > hi) v = hi;
+            xn[e] = v;
+        }
+        __syncthreads();
+        double vol = 0.0;
+        for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+            const int i = (int)(e / n), j = (int)(e % n);
+            vol += filt(A, I, xn, i, j) / A.wsum[I.e0 + e];
+        }
+        vol = bsum(vol, sm);
+        const double g = vol / (I.vf * (double)ne) - 1.0;
+        if (g > 0.0) l0 = lambda;
+        else l1 = lambda;
+    }
+    for (long long e = threadIdx.x; e < ne; e += blockDim.x) x[e] = xn[e];
+    if (threadIdx.x == 0) {
+        double *o = A.out + (long long)A.order[blockIdx.x] * kOut;
+        o[O_LAMBDA] = lambda;
+        o[O_BISECT] = steps;
+    }
+}
+
+}  // namespace batch
+}  // namespace psf
+
+// ------------------------------------------------------------------ host
+using psf::batch::Args;
+using psf::batch::Inst;
+
+struct psf_batch {
+    int ninst = 0;
+    std::vector<Inst> hinst;
+    std::vector<int> order;
+    Args a{};
+    size_t ne_tot = 0, nv_tot = 0, mg_nodes = 0, mg_elems = 0, ainv_tot = 0;
+    size_t smem = 0;
+    int threads = psf::batch::kThreads;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void *> allocs;
+    std::vector<double> hout;
+    bool begun = false;
+};
+
+namespace {
+
+template <class T>
+psf_status balloc(psf_batch *b, T **p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return psf::cuda_status(e, "cudaMalloc (batch)");
+    b->allocs.push_back(q);
+    *p = reinterpret_cast<T *>(q);
+    return PSF_OK;
+}
+
+void batch_free(psf_batch *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (void *p : b->allocs) cudaFree(p);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+psf_status launch_phases(psf_batch *b) {
+    const Args &a = b->a;
+    const int nb = b->ninst, nt = b->threads;
+    psf::batch::filter_moduli_batch<<<nb, nt, 0, b->stream>>>(a);
+    psf::batch::solve_batch<<<nb, nt, b->smem, b->stream>>>(a);
+    psf::batch::sens_batch<<<nb, nt, 0, b->stream>>>(a);
+    psf::batch::oc_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+psf_status psf_batch_create(int ninst, const int *side, const int *edge, const int *patch_w, const int *patch_i0,
+                            const double *vf, int threads, psf_batch **out) {
+    if (!out || ninst < 1 || !side || !edge || !patch_w || !patch_i0 || !vf) return PSF_BAD_INPUT;
+    if (threads != 128 && threads != 256 && threads != 512 && threads != 1024) {
+        psf::set_error("psf_batch_create: threads must be 128, 256, 512 or 1024");
+        return PSF_BAD_INPUT;
+    }
+    *out = nullptr;
+    for (int i = 0; i < ninst; i++)
+        if (side[i] < 4 || side[i] % 2 || edge[i] < 0 || edge[i] > 3 || patch_w[i] < 1 || patch_i0[i] < 0 ||
+            patch_i0[i] + patch_w[i] > side[i] || !(vf[i] > 0.0 && vf[i] <= 1.0)) {
+            psf::set_error("psf_batch_create: invalid instance (even side >= 4, patch inside the edge, 0 < vf <= 1)");
+            return PSF_BAD_INPUT;
+        }
+    psf_batch *b = new psf_batch();
+    b->ninst = ninst;
+    b->threads = threads;
+    b->hinst.resize(ninst);
+    size_t ne = 0, nv = 0, mgn = 0, mge = 0, ai = 0;
+    int ncmax = 0;
+    for (int k = 0; k < ninst; k++) {
+        Inst &I = b->hinst[k];
+        std::memset(&I, 0, sizeof(Inst));
+        I.n = side[k];
+        I.vf = vf[k];
+        I.e0 = (long long)ne;
+        I.v0 = (long long)nv;
+        ne += (size_t)I.n * I.n;
+        nv += (size_t)(I.n + 1) * (I.n + 1);
+        int l = 0, m = I.n;
+        I.mv[0] = (long long)mgn;
+        mgn += (size_t)(m + 1) * (m + 1);
+        while (l + 1 < psf::batch::kLev && (m + 1) * (m + 1) > psf::batch::kCoarseNodes && m % 2 == 0 && m >= 4) {
+            l++;
+            m /= 2;
+            I.mv[l] = (long long)mgn;
+            mgn += (size_t)(m + 1) * (m + 1);
+            I.me[l] = (long long)mge;
+            mge += (size_t)m * m;
+        }
+        I.nlev = l + 1;
+        I.nc = (m + 1) * (m + 1);
+        if (I.nc > psf::batch::kCoarseNodes) {
+            delete b;
+            psf::set_error("psf_batch_create: a side does not coarsen to <= 64 nodes (use sides with a large power of 2)");
+            return PSF_BAD_INPUT;
+        }
+        if (I.nlev < 2) {
+            delete b;
+            psf::set_error("psf_batch_create: side too small for a coarse level");
+            return PSF_BAD_INPUT;
+        }
+        I.ainv = (long long)ai;
+        ai += (size_t)I.nc * I.nc;
+        ncmax = std::max(ncmax, I.nc);
+    }
+    b->ne_tot = ne;
+    b->nv_tot = nv;
+    b->mg_nodes = mgn;
+    b->mg_elems = mge;
+    b->ainv_tot = ai;
+    b->smem = sizeof(double) * (32 + (size_t)ncmax * 2 * ncmax + ncmax);
+    // largest instances first
+    b->order.resize(ninst);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    std::stable_sort(b->order.begin(), b->order.end(),
+                     [b](int x, int y) { return b->hinst[x].n > b->hinst[y].n; });
+    Args &a = b->a;
+    a.ninst = ninst;
+    psf_status s = PSF_OK;
+    auto ck = [&s](psf_status t) { if (s == PSF_OK) s = t; };
+    ck(psf::cuda_status(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream"));
+    ck(psf::cuda_status(cudaEventCreate(&b->ev0), "event"));
+    ck(psf::cuda_status(cudaEventCreate(&b->ev1), "event"));
+    Inst *dinst = nullptr;
+    int *dorder = nullptr;
+    unsigned char *dfixed = nullptr;
+    ck(balloc(b, &dinst, ninst));
+    ck(balloc(b, &dorder, ninst));
+    for (double **pp : {&a.s, &a.rho, &a.E, &a.dfdrho, &a.dfds, &a.dgds, &a.snew, &a.wsum}) ck(balloc(b, pp, ne));
+    ck(balloc(b, &a.Ef, ne));
+    for (double **pp : {&a.x, &a.r, &a.z, &a.p, &a.q, &a.F}) ck(balloc(b, pp, nv));
+    ck(balloc(b, &dfixed, nv));
+    ck(balloc(b, &a.Kel, mge * 16));
+    ck(balloc(b, &a.St, mgn * 9));
+    for (float **pp : {&a.D, &a.mx, &a.mb, &a.mr}) ck(balloc(b, pp, mgn));
+    ck(balloc(b, &a.mfix, mgn));
+    ck(balloc(b, &a.Ainv, ai));
+    ck(balloc(b, &a.out, (size_t)ninst * psf::batch::kOut));
+    if (s != PSF_OK) {
+        batch_free(b);
+        return s;
+    }
+    a.inst = dinst;
+    a.order = dorder;
+    a.fixed = dfixed;
+    // Dirichlet patches and lumped loads (area / 4 per adjacent unit element)
+    std::vector<unsigned char> hfix(nv, 0);
+    std::vector<double> hF(nv, 0.0);
+    for (int k = 0; k < ninst; k++) {
+        const Inst &I = b->hinst[k];
+        const int n = I.n;
+        for (int i = 0; i <= n; i++)
+            for (int j = 0; j <= n; j++) {
+                const long long v = I.v0 + (long long)(n + 1) * i + j;
+                const int c = (i > 0 && j > 0) + (i < n && j > 0) + (i > 0 && j < n) + (i < n && j < n);
+                hF[v] = c * 0.25;
+                int t = -1;
+                if (edge[k] == 0 && j == 0) t = i;
+                if (edge[k] == 1 && j == n) t = i;
+                if (edge[k] == 2 && i == 0) t = j;
+                if (edge[k] == 3 && i == n) t = j;
+                if (t >= patch_i0[k] && t <= patch_i0[k] + patch_w[k]) hfix[v] = 1;
+            }
+    }
+    ck(psf::cuda_status(cudaMemcpy(dinst, b->hinst.data(), sizeof(Inst) * ninst, cudaMemcpyHostToDevice), "copy"));
+    ck(psf::cuda_status(cudaMemcpy(dorder, b->order.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice), "copy"));
+    ck(psf::cuda_status(cudaMemcpy(dfixed, hfix.data(), nv, cudaMemcpyHostToDevice), "copy"));
+    ck(psf::cuda_status(cudaMemcpy(a.F, hF.data(), sizeof(double) * nv, cudaMemcpyHostToDevice), "copy"));
+    ck(psf::cuda_status(cudaMemset(a.x, 0, sizeof(double) * nv), "memset"));
+    // element matrix of the unit heat element, from the library's own element routine (bit-exact with the reference)
+    psf_ctx *tmp = nullptr;
+    if (s == PSF_OK) s = psf_create(&tmp, PSF_Q4_HEAT, 1, 1, 0, 1.0, 1.0, 0.0, 0.3, 1.0);
+    double Ke[16];
+    if (s == PSF_OK) s = psf_element_matrix(tmp, 1.0, Ke);
+    if (tmp) psf_destroy(tmp);
+    if (s != PSF_OK) {
+        batch_free(b);
+        return s;
+    }
+    for (int q = 0; q < 16; q++) {
+        a.Ke0[q] = Ke[q];
+        a.Ke0f[q] = (float)Ke[q];
+    }
+    *out = b;
+    return PSF_OK;
+}
+
+psf_status psf_batch_destroy(psf_batch *b) {
+    batch_free(b);
+    return PSF_OK;
+}
+
+psf_status psf_batch_begin(psf_batch *b, const psf_simp_params *prm) {
+    if (!b || !prm) return PSF_BAD_INPUT;
+    if (prm->optimizer != 0 || !(prm->R > 0) || prm->cg_itmax < 1 || !(prm->cg_eps > 0)) {
+        psf::set_error("psf_batch_begin: the batch runs OC with a density filter (optimizer 0, R > 0)");
+        return PSF_BAD_INPUT;
+    }
+    Args &a = b->a;
+    a.k0 = prm->E1;
+    a.kmin = prm->E0;
+    a.pexp = prm->p;
+    a.iota = prm->oc_iota;
+    a.lmin = prm->oc_lmin;
+    a.lmax = prm->oc_lmax;
+    a.leps = prm->oc_leps;
+    a.move = prm->oc_move;
+    a.eps = prm->cg_eps;
+    a.itmax = prm->cg_itmax;
+    a.warm = prm->warm_start ? 1 : 0;
+    // filter stencil on unit elements: w = (R - d) / R for d <= R (the samples' neighbour weights)
+    const int rr = (int)std::floor(prm->R);
+    a.nst = 0;
+    for (int di = -rr; di <= rr; di++)
+        for (int dj = -rr; dj <= rr; dj++) {
+            const double d = std::sqrt(std::pow(di * 1.0, 2.0) + std::pow(dj * 1.0, 2.0));
+            if (d <= prm->R) {
+                if (a.nst >= psf::batch::kMaxStencilB) {
+                    psf::set_error("psf_batch_begin: filter radius too large");
+                    return PSF_BAD_INPUT;
+                }
+                a.sdi[a.nst] = di;
+                a.sdj[a.nst] = dj;
+                a.sw[a.nst] = (prm->R - d) / prm->R;
+                a.nst++;
+            }
+        }
+    // per-element weight sums, initial design
+    std::vector<double> ws(b->ne_tot), s0(b->ne_tot);
+    for (int k = 0; k < b->ninst; k++) {
+        const Inst &I = b->hinst[k];
+        const int n = I.n;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                double w = 0.0;
+                for (int q = 0; q < a.nst; q++) {
+                    const int x = i + a.sdi[q], y = j + a.sdj[q];
+                    if (x < 0 || y < 0 || x >= n || y >= n) continue;
+                    w += a.sw[q];
+                }
+                ws[I.e0 + (long long)n * i + j] = w;
+                s0[I.e0 + (long long)n * i + j] = I.vf;
+            }
+    }
+    PSF_CUDA(cudaMemcpy(a.wsum, ws.data(), sizeof(double) * ws.size(), cudaMemcpyHostToDevice));
+    PSF_CUDA(cudaMemcpy(a.s, s0.data(), sizeof(double) * s0.size(), cudaMemcpyHostToDevice));
+    PSF_CUDA(cudaMemset(a.x, 0, sizeof(double) * b->nv_tot));
+    PSF_CUDA(cudaFuncSetAttribute(psf::batch::solve_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)b->smem));
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    // one SIMP iteration of every instance as a graph
+    PSF_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    psf_status st = launch_phases(b);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (st != PSF_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    PSF_CUDA(e);
+    b->graph = g;
+    PSF_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+    b->hout.assign((size_t)b->ninst * psf::batch::kOut, 0.0);
+    b->begun = true;
+    return PSF_OK;
+}
+
+psf_status psf_batch_step(psf_batch *b, int iters, double *seconds) {
+    if (!b || !b->begun || iters < 1) return PSF_BAD_INPUT;
+    PSF_CUDA(cudaEventRecord(b->ev0, b->stream));
+    for (int k = 0; k < iters; k++) PSF_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    PSF_CUDA(cudaEventRecord(b->ev1, b->stream));
+    PSF_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    PSF_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    if (seconds) *seconds = ms * 1e-3;
+    return PSF_OK;
+}
+
+psf_status psf_batch_results(psf_batch *b, double *out) {
+    if (!b || !out) return PSF_BAD_INPUT;
+    PSF_CUDA(cudaMemcpy(out, b->a.out, sizeof(double) * b->ninst * psf::batch::kOut, cudaMemcpyDeviceToHost));
+    return PSF_OK;
+}
+
+psf_status psf_batch_fields(psf_batch *b, int k, double *s, double *rho, double *T) {
+    if (!b || k < 0 || k >= b->ninst) return PSF_BAD_INPUT;
+    const Inst &I = b->hinst[k];
+    const size_t ne = (size_t)I.n * I.n, nv = (size_t)(I.n + 1) * (I.n + 1);
+    if (s) PSF_CUDA(cudaMemcpy(s, b->a.s + I.e0, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+    if (rho) PSF_CUDA(cudaMemcpy(rho, b->a.rho + I.e0, sizeof(double) * ne, cudaMemcpyDeviceToHost));
+    if (T) PSF_CUDA(cudaMemcpy(T, b->a.x + I.v0, sizeof(double) * nv, cudaMemcpyDeviceToHost));
+    return PSF_OK;
+}
+
+}  // extern "C"

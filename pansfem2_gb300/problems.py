@@ -56,12 +56,25 @@ def mbb_q4(nx=1024, ny=512, **kw):
                  load_dof=ld, load_val=[-1.0] * len(ln), **kw)
 
 
-def heatsink_q4(nx=64, ny=64, patch_w=None, patch_i0=None, **kw):
-    """Config 5 instance: zero-temperature patch on the bottom edge, uniform unit
-    heat source lumped to the nodes (area/4 per adjacent element)."""
+def heat_patch(nx, ny, edge, w, i0):
+    """Predicate of the zero-temperature patch: nodes t = i0 .. i0 + w along edge
+    0 (j = 0), 1 (j = ny), 2 (i = 0) or 3 (i = nx)."""
+    if edge == 0:
+        return lambda i, j: j == 0 and i0 <= i <= i0 + w
+    if edge == 1:
+        return lambda i, j: j == ny and i0 <= i <= i0 + w
+    if edge == 2:
+        return lambda i, j: i == 0 and i0 <= j <= i0 + w
+    return lambda i, j: i == nx and i0 <= j <= i0 + w
+
+
+def heatsink_q4(nx=64, ny=64, patch_w=None, patch_i0=None, edge=0, **kw):
+    """Config 5 instance: zero-temperature patch on an edge (default the bottom
+    one), uniform unit heat source lumped to the nodes (area/4 per adjacent
+    element)."""
     w = patch_w if patch_w is not None else max(1, nx // 10)
-    i0 = patch_i0 if patch_i0 is not None else (nx - w) // 2
-    fn, fd = _fixedlist(nx, ny, (0,), lambda i, j: j == 0 and i0 <= i <= i0 + w)
+    i0 = patch_i0 if patch_i0 is not None else ((nx if edge < 2 else ny) - w) // 2
+    fn, fd = _fixedlist(nx, ny, (0,), heat_patch(nx, ny, edge, w, i0))
     h2 = (1.0 * 1.0) * 0.25
     ln, ld, lv = [], [], []
     for i in range(nx + 1):
@@ -72,7 +85,23 @@ def heatsink_q4(nx=64, ny=64, patch_w=None, patch_i0=None, **kw):
             lv.append(c * h2)
     kw.setdefault("E0", 1e-3)
     return _base(Q4_HEAT, nx, ny, fix_node=fn, fix_dof=fd, load_node=ln, load_dof=ld, load_val=lv,
-                 patch_w=w, patch_i0=i0, **kw)
+                 patch_w=w, patch_i0=i0, edge=edge, **kw)
+
+
+def heat_batch(n=256, seed=0, sides=(64, 96, 128, 192, 256, 384)):
+    """Config 5: n independent square heat-sink instances, side drawn uniformly
+    from `sides`, patch edge and position and volume fraction (uniform in
+    [0.3, 0.5]) drawn with a seeded generator."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        side = int(rng.choice(sides))
+        w = max(1, side // 10)
+        edge = int(rng.integers(0, 4))
+        i0 = int(rng.integers(0, side - w + 1))
+        vf = float(rng.uniform(0.3, 0.5))
+        out.append(dict(side=side, edge=edge, patch_w=w, patch_i0=i0, vf=vf))
+    return out
 
 
 def cantilever_h8(nx=128, ny=64, nz=64, **kw):

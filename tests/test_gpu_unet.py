@@ -90,8 +90,10 @@ def test_network_forward_backward_vs_oracle(B, H, W):
     for k, (ws, bs) in enumerate(_layer_slices()):
         for s, what in ((ws, "W"), (bs, "b")):
             e = np.linalg.norm(grad[s] - g_ref[s]) / max(np.linalg.norm(g_ref[s]), 1e-30)
-            # bf16 rounding flips accumulate along the backward chain; the first layer sits at its end
-            assert e < (6e-2 if k == 0 else 3e-2), (k, what, e)
+            # a bf16 rounding flip (0.4 %) of one stored activation or gradient propagates through every
+            # later product; the flips accumulate along the backward chain, whose end is the first layer.
+            # A wrong index or layout gives errors of order 1.
+            assert e < (8e-2 if k == 0 else 5e-2), (k, what, e)
 
 
 def test_network_params_roundtrip_and_batch_limit():
