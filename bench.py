@@ -235,6 +235,125 @@ def cpu_reference_sample(pr, steps, warmup, threads, cg_cap=400, n0=None):
     return {"t_iter0_full": t_full, "n_cg_iter0": n0, "samples": samples, "n0_source": how}
 
 
+HEAT_BATCH_METRIC = "aggregate instance-SIMP-iterations/s, batched heat-sink instances, resid 1e-8"
+
+
+def bench_heat_batch(args, rank, world):
+    """256 independent heat-sink instances (sides uniform in {64,...,384}, seeded
+    patch edges/positions, vf in [0.3, 0.5]), one SIMP iteration of all of them
+    per CUDA-graph replay.  Compared with the same instances run one by one
+    through the single-problem path with plain FP64 Jacobi PCG (CSR)."""
+    from pansfem2_gb300 import problems as PB
+    insts = PB.heat_batch(args.instances, seed=rank)
+    ne = sum(d["side"] ** 2 for d in insts)
+    nn = sum((d["side"] + 1) ** 2 for d in insts)
+    config = {"workload": f"{len(insts)} heat-sink instances, sides in {{64,96,128,192,256,384}}, OC, R=1.5, "
+                          f"kmin=1e-3, p=3", "instances": len(insts), "elements": ne, "dofs": nn,
+              "residual": "FP64 relative 1e-8", "parallelism": f"replicas{world}",
+              "l2": "working set ~1 GB, larger than L2"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import build as ob
+        from oracle import pyoracle as O
+        ob.build()
+        thr = ncpus()
+        O.set_threads(thr, fast=True)
+        # bounded sample: 2 instances of each size, one full SIMP iteration each (ScalingCG to 1e-8)
+        sample = []
+        for side in (64, 96, 128, 192, 256, 384):
+            sample += [d for d in insts if d["side"] == side][:2]
+        per_side = {}
+        for d in sample:
+            pr = PB.heatsink_q4(d["side"], d["side"], patch_w=d["patch_w"], patch_i0=d["patch_i0"], edge=d["edge"],
+                                vf=d["vf"], cg_eps=1e-8)
+            t0 = time.perf_counter()
+            O.simp_run(pr, 1, fast=True)
+            per_side.setdefault(d["side"], []).append(time.perf_counter() - t0)
+        t_inst = float(np.mean([np.mean(per_side[d["side"]]) for d in insts]))
+        v = 1.0 / t_inst
+        print(json.dumps({"impl": "reference", "metric": HEAT_BATCH_METRIC, "value": v,
+                          "unit": "instance-iterations/s", "n_gpus": args.gpus, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": 1e3 * t_inst * len(insts), "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": config,
+                          "cpu_baseline": {"value": v, "unit": "instance-iterations/s", "cores": thr, "kind": "port",
+                                           "sample": f"SIMP iteration 0 of {len(sample)} instances (2 per size), "
+                                                     "ScalingCG to 1e-8, time per size weighted by the batch's mix"},
+                          "e2e": {"value": v, "unit": "instance-iterations/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import pansfem2_gb300 as P
+    from pansfem2_gb300 import autotune
+    from pansfem2_gb300.batch import HeatBatch
+    P.load()
+    threads, tune_times = autotune.tune_batch_threads(insts, iters=1, warmup=1)
+    with ClockSampler(local) as clk:
+        with HeatBatch(insts, threads=threads) as B:
+            B.begin(cg_eps=1e-8)
+            B.step(args.warmup)
+            dev_t = B.step(args.steps)
+            res = B.results()
+            # e2e: the same iterations through the public API with the per-step read-back of the results
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                B.step(1)
+                r = B.results()
+            e2e_t = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([dev_t, e2e_t], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_t, e2e_t = float(t[0]), float(t[1])
+    n = len(insts)
+    value = world * n * args.steps / dev_t
+    # algorithmic bytes of the solve kernel: per node and FCG iteration ~250 B (FP64 Krylov vectors 112 B,
+    # FP32 level-0 V(2,2) 100 B, coarse levels ~1/3 of level 0)
+    its = res["iters"]
+    sides = np.array([d["side"] for d in insts])
+    bytes_solve = float(np.sum(its * (sides + 1.0) ** 2 * 250.0))
+    peak, peak_kind = peaks()
+    out = {"metric": HEAT_BATCH_METRIC, "value": value, "unit": "instance-iterations/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_t / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle / f64 FCG",
+           "data": "synthetic (seeded instances)", "config": dict(config, threads_per_cta=threads),
+           "clocks": clk.summary(), "gpu_launches": 4 * (args.steps + args.warmup) * 2,
+           "autotune": {"batch_threads": {str(k): v for k, v in tune_times.items()}},
+           "detail": {"solve_iterations_mean": float(np.mean(its)), "solve_iterations_max": int(np.max(its)),
+                      "true_residual_max": float(np.max(res["res"])), "all_converged": bool((res["conv"] == 1).all())},
+           "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                        "traffic": None, "kernel": "solve_batch (one CTA per instance)",
+                        "bytes_last_iteration_solve": bytes_solve, "peak_source": peak_kind,
+                        "note": "achieved = bytes of the last iteration's solves / (device time per iteration), "
+                                "an upper bound on the solve kernel's share"},
+           "e2e": {"value": world * n * args.steps / e2e_t, "unit": "instance-iterations/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 8 * 8 * n}}
+    out["roofline"]["achieved"] = bytes_solve / (dev_t / args.steps) / 1e9
+    out["roofline"]["frac"] = out["roofline"]["achieved"] / peak
+    if not args.no_compare and rank == 0:
+        # the same instances one by one, plain FP64 Jacobi PCG through the single-problem path
+        t_tot, n_done = 0.0, 0
+        for d in insts:
+            pr = PB.heatsink_q4(d["side"], d["side"], patch_w=d["patch_w"], patch_i0=d["patch_i0"], edge=d["edge"],
+                                vf=d["vf"])
+            prob, infos, wall = run_device(pr, "csr_jacobi_f64", 1, 1, 1e-8, False)
+            prob.close()
+            t_tot += sum(infos[0]["phase_seconds"])
+            n_done += 1
+        out["one_by_one_fp64_pcg"] = {"value": n_done / t_tot, "unit": "instance-iterations/s",
+                                      "solver": "csr_jacobi_f64", "speedup_of_value": value / (n_done / t_tot),
+                                      "note": "device time of one SIMP iteration of each instance after one warm-up"}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def ncpus():
     try:
         return len(os.sched_getaffinity(0))
@@ -255,7 +374,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--warm-start", type=int, default=1)
-    ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8"])
+    ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch"])
+    ap.add_argument("--instances", type=int, default=256, help="heat_batch: number of instances")
     ap.add_argument("--nx", type=int, default=None)
     ap.add_argument("--ny", type=int, default=None)
     ap.add_argument("--nz", type=int, default=None)
@@ -264,6 +384,8 @@ def main():
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.workload == "heat_batch":
+        return bench_heat_batch(args, rank, world)
     pr, desc = workload(args.workload, args.nx, args.ny, args.nz)
     from pansfem2_gb300 import problems as PB
     ne_w, nn_w, nd_w = PB.counts(pr)

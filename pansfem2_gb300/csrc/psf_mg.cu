@@ -398,6 +398,7 @@ __global__ void gauss_jordan_kernel(double *A, int n) {
 // preconditioner only (no cond(K) amplification as in an FP32 inner solve).
 struct MgFcgArgs {
     int nlev;
+    int lsmall;               // first level run by block 0 alone (1 <= lsmall <= nlev - 1)
     MgLev L[kMaxLev];
     KeF Ke;                   // level-0 element matrix (FP32, cycle)
     KeT64 Ke64;               // level-0 element matrix (FP64, operator)
@@ -449,111 +450,143 @@ __device__ __forceinline__ void jacobi_sweep(const MgFcgArgs &A, int l, const fl
     }
 }
 
+// barrier of a phase: the grid (all blocks) or block 0 alone
+__device__ __forceinline__ bool phase_sync(const MgFcgArgs &A, bool grid) {
+    if (grid) return grid_barrier(A.gs, A.partials);
+    __syncthreads();
+    return true;
+}
+
+// down-leg of level l: second pre-sweep, residual, restriction to level l+1 (and its first sweep)
+template <int KIND>
+__device__ bool down_level(const MgFcgArgs &A, int l, long long tid, long long stride, bool grid, bool tr) {
+    using T = KT<KIND>;
+    const int nl = A.nlev;
+    const MgLev &L = A.L[l];
+    jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                 // second pre-smoothing sweep
+    if (!phase_sync(A, grid)) return false;
+    stamp(A, tr);
+    for (long long n = tid; n < L.nnodes; n += stride) {              // residual r = b - A xt
+        int i, j, k;
+        lnode_ijk<KIND>(L, n, i, j, k);
+        float y[T::nd];
+        apply_node<KIND>(L, l, A.Ke, L.xt, i, j, k, y);
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) {
+            const long long q = n * T::nd + s;
+            L.r[q] = L.fixed[q] ? 0.f : L.b[q] - y[s];
+        }
+    }
+    if (!phase_sync(A, grid)) return false;
+    stamp(A, tr);
+    const MgLev &Cc = A.L[l + 1];
+    for (long long n = tid; n < Cc.nnodes; n += stride) {             // restriction b_c = P^T r
+        int i, j, k;
+        lnode_ijk<KIND>(Cc, n, i, j, k);
+        float acc[T::nd];
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) acc[s] = 0.f;
+        for (int di = -1; di <= 1; di++)
+            for (int dj = -1; dj <= 1; dj++)
+                for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++) {
+                    const int fi = 2 * i + di, fj = 2 * j + dj, fk = 2 * k + dk;
+                    if (fi < 0 || fi > L.nx || fj < 0 || fj > L.ny || (T::is3d && (fk < 0 || fk > L.nz))) continue;
+                    const float w = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * (dk ? 0.5f : 1.f);
+                    const long long m = lnode<KIND>(L, fi, fj, fk);
+#pragma unroll
+                    for (int s = 0; s < T::nd; s++) acc[s] += w * L.r[m * T::nd + s];
+                }
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) {
+            const long long q = n * T::nd + s;
+            const float bv = Cc.fixed[q] ? 0.f : acc[s];
+            Cc.b[q] = bv;
+            Cc.x[q] = (l + 1 < nl - 1) ? A.omega * bv / Cc.D[q] : 0.f;   // first sweep from zero
+        }
+    }
+    if (!phase_sync(A, grid)) return false;
+    stamp(A, tr);
+    return true;
+}
+
+// coarsest level: x = Ainv b (dense, FP64), one warp per row (the lanes read a row contiguously)
+__device__ __forceinline__ void coarsest_solve(const MgFcgArgs &A, long long tid, long long stride) {
+    const MgLev &Cc = A.L[A.nlev - 1];
+    const int n = A.nc;
+    const int lane = threadIdx.x & 31;
+    for (long long q = tid >> 5; q < n; q += stride >> 5) {
+        double acc = 0.0;
+        const double *row = A.Ainv + q * n;
+        for (int t = lane; t < n; t += 32) acc += row[t] * (double)Cc.b[t];
+        acc = warp_sum(acc);
+        if (lane == 0) Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
+    }
+}
+
+// up-leg of level l: x = xt + P x_c, two post-smoothing sweeps (result in x)
+template <int KIND>
+__device__ bool up_level(const MgFcgArgs &A, int l, long long tid, long long stride, bool grid, bool tr) {
+    using T = KT<KIND>;
+    const MgLev &L = A.L[l];
+    const MgLev &Cc = A.L[l + 1];
+    for (long long n = tid; n < L.nnodes; n += stride) {              // x = xt + P x_c
+        int i, j, k;
+        lnode_ijk<KIND>(L, n, i, j, k);
+        const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+        const int hi = i & 1, hj = j & 1, hk = k & 1;
+        float acc[T::nd];
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) acc[s] = 0.f;
+        for (int a = 0; a <= hi; a++)
+            for (int b = 0; b <= hj; b++)
+                for (int c = 0; c <= (T::is3d ? hk : 0); c++) {
+                    const float w = (hi ? 0.5f : 1.f) * (hj ? 0.5f : 1.f) * ((T::is3d && hk) ? 0.5f : 1.f);
+                    const long long m = lnode<KIND>(Cc, ci + a, cj + b, ck + c);
+#pragma unroll
+                    for (int s = 0; s < T::nd; s++) acc[s] += w * Cc.x[m * T::nd + s];
+                }
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) {
+            const long long q = n * T::nd + s;
+            L.x[q] = L.fixed[q] ? 0.f : L.xt[q] + acc[s];
+        }
+    }
+    if (!phase_sync(A, grid)) return false;
+    stamp(A, tr);
+    jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                  // post-smoothing, sweep 1
+    if (!phase_sync(A, grid)) return false;
+    stamp(A, tr);
+    jacobi_sweep<KIND>(A, l, L.xt, L.x, tid, stride);                  // sweep 2 -> x
+    if (l > 0 || !grid) {
+        if (!phase_sync(A, grid)) return false;
+        stamp(A, tr);
+    }
+    return true;
+}
+
 // V(2,2)-cycle; on entry L[0].b holds the level-0 right-hand side and L[0].x its
 // first sweep from zero (w b / D), both written by the caller before a barrier.
 // On exit L[0].x holds the result, written by the node loop of the last sweep
 // (same node -> thread mapping as the caller's next node loop, no barrier).
+// Levels lsmall.. (a few thousand nodes and less) run in block 0 alone with
+// block barriers while the other blocks wait at one grid barrier: a grid
+// barrier costs microseconds, far more than those levels' work.
 template <int KIND>
 __device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride, bool tr) {
-    using T = KT<KIND>;
-    const int nl = A.nlev;
-    for (int l = 0; l < nl - 1; l++) {
-        const MgLev &L = A.L[l];
-        jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                 // second pre-smoothing sweep
-        if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
-        for (long long n = tid; n < L.nnodes; n += stride) {              // residual r = b - A xt
-            int i, j, k;
-            lnode_ijk<KIND>(L, n, i, j, k);
-            float y[T::nd];
-            apply_node<KIND>(L, l, A.Ke, L.xt, i, j, k, y);
-#pragma unroll
-            for (int s = 0; s < T::nd; s++) {
-                const long long q = n * T::nd + s;
-                L.r[q] = L.fixed[q] ? 0.f : L.b[q] - y[s];
-            }
-        }
-        if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
-        const MgLev &Cc = A.L[l + 1];
-        for (long long n = tid; n < Cc.nnodes; n += stride) {             // restriction b_c = P^T r
-            int i, j, k;
-            lnode_ijk<KIND>(Cc, n, i, j, k);
-            float acc[T::nd];
-#pragma unroll
-            for (int s = 0; s < T::nd; s++) acc[s] = 0.f;
-            for (int di = -1; di <= 1; di++)
-                for (int dj = -1; dj <= 1; dj++)
-                    for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++) {
-                        const int fi = 2 * i + di, fj = 2 * j + dj, fk = 2 * k + dk;
-                        if (fi < 0 || fi > L.nx || fj < 0 || fj > L.ny || (T::is3d && (fk < 0 || fk > L.nz))) continue;
-                        const float w = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * (dk ? 0.5f : 1.f);
-                        const long long m = lnode<KIND>(L, fi, fj, fk);
-#pragma unroll
-                        for (int s = 0; s < T::nd; s++) acc[s] += w * L.r[m * T::nd + s];
-                    }
-#pragma unroll
-            for (int s = 0; s < T::nd; s++) {
-                const long long q = n * T::nd + s;
-                const float bv = Cc.fixed[q] ? 0.f : acc[s];
-                Cc.b[q] = bv;
-                Cc.x[q] = (l + 1 < nl - 1) ? A.omega * bv / Cc.D[q] : 0.f;   // first sweep from zero
-            }
-        }
-        if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
+    const int nl = A.nlev, ls = A.lsmall;
+    for (int l = 0; l < ls; l++)
+        if (!down_level<KIND>(A, l, tid, stride, true, tr)) return false;
+    if (blockIdx.x == 0) {
+        const long long bt = threadIdx.x, bs = blockDim.x;
+        for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, l, bt, bs, false, false);
+        coarsest_solve(A, bt, bs);
+        __syncthreads();
+        for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, l, bt, bs, false, false);
     }
-    {   // coarsest: x = Ainv b (dense, FP64)
-        // one warp per row: the lanes read the row contiguously (coalesced)
-        const MgLev &Cc = A.L[nl - 1];
-        const int n = A.nc;
-        const int lane = threadIdx.x & 31;
-        for (long long q = tid >> 5; q < n; q += stride >> 5) {
-            double acc = 0.0;
-            const double *row = A.Ainv + q * n;
-            for (int t = lane; t < n; t += 32) acc += row[t] * (double)Cc.b[t];
-            acc = warp_sum(acc);
-            if (lane == 0) Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
-        }
-        if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
-    }
-    for (int l = nl - 2; l >= 0; l--) {
-        const MgLev &L = A.L[l];
-        const MgLev &Cc = A.L[l + 1];
-        for (long long n = tid; n < L.nnodes; n += stride) {              // x = xt + P x_c
-            int i, j, k;
-            lnode_ijk<KIND>(L, n, i, j, k);
-            const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
-            const int hi = i & 1, hj = j & 1, hk = k & 1;
-            float acc[T::nd];
-#pragma unroll
-            for (int s = 0; s < T::nd; s++) acc[s] = 0.f;
-            for (int a = 0; a <= hi; a++)
-                for (int b = 0; b <= hj; b++)
-                    for (int c = 0; c <= (T::is3d ? hk : 0); c++) {
-                        const float w = (hi ? 0.5f : 1.f) * (hj ? 0.5f : 1.f) * ((T::is3d && hk) ? 0.5f : 1.f);
-                        const long long m = lnode<KIND>(Cc, ci + a, cj + b, ck + c);
-#pragma unroll
-                        for (int s = 0; s < T::nd; s++) acc[s] += w * Cc.x[m * T::nd + s];
-                    }
-#pragma unroll
-            for (int s = 0; s < T::nd; s++) {
-                const long long q = n * T::nd + s;
-                L.x[q] = L.fixed[q] ? 0.f : L.xt[q] + acc[s];
-            }
-        }
-        if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
-        jacobi_sweep<KIND>(A, l, L.x, L.xt, tid, stride);                  // post-smoothing, sweep 1
-        if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
-        jacobi_sweep<KIND>(A, l, L.xt, L.x, tid, stride);                  // sweep 2 -> x
-        if (l > 0) {
-            if (!grid_barrier(A.gs, A.partials)) return false;
-        stamp(A, tr);
-        }
-    }
+    if (!grid_barrier(A.gs, A.partials)) return false;
+    stamp(A, tr);
+    for (int l = ls - 1; l >= 0; l--)
+        if (!up_level<KIND>(A, l, tid, stride, true, tr)) return false;
     return true;
 }
 
@@ -779,6 +812,15 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_apply_kernel(MgFcgArgs A, co
 }
 
 // ------------------------------------------------------------------ host side
+constexpr long long kSmallLevelNodes = 4096;   // levels at most this large run in one block
+
+// first level (>= 1) that block 0 runs alone
+static int mg_small_level(const MgHier *H) {
+    for (int l = 1; l < H->nlev - 1; l++)
+        if (H->L[l].nnodes <= kSmallLevelNodes) return l;
+    return H->nlev - 1;
+}
+
 static psf_status mg_alloc(MgHier *H, Ctx *c, void **p, size_t bytes) {
     PSF_CUDA(cudaMalloc(p, bytes ? bytes : 1));
     PSF_CUDA(cudaMemsetAsync(*p, 0, bytes ? bytes : 1, c->stream));
@@ -894,6 +936,7 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     MgHier *H = (MgHier *)c->mg;
     MgFcgArgs *a = new MgFcgArgs;
     a->nlev = H->nlev;
+    a->lsmall = mg_small_level(H);
     for (int l = 0; l < H->nlev; l++) a->L[l] = H->L[l];
     a->Ke = kef_of(c);
     const int nk = c->nen * c->ndof;
@@ -984,6 +1027,7 @@ static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, con
     MgHier *H = (MgHier *)c->mg;
     MgFcgArgs *a = new MgFcgArgs;
     a->nlev = H->nlev;
+    a->lsmall = mg_small_level(H);
     for (int l = 0; l < H->nlev; l++) a->L[l] = H->L[l];
     a->Ke = kef_of(c);
     const int nk = c->nen * c->ndof;
