@@ -319,7 +319,7 @@ psf_status psf_export_wait(psf_ctx *ctx);
  * uniform unit source lumped to the nodes, zero-temperature patch of nodes
  * patch_i0 .. patch_i0 + patch_w on edge 0: j = 0, 1: j = side, 2: i = 0,
  * 3: i = side; even sides whose halving reaches <= 64 nodes), each with its own
- * volume fraction.  One CTA of `threads` threads owns an instance in each
+ * volume fraction.  One CTA of `threads` (128, 256 or 512) threads owns an instance in each
  * phase; one SIMP iteration of all instances (filter + conductivities,
  * multigrid-preconditioned FCG to the FP64 true residual cg_eps, compliance +
  * sensitivities, OC) is captured as one CUDA graph by psf_batch_begin. */

@@ -7,7 +7,7 @@ processes, keyed by the GPU name and a signature of the workload.
 
 Tuned today:
   batch_threads  threads per CTA of the batched heat-conduction SIMP (one CTA
-                 per instance): 128 / 256 / 512 / 1024.  Fewer threads leave
+                 per instance): 128 / 256 / 512 (the kernels' launch bound).  Fewer threads leave
                  room for more CTAs per SM (small instances); more threads
                  shorten the largest instances' critical path.
 """
@@ -51,7 +51,7 @@ def _key(kind, sig):
     return f"{kind}|{_gpu_name()}|{h}"
 
 
-def tune_batch_threads(instances, candidates=(128, 256, 512, 1024), iters=2, warmup=1, cg_eps=1e-8, log=None):
+def tune_batch_threads(instances, candidates=(128, 256, 512), iters=2, warmup=1, cg_eps=1e-8, log=None):
     """Threads per CTA for HeatBatch(instances): the candidate with the least device
     time for `iters` SIMP iterations after `warmup` iterations (each candidate starts
     from the same initial design).  Returns (threads, {threads: seconds})."""

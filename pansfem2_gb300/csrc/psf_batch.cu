@@ -49,6 +49,8 @@ struct Args {
     const int *order;        // block b processes instance order[b]
     // level-0 element arrays
     double *s, *rho, *E, *dfdrho, *dfds, *dgds, *snew, *wsum;
+    double *vw;              // volume weight of each design variable: sum over e in N(j) of w_ej / wsum_e
+    double *Bp;              // per OC call: x_j (-dfdx_j / dgdx_j)^iota
     float *Ef;
     // level-0 node arrays (FP64 Krylov vectors, loads, fixed flags)
     double *x, *r, *z, *p, *q, *F;
@@ -64,7 +66,8 @@ struct Args {
     double k0, kmin, pexp, iota, lmin, lmax, leps, move, eps;
     int itmax, warm;
     double Ke0[16];
-    float Ke0f[16];
+    float Ke0f[16];          // float part of Ke0 (the cycle uses it alone)
+    float Ke0lo[16];         // Ke0 - Ke0f: Ke0f + Ke0lo carries 48 bits (double-single operator)
     int nst;                 // filter stencil
     int sdi[kMaxStencilB], sdj[kMaxStencilB];
     double sw[kMaxStencilB];
@@ -90,6 +93,14 @@ __device__ __forceinline__ double bsum(double v, double *sm) {
 
 __device__ __forceinline__ int corner(int di, int dj) { return di ? (dj ? 2 : 1) : (dj ? 3 : 0); }
 
+// x^p for the penalty exponent (the samples' p = 3 as products; FP64 pow is slow on one SM)
+__device__ __forceinline__ double powp(double x, double p) {
+    if (p == 3.0) return x * x * x;
+    if (p == 2.0) return x * x;
+    if (p == 1.0) return x;
+    return pow(x, p);
+}
+
 // FP64 operator row of node (i, j) of level 0: y = sum over the 4 surrounding elements of E_e Ke0 x_e
 __device__ __forceinline__ double op64(const Args &A, const Inst &I, const double *xv, int i, int j) {
     const int n = I.n;
@@ -109,6 +120,50 @@ __device__ __forceinline__ double op64(const Args &A, const Inst &I, const doubl
                 acc += A.Ke0[li * 4 + lb] * xv[(long long)(n + 1) * bi + bj];
             }
             y += Ee * acc;
+        }
+    return y;
+}
+
+// error-free transformations: TwoProduct with the FMA (Ogita, Rump, Oishi 2005), TwoSum (Knuth)
+__device__ __forceinline__ float ds_two_prod(float a, float b, float &e) {
+    const float p = a * b;
+    e = __fmaf_rn(a, b, -p);
+    return p;
+}
+__device__ __forceinline__ float ds_two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float v = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+    return s;
+}
+
+// the FCG operator row in double-single: each element's Ke0 x_e as a compensated dot
+// product of float pairs (about 1e-14 relative), E_e scaling and the node sum in FP64;
+// one SM's FP64 rate would otherwise bound the largest instances
+__device__ __forceinline__ double opds(const Args &A, const Inst &I, const double *xv, int i, int j) {
+    const int n = I.n;
+    double y = 0.0;
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++) {
+            const int ei = i - 1 + ci, ej = j - 1 + cj;
+            if (ei < 0 || ej < 0 || ei >= n || ej >= n) continue;
+            const double Ee = A.E[I.e0 + (long long)n * ei + ej];
+            const int li = corner(1 - ci, 1 - cj);
+            float ps = 0.0f, cs = 0.0f;
+#pragma unroll
+            for (int lb = 0; lb < 4; lb++) {
+                const int bi = ei + (lb == 1 || lb == 2), bj = ej + (lb == 2 || lb == 3);
+                const double u = xv[(long long)(n + 1) * bi + bj];
+                const float uh = __double2float_rn(u), ul = __double2float_rn(u - (double)uh);
+                const float kh = A.Ke0f[li * 4 + lb], kl = A.Ke0lo[li * 4 + lb];
+                float pe, se;
+                const float pr = ds_two_prod(kh, uh, pe);
+                ps = ds_two_sum(ps, pr, se);
+                cs += se + pe + __fmaf_rn(kh, ul, kl * uh);
+            }
+            y += Ee * ((double)ps + (double)cs);
         }
     return y;
 }
@@ -429,7 +484,7 @@ __global__ void __launch_bounds__(kThreads) filter_moduli_batch(const __grid_con
         const int i = (int)(e / n), j = (int)(e % n);
         const double r = filt(A, I, s, i, j) / A.wsum[I.e0 + e];
         A.rho[I.e0 + e] = r;
-        const double rp = pow(r, A.pexp);
+        const double rp = powp(r, A.pexp);
         const double Ee = A.k0 * rp + A.kmin * (1.0 - rp);
         A.E[I.e0 + e] = Ee;
         A.Ef[I.e0 + e] = (float)Ee;
@@ -507,7 +562,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
             double pqa = 0.0;
             for (long long v = tid; v < nn; v += nt) {
                 const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
-                const double qv = fx[v] ? 0.0 : op64(A, I, p, i, j);
+                const double qv = fx[v] ? 0.0 : opds(A, I, p, i, j);
                 q[v] = qv;
                 pqa += p[v] * qv;
             }
@@ -566,7 +621,7 @@ __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ A
             for (int b = 0; b < 4; b++) v += A.Ke0[a * 4 + b] * te[b];
             qv += te[a] * v;
         }
-        A.dfdrho[I.e0 + e] = -A.pexp * (-A.kmin + A.k0) * pow(A.rho[I.e0 + e], A.pexp - 1.0) * qv;
+        A.dfdrho[I.e0 + e] = -A.pexp * (-A.kmin + A.k0) * powp(A.rho[I.e0 + e], A.pexp - 1.0) * qv;
         f += A.E[I.e0 + e] * qv;
     }
     f = bsum(f, sm);
@@ -587,40 +642,48 @@ __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ A
     }
 }
 
-// OC (OC.h:76-107) with the samples' filtered-volume constraint, bisection inside the block
+// OC (OC.h:76-107) with the samples' filtered-volume constraint, bisection inside the block.
+// The trial design is x (-dfdx / (dgdx lambda))^iota = [x (-dfdx / dgdx)^iota] lambda^-iota, so the
+// per-element power is taken once per update and a bisection step costs a multiplication and a
+// clamp per element; the filtered volume sum_e (sum_j w_ej x_j) / wsum_e is sum_j vw_j x_j with the
+// weights vw precomputed.
 __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Args A) {
     __shared__ double sm[32];
     const Inst &I = inst_of(A);
     const int n = I.n;
     const long long ne = (long long)n * n;
-    double *x = A.s + I.e0, *xn = A.snew + I.e0;
-    const double *dfdx = A.dfds + I.e0, *dgdx = A.dgds + I.e0;
+    double *x = A.s + I.e0, *xn = A.snew + I.e0, *Bp = A.Bp + I.e0;
+    const double *dfdx = A.dfds + I.e0, *dgdx = A.dgds + I.e0, *vw = A.vw + I.e0;
+    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+        const double b = -dfdx[e] / dgdx[e];
+        Bp[e] = x[e] * (A.iota == 0.5 ? sqrt(b) : pow(b, A.iota));
+    }
+    __syncthreads();
+    const double vscale = 1.0 / (I.vf * (double)ne);
     double l0 = A.lmin, l1 = A.lmax, lambda = 0.0;
     int steps = 0;
     while ((l1 - l0) / (l1 + l0) > A.leps && steps < 4000) {
         lambda = 0.5 * (l1 + l0);
         steps++;
+        const double li = A.iota == 0.5 ? 1.0 / sqrt(lambda) : pow(lambda, -A.iota);
+        double vol = 0.0;
         for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
             const double xe = x[e];
-            double v = pow(-dfdx[e] / (dgdx[e] * lambda), A.iota) * xe;
+            double v = Bp[e] * li;
             const double lo0 = (1.0 - A.move) * xe, hi0 = (1.0 + A.move) * xe;
             const double lo = (0.0 < lo0) ? lo0 : 0.0;
             const double hi = (hi0 < 1.0) ? hi0 : 1.0;
             if (v < lo) v = lo;
             else if (v > hi) v = hi;
             xn[e] = v;
-        }
-        __syncthreads();
-        double vol = 0.0;
-        for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
-            const int i = (int)(e / n), j = (int)(e % n);
-            vol += filt(A, I, xn, i, j) / A.wsum[I.e0 + e];
+            vol += vw[e] * v;
         }
         vol = bsum(vol, sm);
-        const double g = vol / (I.vf * (double)ne) - 1.0;
+        const double g = vol * vscale - 1.0;
         if (g > 0.0) l0 = lambda;
         else l1 = lambda;
     }
+    __syncthreads();
     for (long long e = threadIdx.x; e < ne; e += blockDim.x) x[e] = xn[e];
     if (threadIdx.x == 0) {
         double *o = A.out + (long long)A.order[blockIdx.x] * kOut;
@@ -695,8 +758,8 @@ extern "C" {
 psf_status psf_batch_create(int ninst, const int *side, const int *edge, const int *patch_w, const int *patch_i0,
                             const double *vf, int threads, psf_batch **out) {
     if (!out || ninst < 1 || !side || !edge || !patch_w || !patch_i0 || !vf) return PSF_BAD_INPUT;
-    if (threads != 128 && threads != 256 && threads != 512 && threads != 1024) {
-        psf::set_error("psf_batch_create: threads must be 128, 256, 512 or 1024");
+    if (threads != 128 && threads != 256 && threads != psf::batch::kThreads) {
+        psf::set_error("psf_batch_create: threads must be 128, 256 or 512 (the kernels' launch bound)");
         return PSF_BAD_INPUT;
     }
     *out = nullptr;
@@ -771,7 +834,8 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     unsigned char *dfixed = nullptr;
     ck(balloc(b, &dinst, ninst));
     ck(balloc(b, &dorder, ninst));
-    for (double **pp : {&a.s, &a.rho, &a.E, &a.dfdrho, &a.dfds, &a.dgds, &a.snew, &a.wsum}) ck(balloc(b, pp, ne));
+    for (double **pp : {&a.s, &a.rho, &a.E, &a.dfdrho, &a.dfds, &a.dgds, &a.snew, &a.wsum, &a.vw, &a.Bp})
+        ck(balloc(b, pp, ne));
     ck(balloc(b, &a.Ef, ne));
     for (double **pp : {&a.x, &a.r, &a.z, &a.p, &a.q, &a.F}) ck(balloc(b, pp, nv));
     ck(balloc(b, &dfixed, nv));
@@ -825,6 +889,7 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     for (int q = 0; q < 16; q++) {
         a.Ke0[q] = Ke[q];
         a.Ke0f[q] = (float)Ke[q];
+        a.Ke0lo[q] = (float)(Ke[q] - (double)a.Ke0f[q]);
     }
     *out = b;
     return PSF_OK;
@@ -887,6 +952,23 @@ psf_status psf_batch_begin(psf_batch *b, const psf_simp_params *prm) {
                 s0[I.e0 + (long long)n * i + j] = I.vf;
             }
     }
+    // volume weights vw_j = sum over e in N(j) of w_ej / wsum_e (the filter is symmetric: w_ej = w_je)
+    std::vector<double> vw(b->ne_tot, 0.0);
+    for (int k = 0; k < b->ninst; k++) {
+        const Inst &I = b->hinst[k];
+        const int n = I.n;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                double acc = 0.0;
+                for (int q = 0; q < a.nst; q++) {
+                    const int x = i + a.sdi[q], y = j + a.sdj[q];
+                    if (x < 0 || y < 0 || x >= n || y >= n) continue;
+                    acc += a.sw[q] / ws[I.e0 + (long long)n * x + y];
+                }
+                vw[I.e0 + (long long)n * i + j] = acc;
+            }
+    }
+    PSF_CUDA(cudaMemcpy(a.vw, vw.data(), sizeof(double) * vw.size(), cudaMemcpyHostToDevice));
     PSF_CUDA(cudaMemcpy(a.wsum, ws.data(), sizeof(double) * ws.size(), cudaMemcpyHostToDevice));
     PSF_CUDA(cudaMemcpy(a.s, s0.data(), sizeof(double) * s0.size(), cudaMemcpyHostToDevice));
     PSF_CUDA(cudaMemset(a.x, 0, sizeof(double) * b->nv_tot));

@@ -109,8 +109,9 @@ psf_status psf_csr_spmv(int n, const int32_t *indptr, const int32_t *indices, co
 psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, const double *data, const double *b,
                          int solver, int itmax, double eps, double *x, psf_solve_info *info) {
     if (!csr_ok(n, indptr, indices, data) || !b || !x) { set_error("psf_csr_solve: invalid CSR arrays"); return PSF_BAD_INPUT; }
-    if (solver != PSF_SOLVE_CSR_JACOBI_F64 && solver != PSF_SOLVE_CSR_CG_F64) {
-        set_error("psf_csr_solve: solver must be PSF_SOLVE_CSR_JACOBI_F64 or PSF_SOLVE_CSR_CG_F64");
+    if (solver != PSF_SOLVE_CSR_JACOBI_F64 && solver != PSF_SOLVE_CSR_CG_F64 && solver != PSF_SOLVE_CSR_BICGSTAB_F64) {
+        set_error("psf_csr_solve: solver must be PSF_SOLVE_CSR_JACOBI_F64, PSF_SOLVE_CSR_CG_F64 or "
+                  "PSF_SOLVE_CSR_BICGSTAB_F64");
         return PSF_BAD_INPUT;
     }
     if (itmax < 1 || !(eps > 0)) { set_error("psf_csr_solve: itmax >= 1 and eps > 0 required"); return PSF_BAD_INPUT; }
@@ -126,7 +127,7 @@ psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, c
     PSF_CUDA(cudaMallocAsync((void **)&dd, sizeof(double) * (nnz + 1), s));
     PSF_CUDA(cudaMallocAsync((void **)&db, sizeof(double) * (n + 1), s));
     PSF_CUDA(cudaMallocAsync((void **)&dx, sizeof(double) * (n + 1), s));
-    PSF_CUDA(cudaMallocAsync((void **)&w, sizeof(double) * 5 * (n + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&w, sizeof(double) * 6 * (n + 1), s));
     PSF_CUDA(cudaMemcpyAsync(dp, indptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(di, indices, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dd, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
@@ -137,8 +138,14 @@ psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, c
     c->klaunch = 0;
     int it = 0, conv = 0;
     double rr = 0, bb = 0;
-    psf_status st = pcg_csr_any(c, n, dp, di, dg, dd, db, dx, w, solver == PSF_SOLVE_CSR_JACOBI_F64 ? 1 : 0, itmax,
-                                eps, &it, &rr, &bb, &conv);
+    psf_status st;
+    if (solver == PSF_SOLVE_CSR_BICGSTAB_F64) {
+        double *const v[6] = {w, w + (n + 1), w + 2 * (n + 1), w + 3 * (n + 1), w + 4 * (n + 1), w + 5 * (n + 1)};
+        st = bicgstab_csr_any(c, n, dp, di, dd, db, dx, v, itmax, eps, &it, &rr, &bb, &conv);
+    } else {
+        st = pcg_csr_any(c, n, dp, di, dg, dd, db, dx, w, solver == PSF_SOLVE_CSR_JACOBI_F64 ? 1 : 0, itmax, eps, &it,
+                         &rr, &bb, &conv);
+    }
     if (st == PSF_OK) {
         PSF_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     }

@@ -35,6 +35,10 @@ struct KeF {
 struct KeT64 {
     double v[576];
 };
+// the FP64 element matrix split into float pairs hi + lo (48 significant bits)
+struct KeDS {
+    float hi[576], lo[576];
+};
 
 static inline psf_status residual64_check(Ctx *c, const double *b, const double *x, double *r, double *rn, double *bn) {
     return residual64_pub(c, b, x, r, rn, bn);
@@ -398,10 +402,12 @@ __global__ void gauss_jordan_kernel(double *A, int n) {
 // preconditioner only (no cond(K) amplification as in an FP32 inner solve).
 struct MgFcgArgs {
     int nlev;
+    int ds;                   // 1: the FCG operator K p in double-single (FP32 pipes), 0: FP64
     int lsmall;               // first level run by block 0 alone (1 <= lsmall <= nlev - 1)
     MgLev L[kMaxLev];
     KeF Ke;                   // level-0 element matrix (FP32, cycle)
     KeT64 Ke64;               // level-0 element matrix (FP64, operator)
+    KeDS Kds;                 // the same as float pairs (double-single operator)
     const double *Ainv;
     int nc;
     float omega;
@@ -642,6 +648,87 @@ __device__ __forceinline__ double apply64_node(const MgFcgArgs &A, const double 
     return d;
 }
 
+// ---- double-single arithmetic: error-free transformations on the FP32 pipes
+// TwoProduct with the FMA (Ogita, Rump, Oishi 2005): a b = p + e exactly
+__device__ __forceinline__ float ds_two_prod(float a, float b, float &e) {
+    const float p = a * b;
+    e = __fmaf_rn(a, b, -p);
+    return p;
+}
+// TwoSum (Knuth): a + b = s + e exactly
+__device__ __forceinline__ float ds_two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float v = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+    return s;
+}
+
+// q = K v for node n with each element's K0 u_e product in double-single
+// (compensated dot product, Ogita-Rump-Oishi "Dot2": about twice float
+// precision, ~1e-14) and the scaling by E_e and the node sum in FP64.  GB300's
+// FP64 rate is a small fraction of its FP32 rate: this moves the 8 x 8
+// products (Q4) or 24 x 24 (H8) of every element to the FP32 pipes.
+template <int KIND>
+__device__ __forceinline__ double applyds_node(const MgFcgArgs &A, const double *__restrict__ v, long long n,
+                                               double *__restrict__ out) {
+    using T = KT<KIND>;
+    const MgLev &L = A.L[0];
+    int i, j, k;
+    lnode_ijk<KIND>(L, n, i, j, k);
+    double y[T::nd];
+#pragma unroll
+    for (int a = 0; a < T::nd; a++) y[a] = 0.0;
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++)
+#pragma unroll
+            for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
+                const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
+                const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0);
+                const double Ee = A.Ep64[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
+                                                 : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
+                if (Ee == 0.0) continue;
+                // one pass over the element's dofs: each value is split once and feeds every row of this node
+                float ps[T::nd], cs[T::nd];
+#pragma unroll
+                for (int a = 0; a < T::nd; a++) ps[a] = cs[a] = 0.0f;
+#pragma unroll
+                for (int q = 0; q < T::nen; q++) {
+                    int qi, qj, qk;
+                    corner_of(q, qi, qj, qk);
+                    const long long m = lnode<KIND>(L, min(max(ei + qi, 0), L.nx), min(max(ej + qj, 0), L.ny),
+                                                    T::is3d ? min(max(ek + qk, 0), L.nz) : 0);
+#pragma unroll
+                    for (int b = 0; b < T::nd; b++) {
+                        const double u = v[m * T::nd + b];
+                        const float uh = __double2float_rn(u);
+                        const float ul = __double2float_rn(u - (double)uh);
+                        const int l = q * T::nd + b;
+#pragma unroll
+                        for (int a = 0; a < T::nd; a++) {
+                            const int kk = (li * T::nd + a) * T::nk + l;
+                            float pe, se;
+                            const float pr = ds_two_prod(A.Kds.hi[kk], uh, pe);
+                            ps[a] = ds_two_sum(ps[a], pr, se);
+                            cs[a] += se + pe + __fmaf_rn(A.Kds.hi[kk], ul, A.Kds.lo[kk] * uh);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < T::nd; a++) y[a] += Ee * ((double)ps[a] + (double)cs[a]);
+            }
+    double d = 0.0;
+#pragma unroll
+    for (int a = 0; a < T::nd; a++) {
+        const long long t = n * T::nd + a;
+        const double qv = L.fixed[t] ? 0.0 : y[a];
+        out[t] = qv;
+        d += v[t] * qv;
+    }
+    return d;
+}
+
 constexpr int kMgThreads = 512;   // one block per SM: half the barrier arrivals of 2 x 256
 
 template <int KIND>
@@ -735,7 +822,8 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
         stamp(A, tr);
         // ---- q = K p, p.q
         double pq[1] = {0.0};
-        for (long long n = tid; n < L0.nnodes; n += stride) pq[0] += apply64_node<KIND>(A, A.p, n, A.q);
+        for (long long n = tid; n < L0.nnodes; n += stride)
+            pq[0] += A.ds ? applyds_node<KIND>(A, A.p, n, A.q) : apply64_node<KIND>(A, A.p, n, A.q);
         block_sum<1>(pq, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, pq, 0.0)) return;
         stamp(A, tr);
@@ -940,7 +1028,15 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     for (int l = 0; l < H->nlev; l++) a->L[l] = H->L[l];
     a->Ke = kef_of(c);
     const int nk = c->nen * c->ndof;
-    for (int q = 0; q < nk * nk; q++) a->Ke64.v[q] = c->Ke0_host[q];
+    for (int q = 0; q < nk * nk; q++) {
+        a->Ke64.v[q] = c->Ke0_host[q];
+        const float h = (float)c->Ke0_host[q];
+        a->Kds.hi[q] = h;
+        a->Kds.lo[q] = (float)(c->Ke0_host[q] - (double)h);
+    }
+    // PSF_MG_FP64_OPERATOR=1 keeps the FCG operator in native FP64
+    const char *f64op = getenv("PSF_MG_FP64_OPERATOR");
+    a->ds = (f64op && *f64op == '1') ? 0 : 1;
     a->Ainv = H->Ac;
     a->nc = H->nc;
     a->omega = 1.0f;   // l1-Jacobi: convergent for any SPD operator

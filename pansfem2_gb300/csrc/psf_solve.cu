@@ -528,6 +528,149 @@ psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *ind
     return PSF_OK;
 }
 
+// ------------------------------------------------------------------ BiCGSTAB (CG.h:158-193)
+struct BicgArgs {
+    long long rows;
+    const int *indptr, *indices;
+    const double *data, *b;
+    double *x, *r, *rd, *p, *Ap, *s, *As;
+    int itmax;
+    double eps;
+    GridSync *gs;
+    double *partials;
+    double *out;
+};
+
+// y[i] = (A v)[i] for the rows of this warp group: four lanes per row, warp-uniform loop
+__device__ __forceinline__ void csr_rows4(const BicgArgs &A, const double *__restrict__ v, double *__restrict__ y,
+                                          long long tid, long long rstride, double *dot_with, double *dot_out,
+                                          double *dot_self) {
+    const int sub = threadIdx.x & 3;
+    for (long long base = (tid >> 5) << 3; base < A.rows; base += rstride) {
+        const long long i = base + ((threadIdx.x & 31) >> 2);
+        double acc = 0.0;
+        if (i < A.rows)
+            for (int q = A.indptr[i] + sub; q < A.indptr[i + 1]; q += 4) acc += A.data[q] * v[A.indices[q]];
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (sub == 0 && i < A.rows) {
+            y[i] = acc;
+            if (dot_with) *dot_out += dot_with[i] * acc;
+            if (dot_self) *dot_self += acc * acc;
+        }
+    }
+}
+
+// BiCGSTAB of the reference (x0 = 0, shadow residual rd = r0, stop on ||r|| < eps ||b||),
+// one persistent launch with five grid phases per iteration
+__global__ void __launch_bounds__(256) bicgstab_csr_kernel(BicgArgs A) {
+    __shared__ double sm[32 * 2];
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long rstride = stride >> 2;
+    {
+        double acc[2] = {0.0, 0.0};
+        for (long long i = tid; i < A.rows; i += stride) {
+            const double bv = A.b[i];
+            A.x[i] = 0.0;
+            A.r[i] = bv;           // r0 = b - A 0
+            A.rd[i] = bv;
+            A.p[i] = bv;
+            acc[0] += bv * bv;     // rd . r
+            acc[1] += bv * bv;
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+    }
+    double rdr = gs_result(A.gs, 0);
+    const double bnorm = sqrt(gs_result(A.gs, 1));
+    double rr = gs_result(A.gs, 1);
+    int it = 0, conv = 0;
+    for (; it < A.itmax; it++) {
+        // Ap = A p, rd . Ap
+        double d1[1] = {0.0};
+        csr_rows4(A, A.p, A.Ap, tid, rstride, A.rd, &d1[0], nullptr);
+        block_sum<1>(d1, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, d1, 0.0)) return;
+        const double alpha = rdr / gs_result(A.gs, 0);
+        // s = r - alpha Ap
+        for (long long i = tid; i < A.rows; i += stride) A.s[i] = 1.0 * A.r[i] + (-alpha) * A.Ap[i];
+        if (!grid_barrier(A.gs, A.partials)) return;
+        // As = A s, As . s, As . As
+        double d2[2] = {0.0, 0.0};
+        csr_rows4(A, A.s, A.As, tid, rstride, A.s, &d2[0], &d2[1]);
+        block_sum<2>(d2, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, d2, 0.0)) return;
+        const double omega = gs_result(A.gs, 0) / gs_result(A.gs, 1);
+        // x += alpha p + omega s, r = s - omega As, rd . r, r . r
+        double d3[2] = {0.0, 0.0};
+        for (long long i = tid; i < A.rows; i += stride) {
+            A.x[i] = 1.0 * A.x[i] + alpha * A.p[i] + omega * A.s[i];
+            const double rv = 1.0 * A.s[i] + (-omega) * A.As[i];
+            A.r[i] = rv;
+            d3[0] += A.rd[i] * rv;
+            d3[1] += rv * rv;
+        }
+        block_sum<2>(d3, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, d3, 0.0)) return;
+        const double rdr1 = gs_result(A.gs, 0);
+        rr = gs_result(A.gs, 1);
+        const double beta = alpha / omega * rdr1 / rdr;
+        rdr = rdr1;
+        if (sqrt(rr) < A.eps * bnorm) { it++; conv = 1; break; }
+        if (!isfinite(rr)) { it++; break; }
+        // p = beta p + r - beta omega Ap
+        const double mbo = -beta * omega;
+        for (long long i = tid; i < A.rows; i += stride) A.p[i] = beta * A.p[i] + 1.0 * A.r[i] + mbo * A.Ap[i];
+        if (!grid_barrier(A.gs, A.partials)) return;
+    }
+    if (tid == 0) {
+        A.out[0] = it;
+        A.out[1] = rr;
+        A.out[2] = bnorm * bnorm;
+        A.out[3] = conv;
+    }
+}
+
+// v: six work vectors of `rows` doubles (r, rd, p, Ap, s, As)
+psf_status bicgstab_csr_any(Ctx *c, long long rows, const int *indptr, const int *indices, const double *data,
+                            const double *b, double *x, double *const v[6], int itmax, double eps, int *iters,
+                            double *rr, double *bb, int *conv) {
+    BicgArgs a;
+    a.rows = rows;
+    a.indptr = indptr; a.indices = indices; a.data = data;
+    a.b = b;
+    a.x = x;
+    const long long n = rows;
+    a.r = v[0]; a.rd = v[1]; a.p = v[2]; a.Ap = v[3]; a.s = v[4]; a.As = v[5];
+    a.itmax = itmax;
+    a.eps = eps;
+    a.gs = c->gs;
+    a.partials = c->partials;
+    a.out = c->scal + 12;
+    int per_sm = 0;
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bicgstab_csr_kernel, 256, 0));
+    if (per_sm < 1) { set_error("persistent BiCGSTAB kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
+    int blocks = c->num_sms * (per_sm < 4 ? per_sm : 4);
+    long long need = (n * 4 + 255) / 256;
+    if (blocks > need) blocks = (int)need;
+    if (blocks < 1) blocks = 1;
+    void *args[] = {&a};
+    PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
+    PSF_CHECK(launch_coop(c, (const void *)bicgstab_csr_kernel, blocks, 256, args));
+    PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
+    PSF_CHECK(read_sync_status(c));
+    PSF_CHECK(add_kernel_time(c));
+    double h[4];
+    PSF_CUDA(cudaMemcpyAsync(h, a.out, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    *iters = (int)h[0];
+    *rr = h[1];
+    *bb = h[2];
+    *conv = (int)h[3];
+    return PSF_OK;
+}
+
 // Cooperative launch of pcg_csr_kernel (ScalingCG) on caller-owned device
 // buffers and the caller's stream, without a context and without allocating:
 // w holds 5*rows doubles, gs is zeroed here, partials holds (kMaxRed+2)*blocks
@@ -688,6 +831,21 @@ psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve
     } else if (solver == PSF_SOLVE_IR_MG_F32) {
         st = mg_solve(c, itmax, eps, warm, &inf);
         if (st != PSF_OK && st != PSF_NOT_CONVERGED) return st;
+    } else if (solver == PSF_SOLVE_CSR_BICGSTAB_F64) {
+        if (!c->have_values) { set_error("psf_solve: assemble first"); return PSF_BAD_INPUT; }
+        int it, conv;
+        double rr, bb;
+        // six vectors of nfree: five in w64[0] (5 * ndofs long), the sixth in w64[1]
+        const long long nf = c->nfree;
+        double *const v[6] = {c->w64[0], c->w64[0] + nf, c->w64[0] + 2 * nf, c->w64[0] + 3 * nf,
+                              c->w64[0] + 4 * nf, c->w64[1]};
+        PSF_CHECK(bicgstab_csr_any(c, nf, c->indptr, c->indices, c->data, c->F, c->u, v, itmax, eps, &it, &rr,
+                                   &bb, &conv));
+        inf.iterations = it;
+        inf.outer_iterations = 1;
+        inf.rel_residual_recurrence = bb > 0 ? sqrt(rr / bb) : 0.0;
+        PSF_CHECK(scatter_reduced(c, c->u, c->un));
+        if (!conv) st = PSF_NOT_CONVERGED;
     } else if (solver == PSF_SOLVE_IR_LEARNED_F32) {
         st = learned_solve(c, itmax, eps, warm, &inf);
         if (st != PSF_OK && st != PSF_NOT_CONVERGED) return st;
