@@ -42,7 +42,9 @@ def workload(name="mbb2d", nx=None, ny=None, nz=None):
     headline); h8: the 3D H8 cantilever, 128x64x64 elements (1,635,075 dofs),
     OC, vf 0.15, filter radius 2."""
     from pansfem2_gb300 import problems as PB
-    if name == "h8":
+    if name == "c1":
+        nx, ny = nx or 60, ny or 30
+        return PB.cantilever_q4(nx, ny), f"cantilever {nx}x{ny} Q4 plane strain, OC, R=1.5, vf=0.5, PCG 1e-10"
         nx, ny, nz = nx or 128, ny or 64, nz or 64
         pr = PB.cantilever_h8(nx, ny, nz)
         desc = f"H8 cantilever {nx}x{ny}x{nz}, OC, R=2, vf=0.15"
@@ -374,8 +376,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--warm-start", type=int, default=1)
-    ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch"])
+    ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch", "c1"])
     ap.add_argument("--instances", type=int, default=256, help="heat_batch: number of instances")
+    ap.add_argument("--eps", type=float, default=1e-8, help="relative residual of every solve")
     ap.add_argument("--nx", type=int, default=None)
     ap.add_argument("--ny", type=int, default=None)
     ap.add_argument("--nz", type=int, default=None)
@@ -390,7 +393,7 @@ def main():
     from pansfem2_gb300 import problems as PB
     ne_w, nn_w, nd_w = PB.counts(pr)
     config = {"workload": desc, "dofs": nn_w * nd_w, "elements": ne_w,
-              "residual": "FP64 relative 1e-8", "l2": "inputs larger than L2 (CSR 227 MB) for the FP64 path; "
+              "residual": f"FP64 relative {args.eps:g}", "l2": "inputs larger than L2 (CSR 227 MB) for the FP64 path; "
               "FP32 matrix-free working set ~40 MB is L2-resident", "parallelism": f"replicas{world}"}
 
     if args.impl == "reference":
@@ -429,7 +432,7 @@ def main():
     # ---- value: device-resident design
     barrier()
     with ClockSampler(local) as clk:
-        prob, infos, wall = run_device(pr, args.solver, args.warmup, args.steps, 1e-8, bool(args.warm_start))
+        prob, infos, wall = run_device(pr, args.solver, args.warmup, args.steps, args.eps, bool(args.warm_start))
     barrier()
     dev_t = sum(sum(i["phase_seconds"]) for i in infos)
     if world > 1:
@@ -481,7 +484,7 @@ def main():
     # ---- e2e through host buffers
     if not args.no_e2e:
         barrier()
-        einfos, ewall, h2d, d2h = run_e2e(pr, args.solver, args.warmup, args.steps, 1e-8, bool(args.warm_start))
+        einfos, ewall, h2d, d2h = run_e2e(pr, args.solver, args.warmup, args.steps, args.eps, bool(args.warm_start))
         barrier()
         if world > 1:
             t = torch.tensor([ewall], device="cuda")
@@ -495,7 +498,7 @@ def main():
         barrier()
         bsolver = args.baseline_solver or ("ebe_jacobi_f64" if args.workload == "h8" else "csr_jacobi_f64")
         args.baseline_solver = bsolver
-        bprob, binfos, bwall = run_device(pr, bsolver, args.warmup, args.steps, 1e-8, False)
+        bprob, binfos, bwall = run_device(pr, bsolver, args.warmup, args.steps, args.eps, False)
         bprob.close()
         bt = sum(sum(i["phase_seconds"]) for i in binfos)
         out["fp64_gpu_pcg"] = {"solver": args.baseline_solver, "value": args.steps / bt, "unit": UNIT,

@@ -335,6 +335,9 @@ psf_status psf_batch_step(psf_batch *batch, int iters, double *seconds);
 /* per instance 8 values: f, g, OC lambda, solver iterations, FP64 relative
  * residual, converged, refinement passes, bisection steps */
 psf_status psf_batch_results(psf_batch *batch, double *out);
+/* one SIMP iteration without the graph, device seconds of the four phases
+ * (filter + conductivities, solve, sensitivities, OC) */
+psf_status psf_batch_profile(psf_batch *batch, double *phase_seconds);
 psf_status psf_batch_fields(psf_batch *batch, int instance, double *s, double *rho, double *T);
 
 #ifdef __cplusplus

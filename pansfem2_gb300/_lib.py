@@ -39,6 +39,7 @@ EXPORTS = [
     "psf_learned_attach", "psf_learned_apply", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
     "psf_learned_harvest", "psf_learned_train", "psf_learned_eval", "psf_export_vtk", "psf_export_wait",
     "psf_batch_create", "psf_batch_destroy", "psf_batch_begin", "psf_batch_step", "psf_batch_results",
+    "psf_batch_profile",
     "psf_batch_fields",
 ]
 
@@ -157,6 +158,7 @@ def load(path=LIB_PATH):
         "psf_batch_begin": [vp, C.POINTER(SimpParams)],
         "psf_batch_step": [vp, C.c_int, dp],
         "psf_batch_results": [vp, dp],
+        "psf_batch_profile": [vp, dp],
         "psf_batch_fields": [vp, C.c_int, dp, dp, dp],
         "psf_export_wait": [vp],
     }

@@ -66,6 +66,12 @@ class HeatBatch:
         L.check(L.load().psf_batch_step(self._h, int(iters), C.byref(t)))
         return t.value
 
+    def profile(self):
+        """One SIMP iteration without the graph: device seconds per phase."""
+        out = np.zeros(4)
+        L.check(L.load().psf_batch_profile(self._h, L.ptr(out)))
+        return dict(zip(("filter_moduli", "solve", "sens", "oc"), out))
+
     def results(self):
         out = np.zeros((self.n, 8))
         L.check(L.load().psf_batch_results(self._h, L.ptr(out)))

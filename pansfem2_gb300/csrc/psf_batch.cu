@@ -1007,6 +1007,31 @@ psf_status psf_batch_step(psf_batch *b, int iters, double *seconds) {
     return PSF_OK;
 }
 
+psf_status psf_batch_profile(psf_batch *b, double *phase_seconds) {
+    if (!b || !b->begun || !phase_seconds) return PSF_BAD_INPUT;
+    cudaEvent_t ev[5];
+    for (auto &e : ev) PSF_CUDA(cudaEventCreate(&e));
+    const Args &a = b->a;
+    const int nb = b->ninst, nt = b->threads;
+    PSF_CUDA(cudaEventRecord(ev[0], b->stream));
+    psf::batch::filter_moduli_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(cudaEventRecord(ev[1], b->stream));
+    psf::batch::solve_batch<<<nb, nt, b->smem, b->stream>>>(a);
+    PSF_CUDA(cudaEventRecord(ev[2], b->stream));
+    psf::batch::sens_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(cudaEventRecord(ev[3], b->stream));
+    psf::batch::oc_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(cudaEventRecord(ev[4], b->stream));
+    PSF_CUDA(cudaEventSynchronize(ev[4]));
+    for (int k = 0; k < 4; k++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+        phase_seconds[k] = ms * 1e-3;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return PSF_OK;
+}
+
 psf_status psf_batch_results(psf_batch *b, double *out) {
     if (!b || !out) return PSF_BAD_INPUT;
     PSF_CUDA(cudaMemcpy(out, b->a.out, sizeof(double) * b->ninst * psf::batch::kOut, cudaMemcpyDeviceToHost));

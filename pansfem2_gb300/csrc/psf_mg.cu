@@ -1034,9 +1034,11 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
         a->Kds.hi[q] = h;
         a->Kds.lo[q] = (float)(c->Ke0_host[q] - (double)h);
     }
-    // PSF_MG_FP64_OPERATOR=1 keeps the FCG operator in native FP64
-    const char *f64op = getenv("PSF_MG_FP64_OPERATOR");
-    a->ds = (f64op && *f64op == '1') ? 0 : 1;
+    // PSF_MG_DS_OPERATOR=1 computes the FCG operator in double-single.  Measured on the
+    // 1M-dof MBB beam it is slower than native FP64 here (46.5 vs 52.1 SIMP iterations/s): the
+    // compensated sums form a dependent chain that 16 warps per SM cannot hide.
+    const char *dsop = getenv("PSF_MG_DS_OPERATOR");
+    a->ds = (dsop && *dsop == '1') ? 1 : 0;
     a->Ainv = H->Ac;
     a->nc = H->nc;
     a->omega = 1.0f;   // l1-Jacobi: convergent for any SPD operator
