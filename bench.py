@@ -356,6 +356,74 @@ def bench_heat_batch(args, rank, world):
         torch.distributed.destroy_process_group()
 
 
+LEARNED_METRIC = "SIMP iters/s at 263K DOF (512x256 MBB), resid 1e-8: learned FCG vs Jacobi PCG"
+
+
+def bench_learned2d(args, rank, world):
+    """The learned preconditioner end to end at 512x256: training pairs harvested from
+    seeded SIMP runs (vf uniform in [0.3, 0.6], point loads on the right edge, designs
+    along the first iterations), the U-Net trained on the GPU (energy loss), then SIMP
+    iterations of the MBB beam with the learned FCG, the multigrid FCG without the
+    network, and the plain FP64 Jacobi PCG."""
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    import pansfem2_gb300 as P
+    from pansfem2_gb300 import learned as Ln
+    from pansfem2_gb300 import problems as PB
+    P.load()
+    nx, ny = args.nx or 512, args.ny or 256
+    H, W = nx + 1, ny + 1
+    rng = np.random.default_rng(rank)
+    ts = Ln.TrainSet(H, W, args.pairs)
+    t0 = time.perf_counter()
+    runs, iters_per_run = 8, 24
+    per_design = max(1, args.pairs // (runs * (iters_per_run // 2)))
+    while len(ts) < args.pairs:
+        pr = PB.mbb_q4(nx, ny, vf=float(rng.uniform(0.3, 0.6)), load_right=int(rng.integers(ny // 4, ny + 1)))
+        with P.Problem(pr) as prob:
+            prob.setup_bc()
+            prob.attach_learned(None, pre_mg=True, nu_post=1, use_net=False)
+            prob.simp_begin(solver="ir_mg_f32", cg_eps=1e-8, warm_start=True)
+            for k in range(iters_per_run):
+                prob.simp_step()
+                if k % 2 == 1 and len(ts) < args.pairs:
+                    prob.harvest(ts, min(per_design, args.pairs - len(ts)), iters=[0, 1, 2, 3, 4, 6, 8, 12, 16])
+    t_harvest = time.perf_counter() - t0
+    net = Ln.UNet(H, W, batch=8, seed=3)
+    t0 = time.perf_counter()
+    hist = Ln.train(net, ts, args.train_steps, batch=8, lr=1e-3, seed=5, loss="energy")
+    t_train = time.perf_counter() - t0
+    pr = PB.mbb_q4(nx, ny)
+    res = {}
+    for solver in ("ir_learned_f32", "ir_mg_f32", "csr_jacobi_f64"):
+        with P.Problem(pr) as prob:
+            prob.setup_bc()
+            if solver == "ir_learned_f32":
+                prob.attach_learned(net, pre_mg=True, nu_post=1)
+            prob.simp_begin(solver=solver, cg_eps=args.eps, warm_start=solver != "csr_jacobi_f64")
+            for _ in range(args.warmup):
+                prob.simp_step()
+            infos = [prob.simp_step() for _ in range(args.steps)]
+        t = sum(sum(i["phase_seconds"]) for i in infos)
+        res[solver] = {"value": args.steps / t, "krylov_iterations": sum(i["solve"]["iterations"] for i in infos),
+                       "fell_back": sum(i["solve"]["fell_back"] for i in infos),
+                       "true_residual_max": max(i["solve"]["rel_residual"] for i in infos), "f_last": infos[-1]["f"]}
+    out = {"metric": LEARNED_METRIC, "value": res["ir_learned_f32"]["value"], "unit": "SIMP iterations/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 / res["ir_learned_f32"]["value"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "bf16 network / f32 cycle / f64 FCG", "data": "synthetic",
+           "config": {"workload": f"MBB half beam {nx}x{ny} Q4, MMA, R=3, vf=0.4; U-Net 4 levels 16->128",
+                      "pairs": len(ts), "train_steps": args.train_steps, "residual": f"FP64 relative {args.eps:g}"},
+           "training": {"harvest_s": t_harvest, "train_s": t_train, "energy_loss_first": float(hist[:20].mean()),
+                        "energy_loss_last": float(hist[-100:].mean())},
+           "solvers": res,
+           "learned_vs_fp64_pcg": res["ir_learned_f32"]["value"] / res["csr_jacobi_f64"]["value"],
+           "learned_vs_multigrid": res["ir_learned_f32"]["value"] / res["ir_mg_f32"]["value"],
+           "compliance_rel_diff_vs_fp64": abs(res["ir_learned_f32"]["f_last"] - res["csr_jacobi_f64"]["f_last"]) /
+           abs(res["csr_jacobi_f64"]["f_last"])}
+    print(json.dumps(out))
+
+
 def ncpus():
     try:
         return len(os.sched_getaffinity(0))
@@ -376,7 +444,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--warm-start", type=int, default=1)
-    ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch", "c1"])
+    ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch", "c1", "learned2d"])
+    ap.add_argument("--pairs", type=int, default=4000, help="learned2d: training pairs")
+    ap.add_argument("--train-steps", type=int, default=3000, help="learned2d: Adam steps")
     ap.add_argument("--instances", type=int, default=256, help="heat_batch: number of instances")
     ap.add_argument("--eps", type=float, default=1e-8, help="relative residual of every solve")
     ap.add_argument("--nx", type=int, default=None)
@@ -389,6 +459,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.workload == "heat_batch":
         return bench_heat_batch(args, rank, world)
+    if args.workload == "learned2d":
+        return bench_learned2d(args, rank, world)
     pr, desc = workload(args.workload, args.nx, args.ny, args.nz)
     from pansfem2_gb300 import problems as PB
     ne_w, nn_w, nd_w = PB.counts(pr)
@@ -400,7 +472,7 @@ def main():
         if rank != 0:
             return
         thr = ncpus()
-        r = cpu_reference_sample(pr, args.steps, args.warmup, thr,
+        r = cpu_reference_sample(pr, min(args.steps, 5), min(args.warmup, 1), thr,
                                  n0="extrapolate" if args.workload == "h8" else "full")
         t = float(np.mean(r["samples"]))
         v = 1.0 / t
@@ -511,7 +583,7 @@ def main():
     # ---- CPU baseline (rank 0 at N=1 only)
     if rank == 0 and world == 1 and not args.no_cpu:
         thr = ncpus()
-        if args.workload == "mbb2d":
+        if args.workload in ("mbb2d", "c1"):
             r = cpu_reference_sample(pr, 0, 0, thr, n0="full")
             t = r["t_iter0_full"]
             sample = (f"SIMP iteration 0 in full on the host (ScalingCG to 1e-8: {r['n_cg_iter0']} iterations), "

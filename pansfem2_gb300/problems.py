@@ -43,12 +43,17 @@ def cantilever_q4(nx=60, ny=30, **kw):
                  load_val=[-1.0] * len(ln), **kw)
 
 
-def mbb_q4(nx=1024, ny=512, **kw):
+def mbb_q4(nx=1024, ny=512, load_right=None, **kw):
     """Config 2: MBB half beam.  u_x = 0 on the left edge, u_y = 0 at the bottom-right
-    node, unit downward load at the top-left node; MMA, vf 0.4, filter radius 3."""
+    node, unit downward load at the top-left node; MMA, vf 0.4, filter radius 3.
+    load_right = j moves the load to the right-edge node (nx, j) (the learned
+    preconditioner's training runs)."""
     fn, fd = _fixedlist(nx, ny, (0,), lambda i, j: i == 0)
     fn2, fd2 = _fixedlist(nx, ny, (1,), lambda i, j: i == nx and j == 0)
-    ln, ld = _fixedlist(nx, ny, (1,), lambda i, j: i == 0 and j == ny)
+    if load_right is None:
+        ln, ld = _fixedlist(nx, ny, (1,), lambda i, j: i == 0 and j == ny)
+    else:
+        ln, ld = _fixedlist(nx, ny, (1,), lambda i, j: i == nx and j == load_right)
     kw.setdefault("vf", 0.4)
     kw.setdefault("R", 3.0)
     kw.setdefault("optimizer", 1)
