@@ -45,6 +45,7 @@ def workload(name="mbb2d", nx=None, ny=None, nz=None):
     if name == "c1":
         nx, ny = nx or 60, ny or 30
         return PB.cantilever_q4(nx, ny), f"cantilever {nx}x{ny} Q4 plane strain, OC, R=1.5, vf=0.5, PCG 1e-10"
+    if name == "h8":
         nx, ny, nz = nx or 128, ny or 64, nz or 64
         pr = PB.cantilever_h8(nx, ny, nz)
         desc = f"H8 cantilever {nx}x{ny}x{nz}, OC, R=2, vf=0.15"
@@ -53,7 +54,7 @@ def workload(name="mbb2d", nx=None, ny=None, nz=None):
     return PB.mbb_q4(nx, ny), f"MBB half beam {nx}x{ny} Q4 plane strain, MMA, R=3, vf=0.4"
 
 
-def mg_levels(pr, coarse_dofs=100):
+def mg_levels(pr, coarse_dofs=40):
     """Node counts of the multigrid hierarchy (halving every axis while all are
     even, until a level has <= coarse_dofs dofs), as psf_mg.cu builds it."""
     from pansfem2_gb300 import problems as PB
@@ -295,9 +296,9 @@ def bench_heat_batch(args, rank, world):
     from pansfem2_gb300 import autotune
     from pansfem2_gb300.batch import HeatBatch
     P.load()
-    threads, tune_times = autotune.tune_batch_threads(insts, iters=1, warmup=1)
+    (threads, cluster), tune_times = autotune.tune_batch(insts, iters=1, warmup=1)
     with ClockSampler(local) as clk:
-        with HeatBatch(insts, threads=threads) as B:
+        with HeatBatch(insts, threads=threads, cluster=cluster) as B:
             B.begin(cg_eps=1e-8)
             B.step(args.warmup)
             dev_t = B.step(args.steps)
@@ -323,9 +324,10 @@ def bench_heat_batch(args, rank, world):
     out = {"metric": HEAT_BATCH_METRIC, "value": value, "unit": "instance-iterations/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_t / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle / f64 FCG",
-           "data": "synthetic (seeded instances)", "config": dict(config, threads_per_cta=threads),
+           "data": "synthetic (seeded instances)",
+           "config": dict(config, threads_per_cta=threads, ctas_per_instance=cluster),
            "clocks": clk.summary(), "gpu_launches": 4 * (args.steps + args.warmup) * 2,
-           "autotune": {"batch_threads": {str(k): v for k, v in tune_times.items()}},
+           "autotune": {"batch_threads_x_cluster": tune_times},
            "detail": {"solve_iterations_mean": float(np.mean(its)), "solve_iterations_max": int(np.max(its)),
                       "true_residual_max": float(np.max(res["res"])), "all_converged": bool((res["conv"] == 1).all())},
            "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,

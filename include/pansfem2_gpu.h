@@ -319,13 +319,14 @@ psf_status psf_export_wait(psf_ctx *ctx);
  * uniform unit source lumped to the nodes, zero-temperature patch of nodes
  * patch_i0 .. patch_i0 + patch_w on edge 0: j = 0, 1: j = side, 2: i = 0,
  * 3: i = side; even sides whose halving reaches <= 64 nodes), each with its own
- * volume fraction.  One CTA of `threads` (128, 256 or 512) threads owns an instance in each
+ * volume fraction.  A team of `cluster` CTAs (1, 2, 4 or 8: a thread-block
+ * cluster) of `threads` (128, 256 or 512) threads owns an instance in each
  * phase; one SIMP iteration of all instances (filter + conductivities,
  * multigrid-preconditioned FCG to the FP64 true residual cg_eps, compliance +
  * sensitivities, OC) is captured as one CUDA graph by psf_batch_begin. */
 typedef struct psf_batch psf_batch;
 psf_status psf_batch_create(int ninst, const int *side, const int *edge, const int *patch_w, const int *patch_i0,
-                            const double *vf, int threads, psf_batch **batch);
+                            const double *vf, int threads, int cluster, psf_batch **batch);
 psf_status psf_batch_destroy(psf_batch *batch);
 /* shared parameters: E1 = k0, E0 = kmin, p, R, OC parameters, cg_eps, cg_itmax,
  * warm_start (optimizer must be 0); starts every instance at s = vf */

@@ -6,10 +6,11 @@ are cached per process and, when PSF_TUNE_CACHE names a JSON file, across
 processes, keyed by the GPU name and a signature of the workload.
 
 Tuned today:
-  batch_threads  threads per CTA of the batched heat-conduction SIMP (one CTA
-                 per instance): 128 / 256 / 512 (the kernels' launch bound).  Fewer threads leave
-                 room for more CTAs per SM (small instances); more threads
-                 shorten the largest instances' critical path.
+  batch          threads per CTA (256 / 512) and CTAs per instance (a thread-block
+                 cluster of 1, 2, 4 or 8) of the batched heat-conduction SIMP.  More
+                 CTAs per instance shorten the largest instances' critical path
+                 (one SM's bandwidth and FP64 rate bound a lone CTA); fewer leave
+                 room for more instances at once.
 """
 import hashlib
 import json
@@ -51,27 +52,36 @@ def _key(kind, sig):
     return f"{kind}|{_gpu_name()}|{h}"
 
 
-def tune_batch_threads(instances, candidates=(128, 256, 512), iters=2, warmup=1, cg_eps=1e-8, log=None):
-    """Threads per CTA for HeatBatch(instances): the candidate with the least device
-    time for `iters` SIMP iterations after `warmup` iterations (each candidate starts
-    from the same initial design).  Returns (threads, {threads: seconds})."""
+def tune_batch(instances, candidates=((256, 1), (512, 1), (256, 4), (512, 2), (512, 4), (512, 8)), iters=2,
+               warmup=1, cg_eps=1e-8, log=None):
+    """(threads per CTA, CTAs per instance) for HeatBatch(instances): the candidate with
+    the least device time for `iters` SIMP iterations after `warmup` iterations (each
+    candidate starts from the same initial design).  Returns ((threads, cluster),
+    {"threads x cluster": seconds})."""
     from .batch import HeatBatch
     _load()
-    key = _key("batch_threads", {"inst": [(d["side"], d["edge"], d["patch_w"], d["patch_i0"], round(d["vf"], 6))
-                                          for d in instances], "eps": cg_eps, "cands": list(candidates)})
+    key = _key("batch", {"inst": [(d["side"], d["edge"], d["patch_w"], d["patch_i0"], round(d["vf"], 6))
+                                  for d in instances], "eps": cg_eps, "cands": [list(c) for c in candidates]})
     if key in _CACHE:
         ent = _CACHE[key]
-        return ent["best"], {int(k): v for k, v in ent["times"].items()}
+        return tuple(ent["best"]), ent["times"]
     times = {}
-    for t in candidates:
-        with HeatBatch(instances, threads=t) as B:
-            B.begin(cg_eps=cg_eps)
-            if warmup:
-                B.step(warmup)
-            times[t] = B.step(iters)
+    for t, c in candidates:
+        try:
+            with HeatBatch(instances, threads=t, cluster=c) as B:
+                B.begin(cg_eps=cg_eps)
+                if warmup:
+                    B.step(warmup)
+                sec = B.step(iters)
+        except Exception as e:   # a shape the device cannot launch is skipped
+            if log:
+                log(f"autotune batch {t}x{c}: {e}")
+            continue
+        times[f"{t}x{c}"] = sec
         if log:
-            log(f"autotune batch_threads {t}: {times[t] * 1e3:.2f} ms for {iters} iterations")
+            log(f"autotune batch {t}x{c}: {sec * 1e3:.2f} ms for {iters} iterations")
     best = min(times, key=times.get)
-    _CACHE[key] = {"best": best, "times": times}
+    bt, bc = (int(v) for v in best.split("x"))
+    _CACHE[key] = {"best": [bt, bc], "times": times}
     _store()
-    return best, times
+    return (bt, bc), times

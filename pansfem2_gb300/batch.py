@@ -13,8 +13,9 @@ RESULT_FIELDS = ("f", "g", "lambda", "iters", "res", "conv", "passes", "bisect")
 
 
 class HeatBatch:
-    def __init__(self, instances, threads=512):
-        """instances: dicts with side, edge, patch_w, patch_i0, vf (problems.heat_batch)."""
+    def __init__(self, instances, threads=512, cluster=1):
+        """instances: dicts with side, edge, patch_w, patch_i0, vf (problems.heat_batch);
+        a team of `cluster` CTAs (a thread-block cluster) of `threads` threads per instance."""
         self.inst = [dict(d) for d in instances]
         n = len(self.inst)
         arr = lambda k, t: np.ascontiguousarray([d[k] for d in self.inst], dtype=t)  # noqa: E731
@@ -23,7 +24,8 @@ class HeatBatch:
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
         h = C.c_void_p()
         L.check(L.load().psf_batch_create(n, ip(self._keep[0]), ip(self._keep[1]), ip(self._keep[2]),
-                                          ip(self._keep[3]), L.ptr(self._keep[4]), int(threads), C.byref(h)))
+                                          ip(self._keep[3]), L.ptr(self._keep[4]), int(threads), int(cluster),
+                                          C.byref(h)))
         self._h, self.n = h, n
 
     def close(self):

@@ -4,9 +4,11 @@
 // (filter + moduli + volume; solve; compliance + sensitivities + filtered
 // sensitivities; OC), captured once as a CUDA graph and replayed.
 //
-// One CTA owns one instance for the whole phase, so every reduction and every
-// barrier of an instance is block-local (__syncthreads, shared memory): no grid
-// barrier, no atomics, deterministic.  Instances are launched largest first.
+// A team owns one instance for the whole phase: one CTA, or the CTAs of a
+// thread-block cluster (2, 4 or 8), so every barrier of an instance is a block or
+// cluster barrier and every reduction is block-local or a fixed-order sum over
+// the team: no grid barrier, no atomics, deterministic.  Instances are launched
+// largest first.
 // The solve is flexible CG in FP64 (operator, dot products, recurrences) whose
 // preconditioner is one FP32 V(2,2) multigrid cycle per iteration: l1-Jacobi
 // smoothing, Galerkin coarse operators built element by element inside the
@@ -62,6 +64,7 @@ struct Args {
     unsigned char *mfix;     // per node, all levels (level 0 copies the Dirichlet flags)
     float *Ainv;
     double *out;             // per instance, kOut values
+    double *red;             // per instance, 2 x kMaxCluster reduction slots
     // parameters
     double k0, kmin, pexp, iota, lmin, lmax, leps, move, eps;
     int itmax, warm;
@@ -89,6 +92,59 @@ __device__ __forceinline__ double bsum(double v, double *sm) {
     double t = lane < nw ? sm[lane] : 0.0;
     t = warp_sum(t);
     return t;
+}
+
+// ---- the team of an instance: the CTAs of one thread-block cluster (a lone CTA when the
+// launch has no clusters).  Loops run over the team's threads, instance-wide barriers are
+// cluster barriers (release / acquire at cluster scope), and sums go through per-instance
+// slots in global memory, read in rank order: deterministic for a fixed team size.
+constexpr int kMaxCluster = 8;
+
+struct Team {
+    int rank, size, idx;
+    long long tid, nt;
+};
+
+__device__ __forceinline__ unsigned cl_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cl_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cl_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ Team team(const Args &A) {
+    Team t;
+    t.size = (int)cl_size();
+    t.rank = (int)cl_rank();
+    t.tid = (long long)t.rank * blockDim.x + threadIdx.x;
+    t.nt = (long long)t.size * blockDim.x;
+    t.idx = A.order[blockIdx.x / t.size];
+    return t;
+}
+
+__device__ __forceinline__ void tsync(const Team &T) {
+    if (T.size > 1) cl_sync();
+    else __syncthreads();
+}
+
+// team-wide sum; the two slot sets alternate so that a set is rewritten only after a later barrier
+__device__ __forceinline__ double tsum(const Args &A, const Team &T, double v, double *sm, int &par) {
+    const double b = bsum(v, sm);
+    if (T.size == 1) return b;
+    double *slot = A.red + ((long long)T.idx * 2 + par) * kMaxCluster;
+    if (threadIdx.x == 0) slot[T.rank] = b;
+    par ^= 1;
+    cl_sync();
+    double s = 0.0;
+    for (int k = 0; k < T.size; k++) s += __ldcg(slot + k);
+    return s;
 }
 
 __device__ __forceinline__ int corner(int di, int dj) { return di ? (dj ? 2 : 1) : (dj ? 3 : 0); }
@@ -205,8 +261,8 @@ __device__ __forceinline__ float opl(const Args &A, const Inst &I, int l, const 
 }
 
 // ------------------------------------------------------------------ multigrid setup (inside the block)
-__device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+__device__ void mg_setup(const Args &A, const Team &T, const Inst &I, double *sm) {
+    const long long tid = T.tid, nt = T.nt;
     // level 0: l1 row sums (E >= 0) and the fixed flags
     {
         const int m = I.n;
@@ -228,7 +284,7 @@ __device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
             A.D[I.mv[0] + v] = fx ? 1.0f : d;
         }
     }
-    __syncthreads();
+    tsync(T);
     for (int l = 1; l < I.nlev; l++) {
         const int mf = I.n >> (l - 1), mc = I.n >> l;
         const long long nnc = (long long)(mc + 1) * (mc + 1);
@@ -237,7 +293,7 @@ __device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
             const int i = (int)(v / (mc + 1)), j = (int)(v % (mc + 1));
             A.mfix[I.mv[l] + v] = A.mfix[I.mv[l - 1] + (long long)(mf + 1) * (2 * i) + 2 * j];
         }
-        __syncthreads();
+        tsync(T);
         // Galerkin element matrices: Kc = sum over the 4 fine children of P_f^T K_f P_f
         const long long nec = (long long)mc * mc;
         for (long long e = tid; e < nec; e += nt) {
@@ -303,7 +359,7 @@ __device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
 #pragma unroll
             for (int q = 0; q < 16; q++) dst[q] = Kc[q];
         }
-        __syncthreads();
+        tsync(T);
         // 9-point stencils and l1 diagonals (identity rows on fixed nodes)
         for (long long v = tid; v < nnc; v += nt) {
             const int i = (int)(v / (mc + 1)), j = (int)(v % (mc + 1));
@@ -334,15 +390,17 @@ __device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
             for (int q = 0; q < 9; q++) dst[q] = st[q];
             A.D[I.mv[l] + v] = d > 0.0f ? d : 1.0f;
         }
-        __syncthreads();
+        tsync(T);
     }
-    // coarsest level: dense matrix from the stencils, Gauss-Jordan inverse in shared memory (FP64)
-    {
+    // coarsest level: dense matrix from the stencils, Gauss-Jordan inverse in the shared memory of
+    // the team's first CTA (FP64)
+    if (T.rank == 0) {
+        const int btid = threadIdx.x, bnt = blockDim.x;
         const int l = I.nlev - 1, mc = I.n >> l, nc = I.nc;
         double *M = sm;   // nc x 2nc
-        for (int t = tid; t < nc * 2 * nc; t += nt) M[t] = 0.0;
+        for (int t = btid; t < nc * 2 * nc; t += bnt) M[t] = 0.0;
         __syncthreads();
-        for (int v = tid; v < nc; v += nt) {
+        for (int v = btid; v < nc; v += bnt) {
             const int i = v / (mc + 1), j = v % (mc + 1);
             const float *st = A.St + (I.mv[l] + v) * 9;
             for (int di = -1; di <= 1; di++)
@@ -359,23 +417,24 @@ __device__ void mg_setup(const Args &A, const Inst &I, double *sm) {
             // the coarse operator is SPD (fixed rows identity): no pivoting
             const double piv = M[k * 2 * nc + k];
             __syncthreads();
-            for (int c = tid; c < 2 * nc; c += nt) M[k * 2 * nc + c] /= piv;
-            for (int r = tid; r < nc; r += nt) fcol[r] = (r == k) ? 0.0 : M[r * 2 * nc + k];
+            for (int c = btid; c < 2 * nc; c += bnt) M[k * 2 * nc + c] /= piv;
+            for (int r = btid; r < nc; r += bnt) fcol[r] = (r == k) ? 0.0 : M[r * 2 * nc + k];
             __syncthreads();
-            for (int t = tid; t < nc * 2 * nc; t += nt) {
+            for (int t = btid; t < nc * 2 * nc; t += bnt) {
                 const int r = t / (2 * nc), c = t % (2 * nc);
                 if (r != k) M[t] -= fcol[r] * M[k * 2 * nc + c];
             }
             __syncthreads();
         }
-        for (int t = tid; t < nc * nc; t += nt) A.Ainv[I.ainv + t] = (float)M[(t / nc) * 2 * nc + nc + (t % nc)];
-        __syncthreads();
+        for (int t = btid; t < nc * nc; t += bnt) A.Ainv[I.ainv + t] = (float)M[(t / nc) * 2 * nc + nc + (t % nc)];
     }
+    tsync(T);
 }
 
 // ------------------------------------------------------------------ the V(2,2) cycle (FP32)
-__device__ void jacobi_sweep(const Args &A, const Inst &I, int l) {
-    const int m = I.n >> l, tid = threadIdx.x, nt = blockDim.x;
+__device__ void jacobi_sweep(const Args &A, const Team &T, const Inst &I, int l) {
+    const int m = I.n >> l;
+    const long long tid = T.tid, nt = T.nt;
     const long long nn = (long long)(m + 1) * (m + 1);
     const float *x = A.mx + I.mv[l];
     float *t = A.mr + I.mv[l];
@@ -384,17 +443,17 @@ __device__ void jacobi_sweep(const Args &A, const Inst &I, int l) {
         const int i = (int)(v / (m + 1)), j = (int)(v % (m + 1));
         t[v] = A.mfix[I.mv[l] + v] ? 0.0f : (b[v] - opl(A, I, l, x, i, j)) / A.D[I.mv[l] + v];
     }
-    __syncthreads();
+    tsync(T);
     float *xw = A.mx + I.mv[l];
     for (long long v = tid; v < nn; v += nt) xw[v] += t[v];
-    __syncthreads();
+    tsync(T);
 }
 
-__device__ void vcycle(const Args &A, const Inst &I) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+__device__ void vcycle(const Args &A, const Team &T, const Inst &I) {
+    const long long tid = T.tid, nt = T.nt;
     for (int l = 0; l < I.nlev - 1; l++) {
-        jacobi_sweep(A, I, l);
-        jacobi_sweep(A, I, l);
+        jacobi_sweep(A, T, I, l);
+        jacobi_sweep(A, T, I, l);
         // residual into mr
         const int m = I.n >> l;
         const long long nn = (long long)(m + 1) * (m + 1);
@@ -406,7 +465,7 @@ __device__ void vcycle(const Args &A, const Inst &I) {
                 r[v] = A.mfix[I.mv[l] + v] ? 0.0f : b[v] - opl(A, I, l, x, i, j);
             }
         }
-        __syncthreads();
+        tsync(T);
         // restriction (P^T, fixed nodes masked) and the first sweep of the coarse level from zero
         const int mc = m >> 1;
         const long long nnc = (long long)(mc + 1) * (mc + 1);
@@ -426,18 +485,18 @@ __device__ void vcycle(const Args &A, const Inst &I) {
             A.mb[I.mv[l + 1] + v] = acc;
             A.mx[I.mv[l + 1] + v] = 0.0f;
         }
-        __syncthreads();
+        tsync(T);
     }
     // coarsest: x = Ainv b
     {
         const int l = I.nlev - 1, nc = I.nc;
         const float *Ai = A.Ainv + I.ainv, *b = A.mb + I.mv[l];
-        for (int v = tid; v < nc; v += nt) {
+        for (long long v = tid; v < nc; v += nt) {
             float acc = 0.0f;
             for (int c = 0; c < nc; c++) acc += Ai[v * nc + c] * b[c];
             A.mx[I.mv[l] + v] = acc;
         }
-        __syncthreads();
+        tsync(T);
     }
     for (int l = I.nlev - 2; l >= 0; l--) {
         const int m = I.n >> l, mc = m >> 1;
@@ -452,14 +511,13 @@ __device__ void vcycle(const Args &A, const Inst &I) {
                                      xc[(long long)(mc + 1) * i1 + j0] + xc[(long long)(mc + 1) * i1 + j1]);
             x[v] += c;
         }
-        __syncthreads();
-        jacobi_sweep(A, I, l);
-        jacobi_sweep(A, I, l);
+        tsync(T);
+        jacobi_sweep(A, T, I, l);
+        jacobi_sweep(A, T, I, l);
     }
 }
 
 // ------------------------------------------------------------------ phase kernels
-__device__ __forceinline__ const Inst &inst_of(const Args &A) { return A.inst[A.order[blockIdx.x]]; }
 
 __device__ __forceinline__ double filt(const Args &A, const Inst &I, const double *v, int i, int j) {
     const int n = I.n;
@@ -475,12 +533,14 @@ __device__ __forceinline__ double filt(const Args &A, const Inst &I, const doubl
 // rho = filter(s), E = kmin + (k0 - kmin) rho^p, g = sum(rho) / (vf n^2) - 1
 __global__ void __launch_bounds__(kThreads) filter_moduli_batch(const __grid_constant__ Args A) {
     __shared__ double sm[32];
-    const Inst &I = inst_of(A);
+    const Team T = team(A);
+    const Inst &I = A.inst[T.idx];
+    int par = 0;
     const int n = I.n;
     const long long ne = (long long)n * n;
     const double *s = A.s + I.e0;
     double vol = 0.0;
-    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+    for (long long e = T.tid; e < ne; e += T.nt) {
         const int i = (int)(e / n), j = (int)(e % n);
         const double r = filt(A, I, s, i, j) / A.wsum[I.e0 + e];
         A.rho[I.e0 + e] = r;
@@ -490,22 +550,25 @@ __global__ void __launch_bounds__(kThreads) filter_moduli_batch(const __grid_con
         A.Ef[I.e0 + e] = (float)Ee;
         vol += r;
     }
-    vol = bsum(vol, sm);
-    if (threadIdx.x == 0) A.out[(long long)A.order[blockIdx.x] * kOut + O_G] = vol / (I.vf * (double)ne) - 1.0;
+    vol = tsum(A, T, vol, sm, par);
+    if (T.tid == 0) A.out[(long long)T.idx * kOut + O_G] = vol / (I.vf * (double)ne) - 1.0;
 }
 
 // flexible CG (FP64) with one FP32 V-cycle per iteration; FP64 true residual checks
 __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ Args A) {
     extern __shared__ double dyn[];
     double *sm = dyn;            // 32 doubles of reduction space, then the coarse inverse workspace
-    const Inst &I = inst_of(A);
-    const int idx = A.order[blockIdx.x];
-    const int n = I.n, tid = threadIdx.x, nt = blockDim.x;
+    const Team T = team(A);
+    const Inst &I = A.inst[T.idx];
+    int par = 0;
+    const int idx = T.idx;
+    const int n = I.n;
+    const long long tid = T.tid, nt = T.nt;
     const long long nn = (long long)(n + 1) * (n + 1);
     double *x = A.x + I.v0, *r = A.r + I.v0, *z = A.z + I.v0, *p = A.p + I.v0, *q = A.q + I.v0;
     const double *F = A.F + I.v0;
     const unsigned char *fx = A.fixed + I.v0;
-    mg_setup(A, I, sm + 32);
+    mg_setup(A, T, I, sm + 32);
     int total = 0, passes = 0;
     bool conv = false;
     double rr = 0.0, bb = 0.0;
@@ -516,7 +579,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
         for (long long v = tid; v < nn; v += nt) {
             if (pass == 0 && !A.warm) x[v] = 0.0;
         }
-        __syncthreads();
+        tsync(T);
         for (long long v = tid; v < nn; v += nt) {
             const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
             const double bv = fx[v] ? 0.0 : F[v];
@@ -527,8 +590,8 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
             acc[0] += rv * rv;
             acc[1] += bv * bv;
         }
-        rr = bsum(acc[0], sm);
-        bb = bsum(acc[1], sm);
+        rr = tsum(A, T, acc[0], sm, par);
+        bb = tsum(A, T, acc[1], sm, par);
         if (bb == 0.0 || rr <= A.eps * A.eps * bb) {
             conv = true;
             break;
@@ -544,8 +607,8 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
                 A.mb[I.mv[0] + v] = bv;
                 A.mx[I.mv[0] + v] = fx[v] ? 0.0f : bv / A.D[I.mv[0] + v];
             }
-            __syncthreads();
-            vcycle(A, I);
+            tsync(T);
+            vcycle(A, T, I);
             double a3[3] = {0.0, 0.0, 0.0};
             for (long long v = tid; v < nn; v += nt) {
                 const double zv = fx[v] ? 0.0 : rn * (double)A.mx[I.mv[0] + v];
@@ -554,11 +617,11 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
                 a3[1] += zv * r[v];
                 a3[2] += p[v] * r[v];
             }
-            const double zq = bsum(a3[0], sm), zr = bsum(a3[1], sm), pr0 = bsum(a3[2], sm);
+            const double zq = tsum(A, T, a3[0], sm, par), zr = tsum(A, T, a3[1], sm, par), pr0 = tsum(A, T, a3[2], sm, par);
             const double beta = it > 0 ? zq / pq_prev : 0.0;
             const double pr = zr - beta * pr0;
             for (long long v = tid; v < nn; v += nt) p[v] = z[v] - beta * p[v];
-            __syncthreads();
+            tsync(T);
             double pqa = 0.0;
             for (long long v = tid; v < nn; v += nt) {
                 const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
@@ -566,7 +629,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
                 q[v] = qv;
                 pqa += p[v] * qv;
             }
-            const double pq = bsum(pqa, sm);
+            const double pq = tsum(A, T, pqa, sm, par);
             if (!(pq > 0.0)) break;
             const double alpha = pr / pq;
             double ra = 0.0;
@@ -576,7 +639,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
                 r[v] = rv;
                 ra += rv * rv;
             }
-            rr = bsum(ra, sm);
+            rr = tsum(A, T, ra, sm, par);
             pq_prev = pq;
             if (rr <= A.eps * A.eps * bb || !isfinite(rr)) break;
         }
@@ -587,10 +650,10 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
             const double rv = fx[v] ? 0.0 : F[v] - op64(A, I, x, i, j);
             ta += rv * rv;
         }
-        rr = bsum(ta, sm);
+        rr = tsum(A, T, ta, sm, par);
         conv = rr <= A.eps * A.eps * bb;
     }
-    if (tid == 0) {
+    if (T.tid == 0) {
         double *o = A.out + (long long)idx * kOut;
         o[O_ITERS] = total;
         o[O_RES] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
@@ -602,17 +665,19 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
 // f = sum_e E_e T_e.Ke0 T_e; dfdrho = -p (k0 - kmin) rho^(p-1) T_e.Ke0 T_e; filtered sensitivities
 __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ Args A) {
     __shared__ double sm[32];
-    const Inst &I = inst_of(A);
+    const Team T = team(A);
+    const Inst &I = A.inst[T.idx];
+    int par = 0;
     const int n = I.n;
     const long long ne = (long long)n * n;
-    const double *T = A.x + I.v0;
+    const double *Tv = A.x + I.v0;
     double f = 0.0;
-    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+    for (long long e = T.tid; e < ne; e += T.nt) {
         const int i = (int)(e / n), j = (int)(e % n);
         double te[4];
 #pragma unroll
         for (int a = 0; a < 4; a++)
-            te[a] = T[(long long)(n + 1) * (i + (a == 1 || a == 2)) + (j + (a == 2 || a == 3))];
+            te[a] = Tv[(long long)(n + 1) * (i + (a == 1 || a == 2)) + (j + (a == 2 || a == 3))];
         double qv = 0.0;
 #pragma unroll
         for (int a = 0; a < 4; a++) {
@@ -624,11 +689,11 @@ __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ A
         A.dfdrho[I.e0 + e] = -A.pexp * (-A.kmin + A.k0) * powp(A.rho[I.e0 + e], A.pexp - 1.0) * qv;
         f += A.E[I.e0 + e] * qv;
     }
-    f = bsum(f, sm);
-    if (threadIdx.x == 0) A.out[(long long)A.order[blockIdx.x] * kOut + O_F] = f;
-    __syncthreads();
+    f = tsum(A, T, f, sm, par);
+    if (T.tid == 0) A.out[(long long)T.idx * kOut + O_F] = f;
+    tsync(T);
     const double dg = 1.0 / (I.vf * (double)ne);
-    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+    for (long long e = T.tid; e < ne; e += T.nt) {
         const int i = (int)(e / n), j = (int)(e % n);
         const double w = A.wsum[I.e0 + e];
         A.dfds[I.e0 + e] = filt(A, I, A.dfdrho + I.e0, i, j) / w;
@@ -649,16 +714,18 @@ __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ A
 // weights vw precomputed.
 __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Args A) {
     __shared__ double sm[32];
-    const Inst &I = inst_of(A);
+    const Team T = team(A);
+    const Inst &I = A.inst[T.idx];
+    int par = 0;
     const int n = I.n;
     const long long ne = (long long)n * n;
     double *x = A.s + I.e0, *xn = A.snew + I.e0, *Bp = A.Bp + I.e0;
     const double *dfdx = A.dfds + I.e0, *dgdx = A.dgds + I.e0, *vw = A.vw + I.e0;
-    for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+    for (long long e = T.tid; e < ne; e += T.nt) {
         const double b = -dfdx[e] / dgdx[e];
         Bp[e] = x[e] * (A.iota == 0.5 ? sqrt(b) : pow(b, A.iota));
     }
-    __syncthreads();
+    tsync(T);
     const double vscale = 1.0 / (I.vf * (double)ne);
     double l0 = A.lmin, l1 = A.lmax, lambda = 0.0;
     int steps = 0;
@@ -667,7 +734,7 @@ __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Arg
         steps++;
         const double li = A.iota == 0.5 ? 1.0 / sqrt(lambda) : pow(lambda, -A.iota);
         double vol = 0.0;
-        for (long long e = threadIdx.x; e < ne; e += blockDim.x) {
+        for (long long e = T.tid; e < ne; e += T.nt) {
             const double xe = x[e];
             double v = Bp[e] * li;
             const double lo0 = (1.0 - A.move) * xe, hi0 = (1.0 + A.move) * xe;
@@ -678,15 +745,15 @@ __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Arg
             xn[e] = v;
             vol += vw[e] * v;
         }
-        vol = bsum(vol, sm);
+        vol = tsum(A, T, vol, sm, par);
         const double g = vol * vscale - 1.0;
         if (g > 0.0) l0 = lambda;
         else l1 = lambda;
     }
-    __syncthreads();
-    for (long long e = threadIdx.x; e < ne; e += blockDim.x) x[e] = xn[e];
-    if (threadIdx.x == 0) {
-        double *o = A.out + (long long)A.order[blockIdx.x] * kOut;
+    tsync(T);
+    for (long long e = T.tid; e < ne; e += T.nt) x[e] = xn[e];
+    if (T.tid == 0) {
+        double *o = A.out + (long long)T.idx * kOut;
         o[O_LAMBDA] = lambda;
         o[O_BISECT] = steps;
     }
@@ -707,6 +774,7 @@ struct psf_batch {
     size_t ne_tot = 0, nv_tot = 0, mg_nodes = 0, mg_elems = 0, ainv_tot = 0;
     size_t smem = 0;
     int threads = psf::batch::kThreads;
+    int cluster = 1;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -740,14 +808,28 @@ void batch_free(psf_batch *b) {
     delete b;
 }
 
+// one phase over all instances: a team of `cluster` CTAs per instance
+cudaError_t launch_phase(psf_batch *b, void (*kern)(Args), size_t smem) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(b->ninst * b->cluster));
+    cfg.blockDim = dim3((unsigned)b->threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = b->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)b->cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = b->cluster > 1 ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, b->a);
+}
+
 psf_status launch_phases(psf_batch *b) {
-    const Args &a = b->a;
-    const int nb = b->ninst, nt = b->threads;
-    psf::batch::filter_moduli_batch<<<nb, nt, 0, b->stream>>>(a);
-    psf::batch::solve_batch<<<nb, nt, b->smem, b->stream>>>(a);
-    psf::batch::sens_batch<<<nb, nt, 0, b->stream>>>(a);
-    psf::batch::oc_batch<<<nb, nt, 0, b->stream>>>(a);
-    PSF_CUDA(cudaGetLastError());
+    PSF_CUDA(launch_phase(b, psf::batch::filter_moduli_batch, 0));
+    PSF_CUDA(launch_phase(b, psf::batch::solve_batch, b->smem));
+    PSF_CUDA(launch_phase(b, psf::batch::sens_batch, 0));
+    PSF_CUDA(launch_phase(b, psf::batch::oc_batch, 0));
     return PSF_OK;
 }
 
@@ -756,8 +838,12 @@ psf_status launch_phases(psf_batch *b) {
 extern "C" {
 
 psf_status psf_batch_create(int ninst, const int *side, const int *edge, const int *patch_w, const int *patch_i0,
-                            const double *vf, int threads, psf_batch **out) {
+                            const double *vf, int threads, int cluster, psf_batch **out) {
     if (!out || ninst < 1 || !side || !edge || !patch_w || !patch_i0 || !vf) return PSF_BAD_INPUT;
+    if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != psf::batch::kMaxCluster) {
+        psf::set_error("psf_batch_create: cluster must be 1, 2, 4 or 8");
+        return PSF_BAD_INPUT;
+    }
     if (threads != 128 && threads != 256 && threads != psf::batch::kThreads) {
         psf::set_error("psf_batch_create: threads must be 128, 256 or 512 (the kernels' launch bound)");
         return PSF_BAD_INPUT;
@@ -772,6 +858,7 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     psf_batch *b = new psf_batch();
     b->ninst = ninst;
     b->threads = threads;
+    b->cluster = cluster;
     b->hinst.resize(ninst);
     size_t ne = 0, nv = 0, mgn = 0, mge = 0, ai = 0;
     int ncmax = 0;
@@ -845,6 +932,7 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     ck(balloc(b, &a.mfix, mgn));
     ck(balloc(b, &a.Ainv, ai));
     ck(balloc(b, &a.out, (size_t)ninst * psf::batch::kOut));
+    ck(balloc(b, &a.red, (size_t)ninst * 2 * psf::batch::kMaxCluster));
     if (s != PSF_OK) {
         batch_free(b);
         return s;
@@ -1011,16 +1099,14 @@ psf_status psf_batch_profile(psf_batch *b, double *phase_seconds) {
     if (!b || !b->begun || !phase_seconds) return PSF_BAD_INPUT;
     cudaEvent_t ev[5];
     for (auto &e : ev) PSF_CUDA(cudaEventCreate(&e));
-    const Args &a = b->a;
-    const int nb = b->ninst, nt = b->threads;
     PSF_CUDA(cudaEventRecord(ev[0], b->stream));
-    psf::batch::filter_moduli_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(launch_phase(b, psf::batch::filter_moduli_batch, 0));
     PSF_CUDA(cudaEventRecord(ev[1], b->stream));
-    psf::batch::solve_batch<<<nb, nt, b->smem, b->stream>>>(a);
+    PSF_CUDA(launch_phase(b, psf::batch::solve_batch, b->smem));
     PSF_CUDA(cudaEventRecord(ev[2], b->stream));
-    psf::batch::sens_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(launch_phase(b, psf::batch::sens_batch, 0));
     PSF_CUDA(cudaEventRecord(ev[3], b->stream));
-    psf::batch::oc_batch<<<nb, nt, 0, b->stream>>>(a);
+    PSF_CUDA(launch_phase(b, psf::batch::oc_batch, 0));
     PSF_CUDA(cudaEventRecord(ev[4], b->stream));
     PSF_CUDA(cudaEventSynchronize(ev[4]));
     for (int k = 0; k < 4; k++) {

@@ -932,6 +932,7 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     psf_solve_info inf{};
     psf_status s = mg_solve(c, 20000, 1e-8, false, &inf);
     c->Fn = Fn_saved;
+    if (s == PSF_NOT_CONVERGED) return PSF_NOT_CONVERGED;   // the caller skips this pair
     if (s != PSF_OK) return s;
     PSF_CUDA(cudaMemcpyAsync(e64, c->un, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st));
     tgt_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, e64, L->isd, L->sc, tgt_out, mask_out, L->part);
@@ -1034,6 +1035,7 @@ psf_status learned_harvest(Ctx *c, psf_trainset *ts, int npairs, const int *iter
             default: s = harvest_pair<PSF_Q4_HEAT>(c, L, rbuf, rhs, ebuf, ts, slot);
         }
         if (s == PSF_OK) ts->n++;
+        else if (s == PSF_NOT_CONVERGED) s = PSF_OK;   // no exact target for this residual: skip the pair
     }
     cudaMemcpyAsync(c->un, un_saved, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, st);
     if (s == PSF_OK) s = gather_reduced(c, c->un, c->u);

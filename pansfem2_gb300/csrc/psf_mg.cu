@@ -26,8 +26,8 @@ namespace psf {
 
 constexpr int kMaxLev = 14;
 // coarsen while the level has more dofs than this: the dense FP64 inverse of the
-// coarsest level costs O(n^3) on one block, so keep n at about a hundred
-constexpr long long kCoarseDofs = 100;
+// coarsest level is built by one block in n dependent steps, so keep n small
+constexpr long long kCoarseDofs = 40;
 
 struct KeF {
     float v[576];

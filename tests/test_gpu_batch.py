@@ -28,10 +28,12 @@ def gpu():
     return P
 
 
-@pytest.fixture(scope="module")
-def batched(gpu):
+@pytest.fixture(scope="module", params=[(256, 1), (256, 4), (512, 8)], ids=lambda p: f"{p[0]}x{p[1]}")
+def batched(gpu, request):
+    """threads per CTA x CTAs per instance (a thread-block cluster)"""
     from pansfem2_gb300.batch import HeatBatch
-    with HeatBatch(INSTANCES, threads=256) as B:
+    threads, cluster = request.param
+    with HeatBatch(INSTANCES, threads=threads, cluster=cluster) as B:
         B.begin(cg_eps=1e-10, cg_itmax=5000, warm_start=True)
         fs, res = [], []
         for _ in range(ITERS):
