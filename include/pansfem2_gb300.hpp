@@ -226,6 +226,32 @@ private:
     std::vector<T> w_;
 };
 
+// ------------------------------------------------------------------ SensitivityFilter (SensitivityFilter.h:16-99)
+// Sigmund's scheme (SensitivityFilter) and Borrvall's (SensitivityFilter2) on the
+// structured grid's filter of radius R.
+template <class T>
+class SensitivityFilter {
+public:
+    SensitivityFilter(Problem &p, double R, int mode = 0) : n_((int)p.ne()), mode_(mode), prob_(&p) {
+        check(psf_filter_setup(p.ctx(), R), false);
+    }
+    std::vector<T> GetFilteredSensitivitis(std::vector<T> s, std::vector<T> dfds) {
+        std::vector<T> out(n_);
+        check(psf_sensitivity_filter(prob_->ctx(), mode_, s.data(), dfds.data(), out.data()), false);
+        return out;
+    }
+
+private:
+    int n_, mode_;
+    Problem *prob_;
+};
+
+template <class T>
+class SensitivityFilter2 : public SensitivityFilter<T> {
+public:
+    SensitivityFilter2(Problem &p, double R) : SensitivityFilter<T>(p, R, 1) {}
+};
+
 // ------------------------------------------------------------------ OC (OC.h:16-107)
 // The samples' constraint callback (sample_optimize_density_oc.cpp:198-207):
 // filtered volume fraction g(x) = sum_i scale1*rho_i(x)/(vf*n) - scale1.

@@ -119,6 +119,10 @@ psf_status psf_filter_setup(psf_ctx *ctx, double R);
 psf_status psf_filter_forward(psf_ctx *ctx, const double *s, double *rho);
 /* GetFilteredSensitivitis (DensityFilter.h:59-71): dfds_i = sum_j w_ij dfdrho_j / wsum_i. */
 psf_status psf_filter_backward(psf_ctx *ctx, const double *dfdrho, double *dfds);
+/* SensitivityFilter::GetFilteredSensitivitis (Sigmund's scheme, SensitivityFilter.h:38-50) for
+ * mode 0, SensitivityFilter2 (Borrvall's scheme, :78-90) for mode 1, on the filter of
+ * psf_filter_setup: out_i = sum_j w_ij s_j d_j / (wsum_i s_i), resp. / sum_j w_ij s_j (host arrays) */
+psf_status psf_sensitivity_filter(psf_ctx *ctx, int mode, const double *s, const double *dfds_in, double *dfds_out);
 
 /* Compliance and sensitivities of sample_optimize_density_oc.cpp:136-162 for the
  * solved u: f = scale0 * u.K u and dfdrho_e = -scale0*p*(E1 - E0)*rho_e^(p-1) u_e.Ke(1) u_e.

@@ -834,6 +834,21 @@ void orc_density_filter_sens(int n, const int *ptr, const int *idx, const double
     }
 }
 
+/* SensitivityFilter::GetFilteredSensitivitis (Sigmund's scheme, SensitivityFilter.h:38-50),
+ * mode 0: dfds_i = sum_j w_ij s_j d_j / (wsum_i s_i);
+ * SensitivityFilter2 (Borrvall's scheme, :78-90), mode 1: / sum_j w_ij s_j */
+void orc_sensitivity_filter(int n, const int *ptr, const int *idx, const double *w, const double *s,
+                            const double *d, int mode, double *out) {
+    for (int i = 0; i < n; i++) {
+        double wsum = 0.0, v = 0.0;
+        for (int k = ptr[i]; k < ptr[i + 1]; k++) {
+            v += w[k] * s[idx[k]] * d[idx[k]];
+            wsum += mode ? w[k] * s[idx[k]] : w[k];
+        }
+        out[i] = mode ? v / wsum : v / (wsum * s[i]);
+    }
+}
+
 /* HeavisideFilter::GetFilteredVariables (HeavisideFilter.h:60-73) */
 void orc_heaviside_filter(int n, const int *ptr, const int *idx, const double *w, double beta,
                           const double *s, double *rho) {

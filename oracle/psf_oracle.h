@@ -93,6 +93,8 @@ long long orc_neighbors(int ne, int dim, const double *cg, double R, const int *
 void orc_free(void *p);
 void orc_density_filter(int n, const int *ptr, const int *idx, const double *w,
                         const double *s, double *rho);                       /* DensityFilter.h:44-56 */
+void orc_sensitivity_filter(int n, const int *ptr, const int *idx, const double *w, const double *s,
+                            const double *d, int mode, double *out);
 void orc_density_filter_sens(int n, const int *ptr, const int *idx, const double *w,
                              const double *dfdrho, double *dfds);            /* DensityFilter.h:59-71 */
 void orc_heaviside_filter(int n, const int *ptr, const int *idx, const double *w, double beta,

@@ -213,6 +213,14 @@ def density_filter_sens(ptr, idx, w, d):
     return out
 
 
+def sensitivity_filter(ptr, idx, w, s, d, mode=0):
+    """SensitivityFilter (mode 0, Sigmund) / SensitivityFilter2 (mode 1, Borrvall)."""
+    out = np.zeros(len(ptr) - 1)
+    _lib().orc_sensitivity_filter(len(out), P(i32(ptr), ip), P(i32(idx), ip), P(f64(w)), P(f64(s)), P(f64(d)),
+                                  int(mode), P(out))
+    return out
+
+
 def heaviside_filter(ptr, idx, w, beta, s):
     out = np.zeros(len(ptr) - 1)
     _lib().orc_heaviside_filter(len(out), P(i32(ptr), ip), P(i32(idx), ip), P(f64(w)), C.c_double(beta),

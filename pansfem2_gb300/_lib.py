@@ -29,7 +29,8 @@ SOLVERS = {
 EXPORTS = [
     "psf_create", "psf_destroy", "psf_last_error", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
     "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_solve",
-    "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_compliance_sensitivity",
+    "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_sensitivity_filter",
+    "psf_compliance_sensitivity",
     "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_simp_begin", "psf_simp_step",
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
@@ -116,6 +117,7 @@ def load(path=LIB_PATH):
         "psf_filter_setup": [vp, C.c_double],
         "psf_filter_forward": [vp, dp, dp],
         "psf_filter_backward": [vp, dp, dp],
+        "psf_sensitivity_filter": [vp, C.c_int, dp, dp, dp],
         "psf_compliance_sensitivity": [vp, dp, C.c_double, C.c_double, C.c_double, C.c_double, dp, dp],
         "psf_oc_update": [vp, dp, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                           C.c_double, C.c_double, dp],

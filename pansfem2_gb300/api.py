@@ -135,6 +135,12 @@ class Problem:
         check(self.L.psf_filter_backward(self.h, ptr(d), ptr(out)))
         return out
 
+    def sensitivity_filter(self, s, d, mode=0):
+        """SensitivityFilter (mode 0) / SensitivityFilter2 (mode 1) of d at design s."""
+        out = np.zeros(self.ne)
+        check(self.L.psf_sensitivity_filter(self.h, int(mode), ptr(f64(s)), ptr(f64(d)), ptr(out)))
+        return out
+
     def compliance_sensitivity(self, rho):
         rho = f64(rho)
         f = C.c_double()

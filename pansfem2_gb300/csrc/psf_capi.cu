@@ -261,6 +261,21 @@ psf_status psf_filter_backward(psf_ctx *h, const double *dfdrho, double *dfds) {
     return d2h_sync(c, dfds, c->dfds, sizeof(double) * c->ne);
 }
 
+psf_status psf_sensitivity_filter(psf_ctx *h, int mode, const double *s, const double *dfds_in, double *dfds_out) {
+    CTX_CHECK(h);
+    Ctx *c = &h->c;
+    if (!s || !dfds_in || !dfds_out || mode < 0 || mode > 1) {
+        set_error("psf_sensitivity_filter: null array or mode not 0/1");
+        return PSF_BAD_INPUT;
+    }
+    if (c->filt_n <= 0) { set_error("psf_sensitivity_filter: call psf_filter_setup first"); return PSF_BAD_INPUT; }
+    // scratch: snew (design), dfdrho (input), dfds (output)
+    PSF_CHECK(h2d(c, c->snew, s, sizeof(double) * c->ne));
+    PSF_CHECK(h2d(c, c->dfdrho, dfds_in, sizeof(double) * c->ne));
+    PSF_CHECK(sensitivity_filter(c, c->snew, c->dfdrho, mode, c->dfds));
+    return d2h_sync(c, dfds_out, c->dfds, sizeof(double) * c->ne);
+}
+
 psf_status psf_compliance_sensitivity(psf_ctx *h, const double *rho, double E1, double E0, double p,
                                       double scale0, double *f, double *dfdrho) {
     CTX_CHECK(h);
@@ -295,7 +310,7 @@ psf_status psf_mma_init(psf_ctx *h, double a0, double a, double cc, double d, do
         PSF_CHECK(dzalloc(c, &c->mma_U, c->ne));
         PSF_CHECK(dzalloc(c, &c->mma_xkm1, c->ne));
         PSF_CHECK(dzalloc(c, &c->mma_xkm2, c->ne));
-        PSF_CHECK(dzalloc(c, &c->mma_work, 15 * c->ne));
+        PSF_CHECK(dzalloc(c, &c->mma_work, 17 * c->ne));
     } else {
         PSF_CUDA(cudaMemsetAsync(c->mma_xkm1, 0, sizeof(double) * c->ne, c->stream));
         PSF_CUDA(cudaMemsetAsync(c->mma_xkm2, 0, sizeof(double) * c->ne, c->stream));

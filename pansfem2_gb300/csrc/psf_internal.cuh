@@ -164,6 +164,7 @@ psf_status gather_reduced(Ctx *c, const double *nodal, double *red);   // psf_me
 psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_solve.cu
 psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward);               // psf_opt.cu
 psf_status heaviside_back(Ctx *c, const double *d, double *out);                            // psf_opt.cu
+psf_status sensitivity_filter(Ctx *c, const double *s, const double *d, int mode, double *out);  // psf_opt.cu
 psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, double p, double scale0,
                            double *f_dev, double *dfdrho);                                 // psf_opt.cu
 psf_status oc_update(Ctx *c, double *x, const double *dfdx, const double *dgdx, double iota, double lmin,

@@ -249,7 +249,7 @@ struct MmaArgs {
     const double *dfdx, *dgdx;
     double g;                         // constraint value
     double *L, *U, *xkm1, *xkm2;      // state
-    double *w;                        // 15*n work
+    double *w;                        // 17*n work
     int k;                            // outer counter
     double a0, a, c, d, xmin, xmax;
     double raa0, albefa, move, asyinit, asydecr, asyincr;
@@ -274,6 +274,7 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
            *x = A.w + 6 * n, *gsi = A.w + 7 * n, *ita = A.w + 8 * n, *G = A.w + 9 * n, *Dx = A.w + 10 * n,
            *dtx = A.w + 11 * n, *dx = A.w + 12 * n, *dgsi = A.w + 13 * n;
     double *dita = A.w + 14 * n;
+    double *iam = A.w + 15 * n, *ibm = A.w + 16 * n;   // 1 / (x - alpha), 1 / (beta - x) at the Newton point
     const double xr = A.xmax - A.xmin;
     // ---- asymptotes, move limits, p/q, b (MMA.h:118-175), start point (:178-197)
     {
@@ -346,6 +347,7 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
             const double iDx = 1.0 / Dxj;
             const double dtxj = plj * iux2 - qlj * ixl2 - eps * ia + eps * ib;
             G[j] = Gj; Dx[j] = iDx; dtx[j] = dtxj;
+            iam[j] = ia; ibm[j] = ib;
             acc[0] += Gj * Gj * iDx;
             acc[1] += Gj * dtxj * iDx;
             acc[2] += p1[j] * iux + q1[j] * ixl;
@@ -387,7 +389,7 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
         // ---- phase 2: Newton direction in x, step-length bound
         double tx = -INFINITY;
         for (long long j = tid; j < n; j += stride) {
-            const double xj = x[j], ia = 1.0 / (xj - al[j]), ib = 1.0 / (be[j] - xj);
+            const double ia = iam[j], ib = ibm[j];   // x is unchanged since phase 1
             const double dxj = -(dtx[j] + G[j] * dl) * Dx[j];   // Dx holds 1/Dx
             const double dg = -gsi[j] * dxj * ia - gsi[j] + eps * ia;
             const double di = ita[j] * dxj * ib - ita[j] + eps * ib;
@@ -498,6 +500,38 @@ psf_status filter_setup(Ctx *c, double R) {
     delete S;
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
+}
+
+// SensitivityFilter (Sigmund, SensitivityFilter.h:38-50): sum_j w_ij s_j d_j / (wsum_i s_i);
+// SensitivityFilter2 (Borrvall, :78-90): sum_j w_ij s_j d_j / sum_j w_ij s_j
+__global__ void sens_filter_kernel(const __grid_constant__ Stencil S, long long ne, const double *__restrict__ s,
+                                   const double *__restrict__ d, const double *__restrict__ wsum, int mode,
+                                   double *__restrict__ out) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        elem_ijk(S, e, i, j, k);
+        double v = 0.0, ws = 0.0;
+        for (int q = 0; q < S.n; q++) {
+            const int a = i + S.di[q], b = j + S.dj[q], c = k + S.dk[q];
+            if (a < 0 || a >= S.nx || b < 0 || b >= S.ny || (S.is3d && (c < 0 || c >= S.nz))) continue;
+            const long long m = S.is3d ? ((long long)S.ny * a + b) * S.nz + c : (long long)S.ny * a + b;
+            v += S.w[q] * s[m] * d[m];
+            ws += S.w[q] * s[m];
+        }
+        out[e] = mode ? v / ws : v / (wsum[e] * s[e]);
+    }
+}
+
+psf_status sensitivity_filter(Ctx *c, const double *s, const double *d, int mode, double *out) {
+    Stencil *S = new Stencil;
+    psf_status st = get_stencil(c, S);
+    if (st == PSF_OK) {
+        sens_filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, s, d, c->filt_wsum, mode,
+                                                                                out);
+        if (cudaGetLastError() != cudaSuccess) st = PSF_CUDA_ERROR;
+    }
+    delete S;
+    return st;
 }
 
 __global__ void mul_kernel(long long n, const double *__restrict__ a, const double *__restrict__ b,

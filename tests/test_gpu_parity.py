@@ -236,3 +236,23 @@ def test_full_size_properties_mbb_1024x512(gpu):
         # same solution from every path (to the accuracy a 1e-8 residual buys)
         for solver in ("ir_jacobi_f32", "ir_mg_f32"):
             assert rel(sols[solver], sols["ebe_jacobi_f64"]) < 1e-5, solver
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("name", ["cantilever_60x30_oc", "cantilever_h8_6x3x3_oc"])
+def test_sensitivity_filters_match_oracle(gpu, name, mode):
+    """SensitivityFilter (Sigmund, mode 0) and SensitivityFilter2 (Borrvall, mode 1) on the
+    grid's filter against the oracle's list form (neighbour lists of the reference samples)."""
+    g, pr = load(name), CASES[name]()
+    coords, conn, dim = geometry(pr)
+    ne = PB.counts(pr)[0]
+    ptr, idx, w = O.neighbors(O.centroids(conn, coords, dim), pr["R"])
+    rng = np.random.default_rng(mode + ne)
+    s = rng.uniform(0.05, 1.0, ne)
+    d = -rng.uniform(0.0, 10.0, ne)
+    ref = O.sensitivity_filter(ptr, idx, w, s, d, mode)
+    with gpu.Problem(pr) as P:
+        P.setup_bc()
+        P.filter_setup()
+        out = P.sensitivity_filter(s, d, mode)
+    assert np.max(np.abs(out - ref)) <= TOL_FILTER * np.max(np.abs(ref))
