@@ -393,7 +393,7 @@ def bench_learned2d(args, rank, world):
     t_harvest = time.perf_counter() - t0
     net = Ln.UNet(H, W, batch=8, seed=3)
     t0 = time.perf_counter()
-    hist = Ln.train(net, ts, args.train_steps, batch=8, lr=1e-3, seed=5, loss="energy")
+    hist = Ln.train(net, ts, args.train_steps, batch=8, lr=1e-3, seed=5, loss="angle")
     t_train = time.perf_counter() - t0
     pr = PB.mbb_q4(nx, ny)
     res = {}

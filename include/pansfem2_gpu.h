@@ -299,13 +299,18 @@ psf_status psf_learned_harvest(psf_ctx *ctx, psf_trainset *ts, int npairs, const
  * cosine decay from lr).  loss_mode 0: mean squared error of the target
  * D^1/2 K^-1 r1 / s; 1: energy norm of the correction's error,
  * (y - t) . K^ (y - t) / t . K^ t with K^ = D^-1/2 K D^-1/2 (the norm flexible
- * CG minimises).  loss_hist (may be NULL) receives per step the loss relative
- * to that of a zero output (1 = nothing learned) */
+ * CG minimises); 2: its scale-free form 1 - (y . rhat)^2 / ((y . K^ y)(t . rhat)),
+ * the error left by the best multiple of the correction (the solver applies the
+ * correction with that energy-optimal step; batch <= 16).  loss_hist (may be NULL)
+ * receives per step the loss relative to that of a zero output (1 = nothing learned) */
 psf_status psf_learned_train(psf_unet *net, psf_trainset *ts, int steps, int batch, float lr, uint64_t seed,
                              int loss_mode, double *loss_hist);
 /* mean over pairs [first, first + count) of the energy-norm error of the
- * network's correction relative to that of no correction (1 = no gain) */
-psf_status psf_learned_eval(psf_unet *net, psf_trainset *ts, int first, int count, double *mean_rel_energy);
+ * network's correction relative to that of no correction (1 = no gain):
+ * mode 1 as the network outputs it, mode 2 with the energy-optimal step the
+ * solver applies */
+psf_status psf_learned_eval(psf_unet *net, psf_trainset *ts, int first, int count, int mode,
+                            double *mean_rel_energy);
 
 /* ---------------- VTK output ---------------- */
 /* Replaces the per-iteration dump of sample_optimize_density_oc.cpp:173-181

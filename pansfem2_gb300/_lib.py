@@ -153,7 +153,7 @@ def load(path=LIB_PATH):
         "psf_trainset_size": [vp],
         "psf_learned_harvest": [vp, vp, C.c_int, ip, C.c_int],
         "psf_learned_train": [vp, vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_int, dp],
-        "psf_learned_eval": [vp, vp, C.c_int, C.c_int, dp],
+        "psf_learned_eval": [vp, vp, C.c_int, C.c_int, C.c_int, dp],
         "psf_export_vtk": [vp, C.c_char_p, C.c_int],
         "psf_batch_create": [C.c_int, ip, ip, ip, ip, dp, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
         "psf_batch_destroy": [vp],

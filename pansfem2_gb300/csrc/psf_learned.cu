@@ -52,6 +52,7 @@ using unet::bf16;
 constexpr int kLpBlocks = 608;
 constexpr int kLpThreads = 256;
 constexpr int kGraphIters = 4;   // FCG iterations per host check
+constexpr int kMaxBatchAngle = 16;   // training batch limit of the scale-free loss
 
 // scalar slots
 enum { S_SCALE = 0, S_ZQ, S_PQPREV, S_PQ, S_RP, S_RR, S_BB, S_EPS2, S_FIRST, S_OMEGA, S_NSC = 16 };
@@ -893,6 +894,115 @@ __global__ void __launch_bounds__(kLpThreads) energy_kernel(int nx, int ny, KeT<
     write_parts<1>(v, part);
 }
 
+// the scale-free form of the energy loss (the solver rescales the correction by its
+// energy-optimal step omega): per sample L_b = 1 - (y . rhat)^2 / ((y . K^ y) c_b), the
+// K-norm error left by the best multiple of the correction.  Pass 1: K^ y into ky and the
+// per-block, per-sample partial sums of y . rhat and y . K^ y.
+template <int KIND>
+__global__ void __launch_bounds__(kLpThreads) angle_ab_kernel(int nx, int ny, KeT<float> Ke, int B,
+                                                              const float *__restrict__ out,
+                                                              const float *__restrict__ rhat,
+                                                              const float *__restrict__ isd,
+                                                              const float *__restrict__ epad, float oscale,
+                                                              float *__restrict__ ky, double *part) {
+    constexpr int nd = ndof_of<KIND>();
+    const long long P = (long long)(nx + 1) * (ny + 1), Pe = (long long)(nx + 2) * (ny + 2);
+    Geo g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = 0;
+    g.nnodes = P;
+    double acc[kMaxBatchAngle][2];
+#pragma unroll
+    for (int b = 0; b < kMaxBatchAngle; b++) acc[b][0] = acc[b][1] = 0.0;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < (long long)B * P;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(idx / P);
+        const long long n = idx - (long long)b * P;
+        const float *yb = out + (size_t)b * P * 2, *ib = isd + (size_t)b * P * 2, *rb = rhat + (size_t)b * P * 2;
+        int i, j, k;
+        node_ijk<KIND>(g, n, i, j, k);
+        float kv[nd];
+        ebe_node<float, KIND>(g, Ke, epad + (size_t)b * Pe, i, j, k,
+                              [&](long long q) {
+                                  const long long m = q / nd;
+                                  const int d = (int)(q - m * nd);
+                                  return ib[m * 2 + d] * oscale * yb[m * 2 + d];
+                              },
+                              kv);
+        double a = 0.0, bs = 0.0;
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            float kh = 0.0f;
+            if (c < nd && ib[n * 2 + c] > 0.0f) {
+                kh = ib[n * 2 + c] * kv[c < nd ? c : 0];
+                const double yh = (double)oscale * yb[n * 2 + c];
+                a += yh * rb[n * 2 + c];
+                bs += yh * kh;
+            }
+            ky[(size_t)b * P * 2 + n * 2 + c] = kh;
+        }
+#pragma unroll
+        for (int q = 0; q < kMaxBatchAngle; q++)
+            if (q == b) {
+                acc[q][0] += a;
+                acc[q][1] += bs;
+            }
+    }
+    // per-sample block sums in a fixed order (deterministic)
+    __shared__ double sm[64];
+    for (int b = 0; b < B; b++) {
+        double v[2] = {acc[0][0], acc[0][1]};
+#pragma unroll
+        for (int q = 1; q < kMaxBatchAngle; q++)
+            if (q == b) {
+                v[0] = acc[q][0];
+                v[1] = acc[q][1];
+            }
+        block_sum<2>(v, sm);
+        if (threadIdx.x == 0) {
+            part[(size_t)blockIdx.x * 2 * kMaxBatchAngle + 2 * b] = v[0];
+            part[(size_t)blockIdx.x * 2 * kMaxBatchAngle + 2 * b + 1] = v[1];
+        }
+    }
+}
+
+// pass 2: fold the partials (fixed block order), the gradient
+// dL_b/dy = oscale (-2 A / (c B) rhat + 2 A^2 / (c B^2) K^ y) / nbatch, and the mean loss
+__global__ void __launch_bounds__(kLpThreads) angle_grad_kernel(long long P, int B, const double *part,
+                                                                const double *__restrict__ cden,
+                                                                const float *__restrict__ rhat,
+                                                                const float *__restrict__ ky,
+                                                                const float *__restrict__ isd, float oscale,
+                                                                float *__restrict__ gout, double *loss) {
+    __shared__ double sAB[kMaxBatchAngle * 2];
+    if (threadIdx.x < 2 * B) {
+        double v = 0.0;
+        for (int blk = 0; blk < kLpBlocks; blk++) v += part[(size_t)blk * 2 * kMaxBatchAngle + threadIdx.x];
+        sAB[threadIdx.x] = v;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0 && loss) {
+        double l = 0.0;
+        for (int b = 0; b < B; b++) {
+            const double A = sAB[2 * b], Bb = sAB[2 * b + 1], c = cden[b];
+            l += (Bb > 0.0 && c > 0.0) ? 1.0 - A * A / (c * Bb) : 1.0;
+        }
+        *loss = l / B;
+    }
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < (long long)B * P * 2;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(idx / (P * 2));
+        const double A = sAB[2 * b], Bb = sAB[2 * b + 1], c = cden[b];
+        float gr = 0.0f;
+        if (isd[idx] > 0.0f && Bb > 0.0 && c > 0.0) {
+            const double d = -2.0 * A / (c * Bb) * rhat[idx] + 2.0 * A * A / (c * Bb * Bb) * ky[idx];
+            gr = (float)(d * oscale / B);
+        }
+        gout[idx] = gr;
+    }
+}
+
 __global__ void energy_loss_kernel(const double *part, int B, double *out) {
     double v[1];
     fold_parts<1>(part, v);
@@ -1050,7 +1160,11 @@ extern "C" {
 
 psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch, float lr, uint64_t seed,
                              int loss_mode, double *loss_hist) {
-    if (!u || !ts || steps < 1 || batch < 1 || ts->n < 1 || loss_mode < 0 || loss_mode > 1) return PSF_BAD_INPUT;
+    if (!u || !ts || steps < 1 || batch < 1 || ts->n < 1 || loss_mode < 0 || loss_mode > 2) return PSF_BAD_INPUT;
+    if (loss_mode == 2 && batch > psf::kMaxBatchAngle) {
+        psf::set_error("psf_learned_train: the scale-free loss takes batches of at most 16");
+        return PSF_BAD_INPUT;
+    }
     psf::unet::Net &net = u->net;
     if (net.H[0] != ts->H || net.W[0] != ts->W || batch > net.cap) {
         psf::set_error("psf_learned_train: network grid or batch capacity does not match the training set");
@@ -1064,7 +1178,7 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
     rhat = mask + P * 2 * batch;
     isdb = rhat + P * 2 * batch;
     epad = isdb + P * 2 * batch;
-    PSF_CUDA(cudaMalloc(&cden, sizeof(double) * (batch + 2 * psf::kLpBlocks)));
+    PSF_CUDA(cudaMalloc(&cden, sizeof(double) * (batch + 2 * (size_t)psf::kLpBlocks * psf::kMaxBatchAngle)));
     epart = cden + batch;
     psf::KeT<float> Kf{};
     for (int q = 0; q < 64; q++) Kf.v[q] = ts->Ke[q];
@@ -1112,7 +1226,7 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
             if (s == PSF_OK)
                 s = psf::cuda_status(cudaMemcpyAsync(mask + b * P * 2, ts->mask + i * P * 2, sizeof(float) * P * 2,
                                                      cudaMemcpyDeviceToDevice, st), "copy");
-            if (s == PSF_OK && loss_mode == 1) {
+            if (s == PSF_OK && loss_mode >= 1) {
                 s = psf::cuda_status(cudaMemcpyAsync(rhat + b * P * 2, ts->rhat + i * P * 2, sizeof(float) * P * 2,
                                                      cudaMemcpyDeviceToDevice, st), "copy");
                 if (s == PSF_OK)
@@ -1144,6 +1258,20 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
                     epart);
             psf::energy_loss_kernel<<<1, 32, 0, st>>>(epart, batch, dl + k);
             s = psf::cuda_status(cudaGetLastError(), "energy loss");
+        }
+        if (s == PSF_OK && loss_mode == 2) {
+            const int nx = ts->H - 1, ny = ts->W - 1;
+            float *ky = tgt;   // the MSE target buffer is free in this mode
+            if (ts->kind == PSF_Q4_HEAT)
+                psf::angle_ab_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, net.out_scale, ky, epart);
+            else
+                psf::angle_ab_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, net.out_scale, ky, epart);
+            psf::angle_grad_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                (long long)P, batch, epart, cden, rhat, ky, isdb, net.out_scale, net.g[psf::unet::kTensors - 1],
+                dl + k);
+            s = psf::cuda_status(cudaGetLastError(), "scale-free energy loss");
         }
         if (s == PSF_OK) s = net.backward(batch, nullptr);
         if (s == PSF_OK) s = net.adam((float)lrk);
@@ -1232,8 +1360,9 @@ psf_status psf_learned_harvest(psf_ctx *h, psf_trainset *ts, int npairs, const i
 
 extern "C" {
 
-psf_status psf_learned_eval(psf_unet *u, psf_trainset *ts, int first, int count, double *mean_rel_energy) {
-    if (!u || !ts || !mean_rel_energy || first < 0 || count < 1 || first + count > ts->n) return PSF_BAD_INPUT;
+psf_status psf_learned_eval(psf_unet *u, psf_trainset *ts, int first, int count, int mode, double *mean_rel_energy) {
+    if (!u || !ts || !mean_rel_energy || first < 0 || count < 1 || first + count > ts->n || mode < 1 || mode > 2)
+        return PSF_BAD_INPUT;
     psf::unet::Net &net = u->net;
     if (net.H[0] != ts->H || net.W[0] != ts->W) {
         psf::set_error("psf_learned_eval: network grid does not match the training set");
@@ -1242,8 +1371,10 @@ psf_status psf_learned_eval(psf_unet *u, psf_trainset *ts, int first, int count,
     const size_t P = (size_t)ts->H * ts->W, Pe = (size_t)(ts->H + 1) * (ts->W + 1);
     const int B = net.cap;
     double *dl = nullptr, *part = nullptr;
-    PSF_CUDA(cudaMalloc(&dl, sizeof(double) * ((size_t)count + 2 * psf::kLpBlocks)));
+    float *ky = nullptr;
+    PSF_CUDA(cudaMalloc(&dl, sizeof(double) * ((size_t)count + 2 * (size_t)psf::kLpBlocks * psf::kMaxBatchAngle)));
     part = dl + count;
+    PSF_CUDA(cudaMalloc(&ky, sizeof(float) * P * 2));
     psf::KeT<float> Kf{};
     for (int q = 0; q < 64; q++) Kf.v[q] = ts->Ke[q];
     cudaStream_t st = net.stream;
@@ -1259,21 +1390,37 @@ psf_status psf_learned_eval(psf_unet *u, psf_trainset *ts, int first, int count,
         if (s == PSF_OK) s = net.forward(nb, nullptr);
         for (int b = 0; b < nb && s == PSF_OK; b++) {
             const size_t j = i + b;
-            if (ts->kind == PSF_Q4_HEAT)
-                psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
-                    nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2, ts->epad + j * Pe,
-                    ts->cden + j, net.out_scale, net.g[psf::unet::kTensors - 1], part);
-            else
-                psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
-                    nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2, ts->epad + j * Pe,
-                    ts->cden + j, net.out_scale, net.g[psf::unet::kTensors - 1], part);
-            psf::energy_loss_kernel<<<1, 32, 0, st>>>(part, 1, dl + i0 + b);
+            float *gsc = net.g[psf::unet::kTensors - 1];   // scratch: the output gradient is not needed
+            if (mode == 1) {
+                if (ts->kind == PSF_Q4_HEAT)
+                    psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                        nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
+                        ts->epad + j * Pe, ts->cden + j, net.out_scale, gsc, part);
+                else
+                    psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                        nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
+                        ts->epad + j * Pe, ts->cden + j, net.out_scale, gsc, part);
+                psf::energy_loss_kernel<<<1, 32, 0, st>>>(part, 1, dl + i0 + b);
+            } else {
+                if (ts->kind == PSF_Q4_HEAT)
+                    psf::angle_ab_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                        nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
+                        ts->epad + j * Pe, net.out_scale, ky, part);
+                else
+                    psf::angle_ab_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                        nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
+                        ts->epad + j * Pe, net.out_scale, ky, part);
+                psf::angle_grad_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (long long)P, 1, part, ts->cden + j, ts->rhat + j * P * 2, ky, ts->isd + j * P * 2, net.out_scale,
+                    gsc, dl + i0 + b);
+            }
             s = psf::cuda_status(cudaGetLastError(), "energy loss");
         }
     }
     if (s == PSF_OK) s = net.check_err();
     if (s == PSF_OK) s = psf::cuda_status(cudaMemcpy(h.data(), dl, sizeof(double) * count, cudaMemcpyDeviceToHost), "copy");
     cudaFree(dl);
+    cudaFree(ky);
     if (s != PSF_OK) return s;
     double m = 0.0;
     for (double v : h) m += v;

@@ -173,22 +173,25 @@ class TrainSet:
             pass
 
 
-LOSS_MODES = {"mse": 0, "energy": 1}
+LOSS_MODES = {"mse": 0, "energy": 1, "angle": 2}
 
 
 def train(net, trainset, steps, batch=8, lr=1e-3, seed=1, loss="energy"):
     """Adam on the GPU (psf_learned_train); returns the loss per step relative to
-    that of a zero output (loss: "energy" = K-norm error, "mse" = squared error)."""
+    that of a zero output (loss: "angle" = K-norm error left by the best multiple of
+    the correction, "energy" = K-norm error, "mse" = squared error)."""
     hist = np.zeros(steps)
     L.check(L.load().psf_learned_train(net._h, trainset._h, int(steps), int(batch), float(lr), int(seed),
                                        LOSS_MODES[loss], L.ptr(hist)))
     return hist
 
 
-def evaluate(net, trainset, first=0, count=None):
+def evaluate(net, trainset, first=0, count=None, optimal_step=True):
     """Mean energy-norm error of the network's correction over pairs
-    [first, first + count), relative to no correction (1 = no gain)."""
+    [first, first + count), relative to no correction (1 = no gain); with the
+    energy-optimal step the solver applies (default) or as output."""
     count = len(trainset) - first if count is None else count
     v = C.c_double()
-    L.check(L.load().psf_learned_eval(net._h, trainset._h, int(first), int(count), C.byref(v)))
+    L.check(L.load().psf_learned_eval(net._h, trainset._h, int(first), int(count), 2 if optimal_step else 1,
+                                      C.byref(v)))
     return v.value
