@@ -226,6 +226,30 @@ private:
     std::vector<T> w_;
 };
 
+// ------------------------------------------------------------------ HeavisideFilter (HeavisideFilter.h:16-98)
+// On the structured grid's filter of radius R; beta starts at 1 (HeavisideFilter.h:48).
+template <class T>
+class HeavisideFilter {
+public:
+    HeavisideFilter(Problem &p, double R) : n_((int)p.ne()), prob_(&p) { check(psf_filter_setup(p.ctx(), R), false); }
+    void UpdateBeta(T beta) { beta_ = beta; }
+    std::vector<T> GetFilteredVariables(std::vector<T> s) {
+        std::vector<T> out(n_);
+        check(psf_heaviside_forward(prob_->ctx(), beta_, s.data(), out.data()), false);
+        return out;
+    }
+    std::vector<T> GetFilteredSensitivitis(std::vector<T> s, std::vector<T> dfdrho) {
+        std::vector<T> out(n_);
+        check(psf_heaviside_backward(prob_->ctx(), beta_, s.data(), dfdrho.data(), out.data()), false);
+        return out;
+    }
+
+private:
+    int n_;
+    Problem *prob_;
+    T beta_ = 1.0;
+};
+
 // ------------------------------------------------------------------ SensitivityFilter (SensitivityFilter.h:16-99)
 // Sigmund's scheme (SensitivityFilter) and Borrvall's (SensitivityFilter2) on the
 // structured grid's filter of radius R.
@@ -321,9 +345,41 @@ private:
     T prev_ = T();
 };
 
+// ------------------------------------------------------------------ CONLIN (CONLIN.h:17-455), m = 1
+template <class T>
+class CONLIN {
+public:
+    CONLIN(Problem &p, int n, int m, T a0, std::vector<T> a, std::vector<T> c, std::vector<T> d,
+           const std::vector<T> &xmin, const std::vector<T> &xmax)
+        : p_(p), n_(n), a0_(a0), a_(a.at(0)), c_(c.at(0)), d_(d.at(0)), xmin_(xmin.at(0)), xmax_(xmax.at(0)) {
+        if (m != 1) throw std::runtime_error("pansfem2_gb300: the device CONLIN solves m = 1 (one constraint)");
+        init();
+    }
+    void SetParameters(T move, T epsvalue) {
+        move_ = move;
+        eps_ = epsvalue;
+        init();
+    }
+    bool IsConvergence(T f) { return std::fabs(f - prev_) / (f + prev_) < eps_; }
+    void UpdateVariables(std::vector<T> &xk, T f, std::vector<T> dfdx, std::vector<T> g,
+                         std::vector<std::vector<T> > dgdx) {
+        int newton = 0;
+        check(psf_conlin_update(p_.ctx(), xk.data(), f, dfdx.data(), g.at(0), dgdx.at(0).data(), &newton));
+        prev_ = f;
+    }
+
+private:
+    void init() { check(psf_conlin_init(p_.ctx(), a0_, a_, c_, d_, xmin_, xmax_, move_, eps_), false); }
+    Problem &p_;
+    int n_;
+    T a0_, a_, c_, d_, xmin_, xmax_;
+    T move_ = 0.5, eps_ = 1.0e-5;
+    T prev_ = T();
+};
+
 // ------------------------------------------------------------------ the whole iteration on the device
 // One call per iteration of the samples' loop body (filter, volume, solve,
-// compliance, sensitivities, filtered sensitivities, OC/MMA update).
+// compliance, sensitivities, filtered sensitivities, OC/MMA/CONLIN update).
 class SimpLoop {
 public:
     SimpLoop(Problem &p, const psf_simp_params &prm, const std::vector<double> *s0 = nullptr) : p_(p) {

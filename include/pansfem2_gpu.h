@@ -124,6 +124,15 @@ psf_status psf_filter_backward(psf_ctx *ctx, const double *dfdrho, double *dfds)
  * psf_filter_setup: out_i = sum_j w_ij s_j d_j / (wsum_i s_i), resp. / sum_j w_ij s_j (host arrays) */
 psf_status psf_sensitivity_filter(psf_ctx *ctx, int mode, const double *s, const double *dfds_in, double *dfds_out);
 
+/* HeavisideFilter (HeavisideFilter.h:16-98) on the filter of psf_filter_setup, host arrays:
+ * GetFilteredVariables: rho_i = H_beta(sum_j w_ij s_j / wsum_i) (HeavisideFilter.h:61-74);
+ * GetFilteredSensitivitis: dfds_i = sum_j w_ij dfdrho_j H'_beta(rt_j) / wsum_i (:77-97),
+ * with H_beta(r) = (tanh(beta/2) + tanh(beta (r - 1/2))) / (2 tanh(beta/2)).  beta is the
+ * value UpdateBeta (:55-57) last set. */
+psf_status psf_heaviside_forward(psf_ctx *ctx, double beta, const double *s, double *rho);
+psf_status psf_heaviside_backward(psf_ctx *ctx, double beta, const double *s, const double *dfdrho,
+                                  double *dfds);
+
 /* Compliance and sensitivities of sample_optimize_density_oc.cpp:136-162 for the
  * solved u: f = scale0 * u.K u and dfdrho_e = -scale0*p*(E1 - E0)*rho_e^(p-1) u_e.Ke(1) u_e.
  * rho (ne) in, dfdrho (ne) out. */
@@ -143,11 +152,22 @@ psf_status psf_mma_init(psf_ctx *ctx, double a0, double a, double c, double d, d
 psf_status psf_mma_update(psf_ctx *ctx, double *x, double f, const double *dfdx, double g,
                           const double *dgdx, int *newton_steps);
 
+/* CONLIN (CONLIN.h:17-455) for m = 1: the constructor's a0, a, c, d, xmin, xmax
+ * (CONLIN.h:55-67) and SetParameters(move, epsvalue) (CONLIN.h:71-74).  The
+ * approximation has q_j / x_j terms, so 0 < xmin < xmax is required. */
+psf_status psf_conlin_init(psf_ctx *ctx, double a0, double a, double c, double d, double xmin,
+                           double xmax, double move, double epsvalue);
+/* CONLIN::UpdateVariables (CONLIN.h:91-365): x (ne) updated in place; returns the
+ * interior-point Newton steps. */
+psf_status psf_conlin_update(psf_ctx *ctx, double *x, double f, const double *dfdx, double g,
+                             const double *dgdx, int *newton_steps);
+
 /* ---------------- the whole SIMP loop on the device ---------------- */
 typedef struct {
     double E1, E0, p;        /* E = E1*rho^p + E0*(1 - rho^p) (sample law) */
     double vf, R, scale0, scale1, rho0;
-    int optimizer;           /* 0 = OC, 1 = MMA */
+    int optimizer;           /* 0 = OC, 1 = MMA, 2 = CONLIN (reads mma_a0, mma_c, mma_d, mma_xmin,
+                                mma_xmax, mma_move, mma_eps) */
     double oc_iota, oc_lmin, oc_lmax, oc_leps, oc_move;
     double mma_raa0, mma_albefa, mma_move, mma_asyinit, mma_asydecr, mma_asyincr, mma_eps;
     double mma_a0, mma_c, mma_d, mma_xmin, mma_xmax;
@@ -167,8 +187,8 @@ typedef struct {
 typedef struct {
     double f, g;             /* objective and volume constraint of this iteration */
     double lambda;           /* last OC lambda */
-    int newton_steps;        /* MMA interior-point steps */
-    int converged;           /* IsConvergence (OC.h:67-73 / MMA.h:107-113) on f */
+    int newton_steps;        /* MMA / CONLIN interior-point steps */
+    int converged;           /* IsConvergence (OC.h:67-73 / MMA.h:107-113 / CONLIN.h:82-87) on f */
     psf_solve_info solve;
     double phase_seconds[6]; /* filter, assemble, solve, sensitivity, filter-back, update */
 } psf_iter_info;
@@ -176,7 +196,7 @@ typedef struct {
 /* Uploads the design s0 (ne, NULL = uniform rho0) and sets up filter/optimiser. */
 psf_status psf_simp_begin(psf_ctx *ctx, const psf_simp_params *prm, const double *s0);
 /* One SIMP iteration on the device (filter, volume, solve, compliance,
- * sensitivities, filtered sensitivities, OC/MMA update). */
+ * sensitivities, filtered sensitivities, OC/MMA/CONLIN update). */
 psf_status psf_simp_step(psf_ctx *ctx, psf_iter_info *info);
 /* The same iteration through host buffers: s_in (ne) is copied to the device
  * first, s_out / rho_out (ne, optional) and u_out (nnodes*ndof, optional) are

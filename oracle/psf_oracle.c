@@ -1317,6 +1317,278 @@ int orc_mma_update(orc_mma *o, double *xk, double f, const double *dfdx, const d
     return newton;
 }
 
+/* ===================== CONLIN (src/Optimize/Solver/CONLIN.h) ===================== */
+/* Convex linearisation: the same primal-dual interior-point subproblem solver as
+ * MMA, on the approximation f~(x) = sum_j p_j x_j + q_j / x_j (terms linear in x_j
+ * where the derivative is positive, in 1/x_j where it is negative) with plain move
+ * limits and no asymptotes or history. */
+struct orc_conlin {
+    int k, n, m;
+    double previousvalue, epsvalue, move;
+    double *xmin, *xmax;
+    double a0, *a, *c, *d;
+};
+
+/* CONLIN::CONLIN (CONLIN.h:55-67) */
+orc_conlin *orc_conlin_create(int n, int m, double a0, const double *a, const double *c, const double *d,
+                              const double *xmin, const double *xmax) {
+    orc_conlin *o = xcalloc(1, sizeof(orc_conlin));
+    o->k = 0; o->n = n; o->m = m;
+    o->previousvalue = 0.0;
+    o->epsvalue = 1.0e-5;
+    o->move = 0.5;
+    o->xmin = dup(xmin, n); o->xmax = dup(xmax, n);
+    o->a0 = a0; o->a = dup(a, m); o->c = dup(c, m); o->d = dup(d, m);
+    return o;
+}
+
+/* CONLIN::SetParameters (CONLIN.h:71-74) */
+void orc_conlin_set_parameters(orc_conlin *o, double move, double epsvalue) {
+    o->move = move;
+    o->epsvalue = epsvalue;
+}
+
+/* CONLIN::IsConvergence (CONLIN.h:82-87) */
+int orc_conlin_is_convergence(orc_conlin *o, double f) {
+    return fabs(f - o->previousvalue) / (f + o->previousvalue) < o->epsvalue;
+}
+
+void orc_conlin_destroy(orc_conlin *o) {
+    if (!o) return;
+    free(o->xmin); free(o->xmax); free(o->a); free(o->c); free(o->d); free(o);
+}
+
+/* CONLIN::KKTNorm (CONLIN.h:369-407) */
+static double conlin_kkt(const orc_conlin *o, const double *x, const double *y, double z,
+                         const double *lam, const double *gsi, const double *ita, const double *mu,
+                         double zeta, const double *s, double eps, const double *p, const double *q,
+                         const double *p0, const double *q0, const double *alpha, const double *beta,
+                         const double *b, double *gbuf) {
+    int n = o->n, m = o->m;
+    double norm = 0.0;
+    for (int i = 0; i < m; i++) gbuf[i] = 0.0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) gbuf[i] += p[(long)i * n + j] * x[j] + q[(long)i * n + j] / x[j];
+    for (int j = 0; j < n; j++) {
+        double plj = p0[j], qlj = q0[j];
+        for (int i = 0; i < m; i++) {
+            plj += lam[i] * p[(long)i * n + j];
+            qlj += lam[i] * q[(long)i * n + j];
+        }
+        norm += pow(plj - qlj / pow(x[j], 2.0) - gsi[j] + ita[j], 2.0);
+        norm += pow(gsi[j] * (x[j] - alpha[j]) - eps, 2.0);
+        norm += pow(ita[j] * (beta[j] - x[j]) - eps, 2.0);
+    }
+    for (int i = 0; i < m; i++) {
+        norm += pow(o->c[i] + o->d[i] * y[i] - lam[i] - mu[i], 2.0);
+        norm += pow(gbuf[i] - o->a[i] * z - y[i] + s[i] - b[i], 2.0);
+        norm += pow(mu[i] * y[i] - eps, 2.0);
+        norm += pow(lam[i] * s[i] - eps, 2.0);
+    }
+    double la = 0.0;
+    for (int i = 0; i < m; i++) la = la + lam[i] * o->a[i];
+    norm += pow(o->a0 - zeta - la, 2.0);
+    norm += pow(zeta * z - eps, 2.0);
+    return sqrt(norm);
+}
+
+/* CONLIN::UpdateVariables (CONLIN.h:91-365).  Returns the interior-point Newton steps. */
+int orc_conlin_update(orc_conlin *o, double *xk, double f, const double *dfdx, const double *g,
+                      const double *dgdx) {
+    int n = o->n, m = o->m;
+    const double *xmin = o->xmin, *xmax = o->xmax;
+    size_t nb = sizeof(double) * (size_t)n, mb = sizeof(double) * (size_t)(m > 0 ? m : 1);
+    double *alpha = xmalloc(nb), *beta = xmalloc(nb), *p0 = xmalloc(nb), *q0 = xmalloc(nb);
+    double *p = xmalloc(nb * m), *q = xmalloc(nb * m), *b = xmalloc(mb);
+    /* move limits (CONLIN.h:92-97) */
+    for (int j = 0; j < n; j++) {
+        alpha[j] = smax(xmin[j], xk[j] - o->move * (xmax[j] - xmin[j]));
+        beta[j] = smin(xmax[j], xk[j] + o->move * (xmax[j] - xmin[j]));
+    }
+    /* p0, q0 (CONLIN.h:100-107) */
+    for (int j = 0; j < n; j++) {
+        double dp = smax(dfdx[j], 0.0), dm = smax(-dfdx[j], 0.0);
+        p0[j] = dp;
+        q0[j] = dm * pow(xk[j], 2.0);
+    }
+    /* p, q, b (CONLIN.h:110-122) */
+    for (int i = 0; i < m; i++) {
+        b[i] = -g[i];
+        for (int j = 0; j < n; j++) {
+            double gij = dgdx[(long)i * n + j];
+            double dp = smax(gij, 0.0), dm = smax(-gij, 0.0);
+            p[(long)i * n + j] = dp;
+            q[(long)i * n + j] = dm * pow(xk[j], 2.0);
+            b[i] += p[(long)i * n + j] * xk[j] + q[(long)i * n + j] / xk[j];
+        }
+    }
+    /* interior point (CONLIN.h:125-359) */
+    double eps = 1.0;
+    double *x = xmalloc(nb), *gsi = xmalloc(nb), *ita = xmalloc(nb);
+    double *y = xmalloc(mb), *lam = xmalloc(mb), *s = xmalloc(mb), *mu = xmalloc(mb);
+    double z = 1.0, zeta = 1.0;
+    for (int i = 0; i < m; i++) { y[i] = 1.0; lam[i] = 1.0; s[i] = 1.0; mu[i] = smax(1.0, 0.5 * o->c[i]); }
+    for (int j = 0; j < n; j++) {
+        x[j] = 0.5 * (alpha[j] + beta[j]);
+        gsi[j] = smax(1.0, 1.0 / (x[j] - alpha[j]));
+        ita[j] = smax(1.0, 1.0 / (beta[j] - x[j]));
+    }
+    double *G = xmalloc(nb * m), *Dx = xmalloc(nb), *dtx = xmalloc(nb), *dx = xmalloc(nb),
+           *dgsi = xmalloc(nb), *dita = xmalloc(nb), *xp = xmalloc(nb), *gp = xmalloc(nb),
+           *ip = xmalloc(nb);
+    double *Dy = xmalloc(mb), *Dl = xmalloc(mb), *dty = xmalloc(mb), *dtl = xmalloc(mb),
+           *Dly = xmalloc(mb), *dtly = xmalloc(mb), *dy = xmalloc(mb), *dl = xmalloc(mb),
+           *dmu = xmalloc(mb), *ds = xmalloc(mb), *yp = xmalloc(mb), *lp = xmalloc(mb),
+           *mp = xmalloc(mb), *sp = xmalloc(mb), *gb = xmalloc(mb);
+    int S = (n > m ? m : n) + 1;
+    double *A = xmalloc(sizeof(double) * S * S), *Bv = xmalloc(sizeof(double) * S),
+           *sol = xmalloc(sizeof(double) * S);
+    int newton = 0;
+    for (int l = 0; eps > 1.0e-7; l++) {
+        if (l >= 100000) break;   /* the reference has no cap; this only guards a runaway */
+        newton++;
+        /* coefficients (CONLIN.h:148-195) */
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < n; j++)
+                G[(long)i * n + j] = p[(long)i * n + j] - q[(long)i * n + j] / pow(x[j], 2.0);
+        for (int j = 0; j < n; j++) {
+            double plj = p0[j], qlj = q0[j];
+            for (int i = 0; i < m; i++) { plj += lam[i] * p[(long)i * n + j]; qlj += lam[i] * q[(long)i * n + j]; }
+            Dx[j] = 2.0 * qlj / pow(x[j], 3.0) + gsi[j] / (x[j] - alpha[j]) + ita[j] / (beta[j] - x[j]);
+            dtx[j] = plj - qlj / pow(x[j], 2.0) - eps / (x[j] - alpha[j]) + eps / (beta[j] - x[j]);
+        }
+        for (int i = 0; i < m; i++) {
+            Dy[i] = o->d[i] + mu[i] / y[i];
+            Dl[i] = s[i] / lam[i];
+            dty[i] = o->c[i] + o->d[i] * y[i] - lam[i] - eps / y[i];
+        }
+        double la = 0.0;
+        for (int i = 0; i < m; i++) la = la + lam[i] * o->a[i];
+        double dtz = o->a0 - eps / z - la;
+        for (int i = 0; i < m; i++) {
+            dtl[i] = -o->a[i] * z - y[i] - b[i] + eps / lam[i];
+            for (int j = 0; j < n; j++) dtl[i] += p[(long)i * n + j] * x[j] + q[(long)i * n + j] / x[j];
+            Dly[i] = Dl[i] + 1.0 / Dy[i];
+            dtly[i] = dtl[i] + dty[i] / Dy[i];
+        }
+        double dz;
+        /* Newton direction (CONLIN.h:197-291), both reductions */
+        if (n > m) {
+            int s1 = m + 1;
+            for (int k2 = 0; k2 < s1 * s1; k2++) A[k2] = 0.0;
+            for (int ii = 0; ii < m; ii++) {
+                for (int jj = 0; jj < m; jj++)
+                    for (int kk = 0; kk < n; kk++)
+                        A[ii * s1 + jj] += G[(long)ii * n + kk] * G[(long)jj * n + kk] / Dx[kk];
+                A[ii * s1 + ii] += Dly[ii];
+                A[ii * s1 + m] = o->a[ii];
+                A[m * s1 + ii] = o->a[ii];
+            }
+            A[m * s1 + m] = -zeta / z;
+            for (int ii = 0; ii < m; ii++) {
+                Bv[ii] = dtly[ii];
+                for (int jj = 0; jj < n; jj++) Bv[ii] -= G[(long)ii * n + jj] * dtx[jj] / Dx[jj];
+            }
+            Bv[m] = dtz;
+            mma_solvels(A, Bv, s1, sol);   /* CONLIN::solvels (CONLIN.h:411-455) is the same elimination */
+            for (int i = 0; i < m; i++) dl[i] = sol[i];
+            dz = sol[m];
+            for (int j = 0; j < n; j++) {
+                dx[j] = -dtx[j] / Dx[j];
+                for (int i = 0; i < m; i++) dx[j] -= G[(long)i * n + j] * dl[i] / Dx[j];
+            }
+        } else {
+            int s1 = n + 1;
+            for (int k2 = 0; k2 < s1 * s1; k2++) A[k2] = 0.0;
+            for (int ii = 0; ii < n; ii++) {
+                for (int jj = 0; jj < n; jj++)
+                    for (int kk = 0; kk < m; kk++)
+                        A[ii * s1 + jj] += G[(long)kk * n + ii] * G[(long)kk * n + jj] / Dly[kk];
+                A[ii * s1 + ii] += Dx[ii];
+                for (int jj = 0; jj < m; jj++) {
+                    A[ii * s1 + n] -= G[(long)jj * n + ii] * o->a[jj] / Dly[jj];
+                    A[n * s1 + ii] -= G[(long)jj * n + ii] * o->a[jj] / Dly[jj];
+                    A[n * s1 + n] += o->a[jj] * o->a[jj] / Dly[jj];
+                }
+            }
+            A[n * s1 + n] += zeta / z;
+            for (int ii = 0; ii < n; ii++) {
+                Bv[ii] = -dtx[ii];
+                for (int jj = 0; jj < m; jj++) Bv[ii] -= G[(long)jj * n + ii] * dtly[jj] / Dly[jj];
+            }
+            Bv[n] = -dtz;
+            for (int jj = 0; jj < m; jj++) Bv[n] += o->a[jj] * dtly[jj] / Dly[jj];
+            mma_solvels(A, Bv, s1, sol);
+            for (int j = 0; j < n; j++) dx[j] = sol[j];
+            dz = sol[n];
+            for (int i = 0; i < m; i++) {
+                dl[i] = -o->a[i] * dz / Dly[i] + dtly[i] / Dly[i];
+                for (int j = 0; j < n; j++) dl[i] += G[(long)i * n + j] * dx[j] / Dly[i];
+            }
+        }
+        for (int i = 0; i < m; i++) {
+            dy[i] = dl[i] / Dy[i] - dty[i] / Dy[i];
+            dmu[i] = -mu[i] * dy[i] / y[i] - mu[i] + eps / y[i];
+            ds[i] = -s[i] * dl[i] / lam[i] - s[i] + eps / lam[i];
+        }
+        for (int j = 0; j < n; j++) {
+            dgsi[j] = -gsi[j] * dx[j] / (x[j] - alpha[j]) - gsi[j] + eps / (x[j] - alpha[j]);
+            dita[j] = ita[j] * dx[j] / (beta[j] - x[j]) - ita[j] + eps / (beta[j] - x[j]);
+        }
+        double dzeta = -zeta * dz / z - zeta + eps / z;
+        /* step length (CONLIN.h:293-322) */
+        double txmax = 0.0;
+        for (int j = 0; j < n; j++) {
+            double t = max4(-1.01 * dx[j] / (x[j] - alpha[j]), 1.01 * dx[j] / (beta[j] - x[j]),
+                            -1.01 * dgsi[j] / gsi[j], -1.01 * dita[j] / ita[j]);
+            if (txmax < t) txmax = t;
+        }
+        double tymax = 0.0;
+        for (int i = 0; i < m; i++) {
+            double t = max4(-1.01 * dy[i] / y[i], -1.01 * dl[i] / lam[i], -1.01 * dmu[i] / mu[i],
+                            -1.01 * ds[i] / s[i]);
+            if (tymax < t) tymax = t;
+        }
+        double tau = 1.0 / max5(1.0, txmax, tymax, -1.01 * dz / z, -1.01 * dzeta / zeta);
+        double dw = conlin_kkt(o, x, y, z, lam, gsi, ita, mu, zeta, s, eps, p, q, p0, q0, alpha, beta, b, gb);
+        double zp = z, zetap = zeta, dw1 = 0.0;
+        /* backtracking on the KKT norm (CONLIN.h:323-339) */
+        for (int ll = 0; ll < 50; ll++) {
+            for (int j = 0; j < n; j++) {
+                xp[j] = x[j] + tau * dx[j];
+                gp[j] = gsi[j] + tau * dgsi[j];
+                ip[j] = ita[j] + tau * dita[j];
+            }
+            for (int i = 0; i < m; i++) {
+                yp[i] = y[i] + tau * dy[i];
+                lp[i] = lam[i] + tau * dl[i];
+                mp[i] = mu[i] + tau * dmu[i];
+                sp[i] = s[i] + tau * ds[i];
+            }
+            zp = z + tau * dz;
+            zetap = zeta + tau * dzeta;
+            dw1 = conlin_kkt(o, xp, yp, zp, lp, gp, ip, mp, zetap, sp, eps, p, q, p0, q0, alpha, beta, b, gb);
+            if (dw1 < dw) break;
+            tau *= 0.5;
+        }
+        /* update w and eps (CONLIN.h:341-358) */
+        memcpy(x, xp, nb); memcpy(gsi, gp, nb); memcpy(ita, ip, nb);
+        memcpy(y, yp, mb); memcpy(lam, lp, mb); memcpy(mu, mp, mb); memcpy(s, sp, mb);
+        z = zp; zeta = zetap;
+        double dw2 = conlin_kkt(o, x, y, z, lam, gsi, ita, mu, zeta, s, eps, p, q, p0, q0, alpha, beta, b, gb);
+        if (dw2 < 0.9 * eps) eps *= 0.1;
+    }
+    o->previousvalue = f;
+    o->k++;
+    memcpy(xk, x, nb);
+    free(alpha); free(beta); free(p0); free(q0); free(p); free(q); free(b); free(x); free(gsi);
+    free(ita); free(y); free(lam); free(s); free(mu); free(G); free(Dx); free(dtx); free(dx);
+    free(dgsi); free(dita); free(xp); free(gp); free(ip); free(Dy); free(Dl); free(dty); free(dtl);
+    free(Dly); free(dtly); free(dy); free(dl); free(dmu); free(ds); free(yp); free(lp); free(mp);
+    free(sp); free(gb); free(A); free(Bv); free(sol);
+    return newton;
+}
+
 /* ===================== the SIMP loop (sample_optimize_density_{oc,mma}.cpp) ===================== */
 int orc_simp_run(const orc_simp_cfg *c, int iters, int stop_on_convergence, orc_simp_out *out) {
     int nen, ndof, dim;
@@ -1352,6 +1624,17 @@ int orc_simp_run(const orc_simp_cfg *c, int iters, int stop_on_convergence, orc_
            *dgds = xmalloc(sizeof(double) * ne), *u = xmalloc(sizeof(double) * nnodes * ndof);
     for (int e = 0; e < ne; e++) s[e] = c->rho0;
     orc_mma *mma = NULL;
+    orc_conlin *conlin = NULL;
+    if (c->optimizer == 2) {
+        /* sample_optimize_density_CONLIN.cpp:75-80: CONLIN(n, 1, a0, {0}, {c}, {d}, xmin, xmax),
+           SetParameters(move, eps) */
+        double *xmn = xmalloc(sizeof(double) * ne), *xmx = xmalloc(sizeof(double) * ne);
+        for (int e = 0; e < ne; e++) { xmn[e] = c->mma_xmin; xmx[e] = c->mma_xmax; }
+        double a = 0.0, cc = c->mma_c, dd = c->mma_d;
+        conlin = orc_conlin_create(ne, 1, c->mma_a0, &a, &cc, &dd, xmn, xmx);
+        orc_conlin_set_parameters(conlin, c->mma_move, c->mma_eps);
+        free(xmn); free(xmx);
+    }
     if (c->optimizer == 1) {
         double *xmn = xmalloc(sizeof(double) * ne), *xmx = xmalloc(sizeof(double) * ne);
         for (int e = 0; e < ne; e++) { xmn[e] = c->mma_xmin; xmx[e] = c->mma_xmax; }
@@ -1419,13 +1702,16 @@ int orc_simp_run(const orc_simp_cfg *c, int iters, int stop_on_convergence, orc_
             if (out->dfds) memcpy(out->dfds + (long)k * ne, dfds, sizeof(double) * ne);
             if (out->u) memcpy(out->u + (long)k * nnodes * ndof, u, sizeof(double) * nnodes * ndof);
         }
-        int conv = c->optimizer == 1 ? orc_mma_is_convergence(mma, f)
-                                     : orc_is_convergence(f, oc_prev, 1.0e-5);
+        int conv = c->optimizer == 1   ? orc_mma_is_convergence(mma, f)
+                   : c->optimizer == 2 ? orc_conlin_is_convergence(conlin, f)
+                                       : orc_is_convergence(f, oc_prev, 1.0e-5);
         if (stop_on_convergence && conv) { done = k + 1; break; }
         double lam = 0.0;
         int newton = 0;
         if (c->optimizer == 1) {
             newton = orc_mma_update(mma, s, f, dfds, &g, dgds);
+        } else if (c->optimizer == 2) {
+            newton = orc_conlin_update(conlin, s, f, dfds, &g, dgds);
         } else {
             lam = orc_oc_update(ne, c->oc_iota, c->oc_lmin, c->oc_lmax, c->oc_leps, c->oc_move, s,
                                 dfds, dgds, nptr, nidx, nw, c->vf, c->scale1, c->heaviside, beta);
@@ -1442,6 +1728,7 @@ int orc_simp_run(const orc_simp_cfg *c, int iters, int stop_on_convergence, orc_
     if (out && out->s_final) memcpy(out->s_final, s, sizeof(double) * ne);
     if (out && out->phase_seconds) memcpy(out->phase_seconds, ph, sizeof ph);
     orc_mma_destroy(mma);
+    orc_conlin_destroy(conlin);
     free(coords); free(conn); free(cg); free(nptr); free(nidx); free(nw); free(fixed); free(n2g);
     free(s); free(rho); free(Ee); free(dfdrho); free(dgdrho); free(dfds); free(dgds); free(u);
     return done;

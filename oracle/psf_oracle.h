@@ -132,6 +132,17 @@ int orc_mma_update(orc_mma *o, double *xk, double f, const double *dfdx, const d
                    const double *dgdx);
 void orc_mma_destroy(orc_mma *o);
 
+/* CONLIN (src/Optimize/Solver/CONLIN.h:17-455), general m, both Newton branches. */
+typedef struct orc_conlin orc_conlin;
+orc_conlin *orc_conlin_create(int n, int m, double a0, const double *a, const double *c, const double *d,
+                              const double *xmin, const double *xmax);
+void orc_conlin_set_parameters(orc_conlin *o, double move, double epsvalue);
+int orc_conlin_is_convergence(orc_conlin *o, double f);
+/* dgdx is m rows of n.  Returns the number of interior-point Newton steps. */
+int orc_conlin_update(orc_conlin *o, double *xk, double f, const double *dfdx, const double *g,
+                      const double *dgdx);
+void orc_conlin_destroy(orc_conlin *o);
+
 /* ---------------- whole SIMP loop (the sample drivers, configurable) ---------------- */
 typedef struct {
     int kind;                 /* ORC_* element kind */
@@ -140,7 +151,7 @@ typedef struct {
     double V, t;              /* Poisson ratio, thickness */
     double E1, E0, p;         /* E = E1*rho^p + E0*(1 - rho^p) (sample law) */
     double vf, R, scale0, scale1, rho0;
-    int optimizer;            /* 0 = OC, 1 = MMA */
+    int optimizer;            /* 0 = OC, 1 = MMA, 2 = CONLIN (a0, c, d, xmin, xmax, move, eps: the mma_ fields) */
     double oc_iota, oc_lmin, oc_lmax, oc_leps, oc_move;
     double mma_raa0, mma_albefa, mma_move, mma_asyinit, mma_asydecr, mma_asyincr, mma_eps;
     double mma_a0, mma_c, mma_d, mma_xmin, mma_xmax;

@@ -41,6 +41,12 @@ def _lib(fast=False):
     lib.orc_mma_set_parameters.argtypes = [C.c_void_p] + [C.c_double] * 7
     lib.orc_mma_is_convergence.argtypes = [C.c_void_p, C.c_double]
     lib.orc_mma_destroy.argtypes = [C.c_void_p]
+    lib.orc_conlin_create.restype = C.c_void_p
+    lib.orc_conlin_create.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp, dp, dp, dp]
+    lib.orc_conlin_update.argtypes = [C.c_void_p, dp, C.c_double, dp, dp, dp]
+    lib.orc_conlin_set_parameters.argtypes = [C.c_void_p, C.c_double, C.c_double]
+    lib.orc_conlin_is_convergence.argtypes = [C.c_void_p, C.c_double]
+    lib.orc_conlin_destroy.argtypes = [C.c_void_p]
     _LIBS[name] = lib
     return lib
 
@@ -279,6 +285,32 @@ class MMA:
     def __del__(self):
         try:
             _lib().orc_mma_destroy(self._h)
+        except Exception:
+            pass
+
+
+class CONLIN:
+    """CONLIN<T> of src/Optimize/Solver/CONLIN.h, state kept in the C oracle."""
+
+    def __init__(self, n, m, a0, a, c, d, xmin, xmax):
+        self.n, self.m = n, m
+        self._h = _lib().orc_conlin_create(n, m, a0, P(f64(a)), P(f64(c)), P(f64(d)), P(f64(xmin)),
+                                           P(f64(xmax)))
+
+    def set_parameters(self, move, eps):
+        _lib().orc_conlin_set_parameters(self._h, move, eps)
+
+    def is_convergence(self, f):
+        return bool(_lib().orc_conlin_is_convergence(self._h, f))
+
+    def update(self, x, f, dfdx, g, dgdx):
+        x = f64(x).copy()
+        newton = _lib().orc_conlin_update(self._h, P(x), f, P(f64(dfdx)), P(f64(g)), P(f64(dgdx).reshape(-1)))
+        return x, newton
+
+    def __del__(self):
+        try:
+            _lib().orc_conlin_destroy(self._h)
         except Exception:
             pass
 

@@ -8,7 +8,8 @@
 //
 // The SIMP loop is the call sequence of
 // sample/optimize/sample_optimize_density_oc.cpp:93-207 (OC) and
-// sample/optimize/sample_optimize_density_mma.cpp:98-203 (MMA), with the
+// sample/optimize/sample_optimize_density_mma.cpp:98-203 (MMA) and
+// sample/optimize/sample_optimize_density_CONLIN.cpp:75-206 (CONLIN, opt=2), with the
 // configuration's parameters in place of the sample's literals, the linear
 // DensityFilter (or the sample's HeavisideFilter with heaviside=1); with
 // vtk=<file> iteration 0 is also written by the reference's VTK writer.  Usage:  ref_driver <mode> out=<file> key=value ...
@@ -41,6 +42,7 @@
 #include "src/Optimize/Solver/OC.h"
 #include "src/PrePost/Export/ExportToVTK.h"
 #include "src/Optimize/Solver/MMA.h"
+#include "src/Optimize/Solver/CONLIN.h"
 #include "src/Optimize/Filter/DensityFilter.h"
 #include "src/Optimize/Filter/HeavisideFilter.h"
 #include "src/PrePost/Mesher/SquareMesh.h"
@@ -165,6 +167,10 @@ static int run_simp() {
                     std::vector<double>(s.size(), argd("xmax", 1.0)));
     mma.SetParameters(argd("raa0", 1.0e-5), argd("albefa", 0.1), move, argd("asyinit", 0.5), argd("asydecr", 0.7),
                       argd("asyincr", 1.2), argd("mma_eps", 1.0e-6));
+    CONLIN<double> conlin(s.size(), 1, argd("a0", 1.0), std::vector<double>(1, 0.0),
+                          std::vector<double>(1, argd("mma_c", 10000.0)), std::vector<double>(1, 0.0),
+                          std::vector<double>(s.size(), argd("xmin", 0.01)), std::vector<double>(s.size(), argd("xmax", 1.0)));
+    conlin.SetParameters(move, argd("mma_eps", 1.0e-6));
 
     Dump out(args("out", "ref.bin"));
     {
@@ -295,6 +301,8 @@ static int run_simp() {
 
         if (optimizer == 1) {
             mma.UpdateVariables(s, f, dfds, {g}, {dgds});
+        } else if (optimizer == 2) {
+            conlin.UpdateVariables(s, f, dfds, {g}, {dgds});
         } else {
             oc.UpdateVariables(s, f, dfds, g, dgds, [&](std::vector<double> _xkp1) {
                 double gg = 0.0;
@@ -310,6 +318,78 @@ static int run_simp() {
     return 0;
 }
 
+// ------------------------------- CONLIN on the optimiser test problems -------------------------------
+// The objective/constraint functions of src/Optimize/Solver/test_MMA.cpp (problem=mma),
+// test_MMA_3.cpp (problem=mma3) and test_MMA_TOY2.cpp (problem=toy2), driven through
+// CONLIN<double> with the tests' constructor arguments and move = 0.5.  Every iteration's
+// inputs (x, f, df, g, dg) and the design CONLIN returns are dumped, so each update can
+// be replayed one step at a time.
+static void eval_problem(const std::string& pb, const std::vector<double>& s, double& f, std::vector<double>& df,
+                         std::vector<double>& g, std::vector<std::vector<double> >& dg) {
+    if (pb == "mma") {
+        const double C1 = 0.0624, C2 = 1.0, cf[5] = {61.0, 37.0, 19.0, 7.0, 1.0};
+        f = C1 * (s[0] + s[1] + s[2] + s[3] + s[4]);
+        df.assign(5, C1);
+        double gg = 0.0;
+        for (int j = 0; j < 5; j++) gg += cf[j] * pow(s[j], -3.0);
+        g.assign(1, gg - C2);
+        dg.assign(1, std::vector<double>(5));
+        for (int j = 0; j < 5; j++) dg[0][j] = -3.0 * cf[j] * pow(s[j], -4.0);
+    } else if (pb == "mma3") {
+        const double C1 = 1.0, C2 = 0.124, q = sqrt(1.0 + pow(s[1], 2.0));
+        f = C1 * s[0] * q;
+        df = {C1 * q, C1 * s[0] * s[1] / q};
+        g = {C2 * q * (8.0 / s[0] + 1.0 / (s[0] * s[1])) - 1.0, C2 * q * (8.0 / s[0] - 1.0 / (s[0] * s[1])) - 1.0};
+        dg = {{C2 * q * (-8.0 / (s[0] * s[0]) - 1.0 / (s[0] * s[0] * s[1])),
+               C2 * s[1] / q * (8.0 / s[0] + 1.0 / (s[0] * s[1])) - C2 * q / (s[0] * s[1] * s[1])},
+              {C2 * q * (-8.0 / (s[0] * s[0]) + 1.0 / (s[0] * s[0] * s[1])),
+               C2 * s[1] / q * (8.0 / s[0] - 1.0 / (s[0] * s[1])) + C2 * q / (s[0] * s[1] * s[1])}};
+    } else {
+        f = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+        df = {2.0 * s[0], 2.0 * s[1], 2.0 * s[2]};
+        g = {pow(s[0] - 5.0, 2.0) + pow(s[1] - 2.0, 2.0) + pow(s[2] - 1.0, 2.0) - 9.0,
+             pow(s[0] - 3.0, 2.0) + pow(s[1] - 4.0, 2.0) + pow(s[2] - 3.0, 2.0) - 9.0};
+        dg = {{2.0 * (s[0] - 5.0), 2.0 * (s[1] - 2.0), 2.0 * (s[2] - 1.0)},
+              {2.0 * (s[0] - 3.0), 2.0 * (s[1] - 4.0), 2.0 * (s[2] - 3.0)}};
+    }
+}
+
+static int run_conlin() {
+    std::string pb = args("problem", "mma");
+    int iters = argi("iters", 10);
+    std::vector<double> s, xmin, xmax;
+    int m;
+    if (pb == "mma") { s.assign(5, 5.0); xmin.assign(5, 1.0); xmax.assign(5, 10.0); m = 1; }
+    else if (pb == "mma3") { s = {1.5, 0.5}; xmin = {0.2, 0.1}; xmax = {4.0, 1.6}; m = 2; }
+    else { s = {4.0, 3.0, 2.0}; xmin.assign(3, 0.0); xmax.assign(3, 5.0); m = 2; }
+    const int n = (int)s.size();
+    CONLIN<double> opt(n, m, 1.0, std::vector<double>(m, 0.0), std::vector<double>(m, 1000.0),
+                       std::vector<double>(m, 1.0), xmin, xmax);
+    opt.SetParameters(argd("move", 0.5), 1.0e-5);
+    std::vector<double> xin, fs, dfs, gs, dgs, xout;
+    for (int k = 0; k < iters; k++) {
+        double f;
+        std::vector<double> df, g;
+        std::vector<std::vector<double> > dg;
+        eval_problem(pb, s, f, df, g, dg);
+        bool finite = std::isfinite(f);
+        for (int j = 0; j < n; j++) finite = finite && std::isfinite(s[j]);
+        if (!finite || opt.IsConvergence(f)) break;
+        xin.insert(xin.end(), s.begin(), s.end());
+        fs.push_back(f);
+        dfs.insert(dfs.end(), df.begin(), df.end());
+        gs.insert(gs.end(), g.begin(), g.end());
+        for (auto& r : dg) dgs.insert(dgs.end(), r.begin(), r.end());
+        opt.UpdateVariables(s, f, df, g, dg);
+        xout.insert(xout.end(), s.begin(), s.end());
+    }
+    Dump out(args("out", "ref.bin"));
+    out.i("nm", {n, m});
+    out.d("xmin", xmin); out.d("xmax", xmax);
+    out.d("xin", xin); out.d("f", fs); out.d("df", dfs); out.d("g", gs); out.d("dg", dgs); out.d("xout", xout);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) { fprintf(stderr, "usage: ref_driver <simp|...> key=value ...\n"); return 2; }
     for (int i = 2; i < argc; i++) {
@@ -319,6 +399,7 @@ int main(int argc, char** argv) {
     }
     std::string mode = argv[1];
     if (mode == "simp") return run_simp();
+    if (mode == "conlin") return run_conlin();
     fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -31,7 +31,8 @@ EXPORTS = [
     "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_solve",
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_sensitivity_filter",
     "psf_compliance_sensitivity",
-    "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_simp_begin", "psf_simp_step",
+    "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_conlin_init", "psf_conlin_update",
+    "psf_heaviside_forward", "psf_heaviside_backward", "psf_simp_begin", "psf_simp_step",
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
     "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
@@ -123,6 +124,10 @@ def load(path=LIB_PATH):
                           C.c_double, C.c_double, dp],
         "psf_mma_init": [vp] + [C.c_double] * 13,
         "psf_mma_update": [vp, dp, C.c_double, dp, C.c_double, dp, ip],
+        "psf_conlin_init": [vp] + [C.c_double] * 8,
+        "psf_heaviside_forward": [vp, C.c_double, dp, dp],
+        "psf_heaviside_backward": [vp, C.c_double, dp, dp, dp],
+        "psf_conlin_update": [vp, dp, C.c_double, dp, C.c_double, dp, ip],
         "psf_simp_begin": [vp, C.POINTER(SimpParams), dp],
         "psf_simp_step": [vp, C.POINTER(IterInfo)],
         "psf_simp_step_host": [vp, dp, dp, dp, dp, C.POINTER(IterInfo)],

@@ -1,7 +1,7 @@
 """Python host over the C ABI: one Problem owns one device context.
 
 Mirrors the reference call sequence of the SIMP samples
-(sample/optimize/sample_optimize_density_{oc,mma}.cpp): boundary conditions
+(sample/optimize/sample_optimize_density_{oc,mma,CONLIN}.cpp): boundary conditions
 and numbering, element matrix, CSR pattern + assembly, solve, compliance and
 sensitivities, density filter, OC / MMA update, or the whole iteration on the
 device (simp_begin / simp_step).
@@ -135,6 +135,18 @@ class Problem:
         check(self.L.psf_filter_backward(self.h, ptr(d), ptr(out)))
         return out
 
+    def heaviside_forward(self, beta, s):
+        """HeavisideFilter::GetFilteredVariables at projection sharpness beta."""
+        out = np.zeros(self.ne)
+        check(self.L.psf_heaviside_forward(self.h, float(beta), ptr(f64(s)), ptr(out)))
+        return out
+
+    def heaviside_backward(self, beta, s, d):
+        """HeavisideFilter::GetFilteredSensitivitis of d at design s."""
+        out = np.zeros(self.ne)
+        check(self.L.psf_heaviside_backward(self.h, float(beta), ptr(f64(s)), ptr(f64(d)), ptr(out)))
+        return out
+
     def sensitivity_filter(self, s, d, mode=0):
         """SensitivityFilter (mode 0) / SensitivityFilter2 (mode 1) of d at design s."""
         out = np.zeros(self.ne)
@@ -170,6 +182,22 @@ class Problem:
         nt = C.c_int()
         check(self.L.psf_mma_update(self.h, ptr(x), float(f), ptr(f64(dfdx)), float(g), ptr(f64(dgdx)),
                                     C.byref(nt)), allow=(PSF_OK, PSF_NOT_CONVERGED))
+        return x, nt.value
+
+    def conlin_init(self, move=None, eps=None):
+        """CONLIN(n, 1, a0, {0}, {c}, {d}, xmin, xmax) + SetParameters(move, eps) (CONLIN.h:55-74)
+        from the problem's mma_a0/c/d/xmin/xmax and mma_move/mma_eps."""
+        pr = self.pr
+        check(self.L.psf_conlin_init(self.h, pr["mma_a0"], 0.0, pr["mma_c"], pr["mma_d"], pr["mma_xmin"],
+                                     pr["mma_xmax"], pr["mma_move"] if move is None else move,
+                                     pr["mma_eps"] if eps is None else eps))
+
+    def conlin_update(self, x, f, dfdx, g, dgdx):
+        """CONLIN::UpdateVariables (CONLIN.h:91-365) for m = 1; returns (x, Newton steps)."""
+        x = f64(x).copy()
+        nt = C.c_int()
+        check(self.L.psf_conlin_update(self.h, ptr(x), float(f), ptr(f64(dfdx)), float(g), ptr(f64(dgdx)),
+                                       C.byref(nt)), allow=(PSF_OK, PSF_NOT_CONVERGED))
         return x, nt.value
 
     # ---------------------------------------------------------------- the whole iteration on the device

@@ -261,6 +261,38 @@ psf_status psf_filter_backward(psf_ctx *h, const double *dfdrho, double *dfds) {
     return d2h_sync(c, dfds, c->dfds, sizeof(double) * c->ne);
 }
 
+static psf_status heaviside_scratch(Ctx *c) {
+    if (c->filt_n <= 0) { set_error("HeavisideFilter: call psf_filter_setup first"); return PSF_BAD_INPUT; }
+    if (!c->dH) PSF_CHECK(dalloc(c, &c->dH, c->ne));
+    if (!c->tmp_ne) PSF_CHECK(dalloc(c, &c->tmp_ne, c->ne));
+    return PSF_OK;
+}
+
+psf_status psf_heaviside_forward(psf_ctx *h, double beta, const double *s, double *rho) {
+    CTX_CHECK(h);
+    Ctx *c = &h->c;
+    if (!s || !rho || !(beta > 0.0)) { set_error("psf_heaviside_forward: null array or beta <= 0"); return PSF_BAD_INPUT; }
+    PSF_CHECK(heaviside_scratch(c));
+    PSF_CHECK(h2d(c, c->snew, s, sizeof(double) * c->ne));
+    PSF_CHECK(heaviside_forward(c, beta, c->snew, c->dfds));
+    return d2h_sync(c, rho, c->dfds, sizeof(double) * c->ne);
+}
+
+psf_status psf_heaviside_backward(psf_ctx *h, double beta, const double *s, const double *dfdrho, double *dfds) {
+    CTX_CHECK(h);
+    Ctx *c = &h->c;
+    if (!s || !dfdrho || !dfds || !(beta > 0.0)) {
+        set_error("psf_heaviside_backward: null array or beta <= 0");
+        return PSF_BAD_INPUT;
+    }
+    PSF_CHECK(heaviside_scratch(c));
+    PSF_CHECK(h2d(c, c->snew, s, sizeof(double) * c->ne));
+    PSF_CHECK(heaviside_forward(c, beta, c->snew, c->dfds));   // dH at filter(s)
+    PSF_CHECK(h2d(c, c->snew, dfdrho, sizeof(double) * c->ne));
+    PSF_CHECK(heaviside_back(c, c->snew, c->dfds));
+    return d2h_sync(c, dfds, c->dfds, sizeof(double) * c->ne);
+}
+
 psf_status psf_sensitivity_filter(psf_ctx *h, int mode, const double *s, const double *dfds_in, double *dfds_out) {
     CTX_CHECK(h);
     Ctx *c = &h->c;
@@ -338,6 +370,39 @@ psf_status psf_mma_update(psf_ctx *h, double *x, double f, const double *dfdx, d
     return st;
 }
 
+psf_status psf_conlin_init(psf_ctx *h, double a0, double a, double cc, double d, double xmin, double xmax,
+                           double move, double epsvalue) {
+    CTX_CHECK(h);
+    Ctx *c = &h->c;
+    if (!(xmax > xmin) || !(xmin > 0.0)) {
+        // the approximation has q_j / x_j terms: the design must stay positive
+        set_error("psf_conlin_init: need 0 < xmin < xmax");
+        return PSF_BAD_INPUT;
+    }
+    if (!(move > 0.0)) { set_error("psf_conlin_init: move must be positive"); return PSF_BAD_INPUT; }
+    if (!c->mma_work) PSF_CHECK(dzalloc(c, &c->mma_work, 17 * c->ne));
+    c->cl_a0 = a0; c->cl_a = a; c->cl_c = cc; c->cl_d = d; c->cl_xmin = xmin; c->cl_xmax = xmax;
+    c->cl_move = move; c->cl_epsvalue = epsvalue;
+    c->cl_k = 0;
+    c->cl_prev = 0.0;
+    c->cl_ready = true;
+    return PSF_OK;
+}
+
+psf_status psf_conlin_update(psf_ctx *h, double *x, double f, const double *dfdx, double g, const double *dgdx,
+                             int *newton_steps) {
+    CTX_CHECK(h);
+    Ctx *c = &h->c;
+    if (!x || !dfdx || !dgdx) { set_error("psf_conlin_update: null array"); return PSF_BAD_INPUT; }
+    PSF_CHECK(h2d(c, c->s, x, sizeof(double) * c->ne));
+    PSF_CHECK(h2d(c, c->dfds, dfdx, sizeof(double) * c->ne));
+    PSF_CHECK(h2d(c, c->dgds, dgdx, sizeof(double) * c->ne));
+    psf_status st = conlin_update(c, c->s, f, c->dfds, g, c->dgds, newton_steps);
+    if (st != PSF_OK && st != PSF_NOT_CONVERGED) return st;
+    PSF_CHECK(d2h_sync(c, x, c->s, sizeof(double) * c->ne));
+    return st;
+}
+
 // ------------------------------------------------------------------ SIMP loop
 psf_status psf_simp_begin(psf_ctx *h, const psf_simp_params *prm, const double *s0) {
     CTX_CHECK(h);
@@ -357,6 +422,10 @@ psf_status psf_simp_begin(psf_ctx *h, const psf_simp_params *prm, const double *
     if (prm->solver == PSF_SOLVE_CSR_JACOBI_F64 && !c->have_csr) PSF_CHECK(build_pattern(c));
     PSF_CHECK(build_rhs(c));
     PSF_CUDA(cudaMemsetAsync(c->un, 0, sizeof(double) * c->ndofs, c->stream));
+    if (prm->optimizer < 0 || prm->optimizer > 2) { set_error("psf_simp_begin: optimizer must be 0, 1 or 2"); return PSF_BAD_INPUT; }
+    if (prm->optimizer == 2)   // sample_optimize_density_CONLIN.cpp:75-80
+        PSF_CHECK(psf_conlin_init(h, prm->mma_a0, 0.0, prm->mma_c, prm->mma_d, prm->mma_xmin, prm->mma_xmax,
+                                  prm->mma_move, prm->mma_eps));
     if (prm->optimizer == 1)
         PSF_CHECK(psf_mma_init(h, prm->mma_a0, 0.0, prm->mma_c, prm->mma_d, prm->mma_xmin, prm->mma_xmax,
                                prm->mma_raa0, prm->mma_albefa, prm->mma_move, prm->mma_asyinit, prm->mma_asydecr,
@@ -413,7 +482,13 @@ psf_status psf_simp_step(psf_ctx *h, psf_iter_info *info) {
     inf.f = fg[0];
     inf.g = fg[1];
     // IsConvergence (OC.h:67-73, MMA.h:107-113), then the update (sample :192-207)
-    if (P.optimizer == 1) {
+    if (P.optimizer == 2) {   // CONLIN::IsConvergence (CONLIN.h:82-87), UpdateVariables (sample :192-204)
+        inf.converged = std::fabs(inf.f - c->cl_prev) / (inf.f + c->cl_prev) < c->cl_epsvalue;
+        if (!inf.converged) {
+            psf_status ms = conlin_update(c, c->s, inf.f, c->dfds, inf.g, c->dgds, &inf.newton_steps);
+            if (ms != PSF_OK && ms != PSF_NOT_CONVERGED) return ms;
+        }
+    } else if (P.optimizer == 1) {
         inf.converged = std::fabs(inf.f - c->mma_prev) / (inf.f + c->mma_prev) < c->mma_epsvalue;
         if (!inf.converged) {
             psf_status ms = mma_update(c, c->s, inf.f, c->dfds, inf.g, c->dgds, &inf.newton_steps);

@@ -101,13 +101,18 @@ struct Ctx {
 
     // MMA state (m = 1)
     double *mma_L = nullptr, *mma_U = nullptr, *mma_xkm1 = nullptr, *mma_xkm2 = nullptr;
-    double *mma_work = nullptr;  // 12*ne scratch
+    double *mma_work = nullptr;  // 17*ne scratch (MMA and CONLIN)
     int mma_k = 0;
     double mma_prev = 0.0, mma_epsvalue = 1e-5;
     double mma_a0 = 1, mma_a = 0, mma_c = 1e4, mma_d = 0, mma_xmin = 0.01, mma_xmax = 1.0;
     double mma_raa0 = 1e-5, mma_albefa = 0.1, mma_move = 0.5, mma_asyinit = 0.5, mma_asydecr = 0.7,
            mma_asyincr = 1.2;
     bool mma_ready = false;
+    // CONLIN (CONLIN.h:17-52): parameters and outer state; work space shared with MMA (mma_work)
+    double cl_a0 = 1, cl_a = 0, cl_c = 1e4, cl_d = 0, cl_xmin = 0.01, cl_xmax = 1.0, cl_move = 0.5;
+    double cl_prev = 0.0, cl_epsvalue = 1e-5;
+    int cl_k = 0;
+    bool cl_ready = false;
 
     // multigrid hierarchy (mixed-precision preconditioner)
     void *mg = nullptr;
@@ -163,6 +168,7 @@ psf_status scatter_reduced(Ctx *c, const double *red, double *nodal);  // psf_me
 psf_status gather_reduced(Ctx *c, const double *nodal, double *red);   // psf_mesh.cu
 psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_solve.cu
 psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward);               // psf_opt.cu
+psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho);
 psf_status heaviside_back(Ctx *c, const double *d, double *out);                            // psf_opt.cu
 psf_status sensitivity_filter(Ctx *c, const double *s, const double *d, int mode, double *out);  // psf_opt.cu
 psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, double p, double scale0,
@@ -171,6 +177,8 @@ psf_status oc_update(Ctx *c, double *x, const double *dfdx, const double *dgdx, 
                      double lmax, double leps, double move, double vf, double scale1, double *lambda);
 psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g, const double *dgdx,
                       int *newton);
+psf_status conlin_update(Ctx *c, double *x, double f, const double *dfdx, double g, const double *dgdx,
+                         int *newton);
 psf_status moduli_from_rho(Ctx *c, const double *rho, double E1, double E0, double p, double *E_dev);
 psf_status mg_free(Ctx *c);
 psf_status learned_free(Ctx *c);                                                       // psf_learned.cu

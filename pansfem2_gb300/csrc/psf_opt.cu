@@ -242,7 +242,13 @@ __global__ void __launch_bounds__(256) oc_kernel(const __grid_constant__ Stencil
     }
 }
 
-// ------------------------------------------------------------------ MMA, m = 1 (MMA.h:116-419)
+// ------------------------------------------------------------------ MMA and CONLIN, m = 1
+// MMA (MMA.h:116-419) and CONLIN (CONLIN.h:91-365) solve their convex subproblem with the
+// same primal-dual interior-point loop (Newton step on the (m+1) reduced system, step bound,
+// backtracking on the KKT norm, eps reduction); they differ in the separable approximation:
+//   MMA     f~_j = p_j / (U_j - x_j) + q_j / (x_j - L_j)   (moving asymptotes, history)
+//   CONLIN  f~_j = p_j x_j + q_j / x_j                      (plain move limits)
+// The kernel is templated on the approximation; everything between is shared.
 struct MmaArgs {
     long long n;
     double *xk;                       // in: current design, out: next design
@@ -265,6 +271,7 @@ __device__ __forceinline__ double sq(double v) { return v * v; }                
 __device__ __forceinline__ double ad(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double mu_(double a, double b) { return __dmul_rn(a, b); }
 
+template <bool kConlin>
 __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
     __shared__ double sm[32 * 4];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -276,11 +283,28 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
     double *dita = A.w + 14 * n;
     double *iam = A.w + 15 * n, *ibm = A.w + 16 * n;   // 1 / (x - alpha), 1 / (beta - x) at the Newton point
     const double xr = A.xmax - A.xmin;
-    // ---- asymptotes, move limits, p/q, b (MMA.h:118-175), start point (:178-197)
+    // ---- asymptotes, move limits, p/q, b (MMA.h:118-175), start point (:178-197);
+    //      CONLIN: move limits, p/q, b (CONLIN.h:92-122), start point (:125-145)
     {
         double acc[1] = {0.0};
         for (long long j = tid; j < n; j += stride) {
             const double xj = A.xk[j];
+            if constexpr (kConlin) {
+                const double alj = dmax(A.xmin, xj - A.move * xr);
+                const double bej = dmin(A.xmax, xj + A.move * xr);
+                al[j] = alj;
+                be[j] = bej;
+                const double df = A.dfdx[j], dg = A.dgdx[j];
+                const double x2 = sq(xj);
+                const double p1j = dmax(dg, 0.0), q1j = dmax(-dg, 0.0) * x2;
+                p0[j] = dmax(df, 0.0); q0[j] = dmax(-df, 0.0) * x2; p1[j] = p1j; q1[j] = q1j;
+                acc[0] += p1j * xj + q1j / xj;
+                const double x0 = 0.5 * (alj + bej);
+                x[j] = x0;
+                gsi[j] = dmax(1.0, 1.0 / (x0 - alj));
+                ita[j] = dmax(1.0, 1.0 / (bej - x0));
+                continue;
+            }
             double L, U;
             if (A.k < 2) {
                 L = xj - A.asyinit * xr;
@@ -337,8 +361,25 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
         // FP64 division is expensive on this part: one reciprocal per distinct
         // denominator (5 per element instead of 12); Dx is stored as 1/Dx
         for (long long j = tid; j < n; j += stride) {
-            const double xj = x[j], Lj = A.L[j], Uj = A.U[j];
+            const double xj = x[j];
             const double plj = p0[j] + lam * p1[j], qlj = q0[j] + lam * q1[j];
+            if constexpr (kConlin) {   // CONLIN.h:148-195
+                const double xa = xj - al[j], bx = be[j] - xj;
+                const double ix = 1.0 / xj, ia = 1.0 / xa, ib = 1.0 / bx;
+                const double ix2 = ix * ix;
+                const double Gj = p1[j] - q1[j] * ix2;
+                const double Dxj = 2.0 * qlj * ix2 * ix + gsi[j] * ia + ita[j] * ib;
+                const double iDx = 1.0 / Dxj;
+                const double dtxj = plj - qlj * ix2 - eps * ia + eps * ib;
+                G[j] = Gj; Dx[j] = iDx; dtx[j] = dtxj;
+                iam[j] = ia; ibm[j] = ib;
+                acc[0] += Gj * Gj * iDx;
+                acc[1] += Gj * dtxj * iDx;
+                acc[2] += p1[j] * xj + q1[j] * ix;
+                acc[3] += sq(plj - qlj * ix2 - gsi[j] + ita[j]) + sq(gsi[j] * xa - eps) + sq(ita[j] * bx - eps);
+                continue;
+            }
+            const double Lj = A.L[j], Uj = A.U[j];
             const double ux = Uj - xj, xl = xj - Lj, xa = xj - al[j], bx = be[j] - xj;
             const double iux = 1.0 / ux, ixl = 1.0 / xl, ia = 1.0 / xa, ib = 1.0 / bx;
             const double iux2 = iux * iux, ixl2 = ixl * ixl;
@@ -419,6 +460,13 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
                 const double xp = ad(x[j], mu_(tau, dx[j])), gp = ad(gsi[j], mu_(tau, dgsi[j])),
                              ip = ad(ita[j], mu_(tau, dita[j]));
                 const double plj = p0[j] + lp * p1[j], qlj = q0[j] + lp * q1[j];
+                if constexpr (kConlin) {   // CONLIN::KKTNorm (CONLIN.h:369-407) at the trial point
+                    const double ixp = 1.0 / xp;
+                    a2[0] += p1[j] * xp + q1[j] * ixp;
+                    a2[1] += sq(plj - qlj * (ixp * ixp) - gp + ip) + sq(gp * (xp - al[j]) - eps) +
+                             sq(ip * (be[j] - xp) - eps);
+                    continue;
+                }
                 const double iux = 1.0 / (A.U[j] - xp), ixl = 1.0 / (xp - A.L[j]);
                 a2[0] += p1[j] * iux + q1[j] * ixl;
                 a2[1] += sq(plj * (iux * iux) - qlj * (ixl * ixl) - gp + ip) + sq(gp * (xp - al[j]) - eps) +
@@ -441,10 +489,12 @@ __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
         y = yp; lam = lp; mu = mp; s = sp; z = zp; zeta = zetap;
         if (dw1 < 0.9 * eps) eps *= 0.1;
     }
-    // ---- history and the new design (MMA.h:413-418)
+    // ---- history and the new design (MMA.h:413-418; CONLIN keeps no history, CONLIN.h:361-364)
     for (long long j = tid; j < n; j += stride) {
-        A.xkm2[j] = A.xkm1[j];
-        A.xkm1[j] = A.xk[j];
+        if constexpr (!kConlin) {
+            A.xkm2[j] = A.xkm1[j];
+            A.xkm1[j] = A.xk[j];
+        }
         A.xk[j] = x[j];
     }
     if (tid == 0) {
@@ -538,6 +588,24 @@ __global__ void mul_kernel(long long n, const double *__restrict__ a, const doub
                            double *__restrict__ out) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
         out[e] = a[e] * b[e];
+}
+
+// projection of filtered densities in place: rt -> H(rt), dH = H'(rt) (HeavisideFilter.h:70, :84)
+__global__ void heaviside_project_kernel(long long n, double beta, double *__restrict__ r, double *__restrict__ dH) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const double rt = r[e];
+        dH[e] = heav_drho(rt, beta);
+        r[e] = heav_rho(rt, beta);
+    }
+}
+
+// HeavisideFilter::GetFilteredVariables (HeavisideFilter.h:61-74) on device arrays:
+// rho = H(filter(s)); dH = H'(filter(s)) is kept for heaviside_back
+psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho) {
+    PSF_CHECK(filter_apply(c, s, rho, false));
+    heaviside_project_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, beta, rho, c->dH);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
 }
 
 // filtered sensitivity through the projection (HeavisideFilter.h:81-97):
@@ -675,10 +743,10 @@ psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g,
     A.gs = c->gs;
     A.partials = c->partials;
     A.out = c->scal + 4;
-    const int blocks = coop_blocks_for(c, (const void *)mma_kernel, 256, c->ne);
+    const int blocks = coop_blocks_for(c, (const void *)mma_kernel<false>, 256, c->ne);
     if (!blocks) { set_error("MMA kernel does not fit"); return PSF_CUDA_ERROR; }
     void *args[] = {&A};
-    PSF_CHECK(launch_coop(c, (const void *)mma_kernel, blocks, 256, args));
+    PSF_CHECK(launch_coop(c, (const void *)mma_kernel<false>, blocks, 256, args));
     PSF_CHECK(read_sync_status(c));
     double h[3];
     PSF_CUDA(cudaMemcpyAsync(h, c->scal + 4, sizeof h, cudaMemcpyDeviceToHost, c->stream));
@@ -687,6 +755,37 @@ psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g,
     c->mma_prev = f;
     c->mma_k++;
     if (h[2] != 0.0) { set_error("MMA interior-point loop hit its step cap"); return PSF_NOT_CONVERGED; }
+    return PSF_OK;
+}
+
+psf_status conlin_update(Ctx *c, double *x, double f, const double *dfdx, double g, const double *dgdx, int *newton) {
+    if (!c->cl_ready) { set_error("psf_conlin_update: call psf_conlin_init first"); return PSF_BAD_INPUT; }
+    MmaArgs A{};
+    A.n = c->ne;
+    A.xk = x;
+    A.dfdx = dfdx;
+    A.dgdx = dgdx;
+    A.g = g;
+    A.w = c->mma_work;
+    A.k = c->cl_k;
+    A.a0 = c->cl_a0; A.a = c->cl_a; A.c = c->cl_c; A.d = c->cl_d; A.xmin = c->cl_xmin; A.xmax = c->cl_xmax;
+    A.move = c->cl_move;
+    A.max_newton = 2000;
+    A.gs = c->gs;
+    A.partials = c->partials;
+    A.out = c->scal + 4;
+    const int blocks = coop_blocks_for(c, (const void *)mma_kernel<true>, 256, c->ne);
+    if (!blocks) { set_error("CONLIN kernel does not fit"); return PSF_CUDA_ERROR; }
+    void *args[] = {&A};
+    PSF_CHECK(launch_coop(c, (const void *)mma_kernel<true>, blocks, 256, args));
+    PSF_CHECK(read_sync_status(c));
+    double h[3];
+    PSF_CUDA(cudaMemcpyAsync(h, c->scal + 4, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    if (newton) *newton = (int)h[0];
+    c->cl_prev = f;
+    c->cl_k++;
+    if (h[2] != 0.0) { set_error("CONLIN interior-point loop hit its step cap"); return PSF_NOT_CONVERGED; }
     return PSF_OK;
 }
 

@@ -43,6 +43,18 @@ def cantilever_q4(nx=60, ny=30, **kw):
                  load_val=[-1.0] * len(ln), **kw)
 
 
+def conlin_cantilever_q4(nx=60, ny=40, **kw):
+    """The CONLIN sample's problem (sample_optimize_density_CONLIN.cpp:23-90): the
+    cantilever with E1 = 210000, E0 = 1e-4, scale0 = 1e5, weight limit 0.5, the
+    Heaviside filter (beta doubled every 40 iterations from 0.5) and CONLIN with
+    move 0.2 and convergence 1e-6 (optimizer 2 reads the mma_a0/c/d/xmin/xmax/move/eps
+    fields)."""
+    for k, v in dict(E1=210000.0, E0=1e-4, scale0=1e5, vf=0.5, R=1.5, optimizer=2, heaviside=1,
+                     mma_move=0.2, mma_eps=1e-6).items():
+        kw.setdefault(k, v)
+    return cantilever_q4(nx, ny, **kw)
+
+
 def mbb_q4(nx=1024, ny=512, load_right=None, **kw):
     """Config 2: MBB half beam.  u_x = 0 on the left edge, u_y = 0 at the bottom-right
     node, unit downward load at the top-left node; MMA, vf 0.4, filter radius 3.

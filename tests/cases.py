@@ -16,6 +16,7 @@ CASES = {
     "heatsink_10x10_oc": lambda: PB.heatsink_q4(10, 10, patch_w=1, patch_i0=4),
     "cantilever_h8_6x3x3_oc": lambda: PB.cantilever_h8(6, 3, 3, vf=0.3, R=1.5),
     "cantilever_12x6_heaviside": lambda: PB.cantilever_q4(12, 6, heaviside=1),
+    "cantilever_60x40_conlin": lambda: PB.conlin_cantilever_q4(60, 40),
 }
 
 

@@ -2,7 +2,8 @@
 
 Runs oracle/_ref/ref_driver (the reference headers compiled by
 oracle/build_ref.sh) on small SIMP problems and the reference's own test mains
-(src/LinearAlgebra/Solvers/test_CG.cpp, src/Optimize/Solver/test_MMA*.cpp), and
+(src/LinearAlgebra/Solvers/test_CG.cpp, src/Optimize/Solver/test_MMA*.cpp), CONLIN on
+the optimiser test problems, and
 stores their outputs as compressed .npz / .txt fixtures.  Needs the reference
 source tree, so it runs only where that tree exists; the fixtures it writes
 are committed and used everywhere else.
@@ -37,8 +38,13 @@ CASES = {
     "cantilever_h8_6x3x3_oc": (["kind=2", "nx=6", "ny=3", "nz=3", "vf=0.3", "R=1.5"], 3, None),
     "cantilever_12x6_heaviside": (["kind=0", "nx=12", "ny=6", "bc=cantilever", "heaviside=1"], 4,
                                   None),
+    "cantilever_60x40_conlin": (["kind=0", "nx=60", "ny=40", "bc=cantilever", "opt=2", "heaviside=1",
+                                 "E1=210000", "E0=1e-4", "scale0=1e5", "move=0.2"], 6,
+                                ["f", "g", "rho", "dfds", "s_after", "nb_ptr", "nb_idx", "nb_w"]),
 }
 TEST_MAINS = ["test_CG", "test_MMA", "test_MMA_3", "test_MMA_TOY2"]
+# CONLIN replayed step by step on the optimiser test problems (ref_driver conlin)
+CONLIN_PROBLEMS = {"mma": 30, "mma3": 30, "toy2": 30}
 
 
 def main():
@@ -62,6 +68,11 @@ def main():
     subprocess.run([os.path.join(REF, "ref_driver"), "simp", f"out={tmp}", "iters=1", "kind=0", "nx=12", "ny=6",
                     "bc=cantilever", f"vtk={vtk}"], check=True, stdout=subprocess.DEVNULL)
     print(f"{os.path.basename(vtk)}: {os.path.getsize(vtk)} bytes")
+    for pb, iters in CONLIN_PROBLEMS.items():
+        subprocess.run([os.path.join(REF, "ref_driver"), "conlin", f"out={tmp}", f"problem={pb}", f"iters={iters}"],
+                       check=True, stdout=subprocess.DEVNULL)
+        np.savez_compressed(os.path.join(HERE, f"conlin_{pb}.npz"), **read_dump(tmp))
+        print(f"conlin_{pb}.npz")
     os.remove(tmp)
     for t in TEST_MAINS:
         out = subprocess.run([os.path.join(REF, t)], check=True, capture_output=True, text=True).stdout

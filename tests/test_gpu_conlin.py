@@ -1,0 +1,130 @@
+"""GPU CONLIN (src/Optimize/Solver/CONLIN.h) for one constraint, against the
+oracle and the reference's own trajectory:
+
+* single updates (CONLIN::UpdateVariables) on random sensitivities: designs
+  within 1e-7 max-abs of the oracle (the interior-point loop sums in another
+  order, and its eps / backtracking decisions are discrete);
+* the CONLIN sample (cantilever 60x40, Heaviside projection, scale0 = 1e5)
+  through psf_simp_step: compliance within 1e-6 relative and densities within
+  1e-6 max-abs of the reference's first iterations;
+* the same sample written against the C++ mirror of the reference API
+  (tests/cpp/sample_conlin_gpu.cpp), with the Heaviside filter as its own
+  entry points;
+* 30 iterations of an MBB beam with CONLIN against the oracle.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from pansfem2_gb300 import problems as PB
+from tests.cases import CASES, load
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import pansfem2_gb300 as P
+    P.load()
+    return P
+
+
+@pytest.mark.parametrize("move", [0.2, 0.5])
+def test_conlin_update_matches_oracle(gpu, move):
+    pr = PB.mbb_q4(48, 24, optimizer=2, mma_move=move)
+    ne = PB.counts(pr)[0]
+    rng = np.random.default_rng(11)
+    ref = O.CONLIN(ne, 1, pr["mma_a0"], [0.0], [pr["mma_c"]], [pr["mma_d"]], np.full(ne, pr["mma_xmin"]),
+                   np.full(ne, pr["mma_xmax"]))
+    ref.set_parameters(move, pr["mma_eps"])
+    x = rng.uniform(0.05, 0.95, ne)
+    with gpu.Problem(pr) as P:
+        P.conlin_init()
+        for k in range(4):
+            # mixed-sign objective sensitivities exercise both the linear and the reciprocal terms
+            dfdx = -rng.uniform(0.1, 2.0, ne) * (1.0 + 0.5 * (rng.random(ne) < 0.2) * -3.0)
+            dgdx = np.full(ne, 1.0 / (pr["vf"] * ne))
+            g = float(np.sum(x) / (pr["vf"] * ne) - 1.0)
+            x_ref, n_ref = ref.update(x, 10.0, dfdx, [g], dgdx)
+            x_gpu, n_gpu = P.conlin_update(x, 10.0, dfdx, g, dgdx)
+            assert n_gpu > 0 and abs(n_gpu - n_ref) <= 2, (k, n_gpu, n_ref)
+            assert np.max(np.abs(x_gpu - x_ref)) < 1e-7, k
+            assert np.all(x_gpu >= pr["mma_xmin"]) and np.all(x_gpu <= pr["mma_xmax"])
+            x = x_ref
+
+
+@pytest.mark.parametrize("solver", ["csr_jacobi_f64", "ir_mg_f32"])
+def test_conlin_sample_trajectory_matches_reference(gpu, solver):
+    name = "cantilever_60x40_conlin"
+    g, pr = load(name), CASES[name]()
+    iters = int(g["iters"][0])
+    ne = PB.counts(pr)[0]
+    with gpu.Problem(pr) as P:
+        P.setup_bc()
+        P.simp_begin(solver=solver, cg_eps=1e-10)
+        for k in range(iters):
+            info = P.simp_step()
+            fl = P.fields()
+            assert info["newton_steps"] > 0 or info["converged"], k
+            assert abs(info["f"] - g["f"][k]) <= 1e-6 * abs(g["f"][k]), (k, info["f"], g["f"][k])
+            assert np.max(np.abs(fl["rho"] - g["rho"].reshape(iters, ne)[k])) < 1e-6, k
+            assert np.max(np.abs(fl["s"] - g["s_after"].reshape(iters, ne)[k])) < 1e-6, k
+
+
+def test_heaviside_entry_points_match_oracle(gpu):
+    pr = CASES["cantilever_60x40_conlin"]()
+    g = load("cantilever_60x40_conlin")
+    ne = PB.counts(pr)[0]
+    rng = np.random.default_rng(3)
+    s = rng.uniform(0.01, 1.0, ne)
+    d = -rng.uniform(0.0, 5.0, ne)
+    with gpu.Problem(pr) as P:
+        P.filter_setup()
+        for beta in (1.0, 8.0, 64.0):
+            rho = P.heaviside_forward(beta, s)
+            dfds = P.heaviside_backward(beta, s, d)
+            rho_ref = O.heaviside_filter(g["nb_ptr"], g["nb_idx"], g["nb_w"], beta, s)
+            dfds_ref = O.heaviside_filter_sens(g["nb_ptr"], g["nb_idx"], g["nb_w"], beta, s, d)
+            assert np.max(np.abs(rho - rho_ref)) < 1e-13, beta
+            assert np.max(np.abs(dfds - dfds_ref)) <= 1e-12 * np.max(np.abs(dfds_ref)), beta
+
+
+def test_cpp_conlin_sample_through_the_mirrored_api(gpu, tmp_path):
+    from pansfem2_gb300 import _lib
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = str(tmp_path / "sample_conlin_gpu")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "sample_conlin_gpu.cpp"), "-o", exe,
+                    "-L", libdir, "-lpansfem2_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    g = load("cantilever_60x40_conlin")
+    iters = int(g["iters"][0])
+    out = subprocess.run([exe, "60", "40", str(iters)], check=True, capture_output=True, text=True).stdout
+    fs = [float(l.split()[3]) for l in out.splitlines() if l.startswith("k ")]
+    assert len(fs) == iters
+    for k in range(iters):
+        assert abs(fs[k] - g["f"][k]) <= 1e-6 * abs(g["f"][k]), (k, fs[k], g["f"][k])
+    cs = float([l for l in out.splitlines() if l.startswith("checksum")][0].split()[1])
+    ne = len(g["nb_ptr"]) - 1
+    assert abs(cs - g["s_after"].reshape(iters, ne)[-1].sum()) <= 1e-6 * ne
+
+
+def test_conlin_mbb_30_iterations_match_oracle(gpu):
+    pr = PB.mbb_q4(48, 24, optimizer=2)
+    iters = 30
+    ref = O.simp_run(pr, iters)
+    with gpu.Problem(pr) as P:
+        P.setup_bc()
+        P.simp_begin(solver="ir_mg_f32", cg_eps=1e-10)
+        fs = np.array([P.simp_step()["f"] for _ in range(iters)])
+        s = P.fields()["s"]
+    rel = np.abs(fs - ref["f"][:iters]) / np.abs(ref["f"][:iters])
+    assert rel.max() < 1e-5, (int(rel.argmax()), rel.max())
+    assert np.max(np.abs(s - ref["s_final"])) < 1e-4
+    assert fs[-1] < 0.5 * fs[0]   # the design improves

@@ -170,6 +170,24 @@ def test_reference_test_MMA_TOY2():
     assert got == ref
 
 
+@pytest.mark.parametrize("problem", ["mma", "mma3", "toy2"])
+def test_conlin_steps_bitexact(problem):
+    """CONLIN::UpdateVariables (CONLIN.h:91-365) replayed one step at a time on the
+    reference's own iterates for the optimiser test problems: n > m (mma: n=5, m=1)
+    and both n <= m reductions (mma3: n=2, m=2; toy2: n=3, m=2)."""
+    d = load("conlin_" + problem)
+    n, m = (int(v) for v in d["nm"])
+    K = len(d["f"])
+    assert K >= 5
+    o = O.CONLIN(n, m, 1.0, [0.0] * m, [1000.0] * m, [1.0] * m, d["xmin"], d["xmax"])
+    o.set_parameters(0.5, 1e-5)
+    for k in range(K):
+        x, newton = o.update(d["xin"][k * n:(k + 1) * n], d["f"][k], d["df"][k * n:(k + 1) * n],
+                             d["g"][k * m:(k + 1) * m], d["dg"][k * m * n:(k + 1) * m * n])
+        assert newton > 0
+        assert same(d["xout"][k * n:(k + 1) * n], x), k
+
+
 def test_reference_test_CG():
     """src/LinearAlgebra/Solvers/test_CG.cpp: 4x4 non-symmetric A built with
     CSR::set, b = A*1, BiCGSTAB2 -> prints 1 four times."""
