@@ -110,10 +110,13 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms.  __enter__ waits
+    for the first sample so that the sampler is live before the work starts;
+    window(t0, t1) (perf_counter times of the timed region) restricts the summary
+    to the samples read during it (plus one sampling period)."""
 
     def __init__(self, index=0):
-        self.index, self.rows, self.proc = index, [], None
+        self.index, self.rows, self.proc, self.win = index, [], None, None
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -125,13 +128,16 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            t_end = time.perf_counter() + 5.0
+            while not self.rows and time.perf_counter() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
     def __exit__(self, *a):
         if self.proc:
@@ -141,19 +147,30 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
+    def window(self, t0, t1):
+        self.win = (t0, t1)
+
     def summary(self):
-        if not self.rows:
+        rows = [r for _, r in self.rows]
+        if self.win:
+            t0, t1 = self.win
+            inside = [r for t, r in self.rows if t0 <= t <= t1 + 0.25]
+            before = [r for t, r in self.rows if t < t0]
+            # a timed region shorter than the period: the sample read just before it
+            rows = inside if inside else before[-1:]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
-        for r in self.rows:
+        for r in rows:
             for k, nm in enumerate(names):
                 if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "reasons": sorted(reasons), "samples": len(rows),
+                "samples_total": len(self.rows)}
 
 
 def run_device(pr, solver, warmup, steps, cg_eps, warm_start):
@@ -169,10 +186,14 @@ def run_device(pr, solver, warmup, steps, cg_eps, warm_start):
         infos.append(prob.simp_step())
     prob.sync()
     wall = time.perf_counter() - t0
+    prob.t_region = (t0, t0 + wall)
     return prob, infos, wall
 
 
-def run_e2e(pr, solver, warmup, steps, cg_eps, warm_start):
+def run_e2e(pr, solver, warmup, steps, cg_eps, warm_start, sample_at=()):
+    """The same SIMP iterations through the public host-buffer call: every step copies
+    the design in from pinned host memory and the next design and densities out.
+    Returns the designs entering the steps listed in sample_at."""
     import pansfem2_gb300 as P
     try:
         import torch
@@ -189,14 +210,33 @@ def run_e2e(pr, solver, warmup, steps, cg_eps, warm_start):
         prob.simp_step_host(s_host, s_next, rho_host)
         s_host[:] = s_next
     prob.sync()
+    want = set(sample_at)
+    designs = {}
     t0 = time.perf_counter()
     infos = []
-    for _ in range(steps):
+    for k in range(steps):
+        if k in want:
+            designs[k] = s_host.copy()
         infos.append(prob.simp_step_host(s_host, s_next, rho_host))
         s_host[:] = s_next
     wall = time.perf_counter() - t0
     prob.close()
-    return infos, wall, 8 * ne, 16 * ne
+    return infos, wall, 8 * ne, 16 * ne, designs
+
+
+def fp64_at_designs(pr, solver, designs, cg_eps):
+    """One SIMP iteration of the plain FP64 PCG path (cold-started solves, as that path
+    runs) from each given design: device seconds of the iteration (CUDA events of its
+    phases), its compliance and its Krylov count."""
+    import pansfem2_gb300 as P
+    out = {}
+    for k, s0 in sorted(designs.items()):
+        with P.Problem(pr) as prob:
+            prob.setup_bc()
+            prob.simp_begin(solver=solver, cg_eps=cg_eps, warm_start=False, s0=s0)
+            info = prob.simp_step()
+        out[k] = {"t": sum(info["phase_seconds"]), "f": info["f"], "iters": info["solve"]["iterations"]}
+    return out
 
 
 def cpu_reference_sample(pr, steps, warmup, threads, cg_cap=400, n0=None):
@@ -301,14 +341,20 @@ def bench_heat_batch(args, rank, world):
         with HeatBatch(insts, threads=threads, cluster=cluster) as B:
             B.begin(cg_eps=1e-8)
             B.step(args.warmup)
-            dev_t = B.step(args.steps)
-            res = B.results()
-            # e2e: the same iterations through the public API with the per-step read-back of the results
             t0 = time.perf_counter()
-            for _ in range(args.steps):
-                B.step(1)
-                r = B.results()
-            e2e_t = time.perf_counter() - t0
+            dev_t = B.step(args.steps)
+            clk.window(t0, time.perf_counter())
+            res = B.results()
+    # e2e: the same iterations (a fresh batch from the same initial designs, the same warm-up)
+    # through the public API, each step followed by the read-back of its results
+    with HeatBatch(insts, threads=threads, cluster=cluster) as B:
+        B.begin(cg_eps=1e-8)
+        B.step(args.warmup)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            B.step(1)
+            r = B.results()
+        e2e_t = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([dev_t, e2e_t], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -326,7 +372,7 @@ def bench_heat_batch(args, rank, world):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle / f64 FCG",
            "data": "synthetic (seeded instances)",
            "config": dict(config, threads_per_cta=threads, ctas_per_instance=cluster),
-           "clocks": clk.summary(), "gpu_launches": 4 * (args.steps + args.warmup) * 2,
+           "clocks": clk.summary(), "gpu_launches": 4 * args.steps,   # 4 phase kernels per iteration
            "autotune": {"batch_threads_x_cluster": tune_times},
            "detail": {"solve_iterations_mean": float(np.mean(its)), "solve_iterations_max": int(np.max(its)),
                       "true_residual_max": float(np.max(res["res"])), "all_converged": bool((res["conv"] == 1).all())},
@@ -397,17 +443,24 @@ def bench_learned2d(args, rank, world):
     t_train = time.perf_counter() - t0
     pr = PB.mbb_q4(nx, ny)
     res = {}
+    clocks = None
     for solver in ("ir_learned_f32", "ir_mg_f32", "csr_jacobi_f64"):
-        with P.Problem(pr) as prob:
+        with P.Problem(pr) as prob, ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
             prob.setup_bc()
             if solver == "ir_learned_f32":
                 prob.attach_learned(net, pre_mg=True, nu_post=1)
             prob.simp_begin(solver=solver, cg_eps=args.eps, warm_start=solver != "csr_jacobi_f64")
             for _ in range(args.warmup):
                 prob.simp_step()
+            prob.sync()
+            t0 = time.perf_counter()
             infos = [prob.simp_step() for _ in range(args.steps)]
+            clk.window(t0, time.perf_counter())
+        if solver == "ir_learned_f32":
+            clocks = clk.summary()
         t = sum(sum(i["phase_seconds"]) for i in infos)
         res[solver] = {"value": args.steps / t, "krylov_iterations": sum(i["solve"]["iterations"] for i in infos),
+                       "kernel_launches": int(args.steps * 14 + sum(i["solve"]["kernel_launches"] for i in infos)),
                        "fell_back": sum(i["solve"]["fell_back"] for i in infos),
                        "true_residual_max": max(i["solve"]["rel_residual"] for i in infos), "f_last": infos[-1]["f"]}
     out = {"metric": LEARNED_METRIC, "value": res["ir_learned_f32"]["value"], "unit": "SIMP iterations/s",
@@ -416,8 +469,9 @@ def bench_learned2d(args, rank, world):
            "vs_baseline": None, "dtype": "bf16 network / f32 cycle / f64 FCG", "data": "synthetic",
            "config": {"workload": f"MBB half beam {nx}x{ny} Q4, MMA, R=3, vf=0.4; U-Net 4 levels 16->128",
                       "pairs": len(ts), "train_steps": args.train_steps, "residual": f"FP64 relative {args.eps:g}"},
-           "training": {"harvest_s": t_harvest, "train_s": t_train, "energy_loss_first": float(hist[:20].mean()),
-                        "energy_loss_last": float(hist[-100:].mean())},
+           "clocks": clocks, "gpu_launches": res["ir_learned_f32"]["kernel_launches"],
+           "training": {"harvest_s": t_harvest, "train_s": t_train, "loss": "angle",
+                        "loss_first": float(hist[:20].mean()), "loss_last": float(hist[-100:].mean())},
            "solvers": res,
            "learned_vs_fp64_pcg": res["ir_learned_f32"]["value"] / res["csr_jacobi_f64"]["value"],
            "learned_vs_multigrid": res["ir_learned_f32"]["value"] / res["ir_mg_f32"]["value"],
@@ -436,7 +490,7 @@ def ncpus():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100, help="timed SIMP iterations (the MBB configuration runs 100)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--solver", default="ir_mg_f32")
@@ -507,6 +561,7 @@ def main():
     barrier()
     with ClockSampler(local) as clk:
         prob, infos, wall = run_device(pr, args.solver, args.warmup, args.steps, args.eps, bool(args.warm_start))
+        clk.window(*prob.t_region)
     barrier()
     dev_t = sum(sum(i["phase_seconds"]) for i in infos)
     if world > 1:
@@ -558,7 +613,10 @@ def main():
     # ---- e2e through host buffers
     if not args.no_e2e:
         barrier()
-        einfos, ewall, h2d, d2h = run_e2e(pr, args.solver, args.warmup, args.steps, args.eps, bool(args.warm_start))
+        nsamp = min(10, args.steps)
+        sample_at = sorted({(i * args.steps) // nsamp for i in range(nsamp)} | {args.steps - 1})
+        einfos, ewall, h2d, d2h, designs = run_e2e(pr, args.solver, args.warmup, args.steps, args.eps,
+                                                   bool(args.warm_start), sample_at=sample_at)
         barrier()
         if world > 1:
             t = torch.tensor([ewall], device="cuda")
@@ -567,38 +625,55 @@ def main():
         out["e2e"] = {"value": world * args.steps / ewall, "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h}
 
-    # ---- plain FP64 GPU PCG on the same steps (the spec denominator)
+    # ---- plain FP64 GPU PCG (the spec denominator) at designs sampled evenly from the
+    #      timed iterations.  That path cold-starts every solve, so one iteration's cost depends
+    #      on its design only: the mean over the samples is its rate over the same iterations.
     if not args.no_compare:
         barrier()
         bsolver = args.baseline_solver or ("ebe_jacobi_f64" if args.workload == "h8" else "csr_jacobi_f64")
         args.baseline_solver = bsolver
-        bprob, binfos, bwall = run_device(pr, bsolver, args.warmup, args.steps, args.eps, False)
-        bprob.close()
-        bt = sum(sum(i["phase_seconds"]) for i in binfos)
-        out["fp64_gpu_pcg"] = {"solver": args.baseline_solver, "value": args.steps / bt, "unit": UNIT,
-                               "iter0_iterations": int(bprob.warm_infos[0]["solve"]["iterations"]),
-                               "krylov_iterations": sum(i["solve"]["iterations"] for i in binfos),
-                               "speedup_of_value": value / (args.steps / bt),
-                               "f_last": binfos[-1]["f"],
-                               "compliance_rel_diff_last": abs(binfos[-1]["f"] - infos[-1]["f"]) / abs(binfos[-1]["f"])}
+        if args.no_e2e:   # the designs come from the host-buffer leg
+            nsamp = min(10, args.steps)
+            sample_at = sorted({(i * args.steps) // nsamp for i in range(nsamp)} | {args.steps - 1})
+            _, _, _, _, designs = run_e2e(pr, args.solver, args.warmup, args.steps, args.eps,
+                                          bool(args.warm_start), sample_at=sample_at)
+        res = fp64_at_designs(pr, bsolver, designs, args.eps)
+        bt = float(np.mean([r["t"] for r in res.values()]))
+        klast = max(res)
+        out["fp64_gpu_pcg"] = {"solver": bsolver, "value": 1.0 / bt, "unit": UNIT,
+                               "sampled_iterations": [args.warmup + k for k in sorted(res)],
+                               "krylov_iterations_per_solve": float(np.mean([r["iters"] for r in res.values()])),
+                               "speedup_of_value": value * bt,
+                               "speedup_of_e2e": (out["e2e"]["value"] * bt) if "e2e" in out else None,
+                               "f_at_last_sample": res[klast]["f"],
+                               "compliance_rel_diff_at_samples": max(abs(res[k]["f"] - infos[k]["f"]) / abs(res[k]["f"])
+                                                                     for k in res),
+                               "note": "one SIMP iteration of the FP64 Jacobi PCG path (cold-started solve) from each "
+                                       "sampled design of the timed trajectory; compliance compared with this "
+                                       "solver's on the same design"}
 
     # ---- CPU baseline (rank 0 at N=1 only)
     if rank == 0 and world == 1 and not args.no_cpu:
         thr = ncpus()
-        if args.workload in ("mbb2d", "c1"):
+        if "fp64_gpu_pcg" in out:
+            # ScalingCG is Jacobi-preconditioned CG: at the sampled designs it needs the FP64 GPU
+            # PCG's iteration count; the host run's time per CG iteration is design-independent
+            n0 = int(round(out["fp64_gpu_pcg"]["krylov_iterations_per_solve"]))
+            r = cpu_reference_sample(pr, 1, 0, thr, cg_cap=200, n0=n0)
+            t = float(np.mean(r["samples"]))
+            sample = (f"one SIMP iteration on the host with ScalingCG capped at 200 iterations, solve time scaled "
+                      f"to {n0} iterations (the mean FP64 Jacobi PCG count at the sampled designs of the timed "
+                      f"iterations), oracle restatement -O3 -fopenmp")
+        elif args.workload in ("mbb2d", "c1"):
             r = cpu_reference_sample(pr, 0, 0, thr, n0="full")
             t = r["t_iter0_full"]
             sample = (f"SIMP iteration 0 in full on the host (ScalingCG to 1e-8: {r['n_cg_iter0']} iterations), "
                       f"oracle restatement -O3 -fopenmp")
         else:
-            n0 = None
-            if "fp64_gpu_pcg" in out:
-                n0 = out["fp64_gpu_pcg"]["iter0_iterations"]
-            r = cpu_reference_sample(pr, 1, 0, thr, cg_cap=200, n0=n0 if n0 else "extrapolate")
+            r = cpu_reference_sample(pr, 1, 0, thr, cg_cap=200, n0="extrapolate")
             t = float(np.mean(r["samples"]))
             sample = (f"one SIMP iteration on the host with ScalingCG capped at 200 iterations, solve time scaled "
-                      f"to {r['n_cg_iter0']} iterations ({'the FP64 GPU PCG count of iteration 0' if n0 else r['n0_source']}), "
-                      f"oracle restatement -O3 -fopenmp")
+                      f"to {r['n_cg_iter0']} iterations ({r['n0_source']}), oracle restatement -O3 -fopenmp")
         out["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": thr, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(out))

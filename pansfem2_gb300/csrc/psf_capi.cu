@@ -342,7 +342,7 @@ psf_status psf_mma_init(psf_ctx *h, double a0, double a, double cc, double d, do
         PSF_CHECK(dzalloc(c, &c->mma_U, c->ne));
         PSF_CHECK(dzalloc(c, &c->mma_xkm1, c->ne));
         PSF_CHECK(dzalloc(c, &c->mma_xkm2, c->ne));
-        PSF_CHECK(dzalloc(c, &c->mma_work, 17 * c->ne));
+        PSF_CHECK(dzalloc(c, &c->mma_work, 21 * c->ne));
     } else {
         PSF_CUDA(cudaMemsetAsync(c->mma_xkm1, 0, sizeof(double) * c->ne, c->stream));
         PSF_CUDA(cudaMemsetAsync(c->mma_xkm2, 0, sizeof(double) * c->ne, c->stream));
@@ -380,7 +380,7 @@ psf_status psf_conlin_init(psf_ctx *h, double a0, double a, double cc, double d,
         return PSF_BAD_INPUT;
     }
     if (!(move > 0.0)) { set_error("psf_conlin_init: move must be positive"); return PSF_BAD_INPUT; }
-    if (!c->mma_work) PSF_CHECK(dzalloc(c, &c->mma_work, 17 * c->ne));
+    if (!c->mma_work) PSF_CHECK(dzalloc(c, &c->mma_work, 21 * c->ne));
     c->cl_a0 = a0; c->cl_a = a; c->cl_c = cc; c->cl_d = d; c->cl_xmin = xmin; c->cl_xmax = xmax;
     c->cl_move = move; c->cl_epsvalue = epsvalue;
     c->cl_k = 0;

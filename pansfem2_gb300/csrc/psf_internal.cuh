@@ -101,7 +101,8 @@ struct Ctx {
 
     // MMA state (m = 1)
     double *mma_L = nullptr, *mma_U = nullptr, *mma_xkm1 = nullptr, *mma_xkm2 = nullptr;
-    double *mma_work = nullptr;  // 17*ne scratch (MMA and CONLIN)
+    double *mma_work = nullptr;  // 21*ne scratch (MMA and CONLIN; the double-word kernel uses all of it)
+    int opt_fp64_fallbacks = 0;  // double-word updates rerun in FP64 (data outside the FP32 pair range)
     int mma_k = 0;
     double mma_prev = 0.0, mma_epsvalue = 1e-5;
     double mma_a0 = 1, mma_a = 0, mma_c = 1e4, mma_d = 0, mma_xmin = 0.01, mma_xmax = 1.0;
@@ -179,6 +180,8 @@ psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g,
                       int *newton);
 psf_status conlin_update(Ctx *c, double *x, double f, const double *dfdx, double g, const double *dgdx,
                          int *newton);
+psf_status mma_dw_update(Ctx *c, bool conlin, double *x, const double *dfdx, double g, const double *dgdx,
+                         int *newton, bool *capped, bool *done);
 psf_status moduli_from_rho(Ctx *c, const double *rho, double E1, double E0, double p, double *E_dev);
 psf_status mg_free(Ctx *c);
 psf_status learned_free(Ctx *c);                                                       // psf_learned.cu

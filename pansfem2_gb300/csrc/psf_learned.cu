@@ -73,6 +73,7 @@ struct Learned {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     float graph_scale = 0.0f;
+    size_t graph_nodes = 0;   // kernel nodes of the captured graph (kGraphIters FCG iterations)
     float inv_e1 = 1.0f;   // 1 / E1 of the design (density features)
     float *dcorr = nullptr;   // the network's correction in x space (before its step length)
     std::vector<void *> allocs;
@@ -659,6 +660,8 @@ static psf_status lp_build_graph(Ctx *c, Learned *L, double *x, double *r, doubl
         return cuda_status(e, "cudaGraphInstantiate (learned FCG)");
     }
     L->graph = gph;
+    L->graph_nodes = 0;
+    cudaGraphGetNodes(gph, nullptr, &L->graph_nodes);
     return PSF_OK;
 }
 
@@ -697,6 +700,7 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     int total = 0, passes = 0;
     bool ok = false, stalled = false;
     double rn = 0.0, bn = 0.0;
+    long long glaunch = 0;
     PSF_CUDA(cudaEventRecord(c->evk0, st));
     for (int pass = 0; pass < 3 && total < limit; pass++) {
         passes++;
@@ -705,6 +709,7 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
         PSF_CUDA(cudaGetLastError());
         for (;;) {
             for (int k = 0; k < 2; k++) PSF_CUDA(cudaGraphLaunch(L->exec, st));
+            glaunch += 2;
             PSF_CUDA(cudaMemcpyAsync(L->hflags, L->flags, sizeof(int) * F_N, cudaMemcpyDeviceToHost, st));
             PSF_CUDA(cudaStreamSynchronize(st));
             if (L->hflags[F_DONE]) break;
@@ -730,7 +735,9 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     float ms = 0.f;
     PSF_CUDA(cudaEventElapsedTime(&ms, c->evk0, c->evk1));
     c->ksec += ms * 1e-3;
-    c->klaunch += passes * (int)((total + kGraphIters - 1) / kGraphIters);
+    // kernels launched: residual + start per pass, every node of every graph launch (the
+    // iterations after convergence skip their work on the device flag but still launch)
+    c->klaunch += 2 * passes + (int)(glaunch * (long long)L->graph_nodes);
     int fb_iters = 0;
     if (!ok && allow_fallback && (stalled || total >= limit)) {
         // fallback: FP64 Jacobi PCG from the current iterate (zero start if the iterate is not finite)

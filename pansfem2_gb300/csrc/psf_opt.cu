@@ -8,6 +8,7 @@
 // the bisection / interior-point loops with data-dependent trip counts stay
 // on the device, every block computing the same scalars.
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <vector>
 
@@ -681,6 +682,13 @@ psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, doub
     return PSF_OK;
 }
 
+// the MMA / CONLIN element-wise arithmetic in double words (psf_optdw.cu) unless
+// PSF_OPT_F64=1 asks for the FP64 kernel (read at every update)
+static bool opt_use_dw() {
+    const char *e = getenv("PSF_OPT_F64");
+    return !(e && e[0] == '1');
+}
+
 static int coop_blocks_for(Ctx *c, const void *fn, int threads, long long work) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1) return 0;
@@ -727,6 +735,17 @@ psf_status oc_update(Ctx *c, double *x, const double *dfdx, const double *dgdx, 
 
 psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g, const double *dgdx, int *newton) {
     if (!c->mma_ready) { set_error("psf_mma_update: call psf_mma_init first"); return PSF_BAD_INPUT; }
+    if (opt_use_dw()) {
+        bool done = false, capped = false;
+        PSF_CHECK(mma_dw_update(c, false, x, dfdx, g, dgdx, newton, &capped, &done));
+        if (done) {
+            c->mma_prev = f;
+            c->mma_k++;
+            if (capped) { set_error("MMA interior-point loop hit its step cap"); return PSF_NOT_CONVERGED; }
+            return PSF_OK;
+        }
+        c->opt_fp64_fallbacks++;
+    }
     MmaArgs A;
     A.n = c->ne;
     A.xk = x;
@@ -760,6 +779,17 @@ psf_status mma_update(Ctx *c, double *x, double f, const double *dfdx, double g,
 
 psf_status conlin_update(Ctx *c, double *x, double f, const double *dfdx, double g, const double *dgdx, int *newton) {
     if (!c->cl_ready) { set_error("psf_conlin_update: call psf_conlin_init first"); return PSF_BAD_INPUT; }
+    if (opt_use_dw()) {
+        bool done = false, capped = false;
+        PSF_CHECK(mma_dw_update(c, true, x, dfdx, g, dgdx, newton, &capped, &done));
+        if (done) {
+            c->cl_prev = f;
+            c->cl_k++;
+            if (capped) { set_error("CONLIN interior-point loop hit its step cap"); return PSF_NOT_CONVERGED; }
+            return PSF_OK;
+        }
+        c->opt_fp64_fallbacks++;
+    }
     MmaArgs A{};
     A.n = c->ne;
     A.xk = x;

@@ -61,3 +61,18 @@ def test_problem_definitions_match_generate_fixedlist_order():
     mbb = PB.mbb_q4(4, 2)
     assert mbb["fix_node"] == [0, 1, 2, 12] and mbb["fix_dof"] == [0, 0, 0, 1]
     assert mbb["load_node"] == [2]
+
+
+def test_double_word_arithmetic_on_host(tmp_path):
+    """The double-word FP32-pair operations the MMA / CONLIN kernels use
+    (pansfem2_gb300/csrc/psf_dw.cuh), compiled for the host: every operation
+    within 2^-44 relative of long double arithmetic on random operands."""
+    cuda_inc = "/usr/local/cuda/include"
+    if not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("no CUDA headers")
+    exe = str(tmp_path / "dw_check")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", cuda_inc, "-I", os.path.join(ROOT, "pansfem2_gb300", "csrc"),
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "dw_check.cpp"),
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout

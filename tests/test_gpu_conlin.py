@@ -36,8 +36,11 @@ def gpu():
     return P
 
 
+@pytest.mark.parametrize("arith", ["double_word", "fp64"])
 @pytest.mark.parametrize("move", [0.2, 0.5])
-def test_conlin_update_matches_oracle(gpu, move):
+def test_conlin_update_matches_oracle(gpu, move, arith, monkeypatch):
+    if arith == "fp64":
+        monkeypatch.setenv("PSF_OPT_F64", "1")
     pr = PB.mbb_q4(48, 24, optimizer=2, mma_move=move)
     ne = PB.counts(pr)[0]
     rng = np.random.default_rng(11)
@@ -113,6 +116,29 @@ def test_cpp_conlin_sample_through_the_mirrored_api(gpu, tmp_path):
     cs = float([l for l in out.splitlines() if l.startswith("checksum")][0].split()[1])
     ne = len(g["nb_ptr"]) - 1
     assert abs(cs - g["s_after"].reshape(iters, ne)[-1].sum()) <= 1e-6 * ne
+
+
+def test_double_word_range_fallback(gpu):
+    """Objective sensitivities below the FP32 pair range (1e-33; the interior-point
+    method itself, in FP64 as in the reference, cannot meet its absolute 1e-7 KKT
+    tolerance at magnitudes far above 1e8, so large values are no test): the
+    double-word kernel declines before writing anything and the FP64 kernel does
+    the update, so the result still matches the oracle."""
+    pr = PB.mbb_q4(48, 24, optimizer=2)
+    ne = PB.counts(pr)[0]
+    rng = np.random.default_rng(2)
+    ref = O.CONLIN(ne, 1, pr["mma_a0"], [0.0], [pr["mma_c"]], [pr["mma_d"]], np.full(ne, pr["mma_xmin"]),
+                   np.full(ne, pr["mma_xmax"]))
+    ref.set_parameters(pr["mma_move"], pr["mma_eps"])
+    x = rng.uniform(0.05, 0.95, ne)
+    dfdx = -rng.uniform(0.1, 2.0, ne) * 1e-33
+    dgdx = np.full(ne, 1.0 / (pr["vf"] * ne))
+    g = float(np.sum(x) / (pr["vf"] * ne) - 1.0)
+    with gpu.Problem(pr) as P:
+        P.conlin_init()
+        x_gpu, _ = P.conlin_update(x, 10.0, dfdx, g, dgdx)
+    x_ref, _ = ref.update(x, 10.0, dfdx, [g], dgdx)
+    assert np.max(np.abs(x_gpu - x_ref)) < 1e-7
 
 
 def test_conlin_mbb_30_iterations_match_oracle(gpu):
