@@ -10,7 +10,8 @@
 // the team: no grid barrier, no atomics, deterministic.  Instances are launched
 // largest first.
 // The solve is flexible CG in FP64 (operator, dot products, recurrences) whose
-// preconditioner is one FP32 V(2,2) multigrid cycle per iteration: l1-Jacobi
+// preconditioner is one FP32 V(2,2) multigrid cycle per iteration: degree-2 Chebyshev on the l1-Jacobi
+// scaled operator (PSF_MG_CHEB as for the single-problem solver; <= 1 selects plain l1-Jacobi)
 // smoothing, Galerkin coarse operators built element by element inside the
 // block (P^T K P with bilinear P, fixed nodes masked), 9-point coarse stencils,
 // and a dense inverse of the coarsest level (<= 64 nodes) in shared memory.
@@ -22,6 +23,7 @@
 // of the same problem to the solver tolerance.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -71,6 +73,9 @@ struct Args {
     double Ke0[16];
     float Ke0f[16];          // float part of Ke0 (the cycle uses it alone)
     float Ke0lo[16];         // Ke0 - Ke0f: Ke0f + Ke0lo carries 48 bits (double-single operator)
+    // smoothing steps of the cycle: d0 = om D^-1 r0, d1 = c2 d0 + c3 D^-1 r1 (x += d each step);
+    // degree-2 Chebyshev on [1/ratio, 1] of the l1-scaled operator, or l1-Jacobi (om = c3 = 1, c2 = 0)
+    float sm_om, sm_c2, sm_c3;
     int nst;                 // filter stencil
     int sdi[kMaxStencilB], sdj[kMaxStencilB];
     double sw[kMaxStencilB];
@@ -432,16 +437,19 @@ __device__ void mg_setup(const Args &A, const Team &T, const Inst &I, double *sm
 }
 
 // ------------------------------------------------------------------ the V(2,2) cycle (FP32)
-__device__ void jacobi_sweep(const Args &A, const Team &T, const Inst &I, int l) {
+// smoothing step `step` (0 or 1) on level l; the correction d is kept in mr between the steps
+__device__ void smooth_step(const Args &A, const Team &T, const Inst &I, int l, int step) {
     const int m = I.n >> l;
     const long long tid = T.tid, nt = T.nt;
     const long long nn = (long long)(m + 1) * (m + 1);
     const float *x = A.mx + I.mv[l];
     float *t = A.mr + I.mv[l];
     const float *b = A.mb + I.mv[l];
+    const float c2 = step ? A.sm_c2 : 0.0f, c3 = step ? A.sm_c3 : A.sm_om;
     for (long long v = tid; v < nn; v += nt) {
         const int i = (int)(v / (m + 1)), j = (int)(v % (m + 1));
-        t[v] = A.mfix[I.mv[l] + v] ? 0.0f : (b[v] - opl(A, I, l, x, i, j)) / A.D[I.mv[l] + v];
+        const float dprev = step ? t[v] : 0.0f;
+        t[v] = A.mfix[I.mv[l] + v] ? 0.0f : c2 * dprev + c3 * (b[v] - opl(A, I, l, x, i, j)) / A.D[I.mv[l] + v];
     }
     tsync(T);
     float *xw = A.mx + I.mv[l];
@@ -452,8 +460,8 @@ __device__ void jacobi_sweep(const Args &A, const Team &T, const Inst &I, int l)
 __device__ void vcycle(const Args &A, const Team &T, const Inst &I) {
     const long long tid = T.tid, nt = T.nt;
     for (int l = 0; l < I.nlev - 1; l++) {
-        jacobi_sweep(A, T, I, l);
-        jacobi_sweep(A, T, I, l);
+        smooth_step(A, T, I, l, 0);
+        smooth_step(A, T, I, l, 1);
         // residual into mr
         const int m = I.n >> l;
         const long long nn = (long long)(m + 1) * (m + 1);
@@ -512,8 +520,8 @@ __device__ void vcycle(const Args &A, const Team &T, const Inst &I) {
             x[v] += c;
         }
         tsync(T);
-        jacobi_sweep(A, T, I, l);
-        jacobi_sweep(A, T, I, l);
+        smooth_step(A, T, I, l, 0);
+        smooth_step(A, T, I, l, 1);
     }
 }
 
@@ -978,6 +986,18 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
         a.Ke0[q] = Ke[q];
         a.Ke0f[q] = (float)Ke[q];
         a.Ke0lo[q] = (float)(Ke[q] - (double)a.Ke0f[q]);
+    }
+    {
+        const char *e = getenv("PSF_MG_CHEB");
+        const double ratio = e ? atof(e) : 40.0;   // the single-problem solver's default (psf_mg.cu)
+        a.sm_om = 1.0f; a.sm_c2 = 0.0f; a.sm_c3 = 1.0f;
+        if (ratio > 1.0) {
+            const double lo = 1.0 / ratio, theta = 0.5 * (1.0 + lo), delta = 0.5 * (1.0 - lo), sigma = theta / delta;
+            const double rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
+            a.sm_om = (float)(1.0 / theta);
+            a.sm_c2 = (float)(rho1 * rho0);
+            a.sm_c3 = (float)(2.0 * rho1 / delta);
+        }
     }
     *out = b;
     return PSF_OK;

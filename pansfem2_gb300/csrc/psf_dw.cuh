@@ -19,6 +19,10 @@
 
 #include <cmath>
 
+#ifdef __CUDACC__
+#include "psf_common.cuh"
+#endif
+
 // Every operation is also compiled for the host (tests/cpp/dw_check.cu checks them there):
 // single-rounding float add / mul / fma on both sides, no contraction.
 #ifdef __CUDA_ARCH__
@@ -130,6 +134,52 @@ __host__ __device__ __forceinline__ D ld(const float2 *p, long long i) {
     return D{v.x, v.y};
 }
 __host__ __device__ __forceinline__ void st(float2 *p, long long i, D v) { p[i] = make_float2(v.h, v.l); }
+
+#ifdef __CUDACC__
+// Block sums of NV double-word values: the warp levels in double words (FP32 pipes),
+// then the per-warp results in FP64 by warp 0, in a fixed order.  Result in thread 0.
+// (A warp tree in FP64 costs every lane five FP64 adds per value, which on GB300's
+// FP64 pipe rivals the element work.)
+template <int NV>
+__device__ __forceinline__ void block_sum_dw(D (&v)[NV], double (&out)[NV], double *smem) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const D t = make(__shfl_xor_sync(0xffffffffu, v[k].h, o), __shfl_xor_sync(0xffffffffu, v[k].l, o));
+            v[k] = add(v[k], t);
+        }
+    }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) smem[k * 32 + wid] = to_double(v[k]);
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) out[k] = warp_sum(lane < nw ? smem[k * 32 + lane] : 0.0);
+    }
+}
+
+// block maximum of double-word values, as a double in thread 0
+__device__ __forceinline__ double block_max_dw(D v, double *smem) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const D t = make(__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o));
+        v = max(v, t);
+    }
+    __syncthreads();
+    if (lane == 0) smem[wid] = to_double(v);
+    __syncthreads();
+    double m = -INFINITY;
+    if (wid == 0) m = warp_max(lane < nw ? smem[lane] : -INFINITY);
+    return m;
+}
+
+#endif
 
 }  // namespace dw
 }  // namespace psf

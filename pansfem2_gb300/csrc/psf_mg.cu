@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <vector>
 
+#include "psf_dw.cuh"
 #include "psf_internal.cuh"
 
 namespace psf {
@@ -67,6 +68,8 @@ struct MgHier {
     std::vector<void *> allocs;
     bool built_for_current_E = false;
     unsigned long long *trace = nullptr;   // phase timestamps (PSF_MG_TRACE)
+    float2 *xw = nullptr, *rw = nullptr, *pw = nullptr, *qw = nullptr, *Ew = nullptr;   // double-word FCG
+    long long npad = 0;
 };
 
 // ------------------------------------------------------------------ geometry helpers
@@ -406,12 +409,11 @@ __global__ void gauss_jordan_kernel(double *A, int n) {
 // preconditioner only (no cond(K) amplification as in an FP32 inner solve).
 struct MgFcgArgs {
     int nlev;
-    int ds;                   // 1: the FCG operator K p in double-single (FP32 pipes), 0: FP64
     int lsmall;               // first level run by block 0 alone (1 <= lsmall <= nlev - 1)
     MgLev L[kMaxLev];
     KeF Ke;                   // level-0 element matrix (FP32, cycle)
     KeT64 Ke64;               // level-0 element matrix (FP64, operator)
-    KeDS Kds;                 // the same as float pairs (double-single operator)
+    KeDS Kds;                 // the same as float pairs hi + lo (double-word operator)
     const double *Ainv;
     int nc;
     float omega;              // first smoothing step from zero: x = omega D^-1 b
@@ -430,6 +432,9 @@ struct MgFcgArgs {
     double *out;              // iterations, |r|^2, |b|^2, converged, V-cycles
     unsigned long long *trace;   // optional: [0] = count, then %globaltimer after each sync of one iteration
     int trace_iter;
+    // double-word Krylov vectors (mg_fcg_dw_kernel): x, r, p, q as FP32 pairs, padded moduli
+    float2 *xw, *rw, *pw, *qw, *Ew;
+    long long npad;           // padded moduli entries
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -662,36 +667,24 @@ __device__ __forceinline__ double apply64_node(const MgFcgArgs &A, const double 
     return d;
 }
 
-// ---- double-single arithmetic: error-free transformations on the FP32 pipes
-// TwoProduct with the FMA (Ogita, Rump, Oishi 2005): a b = p + e exactly
-__device__ __forceinline__ float ds_two_prod(float a, float b, float &e) {
-    const float p = a * b;
-    e = __fmaf_rn(a, b, -p);
-    return p;
-}
-// TwoSum (Knuth): a + b = s + e exactly
-__device__ __forceinline__ float ds_two_sum(float a, float b, float &e) {
-    const float s = __fadd_rn(a, b);
-    const float v = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
-    return s;
-}
+constexpr int kMgThreads = 512;   // one block per SM: half the barrier arrivals of 2 x 256
 
-// q = K v for node n with each element's K0 u_e product in double-single
-// (compensated dot product, Ogita-Rump-Oishi "Dot2": about twice float
-// precision, ~1e-14) and the scaling by E_e and the node sum in FP64.  GB300's
-// FP64 rate is a small fraction of its FP32 rate: this moves the 8 x 8
-// products (Q4) or 24 x 24 (H8) of every element to the FP32 pipes.
+// q = K v for node n with v, q and the moduli as double words (FP32 pairs): each element's
+// K0 u_e row product is a compensated dot product (Ogita, Rump, Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26(6), 2005, Dot2: TwoProd + TwoSum per term, with the
+// low-order products of K0 = Kh + Kl and v = vh + vl folded into the correction), then
+// scaled by E_e and summed over the node's elements in double words.  Returns the partial
+// v.q of the node in double words.  Nothing here runs on the FP64 pipe.
 template <int KIND>
-__device__ __forceinline__ double applyds_node(const MgFcgArgs &A, const double *__restrict__ v, long long n,
-                                               double *__restrict__ out) {
+__device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *__restrict__ v, long long n,
+                                              float2 *__restrict__ out) {
     using T = KT<KIND>;
     const MgLev &L = A.L[0];
     int i, j, k;
     lnode_ijk<KIND>(L, n, i, j, k);
-    double y[T::nd];
+    dw::D y[T::nd];
 #pragma unroll
-    for (int a = 0; a < T::nd; a++) y[a] = 0.0;
+    for (int a = 0; a < T::nd; a++) y[a] = dw::from_float(0.f);
 #pragma unroll
     for (int ci = 0; ci < 2; ci++)
 #pragma unroll
@@ -700,10 +693,9 @@ __device__ __forceinline__ double applyds_node(const MgFcgArgs &A, const double 
             for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
                 const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
                 const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0);
-                const double Ee = A.Ep64[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
-                                                 : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
-                if (Ee == 0.0) continue;
-                // one pass over the element's dofs: each value is split once and feeds every row of this node
+                const float2 Ev = A.Ew[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
+                                               : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
+                if (Ev.x == 0.f) continue;
                 float ps[T::nd], cs[T::nd];
 #pragma unroll
                 for (int a = 0; a < T::nd; a++) ps[a] = cs[a] = 0.0f;
@@ -715,35 +707,37 @@ __device__ __forceinline__ double applyds_node(const MgFcgArgs &A, const double 
                                                     T::is3d ? min(max(ek + qk, 0), L.nz) : 0);
 #pragma unroll
                     for (int b = 0; b < T::nd; b++) {
-                        const double u = v[m * T::nd + b];
-                        const float uh = __double2float_rn(u);
-                        const float ul = __double2float_rn(u - (double)uh);
+                        const float2 u = v[m * T::nd + b];
                         const int l = q * T::nd + b;
 #pragma unroll
                         for (int a = 0; a < T::nd; a++) {
                             const int kk = (li * T::nd + a) * T::nk + l;
                             float pe, se;
-                            const float pr = ds_two_prod(A.Kds.hi[kk], uh, pe);
-                            ps[a] = ds_two_sum(ps[a], pr, se);
-                            cs[a] += se + pe + __fmaf_rn(A.Kds.hi[kk], ul, A.Kds.lo[kk] * uh);
+                            const float pr = dw::two_prod(A.Kds.hi[kk], u.x, pe);
+                            ps[a] = dw::two_sum(ps[a], pr, se);
+                            cs[a] += se + pe + __fmaf_rn(A.Kds.hi[kk], u.y, A.Kds.lo[kk] * u.x);
                         }
                     }
                 }
+                const dw::D Ed = dw::make(Ev.x, Ev.y);
 #pragma unroll
-                for (int a = 0; a < T::nd; a++) y[a] += Ee * ((double)ps[a] + (double)cs[a]);
+                for (int a = 0; a < T::nd; a++) {
+                    float sl;
+                    const float sh = dw::fast_two_sum(ps[a], cs[a], sl);
+                    y[a] = dw::add(y[a], dw::mul(Ed, dw::make(sh, sl)));
+                }
             }
-    double d = 0.0;
+    dw::D d = dw::from_float(0.f);
 #pragma unroll
     for (int a = 0; a < T::nd; a++) {
         const long long t = n * T::nd + a;
-        const double qv = L.fixed[t] ? 0.0 : y[a];
-        out[t] = qv;
-        d += v[t] * qv;
+        const dw::D qv = L.fixed[t] ? dw::from_float(0.f) : y[a];
+        out[t] = make_float2(qv.h, qv.l);
+        const float2 vv = v[t];
+        d = dw::add(d, dw::mul(dw::make(vv.x, vv.y), qv));
     }
     return d;
 }
-
-constexpr int kMgThreads = 512;   // one block per SM: half the barrier arrivals of 2 x 256
 
 template <int KIND>
 __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
@@ -837,7 +831,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
         // ---- q = K p, p.q
         double pq[1] = {0.0};
         for (long long n = tid; n < L0.nnodes; n += stride)
-            pq[0] += A.ds ? applyds_node<KIND>(A, A.p, n, A.q) : apply64_node<KIND>(A, A.p, n, A.q);
+            pq[0] += apply64_node<KIND>(A, A.p, n, A.q);
         block_sum<1>(pq, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, pq, 0.0)) return;
         stamp(A, tr);
@@ -864,6 +858,147 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
         if (rn <= A.eps * bnorm) { it++; conv = 1; break; }
         if (!isfinite(rr)) { it++; break; }
     }
+    if (tid == 0) {
+        A.out[0] = it;
+        A.out[1] = rr;
+        A.out[2] = bnorm * bnorm;
+        A.out[3] = conv;
+        A.out[4] = cycles;
+    }
+}
+
+// The same flexible CG with its Krylov vectors and operator in double words (FP32
+// pairs, ~48-bit significands) instead of FP64: the recurrences keep about 1e-14
+// relative accuracy, far below the 1e-8 the solve needs, while every vector update,
+// dot product and K p runs on the FP32 pipes (GB300's FP64 rate is a small fraction
+// of its FP32 rate; with FP64 vectors the operator alone was a fifth of an iteration).
+// Dot products are reduced in double words per warp and in FP64 across warps and
+// blocks, in a fixed order.  The FP64 true residual of the result is checked by the
+// caller, as for the FP64 kernel.
+template <int KIND>
+__global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
+    using T = KT<KIND>;
+    using dw::D;
+    __shared__ double sm[32 * 4];
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const MgLev &L0 = A.L[0];
+    float2 *X = A.xw, *R = A.rw, *P = A.pw, *Q = A.qw;
+    auto ld = [](const float2 *a, long long t) { const float2 v = a[t]; return dw::make(v.x, v.y); };
+    auto st = [](float2 *a, long long t, D v) { a[t] = make_float2(v.h, v.l); };
+    // ---- start: moduli in double words; r = b - K x0 in FP64 (x0 = 0 unless warm)
+    {
+        for (long long e = tid; e < A.npad; e += stride) {
+            const D Ed = dw::from_double(A.Ep64[e]);
+            A.Ew[e] = make_float2(Ed.h, Ed.l);
+        }
+        double acc[2] = {0.0, 0.0};
+        for (long long n = tid; n < L0.nnodes; n += stride) {
+            if (A.warm) apply64_node<KIND>(A, A.x, n, A.r);   // r = K x0 (own dofs)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                const double bv = L0.fixed[t] ? 0.0 : A.b[t];
+                const double rv = L0.fixed[t] ? 0.0 : (A.warm ? bv - A.r[t] : bv);
+                st(R, t, dw::from_double(rv));
+                st(X, t, A.warm && !L0.fixed[t] ? dw::from_double(A.x[t]) : dw::from_float(0.f));
+                st(P, t, dw::from_float(0.f));
+                st(Q, t, dw::from_float(0.f));
+                acc[0] += bv * bv;
+                acc[1] += rv * rv;
+            }
+        }
+        block_sum<2>(acc, sm);
+        if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
+    }
+    const double bnorm = sqrt(gs_result(A.gs, 0));
+    double rr = gs_result(A.gs, 1);
+    double rn = sqrt(rr), pq_prev = 1.0;
+    int it = 0, conv = (rn <= A.eps * bnorm) ? 1 : 0, cycles = 0;
+    for (; !conv && it < A.itmax; it++) {
+        // ---- preconditioner: one FP32 V-cycle on r / |r|
+        const float sc = (float)(1.0 / rn);
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                const float2 rv = R[t];
+                const float bv = L0.fixed[t] ? 0.f : rv.x * sc + rv.y * sc;
+                L0.b[t] = bv;
+                L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
+            }
+        const bool tr = it == A.trace_iter;
+        stamp(A, tr);
+        if (!grid_barrier(A.gs, A.partials)) return;
+        stamp(A, tr);
+        if (!vcycle<KIND>(A, tid, stride, tr)) return;
+        cycles++;
+        // ---- z = |r| V(r/|r|) (own dofs of L0.x); z.q_prev, z.r, p_prev.r
+        const D rnD = dw::from_double(rn);
+        D a3[3] = {dw::from_float(0.f), dw::from_float(0.f), dw::from_float(0.f)};
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                const D zv = dw::mulf(rnD, L0.x[t]);
+                a3[0] = dw::add(a3[0], dw::mul(zv, ld(Q, t)));
+                a3[1] = dw::add(a3[1], dw::mul(zv, ld(R, t)));
+                a3[2] = dw::add(a3[2], dw::mul(ld(P, t), ld(R, t)));
+            }
+        double s3[3] = {0.0, 0.0, 0.0};
+        dw::block_sum_dw<3>(a3, s3, sm);
+        if (!grid_sync<3, 0>(A.gs, A.partials, s3, 0.0)) return;
+        stamp(A, tr);
+        const double beta = it > 0 ? gs_result(A.gs, 0) / pq_prev : 0.0;
+        const double pr = gs_result(A.gs, 1) - beta * gs_result(A.gs, 2);
+        const D betaD = dw::from_double(beta);
+        // ---- p = z - beta p_prev (own dofs)
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                st(P, t, dw::sub(dw::mulf(rnD, L0.x[t]), dw::mul(betaD, ld(P, t))));
+            }
+        if (!grid_barrier(A.gs, A.partials)) return;
+        stamp(A, tr);
+        // ---- q = K p (double words), p.q
+        D pqd[1] = {dw::from_float(0.f)};
+        for (long long n = tid; n < L0.nnodes; n += stride) pqd[0] = dw::add(pqd[0], applydw_node<KIND>(A, P, n, Q));
+        double pq[1] = {0.0};
+        dw::block_sum_dw<1>(pqd, pq, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, pq, 0.0)) return;
+        stamp(A, tr);
+        const double pqv = gs_result(A.gs, 0);
+        if (!(pqv > 0.0)) { it++; break; }
+        const D alphaD = dw::from_double(pr / pqv);
+        // ---- x += alpha p, r -= alpha q, |r|^2
+        D rad[1] = {dw::from_float(0.f)};
+        for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+            for (int s = 0; s < T::nd; s++) {
+                const long long t = n * T::nd + s;
+                st(X, t, dw::add(ld(X, t), dw::mul(alphaD, ld(P, t))));
+                const D rv = dw::sub(ld(R, t), dw::mul(alphaD, ld(Q, t)));
+                st(R, t, rv);
+                rad[0] = dw::add(rad[0], dw::sq(rv));
+            }
+        double ra[1] = {0.0};
+        dw::block_sum_dw<1>(rad, ra, sm);
+        if (!grid_sync<1, 0>(A.gs, A.partials, ra, 0.0)) return;
+        stamp(A, tr);
+        rr = gs_result(A.gs, 0);
+        rn = sqrt(rr);
+        pq_prev = pqv;
+        if (rn <= A.eps * bnorm) { it++; conv = 1; break; }
+        if (!isfinite(rr)) { it++; break; }
+    }
+    // ---- the solution in FP64 for the caller (own dofs)
+    for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+        for (int s = 0; s < T::nd; s++) {
+            const long long t = n * T::nd + s;
+            A.x[t] = dw::to_double(ld(X, t));
+        }
     if (tid == 0) {
         A.out[0] = it;
         A.out[1] = rr;
@@ -1012,12 +1147,14 @@ static psf_status mg_setup(Ctx *c) {
 
 // Smoother of the V(2,2) cycle: degree-2 Chebyshev on [1/ratio, 1] in the l1-Jacobi
 // preconditioned operator D^-1 A (the l1 row sums bound its spectrum by 1, so the upper
-// end is rigorous).  Measured on the 1M-dof MBB trajectory (100 SIMP iterations, FP64
-// flexible CG to 1e-8): Krylov iterations 14,793 with two plain l1-Jacobi steps, 12,486 /
-// 11,558 / 11,298 / 11,002 / 10,769 with ratio 3 / 6 / 8 / 12 / 20, at the same cost per
-// cycle.  PSF_MG_CHEB=<ratio> overrides the default; a ratio <= 1 selects plain l1-Jacobi
-// (omega = 1, convergent for any SPD operator).
-constexpr double kChebRatio = 20.0;
+// end is rigorous).  Measured on the 1M-dof MBB trajectory (100 SIMP iterations, flexible
+// CG to 1e-8): Krylov iterations 14,793 with two plain l1-Jacobi steps, 12,486 / 11,558 /
+// 11,298 / 11,002 / 10,769 / 10,663 / 10,618 with ratio 3 / 6 / 8 / 12 / 20 / 30 / 50, at
+// the same cost per cycle; on the 128x64x64 H8 cantilever (30 iterations) 2,778 with
+// l1-Jacobi, 2,034 / 1,909 / 1,880 with ratio 8 / 20 / 40.  PSF_MG_CHEB=<ratio> overrides
+// the default; a ratio <= 1 selects plain l1-Jacobi (omega = 1, convergent for any SPD
+// operator).
+constexpr double kChebRatio = 40.0;
 static void mg_smoother(MgFcgArgs *a) {
     a->omega = 1.0f;
     a->sm_c2 = 0.0f;
@@ -1035,10 +1172,10 @@ static void mg_smoother(MgFcgArgs *a) {
 }
 
 template <int KIND>
-static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h) {
-    const void *fn = (const void *)mg_fcg_kernel<KIND>;
+static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h, bool dwords) {
+    const void *fn = dwords ? (const void *)mg_fcg_dw_kernel<KIND> : (const void *)mg_fcg_kernel<KIND>;
     int per_sm = 0;
-    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_fcg_kernel<KIND>, kMgThreads, 0));
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMgThreads, 0));
     if (per_sm < 1) { set_error("multigrid kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
     int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
     long long need = (c->nnodes + kMgThreads - 1) / kMgThreads;
@@ -1076,11 +1213,6 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
         a->Kds.hi[q] = h;
         a->Kds.lo[q] = (float)(c->Ke0_host[q] - (double)h);
     }
-    // PSF_MG_DS_OPERATOR=1 computes the FCG operator in double-single.  Measured on the
-    // 1M-dof MBB beam it is slower than native FP64 here (46.5 vs 52.1 SIMP iterations/s): the
-    // compensated sums form a dependent chain that 16 warps per SM cannot hide.
-    const char *dsop = getenv("PSF_MG_DS_OPERATOR");
-    a->ds = (dsop && *dsop == '1') ? 1 : 0;
     a->Ainv = H->Ac;
     a->nc = H->nc;
     mg_smoother(a);
@@ -1103,6 +1235,20 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     }
     if (warm) PSF_CUDA(cudaMemcpyAsync(a->x, c->un, sizeof(double) * c->ndofs, cudaMemcpyDeviceToDevice, c->stream));
     a->warm = warm ? 1 : 0;
+    // Krylov vectors in double words unless PSF_MG_FCG_F64=1 (FP64 vectors and operator)
+    const char *f64env = getenv("PSF_MG_FCG_F64");
+    const bool dwords = !(f64env && *f64env == '1');
+    if (dwords && !H->xw) {
+        const MgLev &L0 = H->L[0];
+        H->npad = (c->kind == PSF_H8_SOLID) ? (long long)(L0.nx + 2) * (L0.ny + 2) * (L0.nz + 2)
+                                            : (long long)(L0.nx + 2) * (L0.ny + 2);
+        PSF_CHECK(mg_alloc(H, c, (void **)&H->xw, sizeof(float2) * c->ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&H->rw, sizeof(float2) * c->ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&H->pw, sizeof(float2) * c->ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&H->qw, sizeof(float2) * c->ndofs));
+        PSF_CHECK(mg_alloc(H, c, (void **)&H->Ew, sizeof(float2) * H->npad));
+    }
+    a->xw = H->xw; a->rw = H->rw; a->pw = H->pw; a->qw = H->qw; a->Ew = H->Ew; a->npad = H->npad;
     int total = 0, cycles = 0, launches = 0;
     bool ok = false;
     double h[5] = {0, 0, 0, 0, 0};
@@ -1110,9 +1256,9 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     for (int pass = 0; pass < 3 && total < itmax; pass++) {
         a->itmax = itmax - total;
         switch (c->kind) {
-        case PSF_Q4_PLANE_STRAIN: st = mg_fcg_t<0>(c, *a, h); break;
-        case PSF_Q4_HEAT: st = mg_fcg_t<1>(c, *a, h); break;
-        default: st = mg_fcg_t<2>(c, *a, h); break;
+        case PSF_Q4_PLANE_STRAIN: st = mg_fcg_t<0>(c, *a, h, dwords); break;
+        case PSF_Q4_HEAT: st = mg_fcg_t<1>(c, *a, h, dwords); break;
+        default: st = mg_fcg_t<2>(c, *a, h, dwords); break;
         }
         if (st != PSF_OK) break;
         launches++;

@@ -54,49 +54,6 @@ __device__ __forceinline__ int out_of_range(double v) {
 
 __device__ __forceinline__ void dw_add_to(D &acc, D v) { acc = dw::add(acc, v); }
 
-// Block sums of NV double-word values: the warp levels in double words (FP32 pipes),
-// then the per-warp results in FP64 by warp 0, in a fixed order.  Result in thread 0.
-// (A warp tree in FP64 costs every lane five FP64 adds per value, which on GB300's
-// FP64 pipe rivals the element work.)
-template <int NV>
-__device__ __forceinline__ void dw_block_sum(D (&v)[NV], double (&out)[NV], double *smem) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const D t = dw::make(__shfl_xor_sync(0xffffffffu, v[k].h, o), __shfl_xor_sync(0xffffffffu, v[k].l, o));
-            v[k] = dw::add(v[k], t);
-        }
-    }
-    __syncthreads();
-    if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) smem[k * 32 + wid] = dw::to_double(v[k]);
-    }
-    __syncthreads();
-    if (wid == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) out[k] = warp_sum(lane < nw ? smem[k * 32 + lane] : 0.0);
-    }
-}
-
-// block maximum of double-word values, as a double in thread 0
-__device__ __forceinline__ double dw_block_max(D v, double *smem) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const D t = dw::make(__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o));
-        v = dw::max(v, t);
-    }
-    __syncthreads();
-    if (lane == 0) smem[wid] = dw::to_double(v);
-    __syncthreads();
-    double m = -INFINITY;
-    if (wid == 0) m = warp_max(lane < nw ? smem[lane] : -INFINITY);
-    return m;
-}
-
 template <bool kConlin>
 __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
     __shared__ double sm[32 * 4];
@@ -259,7 +216,7 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
         }
         D av[4] = {a0, a1, a2, a3};
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        dw_block_sum<4>(av, acc, sm);
+        dw::block_sum_dw<4>(av, acc, sm);
         if (!grid_sync<4, 0>(A.gs, A.partials, acc, 0.0)) return;
         if (lead) {
             const double SGG = gs_result(A.gs, 0), SGd = gs_result(A.gs, 1), Sg = gs_result(A.gs, 2),
@@ -312,7 +269,7 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
                                 dw::neg(dw::div(dw::mul(c101, di), ita)));
             txd = dw::max(txd, t);
         }
-        double tx = dw_block_max(txd, sm);
+        double tx = dw::block_max_dw(txd, sm);
         {
             double none[1] = {0.0};
             if (!grid_sync<0, 1>(A.gs, A.partials, none, tx)) return;
@@ -361,7 +318,7 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
             }
             D bv[2] = {b0, b1};
             double a2v[2] = {0.0, 0.0};
-            dw_block_sum<2>(bv, a2v, sm);
+            dw::block_sum_dw<2>(bv, a2v, sm);
             if (!grid_sync<2, 0>(A.gs, A.partials, a2v, 0.0)) return;
             if (lead) {
                 const double Sgt = gs_result(A.gs, 0), Skt = gs_result(A.gs, 1);
