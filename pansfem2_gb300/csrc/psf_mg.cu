@@ -110,10 +110,11 @@ __device__ __forceinline__ long long lelem(const MgLev &L, int i, int j, int k) 
     return KT<KIND>::is3d ? ((long long)L.ny * i + j) * L.nz + k : (long long)L.ny * i + j;
 }
 
-// y = (A_l v)(node) for the ndof dofs of node (i,j,k); level 0 uses E*Ke0, coarse levels their element matrices
-template <int KIND>
-__device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &Ke, const float *__restrict__ v, int i,
-                                           int j, int k, float *y) {
+// y = (A_l v)(node) for the ndof dofs of node (i,j,k); level 0 uses E*Ke0, coarse levels their
+// element matrices.  The vector is read through ld(m, mi, mj, mk, b): node m = (mi, mj, mk), dof b.
+template <int KIND, class LD>
+__device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF &Ke, LD ld, int i, int j, int k,
+                                             float *y) {
     using T = KT<KIND>;
 #pragma unroll
     for (int a = 0; a < T::nd; a++) y[a] = 0.f;
@@ -128,11 +129,12 @@ __device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &K
             for (int dj = -1; dj <= 1; dj++)
 #pragma unroll
                 for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++, slot++) {
-                    const long long m = lnode<KIND>(L, min(max(i + di, 0), L.nx), min(max(j + dj, 0), L.ny),
-                                                    T::is3d ? min(max(k + dk, 0), L.nz) : 0);
+                    const int mi = min(max(i + di, 0), L.nx), mj = min(max(j + dj, 0), L.ny),
+                              mk = T::is3d ? min(max(k + dk, 0), L.nz) : 0;
+                    const long long m = lnode<KIND>(L, mi, mj, mk);
                     float vb[T::nd];
 #pragma unroll
-                    for (int b = 0; b < T::nd; b++) vb[b] = v[m * T::nd + b];
+                    for (int b = 0; b < T::nd; b++) vb[b] = ld(m, mi, mj, mk, b);
 #pragma unroll
                     for (int a = 0; a < T::nd; a++)
 #pragma unroll
@@ -159,7 +161,7 @@ __device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &K
                               nk2 = T::is3d ? min(max(ek + qk, 0), L.nz) : 0;
                     const long long m = lnode<KIND>(L, ni, nj, nk2);
 #pragma unroll
-                    for (int b = 0; b < T::nd; b++) ue[q * T::nd + b] = v[m * T::nd + b];
+                    for (int b = 0; b < T::nd; b++) ue[q * T::nd + b] = ld(m, ni, nj, nk2, b);
                 }
                 if (lev == 0) {
                     const float Ee = L.Ep[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
@@ -184,6 +186,13 @@ __device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &K
                     }
                 }
             }
+}
+
+template <int KIND>
+__device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &Ke, const float *__restrict__ v, int i,
+                                           int j, int k, float *y) {
+    apply_node_f<KIND>(L, lev, Ke, [v](long long m, int, int, int, int b) { return v[m * KT<KIND>::nd + b]; }, i, j, k,
+                       y);
 }
 
 // interpolation weight of coarse corner q at fine position (fx, fy, fz) in {0, 1/2, 1}
@@ -432,7 +441,13 @@ struct MgFcgArgs {
     double *out;              // iterations, |r|^2, |b|^2, converged, V-cycles
     unsigned long long *trace;   // optional: [0] = count, then %globaltimer after each sync of one iteration
     int trace_iter;
-    // double-word Krylov vectors (mg_fcg_dw_kernel): x, r, p, q as FP32 pairs, padded moduli
+    // block 0's shared-memory levels: lsm (>= lsmall; nlev = none), byte offsets into dynamic
+    // shared memory of S, D, x, xt, b, r, fixed per level, of the coarsest inverse (-1 = global)
+    int lsm;
+    int nslot;                // stencil floats per node: 3^d slots x nd x nd
+    int smo[kMaxLev][7];
+    int smo_ainv;
+        // double-word Krylov vectors (mg_fcg_dw_kernel): x, r, p, q as FP32 pairs, padded moduli
     float2 *xw, *rw, *pw, *qw, *Ew;
     long long npad;           // padded moduli entries
 };
@@ -455,10 +470,11 @@ __device__ __forceinline__ void stamp(const MgFcgArgs &A, bool on) {
 //   second step: xout = xin + c2 (xin - xprev) + c3 (b - A xin) / D, xprev == nullptr meaning 0
 // (xout may alias xprev: every dof reads its own xprev before writing xout)
 template <int KIND>
-__device__ __forceinline__ void smooth_step(const MgFcgArgs &A, int l, const float *xin, const float *xprev,
-                                            float *xout, bool second, long long tid, long long stride) {
+__device__ __forceinline__ void smooth_step(const MgFcgArgs &A, const MgLev *LV, int l, const float *xin,
+                                            const float *xprev, float *xout, bool second, long long tid,
+                                            long long stride) {
     using T = KT<KIND>;
-    const MgLev &L = A.L[l];
+    const MgLev &L = LV[l];
     const float c2 = second ? A.sm_c2 : 0.f, c3 = second ? A.sm_c3 : A.omega;
     for (long long n = tid; n < L.nnodes; n += stride) {
         int i, j, k;
@@ -484,11 +500,12 @@ __device__ __forceinline__ bool phase_sync(const MgFcgArgs &A, bool grid) {
 
 // down-leg of level l: second pre-sweep, residual, restriction to level l+1 (and its first sweep)
 template <int KIND>
-__device__ bool down_level(const MgFcgArgs &A, int l, long long tid, long long stride, bool grid, bool tr) {
+__device__ bool down_level(const MgFcgArgs &A, const MgLev *LV, int l, long long tid, long long stride, bool grid,
+                           bool tr) {
     using T = KT<KIND>;
     const int nl = A.nlev;
-    const MgLev &L = A.L[l];
-    smooth_step<KIND>(A, l, L.x, nullptr, L.xt, true, tid, stride);    // second pre-smoothing step (x0 = 0)
+    const MgLev &L = LV[l];
+    smooth_step<KIND>(A, LV, l, L.x, nullptr, L.xt, true, tid, stride);   // second pre-smoothing step (x0 = 0)
     if (!phase_sync(A, grid)) return false;
     stamp(A, tr);
     for (long long n = tid; n < L.nnodes; n += stride) {              // residual r = b - A xt
@@ -504,7 +521,7 @@ __device__ bool down_level(const MgFcgArgs &A, int l, long long tid, long long s
     }
     if (!phase_sync(A, grid)) return false;
     stamp(A, tr);
-    const MgLev &Cc = A.L[l + 1];
+    const MgLev &Cc = LV[l + 1];
     for (long long n = tid; n < Cc.nnodes; n += stride) {             // restriction b_c = P^T r
         int i, j, k;
         lnode_ijk<KIND>(Cc, n, i, j, k);
@@ -535,13 +552,14 @@ __device__ bool down_level(const MgFcgArgs &A, int l, long long tid, long long s
 }
 
 // coarsest level: x = Ainv b (dense, FP64), one warp per row (the lanes read a row contiguously)
-__device__ __forceinline__ void coarsest_solve(const MgFcgArgs &A, long long tid, long long stride) {
-    const MgLev &Cc = A.L[A.nlev - 1];
+__device__ __forceinline__ void coarsest_solve(const MgFcgArgs &A, const MgLev *LV, const double *Ainv,
+                                               long long tid, long long stride) {
+    const MgLev &Cc = LV[A.nlev - 1];
     const int n = A.nc;
     const int lane = threadIdx.x & 31;
     for (long long q = tid >> 5; q < n; q += stride >> 5) {
         double acc = 0.0;
-        const double *row = A.Ainv + q * n;
+        const double *row = Ainv + q * n;
         for (int t = lane; t < n; t += 32) acc += row[t] * (double)Cc.b[t];
         acc = warp_sum(acc);
         if (lane == 0) Cc.x[q] = Cc.fixed[q] ? 0.f : (float)acc;
@@ -550,10 +568,11 @@ __device__ __forceinline__ void coarsest_solve(const MgFcgArgs &A, long long tid
 
 // up-leg of level l: x = xt + P x_c, two post-smoothing sweeps (result in x)
 template <int KIND>
-__device__ bool up_level(const MgFcgArgs &A, int l, long long tid, long long stride, bool grid, bool tr) {
+__device__ bool up_level(const MgFcgArgs &A, const MgLev *LV, int l, long long tid, long long stride, bool grid,
+                         bool tr) {
     using T = KT<KIND>;
-    const MgLev &L = A.L[l];
-    const MgLev &Cc = A.L[l + 1];
+    const MgLev &L = LV[l];
+    const MgLev &Cc = LV[l + 1];
     for (long long n = tid; n < L.nnodes; n += stride) {              // x = xt + P x_c
         int i, j, k;
         lnode_ijk<KIND>(L, n, i, j, k);
@@ -578,10 +597,10 @@ __device__ bool up_level(const MgFcgArgs &A, int l, long long tid, long long str
     }
     if (!phase_sync(A, grid)) return false;
     stamp(A, tr);
-    smooth_step<KIND>(A, l, L.x, nullptr, L.xt, false, tid, stride);   // post-smoothing, step 1
+    smooth_step<KIND>(A, LV, l, L.x, nullptr, L.xt, false, tid, stride);   // post-smoothing, step 1
     if (!phase_sync(A, grid)) return false;
     stamp(A, tr);
-    smooth_step<KIND>(A, l, L.xt, L.x, L.x, true, tid, stride);        // step 2 -> x
+    smooth_step<KIND>(A, LV, l, L.xt, L.x, L.x, true, tid, stride);        // step 2 -> x
     if (l > 0 || !grid) {
         if (!phase_sync(A, grid)) return false;
         stamp(A, tr);
@@ -596,22 +615,70 @@ __device__ bool up_level(const MgFcgArgs &A, int l, long long tid, long long str
 // Levels lsmall.. (a few thousand nodes and less) run in block 0 alone with
 // block barriers while the other blocks wait at one grid barrier: a grid
 // barrier costs microseconds, far more than those levels' work.
+// Block 0's view of the hierarchy (shared memory, filled by block0_levels): the levels
+// from A.lsm on have their stencils, diagonals, fixed flags and vectors in dynamic shared
+// memory, the coarsest inverse too.  They are constant during a solve and are read by
+// every phase of block 0's serial part of the cycle.
+struct Block0View {
+    MgLev L[kMaxLev];
+    const double *Ainv;
+};
+
+// Copies the shared-memory levels in (block 0 only; the other blocks return at once).
+__device__ void block0_levels(const MgFcgArgs &A, Block0View &V, unsigned char *dsm) {
+    if (blockIdx.x != 0) return;
+    if (threadIdx.x == 0) {
+        for (int l = 0; l < A.nlev; l++) {
+            V.L[l] = A.L[l];
+            if (l >= A.lsm) {
+                const int *o = A.smo[l];
+                V.L[l].S = (float *)(dsm + o[0]);
+                V.L[l].D = (float *)(dsm + o[1]);
+                V.L[l].x = (float *)(dsm + o[2]);
+                V.L[l].xt = (float *)(dsm + o[3]);
+                V.L[l].b = (float *)(dsm + o[4]);
+                V.L[l].r = (float *)(dsm + o[5]);
+                V.L[l].fixed = dsm + o[6];
+            }
+        }
+        V.Ainv = A.smo_ainv >= 0 ? (const double *)(dsm + A.smo_ainv) : A.Ainv;
+    }
+    for (int l = A.lsm; l < A.nlev; l++) {
+        const MgLev &G = A.L[l];
+        const int *o = A.smo[l];
+        const long long ns = (l > 0) ? G.nnodes * A.nslot : 0;   // stencil floats (levels >= 1)
+        float *S = (float *)(dsm + o[0]);
+        float *D = (float *)(dsm + o[1]);
+        unsigned char *F = dsm + o[6];
+        for (long long t = threadIdx.x; t < ns; t += blockDim.x) S[t] = G.S[t];
+        for (long long t = threadIdx.x; t < G.ndofs; t += blockDim.x) {
+            D[t] = G.D[t];
+            F[t] = G.fixed[t];
+        }
+    }
+    if (A.smo_ainv >= 0) {
+        double *Ai = (double *)(dsm + A.smo_ainv);
+        for (long long t = threadIdx.x; t < (long long)A.nc * A.nc; t += blockDim.x) Ai[t] = A.Ainv[t];
+    }
+    __syncthreads();
+}
+
 template <int KIND>
-__device__ bool vcycle(const MgFcgArgs &A, long long tid, long long stride, bool tr) {
+__device__ bool vcycle(const MgFcgArgs &A, const Block0View &V, long long tid, long long stride, bool tr) {
     const int nl = A.nlev, ls = A.lsmall;
     for (int l = 0; l < ls; l++)
-        if (!down_level<KIND>(A, l, tid, stride, true, tr)) return false;
+        if (!down_level<KIND>(A, A.L, l, tid, stride, true, tr)) return false;
     if (blockIdx.x == 0) {
         const long long bt = threadIdx.x, bs = blockDim.x;
-        for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, l, bt, bs, false, false);
-        coarsest_solve(A, bt, bs);
+        for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, V.L, l, bt, bs, false, false);
+        coarsest_solve(A, V.L, V.Ainv, bt, bs);
         __syncthreads();
-        for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, l, bt, bs, false, false);
+        for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, V.L, l, bt, bs, false, false);
     }
     if (!grid_barrier(A.gs, A.partials)) return false;
     stamp(A, tr);
     for (int l = ls - 1; l >= 0; l--)
-        if (!up_level<KIND>(A, l, tid, stride, true, tr)) return false;
+        if (!up_level<KIND>(A, A.L, l, tid, stride, true, tr)) return false;
     return true;
 }
 
@@ -675,14 +742,12 @@ constexpr int kMgThreads = 512;   // one block per SM: half the barrier arrivals
 // low-order products of K0 = Kh + Kl and v = vh + vl folded into the correction), then
 // scaled by E_e and summed over the node's elements in double words.  Returns the partial
 // v.q of the node in double words.  Nothing here runs on the FP64 pipe.
-template <int KIND>
-__device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *__restrict__ v, long long n,
-                                              float2 *__restrict__ out) {
+template <int KIND, class LD>
+__device__ __forceinline__ void applydw_core(const MgFcgArgs &A, LD vload, long long n, dw::D *y) {
     using T = KT<KIND>;
     const MgLev &L = A.L[0];
     int i, j, k;
     lnode_ijk<KIND>(L, n, i, j, k);
-    dw::D y[T::nd];
 #pragma unroll
     for (int a = 0; a < T::nd; a++) y[a] = dw::from_float(0.f);
 #pragma unroll
@@ -707,7 +772,7 @@ __device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *
                                                     T::is3d ? min(max(ek + qk, 0), L.nz) : 0);
 #pragma unroll
                     for (int b = 0; b < T::nd; b++) {
-                        const float2 u = v[m * T::nd + b];
+                        const float2 u = vload(m * T::nd + b);
                         const int l = q * T::nd + b;
 #pragma unroll
                         for (int a = 0; a < T::nd; a++) {
@@ -727,6 +792,15 @@ __device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *
                     y[a] = dw::add(y[a], dw::mul(Ed, dw::make(sh, sl)));
                 }
             }
+}
+
+template <int KIND>
+__device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *__restrict__ v, long long n,
+                                              float2 *__restrict__ out) {
+    using T = KT<KIND>;
+    const MgLev &L = A.L[0];
+    dw::D y[T::nd];
+    applydw_core<KIND>(A, [v](long long t) { return v[t]; }, n, y);
     dw::D d = dw::from_float(0.f);
 #pragma unroll
     for (int a = 0; a < T::nd; a++) {
@@ -743,6 +817,9 @@ template <int KIND>
 __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
     using T = KT<KIND>;
     __shared__ double sm[32 * 4];
+    __shared__ Block0View B0;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    block0_levels(A, B0, dsm);
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const MgLev &L0 = A.L[0];
@@ -800,7 +877,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
         stamp(A, tr);
         if (!grid_barrier(A.gs, A.partials)) return;
         stamp(A, tr);
-        if (!vcycle<KIND>(A, tid, stride, tr)) return;
+        if (!vcycle<KIND>(A, B0, tid, stride, tr)) return;
         cycles++;
         // ---- z = |r| V(r/|r|); z.q_prev, z.r, p_prev.r
         double a3[3] = {0.0, 0.0, 0.0};
@@ -880,6 +957,9 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
     using T = KT<KIND>;
     using dw::D;
     __shared__ double sm[32 * 4];
+    __shared__ Block0View B0;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    block0_levels(A, B0, dsm);
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const MgLev &L0 = A.L[0];
@@ -931,7 +1011,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
         stamp(A, tr);
         if (!grid_barrier(A.gs, A.partials)) return;
         stamp(A, tr);
-        if (!vcycle<KIND>(A, tid, stride, tr)) return;
+        if (!vcycle<KIND>(A, B0, tid, stride, tr)) return;
         cycles++;
         // ---- z = |r| V(r/|r|) (own dofs of L0.x); z.q_prev, z.r, p_prev.r
         const D rnD = dw::from_double(rn);
@@ -1018,6 +1098,9 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_apply_kernel(MgFcgArgs A, co
     using T = KT<KIND>;
     if (flags && *(volatile const int *)flags) return;
     __shared__ double sm[32 * 4];
+    __shared__ Block0View B0;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    block0_levels(A, B0, dsm);
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const MgLev &L0 = A.L[0];
@@ -1044,7 +1127,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_apply_kernel(MgFcgArgs A, co
             L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
         }
     if (!grid_barrier(A.gs, A.partials)) return;
-    if (!vcycle<KIND>(A, tid, stride, false)) return;
+    if (!vcycle<KIND>(A, B0, tid, stride, false)) return;
     for (long long t = tid; t < L0.ndofs; t += stride) xo[t] = L0.fixed[t] ? 0.0f : (float)(rn * (double)L0.x[t]);
 }
 
@@ -1056,6 +1139,48 @@ static int mg_small_level(const MgHier *H) {
     for (int l = 1; l < H->nlev - 1; l++)
         if (H->L[l].nnodes <= kSmallLevelNodes) return l;
     return H->nlev - 1;
+}
+
+constexpr size_t kMaxDynSmem = 200 * 1024;   // the MG kernels' dynamic shared memory limit (set once per setup)
+
+// Block 0's shared-memory levels: from the coarsest level up, as many whole levels below
+// lsmall (the interface level the grid phases write and read stays global) and the
+// coarsest inverse as fit in PSF_MG_SMEM_KB (default 160) KB of dynamic shared memory.
+// Fills a->lsm, a->smo, a->smo_ainv; returns the bytes.
+static size_t mg_block0_layout(const Ctx *c, const MgHier *H, MgFcgArgs *a) {
+    const int nd = c->ndof;
+    a->nslot = (c->kind == PSF_H8_SOLID ? 27 : 9) * nd * nd;
+    const char *e = getenv("PSF_MG_SMEM_KB");
+    size_t budget = (size_t)(e ? atof(e) : 160.0) * 1024;
+    if (budget > kMaxDynSmem) budget = kMaxDynSmem;
+    auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
+    auto level_bytes = [&](int l) {
+        const MgLev &L = H->L[l];
+        return al((size_t)L.nnodes * a->nslot * 4) + 5 * al((size_t)L.ndofs * 4) + al((size_t)L.ndofs);
+    };
+    const size_t ainv = al((size_t)H->nc * H->nc * 8);
+    a->lsm = H->nlev;
+    a->smo_ainv = -1;
+    size_t total = ainv;
+    if (total > budget) return 0;
+    int lsm = H->nlev;
+    // level lsmall itself stays in global memory: the grid phases write and read it
+    for (int l = H->nlev - 1; l > a->lsmall; l--) {
+        if (total + level_bytes(l) > budget) break;
+        total += level_bytes(l);
+        lsm = l;
+    }
+    size_t off = 0;
+    a->smo_ainv = (int)off;
+    off += ainv;
+    for (int l = lsm; l < H->nlev; l++) {
+        const MgLev &L = H->L[l];
+        a->smo[l][0] = (int)off; off += al((size_t)L.nnodes * a->nslot * 4);
+        for (int k = 1; k <= 5; k++) { a->smo[l][k] = (int)off; off += al((size_t)L.ndofs * 4); }
+        a->smo[l][6] = (int)off; off += al((size_t)L.ndofs);
+    }
+    a->lsm = lsm;
+    return off;
 }
 
 static psf_status mg_alloc(MgHier *H, Ctx *c, void **p, size_t bytes) {
@@ -1130,6 +1255,14 @@ static psf_status mg_setup_t(Ctx *c, MgHier *H) {
     dense_fix_identity<<<grid_for(n, 128), 128, 0, c->stream>>>(H->Ac, Lc.fixed, n);
     gauss_jordan_kernel<<<1, 1024, 0, c->stream>>>(H->Ac, n);
     PSF_CUDA(cudaGetLastError());
+    // the solver kernels may use up to kMaxDynSmem of dynamic shared memory (block 0's levels);
+    // set here, outside any stream capture of their launches
+    PSF_CUDA(cudaFuncSetAttribute((const void *)mg_fcg_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kMaxDynSmem));
+    PSF_CUDA(cudaFuncSetAttribute((const void *)mg_fcg_dw_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kMaxDynSmem));
+    PSF_CUDA(cudaFuncSetAttribute((const void *)mg_apply_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kMaxDynSmem));
     return PSF_OK;
 }
 
@@ -1172,10 +1305,10 @@ static void mg_smoother(MgFcgArgs *a) {
 }
 
 template <int KIND>
-static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h, bool dwords) {
+static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h, bool dwords, size_t smem) {
     const void *fn = dwords ? (const void *)mg_fcg_dw_kernel<KIND> : (const void *)mg_fcg_kernel<KIND>;
     int per_sm = 0;
-    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMgThreads, 0));
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMgThreads, smem));
     if (per_sm < 1) { set_error("multigrid kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
     int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
     long long need = (c->nnodes + kMgThreads - 1) / kMgThreads;
@@ -1183,7 +1316,7 @@ static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h, bool dwords) {
     if (blocks < 1) blocks = 1;
     void *args[] = {&a};
     PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
-    PSF_CHECK(launch_coop(c, fn, blocks, kMgThreads, args));
+    PSF_CHECK(launch_coop(c, fn, blocks, kMgThreads, args, smem));
     PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
     PSF_CHECK(read_sync_status(c));
     PSF_CHECK(add_kernel_time(c));
@@ -1249,6 +1382,7 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
         PSF_CHECK(mg_alloc(H, c, (void **)&H->Ew, sizeof(float2) * H->npad));
     }
     a->xw = H->xw; a->rw = H->rw; a->pw = H->pw; a->qw = H->qw; a->Ew = H->Ew; a->npad = H->npad;
+    const size_t smem = mg_block0_layout(c, H, a);
     int total = 0, cycles = 0, launches = 0;
     bool ok = false;
     double h[5] = {0, 0, 0, 0, 0};
@@ -1256,9 +1390,9 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     for (int pass = 0; pass < 3 && total < itmax; pass++) {
         a->itmax = itmax - total;
         switch (c->kind) {
-        case PSF_Q4_PLANE_STRAIN: st = mg_fcg_t<0>(c, *a, h, dwords); break;
-        case PSF_Q4_HEAT: st = mg_fcg_t<1>(c, *a, h, dwords); break;
-        default: st = mg_fcg_t<2>(c, *a, h, dwords); break;
+        case PSF_Q4_PLANE_STRAIN: st = mg_fcg_t<0>(c, *a, h, dwords, smem); break;
+        case PSF_Q4_HEAT: st = mg_fcg_t<1>(c, *a, h, dwords, smem); break;
+        default: st = mg_fcg_t<2>(c, *a, h, dwords, smem); break;
         }
         if (st != PSF_OK) break;
         launches++;
@@ -1321,6 +1455,7 @@ static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, con
     a->Ainv = H->Ac;
     a->nc = H->nc;
     mg_smoother(a);
+    const size_t smem = mg_block0_layout(c, H, a);
     a->Ep64 = c->Epad;
     a->gs = c->gs;
     a->partials = c->partials;
@@ -1328,7 +1463,7 @@ static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, con
     a->trace_iter = -1;
     int per_sm = 0;
     psf_status st = cuda_status(
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_apply_kernel<KIND>, kMgThreads, 0), "occupancy");
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_apply_kernel<KIND>, kMgThreads, smem), "occupancy");
     if (st == PSF_OK && per_sm < 1) {
         set_error("multigrid apply kernel does not fit on an SM");
         st = PSF_CUDA_ERROR;
@@ -1339,7 +1474,7 @@ static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, con
         if (blocks > need) blocks = (int)need;
         if (blocks < 1) blocks = 1;
         void *args[] = {a, (void *)&r, (void *)&r32, (void *)&xo, (void *)&flags};
-        st = launch_coop(c, (const void *)mg_apply_kernel<KIND>, blocks, kMgThreads, args);
+        st = launch_coop(c, (const void *)mg_apply_kernel<KIND>, blocks, kMgThreads, args, smem);
     }
     delete a;
     return st;

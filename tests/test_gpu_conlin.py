@@ -154,3 +154,32 @@ def test_conlin_mbb_30_iterations_match_oracle(gpu):
     assert rel.max() < 1e-5, (int(rel.argmax()), rel.max())
     assert np.max(np.abs(s - ref["s_final"])) < 1e-4
     assert fs[-1] < 0.5 * fs[0]   # the design improves
+
+
+@pytest.mark.parametrize("optimizer", [1, 2])
+def test_double_word_update_matches_fp64_kernel_at_full_size(gpu, optimizer, monkeypatch):
+    """At the benchmark size (524,288 design variables) one MMA / CONLIN update with the
+    double-word kernel against the FP64 kernel on the same inputs: the designs agree to
+    1e-7 max-abs (the interior point stops at eps = 1e-7; the two differ in rounding only)."""
+    pr = PB.mbb_q4(1024, 512, optimizer=optimizer)
+    ne = PB.counts(pr)[0]
+    rng = np.random.default_rng(21)
+    x = rng.uniform(0.05, 0.95, ne)
+    dfdx = -rng.uniform(0.1, 2.0, ne) * (1.0 - 1.5 * (rng.random(ne) < 0.1))
+    dgdx = np.full(ne, 1.0 / (pr["vf"] * ne))
+    g = float(np.sum(x) / (pr["vf"] * ne) - 1.0)
+    out = {}
+    for arith in ("double_word", "fp64"):
+        if arith == "fp64":
+            monkeypatch.setenv("PSF_OPT_F64", "1")
+        with gpu.Problem(pr) as P:
+            if optimizer == 1:
+                P.mma_init()
+                out[arith] = P.mma_update(x, 10.0, dfdx, g, dgdx)
+            else:
+                P.conlin_init()
+                out[arith] = P.conlin_update(x, 10.0, dfdx, g, dgdx)
+    (xd, nd), (xf, nf) = out["double_word"], out["fp64"]
+    assert abs(nd - nf) <= 2, (nd, nf)
+    assert np.max(np.abs(xd - xf)) < 1e-7
+    assert np.all(xd >= pr["mma_xmin"]) and np.all(xd <= pr["mma_xmax"])
