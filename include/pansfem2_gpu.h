@@ -35,7 +35,8 @@ typedef enum {
 typedef enum {
     PSF_Q4_PLANE_STRAIN = 0, /* PlaneStrainStiffness<ShapeFunction4Square, Gauss4Square> (PlaneStrain.h:20-58) */
     PSF_Q4_HEAT = 1,         /* HeatTransfer<ShapeFunction4Square, Gauss4Square> (HeatTransfer.h:19-43) */
-    PSF_H8_SOLID = 2         /* SolidLinearIsotropicElastic<ShapeFunction8Cubic, Gauss8Cubic> (Solid.h:20-64) */
+    PSF_H8_SOLID = 2,        /* SolidLinearIsotropicElastic<ShapeFunction8Cubic, Gauss8Cubic> (Solid.h:20-64) */
+    PSF_T3_PLANE_STRAIN = 3  /* PlaneStrainStiffness<ShapeFunction3Triangle, Gauss1Triangle> (explicit meshes only) */
 } psf_element_kind;
 
 typedef enum {
@@ -213,6 +214,42 @@ psf_status psf_device_ptr(psf_ctx *ctx, const char *name, void **ptr);
 
 /* Synchronise the context's stream. */
 psf_status psf_sync(psf_ctx *ctx);
+
+/* ---------------- explicit (unstructured) meshes ---------------- */
+/* The reference's general assembly path on a mesh given as coordinates + connectivity
+ * (ImportFromCSV.h:23-101 meshes; sample/planestrain/sample_planestrain.cpp:20-77), on the
+ * device and bit for bit the reference's results:
+ *   element matrices  PlaneStrainStiffness<ShapeFunction3Triangle, Gauss1Triangle> (T3),
+ *                     <ShapeFunction4Square, Gauss4Square> (Q4), HeatTransfer (Q4),
+ *                     SolidLinearIsotropicElastic (H8), each from its element's coordinates;
+ *   numbering         SetDirichlet + Renumbering (BoundaryCondition.h:19-25, Assembling.h:175-186);
+ *   system            Assembling into LILCSR + CSR(LILCSR&) (Assembling.h:46-66, CSR.h:92-105):
+ *                     pattern incl. exact zeros, columns ascending, each entry summed in
+ *                     ascending element order; F -= Ke u_fixed likewise, then the point loads
+ *                     (Assembling.h:151-158);
+ *   solve             ScalingCG (CG.h:419-453) or CG (CG.h:123-154) on that CSR;
+ *   reaction          r = sum_e Ke_e u_e over all dofs (sample_planestrain.cpp:66-77).
+ * coords: nnodes x 2 (3 for H8); conn: nelem x nen (3 T3, 4 Q4, 8 H8), node ids in [0, nnodes).
+ * Element body / surface loads are not modelled: point loads and prescribed values only. */
+typedef struct psf_fem psf_fem;
+psf_status psf_fem_create(int kind, long long nnodes, const double *coords, long long nelem, int nen,
+                          const int32_t *conn, psf_fem **out);
+psf_status psf_fem_destroy(psf_fem *fem);
+/* Dirichlet dofs (node, dof) with prescribed values (NULL = 0); *nfree = free dofs. */
+psf_status psf_fem_set_dirichlet(psf_fem *fem, int n, const int32_t *node, const int32_t *dof,
+                                 const double *value, int *nfree);
+/* point loads, added to F after the element terms, in list order */
+psf_status psf_fem_set_loads(psf_fem *fem, int n, const int32_t *node, const int32_t *dof, const double *value);
+/* element matrices (modulus / conductivity E[e], Poisson ratio V, thickness t) and the CSR system */
+psf_status psf_fem_assemble(psf_fem *fem, const double *E, double V, double t, long long *nnz);
+/* host copies (optional pointers): n2g (nnodes x ndof, -1 fixed), indptr (nfree + 1), indices and
+ * data (nnz), F (nfree) */
+psf_status psf_fem_get_system(psf_fem *fem, int32_t *n2g, int32_t *indptr, int32_t *indices, double *data,
+                              double *F);
+/* solver: PSF_SOLVE_CSR_JACOBI_F64 (ScalingCG) or PSF_SOLVE_CSR_CG_F64 (CG); u_nodal (nnodes x ndof)
+ * receives the free values and the prescribed ones */
+psf_status psf_fem_solve(psf_fem *fem, int solver, int itmax, double eps, double *u_nodal, psf_solve_info *info);
+psf_status psf_fem_reaction(psf_fem *fem, const double *u_nodal, double *r_nodal);
 
 /* ---------------- entry points on the reference's general data structures ---------------- */
 /* CSR<T>::operator* (CSR.h:108-122) on host CSR arrays: indptr (n+1), indices and

@@ -231,6 +231,37 @@ void orc_ke_planestrain_q4(const double *X, double E, double V, double t, double
     }
 }
 
+/* PlaneStrain.h:20-58 with ShapeFunction3Triangle (ShapeFunction.h:87-117) and
+ * Gauss1Triangle (GaussIntegration.h:64-81): one point (1/3, 1/3), weights 1/sqrt(2) each */
+void orc_ke_planestrain_t3(const double *X, double E, double V, double t, double *Ke) {
+    double D[9] = {1.0 - V, V, 0.0, V, 1.0 - V, 0.0, 0.0, 0.0, 0.5 * (1.0 - 2.0 * V)};
+    double sc = E / ((1.0 - 2.0 * V) * (1.0 + V));
+    for (int k = 0; k < 9; k++) D[k] *= sc;
+    memset(Ke, 0, 36 * sizeof(double));
+    const double dN[6] = {1.0, 0.0, -1.0, 0.0, 1.0, -1.0};
+    const double w = 1.0 / sqrt(2.0);
+    double dXdr[4], inv[4], dNdX[6], B[18], Bt[18], BtD[18], K[36];
+    mm(dN, X, dXdr, 2, 3, 2);
+    double J = det2(dXdr);
+    inverse(dXdr, 2, inv);
+    mm(inv, dN, dNdX, 2, 2, 3);
+    for (int n = 0; n < 3; n++) {
+        B[0 * 6 + 2 * n] = dNdX[0 * 3 + n]; B[0 * 6 + 2 * n + 1] = 0.0;
+        B[1 * 6 + 2 * n] = 0.0;             B[1 * 6 + 2 * n + 1] = dNdX[1 * 3 + n];
+        B[2 * 6 + 2 * n] = dNdX[1 * 3 + n]; B[2 * 6 + 2 * n + 1] = dNdX[0 * 3 + n];
+    }
+    transpose(B, Bt, 3, 6);
+    mm(Bt, D, BtD, 6, 3, 3);
+    mm(BtD, B, K, 6, 3, 6);
+    for (int k = 0; k < 36; k++) {
+        double v = K[k] * J;
+        v = v * t;
+        v = v * w;
+        v = v * w;
+        Ke[k] += v;
+    }
+}
+
 /* HeatTransfer.h:19-43: Ke = sum_g B^T B J alpha t w0 w1, B = dXdr^-1 dNdr */
 void orc_ke_heat_q4(const double *X, double alpha, double t, double *Ke) {
     memset(Ke, 0, 16 * sizeof(double));
@@ -306,6 +337,7 @@ void orc_kind_shape(int kind, int *nen, int *ndof, int *dim) {
     switch (kind) {
     case ORC_Q4_PLANE_STRAIN: *nen = 4; *ndof = 2; *dim = 2; break;
     case ORC_Q4_HEAT: *nen = 4; *ndof = 1; *dim = 2; break;
+    case ORC_T3_PLANE_STRAIN: *nen = 3; *ndof = 2; *dim = 2; break;
     default: *nen = 8; *ndof = 3; *dim = 3; break;
     }
 }
@@ -313,6 +345,7 @@ void orc_kind_shape(int kind, int *nen, int *ndof, int *dim) {
 void orc_ke(int kind, const double *X, double E, double V, double t, double *Ke) {
     if (kind == ORC_Q4_PLANE_STRAIN) orc_ke_planestrain_q4(X, E, V, t, Ke);
     else if (kind == ORC_Q4_HEAT) orc_ke_heat_q4(X, E, t, Ke);
+    else if (kind == ORC_T3_PLANE_STRAIN) orc_ke_planestrain_t3(X, E, V, t, Ke);
     else orc_ke_solid_h8(X, E, V, Ke);
 }
 

@@ -19,7 +19,7 @@ extern "C" {
 #endif
 
 /* element kinds (shared numbering with the GPU library) */
-enum { ORC_Q4_PLANE_STRAIN = 0, ORC_Q4_HEAT = 1, ORC_H8_SOLID = 2 };
+enum { ORC_Q4_PLANE_STRAIN = 0, ORC_Q4_HEAT = 1, ORC_H8_SOLID = 2, ORC_T3_PLANE_STRAIN = 3 };
 
 /* ---------------- mesh: src/PrePost/Mesher/SquareMesh.h:61-106 ---------------- */
 void orc_q4_nodes(double lx, double ly, int nx, int ny, double *xy);
@@ -35,6 +35,7 @@ int orc_renumber(int nnodes, int ndof, const unsigned char *fixed, int *n2g);
 /* PlaneStrainStiffness<ShapeFunction4Square, Gauss4Square>  (src/FEM/Equation/PlaneStrain.h:20-58) */
 void orc_ke_planestrain_q4(const double *X, double E, double V, double t, double *Ke);
 /* HeatTransfer<ShapeFunction4Square, Gauss4Square>  (src/FEM/Equation/HeatTransfer.h:19-43) */
+void orc_ke_planestrain_t3(const double *X, double E, double V, double t, double *Ke);   /* T3, Gauss1Triangle */
 void orc_ke_heat_q4(const double *X, double alpha, double t, double *Ke);
 /* SolidLinearIsotropicElastic<ShapeFunction8Cubic, Gauss8Cubic>  (src/FEM/Equation/Solid.h:20-64) */
 void orc_ke_solid_h8(const double *X, double E, double V, double *Ke);

@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _LIBS = {}
 
 Q4_PLANE_STRAIN, Q4_HEAT, H8_SOLID = 0, 1, 2
-_SHAPE = {Q4_PLANE_STRAIN: (4, 2, 2), Q4_HEAT: (4, 1, 2), H8_SOLID: (8, 3, 3)}
+T3_PLANE_STRAIN = 3
+_SHAPE = {Q4_PLANE_STRAIN: (4, 2, 2), Q4_HEAT: (4, 1, 2), H8_SOLID: (8, 3, 3), T3_PLANE_STRAIN: (3, 2, 2)}
 
 dp = C.POINTER(C.c_double)
 ip = C.POINTER(C.c_int)
@@ -114,15 +115,17 @@ def ke(kind, X, E, V=0.3, t=1.0):
     return out.reshape(nen * ndof, nen * ndof)
 
 
-def assemble(kind, conn, coords, E_e, n2g, N, V=0.3, t=1.0):
-    """Returns (indptr, indices, data, F) of the free x free system."""
+def assemble(kind, conn, coords, E_e, n2g, N, V=0.3, t=1.0, ufixed=None):
+    """Returns (indptr, indices, data, F) of the free x free system.  ufixed: nodal prescribed
+    values (nnodes x ndof, used on the fixed dofs: F -= Ke u_fixed as Assembling.h:59-61)."""
     conn, coords, E_e, n2g = i32(conn).reshape(-1), f64(coords).reshape(-1), f64(E_e), i32(n2g)
+    uf = None if ufixed is None else f64(ufixed).reshape(-1)
     ne = E_e.shape[0]
     A = CSR()
     F = np.zeros(N)
     L = _lib()
     L.orc_assemble(kind, ne, P(conn, ip), P(coords), P(E_e), C.c_double(V), C.c_double(t),
-                   P(n2g, ip), None, N, C.byref(A), P(F))
+                   P(n2g, ip), None if uf is None else P(uf), N, C.byref(A), P(F))
     out = A.arrays()
     L.orc_csr_free(C.byref(A))
     return out + (F,)

@@ -390,6 +390,97 @@ static int run_conlin() {
     return 0;
 }
 
+// ------------------------------- explicit meshes -------------------------------
+// mesh=<file>: "kind nnodes nelem nen", coordinates, connectivity, E per element, "V t",
+// "nfix" + (node dof value) lines, "nload" + (node dof value) lines.  The call sequence of
+// sample/planestrain/sample_planestrain.cpp:26-77 (SetDirichlet, Renumbering, element loop
+// with Assembling, point loads, CSR, the solve, Disassembling, the reaction by
+// RemoveBoundaryConditions + Renumbering + Assembling of Ke*ElementVector) with ScalingCG
+// (solver=cg: CG, as that sample uses) to cg_eps.
+static void fem_element(int kind, Matrix<double>& Ke, std::vector<std::vector<std::pair<int, int> > >& n2e,
+                        const std::vector<int>& el, std::vector<Vector<double> >& x, double E, double V, double t) {
+    if (kind == 0) PlaneStrainStiffness<double, ShapeFunction4Square, Gauss4Square>(Ke, n2e, el, {0, 1}, x, E, V, t);
+    else if (kind == 3) PlaneStrainStiffness<double, ShapeFunction3Triangle, Gauss1Triangle>(Ke, n2e, el, {0, 1}, x, E, V, t);
+    else if (kind == 1) HeatTransfer<double, ShapeFunction4Square, Gauss4Square>(Ke, n2e, el, {0}, x, E, t);
+    else SolidLinearIsotropicElastic<double, ShapeFunction8Cubic, Gauss8Cubic>(Ke, n2e, el, {0, 1, 2}, x, E, V);
+}
+
+static int run_fem() {
+    std::ifstream in(args("mesh", "mesh.txt"));
+    if (!in) { fprintf(stderr, "cannot read mesh\n"); return 2; }
+    int kind, nn, ne, nen;
+    in >> kind >> nn >> ne >> nen;
+    const int dim = kind == 2 ? 3 : 2, nd = kind == 1 ? 1 : dim;
+    std::vector<Vector<double> > x(nn, Vector<double>(dim));
+    for (int i = 0; i < nn; i++)
+        for (int d = 0; d < dim; d++) in >> x[i](d);
+    std::vector<std::vector<int> > elements(ne, std::vector<int>(nen));
+    for (int e = 0; e < ne; e++)
+        for (int q = 0; q < nen; q++) in >> elements[e][q];
+    std::vector<double> Ee(ne);
+    for (int e = 0; e < ne; e++) in >> Ee[e];
+    double V, t;
+    in >> V >> t;
+    int nfix, nload;
+    BCList ufixed, qfixed;
+    in >> nfix;
+    for (int k = 0; k < nfix; k++) { int n, d; double v; in >> n >> d >> v; ufixed.push_back({{n, d}, v}); }
+    in >> nload;
+    for (int k = 0; k < nload; k++) { int n, d; double v; in >> n >> d >> v; qfixed.push_back({{n, d}, v}); }
+    std::vector<Vector<double> > u(nn, Vector<double>(nd)), r(nn, Vector<double>(nd));
+    std::vector<std::vector<int> > nodetoglobal(nn, std::vector<int>(nd, 0));
+    SetDirichlet(u, nodetoglobal, ufixed);
+    int KDEGREE = Renumbering(nodetoglobal);
+    LILCSR<double> K(KDEGREE, KDEGREE);
+    std::vector<double> F(KDEGREE, 0.0);
+    for (int e = 0; e < ne; e++) {
+        std::vector<std::vector<std::pair<int, int> > > n2e;
+        Matrix<double> Ke;
+        fem_element(kind, Ke, n2e, elements[e], x, Ee[e], V, t);
+        Assembling(K, F, u, Ke, nodetoglobal, n2e, elements[e]);
+    }
+    Assembling(F, qfixed, nodetoglobal);
+    CSR<double> Kmod(K);
+    Dump out(args("out", "ref.bin"));
+    std::vector<int> n2g;
+    for (auto& nd2 : nodetoglobal) n2g.insert(n2g.end(), nd2.begin(), nd2.end());
+    out.i("n2g", n2g);
+    out.i("indptr", Kmod.indptr);
+    out.i("indices", Kmod.indices);
+    out.d("data", Kmod.data);
+    out.d("F", F);
+    const double eps = argd("cg_eps", 1e-10);
+    std::vector<double> result = args("solver", "scaling_cg") == std::string("cg") ? CG(Kmod, F, 100000, eps)
+                                                                                  : ScalingCG(Kmod, F, 100000, eps);
+    Disassembling(u, result, nodetoglobal);
+    out.d("result", result);
+    RemoveBoundaryConditions(nodetoglobal);
+    KDEGREE = Renumbering(nodetoglobal);
+    std::vector<double> R(KDEGREE, 0.0);
+    for (int e = 0; e < ne; e++) {
+        std::vector<std::vector<std::pair<int, int> > > n2e;
+        Matrix<double> Ke;
+        fem_element(kind, Ke, n2e, elements[e], x, Ee[e], V, t);
+        Vector<double> Keue = Ke * ElementVector(u, n2e, elements[e]);
+        Assembling(R, Keue, nodetoglobal, n2e, elements[e]);
+    }
+    Disassembling(r, R, nodetoglobal);
+    std::vector<double> uh, rh;
+    for (auto& ui : u) for (int d = 0; d < nd; d++) uh.push_back(ui(d));
+    for (auto& ri : r) for (int d = 0; d < nd; d++) rh.push_back(ri(d));
+    out.d("u", uh);
+    out.d("r", rh);
+    {
+        std::vector<std::vector<std::pair<int, int> > > n2e;
+        Matrix<double> Ke;
+        fem_element(kind, Ke, n2e, elements[0], x, Ee[0], V, t);
+        std::vector<double> kv;
+        for (int a = 0; a < Ke.ROW(); a++) for (int b = 0; b < Ke.COL(); b++) kv.push_back(Ke(a, b));
+        out.d("Ke0", kv);
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) { fprintf(stderr, "usage: ref_driver <simp|...> key=value ...\n"); return 2; }
     for (int i = 2; i < argc; i++) {
@@ -400,6 +491,7 @@ int main(int argc, char** argv) {
     std::string mode = argv[1];
     if (mode == "simp") return run_simp();
     if (mode == "conlin") return run_conlin();
+    if (mode == "fem") return run_fem();
     fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

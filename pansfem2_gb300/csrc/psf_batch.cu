@@ -9,10 +9,11 @@
 // cluster barrier and every reduction is block-local or a fixed-order sum over
 // the team: no grid barrier, no atomics, deterministic.  Instances are launched
 // largest first.
-// The solve is flexible CG in FP64 (operator, dot products, recurrences) whose
-// preconditioner is one FP32 V(2,2) multigrid cycle per iteration: degree-2 Chebyshev on the l1-Jacobi
-// scaled operator (PSF_MG_CHEB as for the single-problem solver; <= 1 selects plain l1-Jacobi)
-// smoothing, Galerkin coarse operators built element by element inside the
+// The solve is flexible CG on double-word vectors (FP32 pairs: operator, dot products,
+// recurrences at ~1e-14 relative accuracy on the FP32 pipes; one SM's FP64 rate would bound
+// the largest instances) whose preconditioner is one FP32 V(2,2) multigrid cycle per
+// iteration: degree-2 Chebyshev smoothing on the l1-Jacobi scaled operator (PSF_MG_CHEB as
+// for the single-problem solver; <= 1 selects plain l1-Jacobi), Galerkin coarse operators built element by element inside the
 // block (P^T K P with bilinear P, fixed nodes masked), 9-point coarse stencils,
 // and a dense inverse of the coarsest level (<= 64 nodes) in shared memory.
 // The FP64 true residual decides convergence.
@@ -28,6 +29,7 @@
 #include <numeric>
 #include <vector>
 
+#include "psf_dw.cuh"
 #include "psf_internal.cuh"
 
 namespace psf {
@@ -56,8 +58,9 @@ struct Args {
     double *vw;              // volume weight of each design variable: sum over e in N(j) of w_ej / wsum_e
     double *Bp;              // per OC call: x_j (-dfdx_j / dgdx_j)^iota
     float *Ef;
-    // level-0 node arrays (FP64 Krylov vectors, loads, fixed flags)
-    double *x, *r, *z, *p, *q, *F;
+    float2 *Ew;              // E as double words (the Krylov operator)
+    // level-0 node arrays (Krylov vectors, loads, fixed flags)
+    double *x, *r, *p, *q, *F;   // r, p, q hold double words during a solve
     const unsigned char *fixed;
     // multigrid arrays
     float *Kel;              // 16 floats per coarse element
@@ -72,7 +75,7 @@ struct Args {
     int itmax, warm;
     double Ke0[16];
     float Ke0f[16];          // float part of Ke0 (the cycle uses it alone)
-    float Ke0lo[16];         // Ke0 - Ke0f: Ke0f + Ke0lo carries 48 bits (double-single operator)
+    float Ke0lo[16];         // Ke0 - Ke0f: Ke0f + Ke0lo carries 48 bits (double-word operator)
     // smoothing steps of the cycle: d0 = om D^-1 r0, d1 = c2 d0 + c3 D^-1 r1 (x += d each step);
     // degree-2 Chebyshev on [1/ratio, 1] of the l1-scaled operator, or l1-Jacobi (om = c3 = 1, c2 = 0)
     float sm_om, sm_c2, sm_c3;
@@ -185,46 +188,34 @@ __device__ __forceinline__ double op64(const Args &A, const Inst &I, const doubl
     return y;
 }
 
-// error-free transformations: TwoProduct with the FMA (Ogita, Rump, Oishi 2005), TwoSum (Knuth)
-__device__ __forceinline__ float ds_two_prod(float a, float b, float &e) {
-    const float p = a * b;
-    e = __fmaf_rn(a, b, -p);
-    return p;
-}
-__device__ __forceinline__ float ds_two_sum(float a, float b, float &e) {
-    const float s = __fadd_rn(a, b);
-    const float v = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
-    return s;
-}
-
-// the FCG operator row in double-single: each element's Ke0 x_e as a compensated dot
-// product of float pairs (about 1e-14 relative), E_e scaling and the node sum in FP64;
-// one SM's FP64 rate would otherwise bound the largest instances
-__device__ __forceinline__ double opds(const Args &A, const Inst &I, const double *xv, int i, int j) {
+// the FCG operator row on double words: vector and moduli as FP32 pairs, each element's
+// Ke0 x_e a compensated dot product (Dot2 with the low-order products folded in), the E_e
+// scaling and the node sum in double words; nothing on the FP64 pipe
+__device__ __forceinline__ dw::D opdw(const Args &A, const Inst &I, const float2 *xv, int i, int j) {
     const int n = I.n;
-    double y = 0.0;
+    dw::D y = dw::from_float(0.f);
 #pragma unroll
     for (int ci = 0; ci < 2; ci++)
 #pragma unroll
         for (int cj = 0; cj < 2; cj++) {
             const int ei = i - 1 + ci, ej = j - 1 + cj;
             if (ei < 0 || ej < 0 || ei >= n || ej >= n) continue;
-            const double Ee = A.E[I.e0 + (long long)n * ei + ej];
+            const float2 Ev = A.Ew[I.e0 + (long long)n * ei + ej];
             const int li = corner(1 - ci, 1 - cj);
             float ps = 0.0f, cs = 0.0f;
 #pragma unroll
             for (int lb = 0; lb < 4; lb++) {
                 const int bi = ei + (lb == 1 || lb == 2), bj = ej + (lb == 2 || lb == 3);
-                const double u = xv[(long long)(n + 1) * bi + bj];
-                const float uh = __double2float_rn(u), ul = __double2float_rn(u - (double)uh);
+                const float2 u = xv[(long long)(n + 1) * bi + bj];
                 const float kh = A.Ke0f[li * 4 + lb], kl = A.Ke0lo[li * 4 + lb];
                 float pe, se;
-                const float pr = ds_two_prod(kh, uh, pe);
-                ps = ds_two_sum(ps, pr, se);
-                cs += se + pe + __fmaf_rn(kh, ul, kl * uh);
+                const float pr = dw::two_prod(kh, u.x, pe);
+                ps = dw::two_sum(ps, pr, se);
+                cs += se + pe + __fmaf_rn(kh, u.y, kl * u.x);
             }
-            y += Ee * ((double)ps + (double)cs);
+            float sl;
+            const float sh = dw::fast_two_sum(ps, cs, sl);
+            y = dw::add(y, dw::mul(dw::make(Ev.x, Ev.y), dw::make(sh, sl)));
         }
     return y;
 }
@@ -556,13 +547,15 @@ __global__ void __launch_bounds__(kThreads) filter_moduli_batch(const __grid_con
         const double Ee = A.k0 * rp + A.kmin * (1.0 - rp);
         A.E[I.e0 + e] = Ee;
         A.Ef[I.e0 + e] = (float)Ee;
+        const dw::D Ed = dw::from_double(Ee);
+        A.Ew[I.e0 + e] = make_float2(Ed.h, Ed.l);
         vol += r;
     }
     vol = tsum(A, T, vol, sm, par);
     if (T.tid == 0) A.out[(long long)T.idx * kOut + O_G] = vol / (I.vf * (double)ne) - 1.0;
 }
 
-// flexible CG (FP64) with one FP32 V-cycle per iteration; FP64 true residual checks
+// flexible CG on double-word vectors with one FP32 V-cycle per iteration; FP64 true residual checks
 __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ Args A) {
     extern __shared__ double dyn[];
     double *sm = dyn;            // 32 doubles of reduction space, then the coarse inverse workspace
@@ -573,7 +566,13 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
     const int n = I.n;
     const long long tid = T.tid, nt = T.nt;
     const long long nn = (long long)(n + 1) * (n + 1);
-    double *x = A.x + I.v0, *r = A.r + I.v0, *z = A.z + I.v0, *p = A.p + I.v0, *q = A.q + I.v0;
+    double *x = A.x + I.v0;
+    // the Krylov vectors live in the FP64 arrays' memory as double words (FP32 pairs):
+    // x, r, p, q; the solution returns to FP64 (in place) for every true residual
+    float2 *X = (float2 *)(A.x + I.v0), *R = (float2 *)(A.r + I.v0), *P = (float2 *)(A.p + I.v0),
+           *Q = (float2 *)(A.q + I.v0);
+    auto ld = [](const float2 *a, long long t) { const float2 v = a[t]; return dw::make(v.x, v.y); };
+    auto st = [](float2 *a, long long t, dw::D v) { a[t] = make_float2(v.h, v.l); };
     const double *F = A.F + I.v0;
     const unsigned char *fx = A.fixed + I.v0;
     mg_setup(A, T, I, sm + 32);
@@ -582,7 +581,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
     double rr = 0.0, bb = 0.0;
     for (int pass = 0; pass < 3 && total < A.itmax && !conv; pass++) {
         passes++;
-        // r = F - K x (x = 0 on the first pass unless warm)
+        // r = F - K x in FP64 (x = 0 on the first pass unless warm), then x to double words
         double acc[2] = {0.0, 0.0};
         for (long long v = tid; v < nn; v += nt) {
             if (pass == 0 && !A.warm) x[v] = 0.0;
@@ -592,16 +591,18 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
             const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
             const double bv = fx[v] ? 0.0 : F[v];
             const double rv = fx[v] ? 0.0 : bv - op64(A, I, x, i, j);
-            r[v] = rv;
-            p[v] = 0.0;
-            q[v] = 0.0;
+            st(R, v, dw::from_double(rv));
+            st(P, v, dw::from_float(0.f));
+            st(Q, v, dw::from_float(0.f));
             acc[0] += rv * rv;
             acc[1] += bv * bv;
         }
         rr = tsum(A, T, acc[0], sm, par);
-        bb = tsum(A, T, acc[1], sm, par);
+        bb = tsum(A, T, acc[1], sm, par);   // a team barrier: every neighbour read of x is done
+        for (long long v = tid; v < nn; v += nt) st(X, v, dw::from_double(x[v]));   // in place, own entries
         if (bb == 0.0 || rr <= A.eps * A.eps * bb) {
             conv = true;
+            for (long long v = tid; v < nn; v += nt) x[v] = dw::to_double(ld(X, v));
             break;
         }
         double pq_prev = 1.0;
@@ -611,47 +612,56 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
             const double rn = sqrt(rr);
             const float sc = (float)(1.0 / rn);
             for (long long v = tid; v < nn; v += nt) {
-                const float bv = fx[v] ? 0.0f : (float)r[v] * sc;
+                const float2 rv = R[v];
+                const float bv = fx[v] ? 0.0f : rv.x * sc + rv.y * sc;
                 A.mb[I.mv[0] + v] = bv;
                 A.mx[I.mv[0] + v] = fx[v] ? 0.0f : bv / A.D[I.mv[0] + v];
             }
             tsync(T);
             vcycle(A, T, I);
-            double a3[3] = {0.0, 0.0, 0.0};
+            const dw::D rnD = dw::from_double(rn);
+            dw::D a3[3] = {dw::from_float(0.f), dw::from_float(0.f), dw::from_float(0.f)};
             for (long long v = tid; v < nn; v += nt) {
-                const double zv = fx[v] ? 0.0 : rn * (double)A.mx[I.mv[0] + v];
-                z[v] = zv;
-                a3[0] += zv * q[v];
-                a3[1] += zv * r[v];
-                a3[2] += p[v] * r[v];
+                const dw::D zv = fx[v] ? dw::from_float(0.f) : dw::mulf(rnD, A.mx[I.mv[0] + v]);
+                a3[0] = dw::add(a3[0], dw::mul(zv, ld(Q, v)));
+                a3[1] = dw::add(a3[1], dw::mul(zv, ld(R, v)));
+                a3[2] = dw::add(a3[2], dw::mul(ld(P, v), ld(R, v)));
             }
-            const double zq = tsum(A, T, a3[0], sm, par), zr = tsum(A, T, a3[1], sm, par), pr0 = tsum(A, T, a3[2], sm, par);
+            const double zq = tsum(A, T, dw::to_double(a3[0]), sm, par),
+                         zr = tsum(A, T, dw::to_double(a3[1]), sm, par),
+                         pr0 = tsum(A, T, dw::to_double(a3[2]), sm, par);
             const double beta = it > 0 ? zq / pq_prev : 0.0;
             const double pr = zr - beta * pr0;
-            for (long long v = tid; v < nn; v += nt) p[v] = z[v] - beta * p[v];
+            const dw::D betaD = dw::from_double(beta);
+            for (long long v = tid; v < nn; v += nt) {
+                const dw::D zv = fx[v] ? dw::from_float(0.f) : dw::mulf(rnD, A.mx[I.mv[0] + v]);
+                st(P, v, dw::sub(zv, dw::mul(betaD, ld(P, v))));
+            }
             tsync(T);
-            double pqa = 0.0;
+            dw::D pqa = dw::from_float(0.f);
             for (long long v = tid; v < nn; v += nt) {
                 const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
-                const double qv = fx[v] ? 0.0 : opds(A, I, p, i, j);
-                q[v] = qv;
-                pqa += p[v] * qv;
+                const dw::D qv = fx[v] ? dw::from_float(0.f) : opdw(A, I, P, i, j);
+                st(Q, v, qv);
+                pqa = dw::add(pqa, dw::mul(ld(P, v), qv));
             }
-            const double pq = tsum(A, T, pqa, sm, par);
+            const double pq = tsum(A, T, dw::to_double(pqa), sm, par);
             if (!(pq > 0.0)) break;
-            const double alpha = pr / pq;
-            double ra = 0.0;
+            const dw::D alphaD = dw::from_double(pr / pq);
+            dw::D ra = dw::from_float(0.f);
             for (long long v = tid; v < nn; v += nt) {
-                x[v] += alpha * p[v];
-                const double rv = r[v] - alpha * q[v];
-                r[v] = rv;
-                ra += rv * rv;
+                st(X, v, dw::add(ld(X, v), dw::mul(alphaD, ld(P, v))));
+                const dw::D rv = dw::sub(ld(R, v), dw::mul(alphaD, ld(Q, v)));
+                st(R, v, rv);
+                ra = dw::add(ra, dw::sq(rv));
             }
-            rr = tsum(A, T, ra, sm, par);
+            rr = tsum(A, T, dw::to_double(ra), sm, par);
             pq_prev = pq;
             if (rr <= A.eps * A.eps * bb || !isfinite(rr)) break;
         }
-        // FP64 true residual
+        // x back to FP64 (own entries), then the FP64 true residual
+        for (long long v = tid; v < nn; v += nt) x[v] = dw::to_double(ld(X, v));
+        tsync(T);
         double ta = 0.0;
         for (long long v = tid; v < nn; v += nt) {
             const int i = (int)(v / (n + 1)), j = (int)(v % (n + 1));
@@ -932,7 +942,8 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     for (double **pp : {&a.s, &a.rho, &a.E, &a.dfdrho, &a.dfds, &a.dgds, &a.snew, &a.wsum, &a.vw, &a.Bp})
         ck(balloc(b, pp, ne));
     ck(balloc(b, &a.Ef, ne));
-    for (double **pp : {&a.x, &a.r, &a.z, &a.p, &a.q, &a.F}) ck(balloc(b, pp, nv));
+    ck(balloc(b, &a.Ew, ne));
+    for (double **pp : {&a.x, &a.r, &a.p, &a.q, &a.F}) ck(balloc(b, pp, nv));
     ck(balloc(b, &dfixed, nv));
     ck(balloc(b, &a.Kel, mge * 16));
     ck(balloc(b, &a.St, mgn * 9));

@@ -109,6 +109,31 @@ __device__ void ke_planestrain(const double *X, double E, double V, double t, do
     }
 }
 
+// PlaneStrainStiffness<ShapeFunction3Triangle, Gauss1Triangle> (PlaneStrain.h:20-58 with
+// ShapeFunction.h:87-117 and GaussIntegration.h:64-81): one point (1/3, 1/3), weights 1/sqrt(2)
+__device__ void ke_planestrain_t3(const double *X, double E, double V, double t, double *Ke) {
+    double D[9] = {1.0 - V, V, 0.0, V, 1.0 - V, 0.0, 0.0, 0.0, 0.5 * (1.0 - 2.0 * V)};
+    const double sc = E / ((1.0 - 2.0 * V) * (1.0 + V));
+    for (int k = 0; k < 9; k++) D[k] *= sc;
+    const double dN[6] = {1.0, 0.0, -1.0, 0.0, 1.0, -1.0};   // dN/dr, constant
+    const double w = 1.0 / sqrt(2.0);
+    double J2[4], iv[4], dX[6], B[18], Bt[18], BtD[18], K[36];
+    mm(dN, X, J2, 2, 3, 2);
+    const double J = det2(J2);
+    inv_n(J2, 2, iv);
+    mm(iv, dN, dX, 2, 2, 3);
+    for (int n = 0; n < 3; n++) {
+        B[2 * n] = dX[n];          B[2 * n + 1] = 0.0;
+        B[6 + 2 * n] = 0.0;        B[6 + 2 * n + 1] = dX[3 + n];
+        B[12 + 2 * n] = dX[3 + n]; B[12 + 2 * n + 1] = dX[n];
+    }
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 3; j++) Bt[i * 3 + j] = B[j * 6 + i];
+    mm(Bt, D, BtD, 6, 3, 3);
+    mm(BtD, B, K, 6, 3, 6);
+    for (int k = 0; k < 36; k++) Ke[k] = 0.0 + K[k] * J * t * w * w;
+}
+
 // HeatTransfer (HeatTransfer.h:19-43)
 __device__ void ke_heat(const double *X, double alpha, double t, double *Ke) {
     for (int k = 0; k < 16; k++) Ke[k] = 0.0;
@@ -193,7 +218,40 @@ __global__ void ke_element0_kernel(int kind, int nx, int ny, int nz, double lx, 
     }
 }
 
+// one thread per element of an explicit mesh: Ke_e (nk x nk) from the element's own node
+// coordinates (coords: dim doubles per node), modulus E[e]
+__global__ void fem_ke_kernel(int kind, long long ne, int nen, const int *__restrict__ conn,
+                              const double *__restrict__ coords, const double *__restrict__ E, double V, double t,
+                              double *__restrict__ Ke) {
+    const int dim = kind == PSF_H8_SOLID ? 3 : 2;
+    const int nd = kind == PSF_Q4_HEAT ? 1 : dim;
+    const long long nk = (long long)nen * nd;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+        double X[24];
+        for (int q = 0; q < nen; q++)
+            for (int d = 0; d < dim; d++) X[q * dim + d] = coords[(long long)conn[e * nen + q] * dim + d];
+        double *K = Ke + e * nk * nk;
+        if (kind == PSF_H8_SOLID) {
+            double wk[1008];
+            ke_solid(X, E[e], V, K, wk);
+        } else if (kind == PSF_T3_PLANE_STRAIN) {
+            ke_planestrain_t3(X, E[e], V, t, K);
+        } else if (kind == PSF_Q4_PLANE_STRAIN) {
+            ke_planestrain(X, E[e], V, t, K);
+        } else {
+            ke_heat(X, E[e], t, K);
+        }
+    }
+}
+
 }  // namespace
+
+psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
+                                const double *E, double V, double t, double *Ke) {
+    fem_ke_kernel<<<grid_for(ne, 64, 65536), 64, 0, s>>>(kind, ne, nen, conn, coords, E, V, t, Ke);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
 
 psf_status ke_element0(Ctx *c, double E, double *Ke_dev) {
     double *wk = nullptr;

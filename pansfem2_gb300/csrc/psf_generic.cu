@@ -64,6 +64,9 @@ static psf_status generic_ctx(Ctx **out) {
     return PSF_OK;
 }
 
+// the same internal context for other translation units (explicit meshes, psf_fem.cu)
+psf_status generic_context(Ctx **out) { return generic_ctx(out); }
+
 static bool csr_ok(int n, const int32_t *indptr, const int32_t *indices, const double *data) {
     if (n < 0 || !indptr || (n > 0 && (!indices || !data))) return false;
     if (indptr[0] != 0) return false;

@@ -170,6 +170,9 @@ psf_status gather_reduced(Ctx *c, const double *nodal, double *red);   // psf_me
 psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_solve.cu
 psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward);               // psf_opt.cu
 psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho);
+psf_status generic_context(Ctx **out);   // psf_generic.cu: the process-wide internal context
+psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
+                                const double *E, double V, double t, double *Ke);   // psf_element.cu
 psf_status heaviside_back(Ctx *c, const double *d, double *out);                            // psf_opt.cu
 psf_status sensitivity_filter(Ctx *c, const double *s, const double *d, int mode, double *out);  // psf_opt.cu
 psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, double p, double scale0,

@@ -3,7 +3,7 @@
 Runs oracle/_ref/ref_driver (the reference headers compiled by
 oracle/build_ref.sh) on small SIMP problems and the reference's own test mains
 (src/LinearAlgebra/Solvers/test_CG.cpp, src/Optimize/Solver/test_MMA*.cpp), CONLIN on
-the optimiser test problems, and
+the optimiser test problems, the general assembly path on explicit meshes, and
 stores their outputs as compressed .npz / .txt fixtures.  Needs the reference
 source tree, so it runs only where that tree exists; the fixtures it writes
 are committed and used everywhere else.
@@ -68,6 +68,24 @@ def main():
     subprocess.run([os.path.join(REF, "ref_driver"), "simp", f"out={tmp}", "iters=1", "kind=0", "nx=12", "ny=6",
                     "bc=cantilever", f"vtk={vtk}"], check=True, stdout=subprocess.DEVNULL)
     print(f"{os.path.basename(vtk)}: {os.path.getsize(vtk)} bytes")
+    # explicit meshes (tests/golden/fem_meshes.py): the general assembly path of the reference
+    from tests.golden.fem_meshes import FEM_CASES, write_mesh  # noqa: E402
+    mesh = os.path.join(ROOT, "oracle", "_ref", "mesh.txt")
+    for name, mk in FEM_CASES.items():
+        case = mk()
+        write_mesh(case, mesh)
+        solver = "cg" if name == "fem_planestrain_sample" else "scaling_cg"   # the sample uses CG
+        subprocess.run([os.path.join(REF, "ref_driver"), "fem", f"mesh={mesh}", f"out={tmp}", f"solver={solver}"],
+                       check=True, stdout=subprocess.DEVNULL)
+        d = read_dump(tmp)
+        d.update(kind=np.array([case["kind"]], np.int32), coords=np.asarray(case["coords"], float),
+                 conn=np.asarray(case["conn"], np.int32), E=np.asarray(case["E"], float),
+                 Vt=np.array([case["V"], case["t"]]),
+                 fixed=np.array(case["fixed"], float).reshape(-1, 3), loads=np.array(case["loads"], float).reshape(-1, 3),
+                 solver=np.array([0 if solver == "scaling_cg" else 4], np.int32))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(f"{name}.npz")
+    os.remove(mesh)
     for pb, iters in CONLIN_PROBLEMS.items():
         subprocess.run([os.path.join(REF, "ref_driver"), "conlin", f"out={tmp}", f"problem={pb}", f"iters={iters}"],
                        check=True, stdout=subprocess.DEVNULL)

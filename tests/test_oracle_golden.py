@@ -200,3 +200,32 @@ def test_reference_test_CG():
     got = "".join("%g\n" % v for v in x)
     ref = open(O.os.path.join(O.os.path.dirname(__file__), "..", "tests", "golden", "ref_test_CG.txt")).read()
     assert got == ref
+
+
+FEM_NAMES = ["fem_planestrain_sample", "fem_q4_jitter", "fem_q4_heat_jitter", "fem_t3_jitter", "fem_h8_jitter"]
+
+
+@pytest.mark.parametrize("name", FEM_NAMES)
+def test_fem_explicit_mesh_assembly_bitexact(name):
+    """The general path on explicit meshes (permuted node ids, jittered coordinates, per-element
+    moduli, prescribed nonzero values): numbering, CSR pattern, values and F of the oracle
+    against the reference's SetDirichlet / Renumbering / Assembling / CSR(LILCSR&) run, bit for
+    bit; the element matrix of element 0 too (T3, Q4, Q4 heat, H8)."""
+    g = load(name)
+    kind = int(g["kind"][0])
+    nd = {0: 2, 1: 1, 2: 3, 3: 2}[kind]
+    nn = len(g["coords"])
+    fixed = np.zeros(nn * nd, np.uint8)
+    uf = np.zeros(nn * nd)
+    for n, d, v in g["fixed"]:
+        fixed[int(n) * nd + int(d)] = 1
+        uf[int(n) * nd + int(d)] = v
+    n2g, N = O.renumber(nn, nd, fixed)
+    V, t = g["Vt"]
+    ip, ix, dat, F = O.assemble(kind, g["conn"], g["coords"], g["E"], n2g, N, V, t, ufixed=uf)
+    L = g["loads"]
+    F = O.neumann(F, L[:, 0].astype(int), L[:, 1].astype(int), L[:, 2], nd, n2g)
+    for a, b in ((n2g, "n2g"), (ip, "indptr"), (ix, "indices"), (dat, "data"), (F, "F")):
+        assert same(g[b], a), b
+    X = g["coords"][g["conn"][0]]
+    assert same(g["Ke0"], O.ke(kind, X, g["E"][0], V, t))
