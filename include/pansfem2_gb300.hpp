@@ -13,12 +13,19 @@
 //   * Structured grids: Problem owns the device context of a SquareMesh-style
 //     grid (or its 3D analogue); the matrix-free and multigrid solvers and the
 //     whole-iteration driver SimpLoop work on it.
+//   * Explicit meshes: FemMesh takes the node and element lists the
+//     Import*FromCSV readers fill and replaces the element loop of
+//     Assembling calls; nodes are std::vector<T> rows (or any type built from
+//     one, such as the reference's Vector<T>).
 // Every call throws std::runtime_error with psf_last_error() on a device or
 // input error; nothing falls back to the CPU.
 #pragma once
 
 #include <algorithm>
 #include <cmath>
+#include <fstream>
+#include <iostream>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -403,6 +410,179 @@ public:
 
 private:
     Problem &p_;
+};
+
+// ------------------------------------------------------------------ CSV files (ImportFromCSV.h:22-253)
+// One header line, then whitespace-separated records, each split on ','; the first field is
+// an id.  Nodes and elements are numbered by their position in the file; in the condition
+// files the value fields are the dofs 0, 1, ... and "free" skips one.  Numbers go through
+// std::stod / std::stoi, which throw on a bad field, as in the reference.
+namespace detail {
+template <class Record>
+bool csv_records(const std::string &fname, const char *what, Record record) {
+    std::ifstream in(fname);
+    if (!in) {
+        std::cout << what << " file " << fname << " open error!" << std::endl;
+        return false;
+    }
+    std::string line;
+    std::getline(in, line);   // the header
+    std::string token;
+    while (in >> token) {
+        std::istringstream fields(token);
+        std::string id;
+        std::getline(fields, id, ',');
+        if (!id.empty()) record(id, fields);
+    }
+    return true;
+}
+inline bool csv_conditions(std::vector<std::pair<std::pair<int, int>, double> > &out, const std::string &fname) {
+    return csv_records(fname, "Dirichlet Condition", [&](const std::string &id, std::istringstream &fields) {
+        const int node = std::stoi(id);
+        std::string v;
+        for (int dof = 0; std::getline(fields, v, ','); dof++)
+            if (v != "free") out.push_back({{node, dof}, std::stod(v)});
+    });
+}
+}  // namespace detail
+
+// ImportNodesFromCSV (ImportFromCSV.h:22-58): coordinates in file order
+template <class Node>
+bool ImportNodesFromCSV(std::vector<Node> &nodes, std::string fname) {
+    return detail::csv_records(fname, "Node", [&](const std::string &, std::istringstream &fields) {
+        std::vector<double> x;
+        std::string v;
+        while (std::getline(fields, v, ',')) x.push_back(std::stod(v));
+        nodes.push_back(Node(x));
+    });
+}
+// ImportElementsFromCSV (ImportFromCSV.h:63-98)
+inline bool ImportElementsFromCSV(std::vector<std::vector<int> > &elements, std::string fname) {
+    return detail::csv_records(fname, "Element", [&](const std::string &, std::istringstream &fields) {
+        std::vector<int> el;
+        std::string v;
+        while (std::getline(fields, v, ',')) el.push_back(std::stoi(v));
+        elements.push_back(el);
+    });
+}
+// ImportDirichletFromCSV (ImportFromCSV.h:103-137): ((node, dof), value) in file order
+template <class T>
+bool ImportDirichletFromCSV(std::vector<std::pair<std::pair<int, int>, T> > &ufixed, std::string fname) {
+    return detail::csv_conditions(ufixed, fname);
+}
+// ImportNeumannFromCSV (ImportFromCSV.h:142-176); its open error names the Dirichlet file, as
+// the reference's does
+template <class T>
+bool ImportNeumannFromCSV(std::vector<std::pair<std::pair<int, int>, T> > &qfixed, std::string fname) {
+    return detail::csv_conditions(qfixed, fname);
+}
+// ImportInitialFromCSV (ImportFromCSV.h:181-216): u[node][dof] for the fields that are not
+// "free"; a missing field repeats the one before it, as a failed std::getline leaves it
+template <class Node>
+bool ImportInitialFromCSV(std::vector<Node> &u, std::string fname) {
+    return detail::csv_records(fname, "Initial Condition", [&](const std::string &id, std::istringstream &fields) {
+        const int node = std::stoi(id);
+        std::string v = id;
+        for (int dof = 0; dof < (int)u[node].size(); dof++) {
+            std::getline(fields, v, ',');
+            if (v != "free") u[node][dof] = std::stod(v);
+        }
+    });
+}
+// ImportPeriodicFromCSV (ImportFromCSV.h:221-253): (master, slave) pairs
+inline bool ImportPeriodicFromCSV(std::vector<std::pair<int, int> > &pairs, std::string fname) {
+    return detail::csv_records(fname, "Periodic Boundary Condition", [&](const std::string &id, std::istringstream &fields) {
+        std::string v = id;
+        std::getline(fields, v, ',');
+        pairs.push_back({std::stoi(id), std::stoi(v)});
+    });
+}
+
+// ------------------------------------------------------------------ explicit meshes
+// The general path of sample_planestrain.cpp / sample/solid/sample_linear.cpp on the device:
+// SetDirichlet + Renumbering, the element loop of stiffness routines and Assembling calls,
+// point loads, body forces and edge tractions, CSR(LILCSR&), ScalingCG / CG, Disassembling
+// and the reaction loop.  kind is a psf_element_kind (T3 / Q4 plane strain, Q4 heat, H8).
+class FemMesh {
+public:
+    template <class Node>
+    FemMesh(int kind, const std::vector<Node> &x, const std::vector<std::vector<int> > &elements) {
+        const int dim = kind == PSF_H8_SOLID ? 3 : 2;
+        std::vector<double> xs;
+        std::vector<int32_t> conn;
+        for (auto &xi : x)
+            for (int d = 0; d < dim; d++) xs.push_back(xi[d]);
+        const int nen = elements.empty() ? 0 : (int)elements[0].size();
+        for (auto &el : elements) {
+            if ((int)el.size() != nen) throw std::runtime_error("pansfem2_gb300: elements of different sizes");
+            conn.insert(conn.end(), el.begin(), el.end());
+        }
+        nnodes_ = (long long)x.size();
+        ne_ = (long long)elements.size();
+        ndof_ = kind == PSF_Q4_HEAT ? 1 : dim;
+        check(psf_fem_create(kind, nnodes_, xs.data(), ne_, nen, conn.data(), &fem_), false);
+    }
+    ~FemMesh() { psf_fem_destroy(fem_); }
+    FemMesh(const FemMesh &) = delete;
+    FemMesh &operator=(const FemMesh &) = delete;
+    long long nnodes() const { return nnodes_; }
+    int ndof() const { return ndof_; }
+
+    // SetDirichlet + Renumbering (BoundaryCondition.h:19-25, Assembling.h:175-186); returns KDEGREE
+    int SetDirichlet(const std::vector<std::pair<std::pair<int, int>, double> > &ufixed) {
+        std::vector<int32_t> n, d;
+        std::vector<double> v;
+        for (auto &u : ufixed) { n.push_back(u.first.first); d.push_back(u.first.second); v.push_back(u.second); }
+        int nf = 0;
+        check(psf_fem_set_dirichlet(fem_, (int)n.size(), n.data(), d.data(), v.data(), &nf), false);
+        return nf;
+    }
+    // Assembling(F, qfixed, nodetoglobal) (Assembling.h:151-158)
+    void SetLoads(const std::vector<std::pair<std::pair<int, int>, double> > &qfixed) {
+        std::vector<int32_t> n, d;
+        std::vector<double> v;
+        for (auto &q : qfixed) { n.push_back(q.first.first); d.push_back(q.first.second); v.push_back(q.second); }
+        check(psf_fem_set_loads(fem_, (int)n.size(), n.data(), d.data(), v.data()), false);
+    }
+    // PlaneStrainBodyForce (PlaneStrain.h:503-534) with a uniform f in the element loop
+    void SetBodyForce(double fx, double fy) { check(psf_fem_set_body_force(fem_, fx, fy), false); }
+    // PlaneStrainSurfaceForce<ShapeFunction2Line, Gauss1Line> (PlaneStrain.h:421-452) per edge
+    void SetEdgeLoads(const std::vector<std::vector<int> > &edges, double tx, double ty) {
+        std::vector<int32_t> e;
+        for (auto &ed : edges) {
+            if (ed.size() != 2) throw std::runtime_error("pansfem2_gb300: an edge has 2 nodes");
+            e.insert(e.end(), ed.begin(), ed.end());
+        }
+        check(psf_fem_set_edge_loads(fem_, (int)edges.size(), e.data(), tx, ty), false);
+    }
+    // the element loop with modulus E[e] (conductivity for heat), Poisson ratio V and
+    // thickness t, then CSR(LILCSR&); returns the number of stored entries
+    long long Assemble(const std::vector<double> &E, double V, double t) {
+        if ((long long)E.size() != ne_) throw std::runtime_error("pansfem2_gb300: one modulus per element");
+        long long nnz = 0;
+        check(psf_fem_assemble(fem_, E.data(), V, t, &nnz), false);
+        return nnz;
+    }
+    // ScalingCG (PSF_SOLVE_CSR_JACOBI_F64) or CG (PSF_SOLVE_CSR_CG_F64) + Disassembling: the
+    // nodal solution, nnodes x ndof, prescribed values included; the last iterate when the
+    // solver reaches itrmax
+    std::vector<double> Solve(int solver, int itrmax, double eps, psf_solve_info *info = nullptr) {
+        std::vector<double> u(nnodes_ * ndof_);
+        psf_solve_info tmp;
+        check(psf_fem_solve(fem_, solver, itrmax, eps, u.data(), info ? info : &tmp));
+        return u;
+    }
+    // the reaction loop (sample_planestrain.cpp:66-77): r = sum_e Ke_e u_e over all dofs
+    std::vector<double> Reaction(const std::vector<double> &u) {
+        std::vector<double> r(nnodes_ * ndof_);
+        check(psf_fem_reaction(fem_, u.data(), r.data()), false);
+        return r;
+    }
+
+private:
+    psf_fem *fem_ = nullptr;
+    long long nnodes_ = 0, ne_ = 0;
+    int ndof_ = 0;
 };
 
 }  // namespace PANSFEM2_GB300

@@ -230,7 +230,7 @@ psf_status psf_sync(psf_ctx *ctx);
  *   solve             ScalingCG (CG.h:419-453) or CG (CG.h:123-154) on that CSR;
  *   reaction          r = sum_e Ke_e u_e over all dofs (sample_planestrain.cpp:66-77).
  * coords: nnodes x 2 (3 for H8); conn: nelem x nen (3 T3, 4 Q4, 8 H8), node ids in [0, nnodes).
- * Element body / surface loads are not modelled: point loads and prescribed values only. */
+ * Loads: point loads, prescribed values, uniform body forces and uniform edge tractions. */
 typedef struct psf_fem psf_fem;
 psf_status psf_fem_create(int kind, long long nnodes, const double *coords, long long nelem, int nen,
                           const int32_t *conn, psf_fem **out);
@@ -240,6 +240,12 @@ psf_status psf_fem_set_dirichlet(psf_fem *fem, int n, const int32_t *node, const
                                  const double *value, int *nfree);
 /* point loads, added to F after the element terms, in list order */
 psf_status psf_fem_set_loads(psf_fem *fem, int n, const int32_t *node, const int32_t *dof, const double *value);
+/* plane strain: a uniform body force (PlaneStrainBodyForce, PlaneStrain.h:503-534) on every element,
+ * assembled with each element's terms; uniform tractions on 2-node edges (PlaneStrainSurfaceForce
+ * <ShapeFunction2Line, Gauss1Line>, PlaneStrain.h:421-452), assembled after the point loads, in
+ * edge order (sample_planestrain.cpp:42-60) */
+psf_status psf_fem_set_body_force(psf_fem *fem, double fx, double fy);
+psf_status psf_fem_set_edge_loads(psf_fem *fem, int nedge, const int32_t *edges, double tx, double ty);
 /* element matrices (modulus / conductivity E[e], Poisson ratio V, thickness t) and the CSR system */
 psf_status psf_fem_assemble(psf_fem *fem, const double *E, double V, double t, long long *nnz);
 /* host copies (optional pointers): n2g (nnodes x ndof, -1 fixed), indptr (nfree + 1), indices and

@@ -384,9 +384,87 @@ static int cmp_colval(const void *a, const void *b) {
     return (ca > cb) - (ca < cb);
 }
 
+/* PlaneStrainBodyForce (PlaneStrain.h:503-534), uniform f: Fe = sum_g B^T f J t w0 w1 */
+void orc_body_force(int kind, const double *X, double fx, double fy, double t, double *Fe) {
+    const int nen = kind == ORC_T3_PLANE_STRAIN ? 3 : 4, ng = kind == ORC_T3_PLANE_STRAIN ? 1 : 4;
+    for (int k = 0; k < 2 * nen; k++) Fe[k] = 0.0;
+    for (int g = 0; g < ng; g++) {
+        double r[2], N[4], dN[8], J2[4], w0, w1;
+        if (kind == ORC_T3_PLANE_STRAIN) {
+            r[0] = 1.0 / 3.0; r[1] = 1.0 / 3.0;
+            N[0] = r[0]; N[1] = r[1]; N[2] = 1.0 - r[0] - r[1];
+            const double d[6] = {1.0, 0.0, -1.0, 0.0, 1.0, -1.0};
+            for (int k = 0; k < 6; k++) dN[k] = d[k];
+            w0 = w1 = 1.0 / sqrt(2.0);
+        } else {
+            gauss4(g, r);
+            N[0] = 0.25 * (1.0 - r[0]) * (1.0 - r[1]);
+            N[1] = 0.25 * (1.0 + r[0]) * (1.0 - r[1]);
+            N[2] = 0.25 * (1.0 + r[0]) * (1.0 + r[1]);
+            N[3] = 0.25 * (1.0 - r[0]) * (1.0 + r[1]);
+            dndr_q4(r, dN);
+            w0 = w1 = 1.0;
+        }
+        mm(dN, X, J2, 2, nen, 2);
+        double J = det2(J2);
+        for (int n = 0; n < nen; n++)
+            for (int c = 0; c < 2; c++) {
+                double b0 = c == 0 ? N[n] : 0.0, b1 = c == 0 ? 0.0 : N[n];
+                double v = 0.0;
+                v += b0 * fx;
+                v += b1 * fy;
+                v = v * J;
+                v = v * t;
+                v = v * w0;
+                v = v * w1;
+                Fe[2 * n + c] += v;
+            }
+    }
+}
+
+/* PlaneStrainSurfaceForce<ShapeFunction2Line, Gauss1Line> (PlaneStrain.h:421-452), uniform
+ * traction on the edges (2 nodes each), assembled in edge order into the free dofs */
+void orc_edge_loads(int nedge, const int *edges, const double *coords, double tx, double ty, double t,
+                    const int *n2g, double *F) {
+    for (int k = 0; k < nedge; k++) {
+        double X[4];
+        for (int q = 0; q < 2; q++)
+            for (int d = 0; d < 2; d++) X[q * 2 + d] = coords[(long)edges[2 * k + q] * 2 + d];
+        const double r = 0.0;
+        const double N[2] = {0.5 * (1 - r), 0.5 * (1 + r)}, dN[2] = {-0.5, 0.5};
+        double dd[2];
+        mm(dN, X, dd, 1, 2, 2);
+        double q2 = 0.0;
+        q2 += dd[0] * dd[0];
+        q2 += dd[1] * dd[1];
+        const double dl = sqrt(q2);
+        for (int n = 0; n < 2; n++)
+            for (int c = 0; c < 2; c++) {
+                double b0 = c == 0 ? N[n] : 0.0, b1 = c == 0 ? 0.0 : N[n];
+                double v = 0.0;
+                v += b0 * tx;
+                v += b1 * ty;
+                v = v * dl;
+                v = v * t;
+                v = v * 2.0;
+                double fe = 0.0 + v;
+                int I = n2g[(long)edges[2 * k + n] * 2 + c];
+                if (I != -1) F[I] += fe;
+            }
+    }
+}
+
 int orc_assemble(int kind, int ne, const int *conn, const double *coords, const double *E_e,
                  double V, double t, const int *n2g, const double *ufixed, int N,
                  orc_csr *out, double *F) {
+    return orc_assemble_body(kind, ne, conn, coords, E_e, V, t, n2g, ufixed, N, 0, 0.0, 0.0, out, F);
+}
+
+/* orc_assemble with the uniform body force assembled after each element's stiffness terms
+ * (sample_planestrain.cpp:38-47) */
+int orc_assemble_body(int kind, int ne, const int *conn, const double *coords, const double *E_e,
+                      double V, double t, const int *n2g, const double *ufixed, int N, int body, double bfx,
+                      double bfy, orc_csr *out, double *F) {
     int nen, ndof, dim;
     orc_kind_shape(kind, &nen, &ndof, &dim);
     int nk = nen * ndof;
@@ -415,6 +493,15 @@ int orc_assemble(int kind, int ne, const int *conn, const double *coords, const 
                         }
                     }
             }
+        if (body) {
+            double Fe[8];
+            orc_body_force(kind, X, bfx, bfy, t, Fe);
+            for (int i = 0; i < nen; i++)
+                for (int a = 0; a < ndof; a++) {
+                    int I = n2g[(long)en[i] * ndof + a];
+                    if (I != -1) F[I] += Fe[ndof * i + a];
+                }
+        }
     }
     free(Ke);
     /* CSR(LILCSR&) (CSR.h:92-105): row sizes, per-row sort by column, concatenation */

@@ -60,6 +60,14 @@ typedef struct {
 int orc_assemble(int kind, int ne, const int *conn, const double *coords, const double *E_e,
                  double V, double t, const int *n2g, const double *ufixed, int N,
                  orc_csr *out, double *F);
+/* the same with a uniform body force (PlaneStrainBodyForce) per element (body != 0) */
+int orc_assemble_body(int kind, int ne, const int *conn, const double *coords, const double *E_e,
+                      double V, double t, const int *n2g, const double *ufixed, int N, int body, double bfx,
+                      double bfy, orc_csr *out, double *F);
+void orc_body_force(int kind, const double *X, double fx, double fy, double t, double *Fe);
+/* uniform traction on 2-node edges (PlaneStrainSurfaceForce<ShapeFunction2Line, Gauss1Line>) into F */
+void orc_edge_loads(int nedge, const int *edges, const double *coords, double tx, double ty, double t,
+                    const int *n2g, double *F);
 void orc_csr_free(orc_csr *A);
 void orc_neumann(int nload, const int *node, const int *dof, const double *val, int ndof,
                  const int *n2g, double *F);

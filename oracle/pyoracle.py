@@ -115,7 +115,7 @@ def ke(kind, X, E, V=0.3, t=1.0):
     return out.reshape(nen * ndof, nen * ndof)
 
 
-def assemble(kind, conn, coords, E_e, n2g, N, V=0.3, t=1.0, ufixed=None):
+def assemble(kind, conn, coords, E_e, n2g, N, V=0.3, t=1.0, ufixed=None, body=None):
     """Returns (indptr, indices, data, F) of the free x free system.  ufixed: nodal prescribed
     values (nnodes x ndof, used on the fixed dofs: F -= Ke u_fixed as Assembling.h:59-61)."""
     conn, coords, E_e, n2g = i32(conn).reshape(-1), f64(coords).reshape(-1), f64(E_e), i32(n2g)
@@ -124,11 +124,22 @@ def assemble(kind, conn, coords, E_e, n2g, N, V=0.3, t=1.0, ufixed=None):
     A = CSR()
     F = np.zeros(N)
     L = _lib()
-    L.orc_assemble(kind, ne, P(conn, ip), P(coords), P(E_e), C.c_double(V), C.c_double(t),
-                   P(n2g, ip), None if uf is None else P(uf), N, C.byref(A), P(F))
+    bx, by = (0.0, 0.0) if body is None else body
+    L.orc_assemble_body(kind, ne, P(conn, ip), P(coords), P(E_e), C.c_double(V), C.c_double(t),
+                        P(n2g, ip), None if uf is None else P(uf), N, 0 if body is None else 1, C.c_double(bx),
+                        C.c_double(by), C.byref(A), P(F))
     out = A.arrays()
     L.orc_csr_free(C.byref(A))
     return out + (F,)
+
+
+def edge_loads(F, edges, coords, traction, t, n2g):
+    """Uniform traction on 2-node edges (PlaneStrainSurfaceForce), added to F in edge order."""
+    F = f64(F).copy()
+    e = i32(edges).reshape(-1)
+    _lib().orc_edge_loads(len(e) // 2, P(e, ip), P(f64(coords).reshape(-1)), C.c_double(traction[0]),
+                          C.c_double(traction[1]), C.c_double(t), P(i32(n2g), ip), P(F))
+    return F
 
 
 def neumann(F, nodes, dofs, vals, ndof, n2g):

@@ -38,6 +38,7 @@
 #include "src/FEM/Controller/GaussIntegration.h"
 #include "src/FEM/Controller/BoundaryCondition.h"
 #include "src/FEM/Controller/Assembling.h"
+#include "src/PrePost/Import/ImportFromCSV.h"
 #include "src/LinearAlgebra/Solvers/CG.h"
 #include "src/Optimize/Solver/OC.h"
 #include "src/PrePost/Export/ExportToVTK.h"
@@ -392,7 +393,8 @@ static int run_conlin() {
 
 // ------------------------------- explicit meshes -------------------------------
 // mesh=<file>: "kind nnodes nelem nen", coordinates, connectivity, E per element, "V t",
-// "nfix" + (node dof value) lines, "nload" + (node dof value) lines.  The call sequence of
+// "nfix" + (node dof value) lines, "nload" + (node dof value) lines, optionally
+// "hasbody fx fy nedge tx ty" + (node node) edge lines.  The call sequence of
 // sample/planestrain/sample_planestrain.cpp:26-77 (SetDirichlet, Renumbering, element loop
 // with Assembling, point loads, CSR, the solve, Disassembling, the reaction by
 // RemoveBoundaryConditions + Renumbering + Assembling of Ke*ElementVector) with ScalingCG
@@ -405,28 +407,88 @@ static void fem_element(int kind, Matrix<double>& Ke, std::vector<std::vector<st
     else SolidLinearIsotropicElastic<double, ShapeFunction8Cubic, Gauss8Cubic>(Ke, n2e, el, {0, 1, 2}, x, E, V);
 }
 
-static int run_fem() {
-    std::ifstream in(args("mesh", "mesh.txt"));
-    if (!in) { fprintf(stderr, "cannot read mesh\n"); return 2; }
-    int kind, nn, ne, nen;
-    in >> kind >> nn >> ne >> nen;
-    const int dim = kind == 2 ? 3 : 2, nd = kind == 1 ? 1 : dim;
-    std::vector<Vector<double> > x(nn, Vector<double>(dim));
-    for (int i = 0; i < nn; i++)
-        for (int d = 0; d < dim; d++) in >> x[i](d);
-    std::vector<std::vector<int> > elements(ne, std::vector<int>(nen));
-    for (int e = 0; e < ne; e++)
-        for (int q = 0; q < nen; q++) in >> elements[e][q];
-    std::vector<double> Ee(ne);
-    for (int e = 0; e < ne; e++) in >> Ee[e];
-    double V, t;
-    in >> V >> t;
-    int nfix, nload;
+// csvread csvdir=<dir> nd=<dofs per node>: the six ImportFromCSV.h readers on Node.csv,
+// Element.csv, Dirichlet.csv, Neumann.csv, Initial.csv (into zero vectors of nd entries per
+// node) and Periodic.csv; ragged rows are flattened with their lengths
+static int run_csvread() {
+    const std::string dir = args("csvdir", ".");
+    const int nd = (int)argd("nd", 2);
+    std::vector<Vector<double> > x;
+    std::vector<std::vector<int> > elements;
     BCList ufixed, qfixed;
-    in >> nfix;
-    for (int k = 0; k < nfix; k++) { int n, d; double v; in >> n >> d >> v; ufixed.push_back({{n, d}, v}); }
-    in >> nload;
-    for (int k = 0; k < nload; k++) { int n, d; double v; in >> n >> d >> v; qfixed.push_back({{n, d}, v}); }
+    std::vector<std::pair<int, int> > periodic;
+    if (!ImportNodesFromCSV(x, dir + "/Node.csv") || !ImportElementsFromCSV(elements, dir + "/Element.csv") ||
+        !ImportDirichletFromCSV(ufixed, dir + "/Dirichlet.csv") || !ImportNeumannFromCSV(qfixed, dir + "/Neumann.csv") ||
+        !ImportPeriodicFromCSV(periodic, dir + "/Periodic.csv"))
+        return 2;
+    std::vector<Vector<double> > u(x.size(), Vector<double>(nd));
+    if (!ImportInitialFromCSV(u, dir + "/Initial.csv")) return 2;
+    std::vector<double> xs, fixv, loadv, us;
+    std::vector<int> xlen, cs, clen, fixi, loadi, per;
+    for (auto& xi : x) { xlen.push_back(xi.SIZE()); for (int d = 0; d < xi.SIZE(); d++) xs.push_back(xi(d)); }
+    for (auto& el : elements) { clen.push_back((int)el.size()); cs.insert(cs.end(), el.begin(), el.end()); }
+    for (auto& f : ufixed) { fixi.push_back(f.first.first); fixi.push_back(f.first.second); fixv.push_back(f.second); }
+    for (auto& f : qfixed) { loadi.push_back(f.first.first); loadi.push_back(f.first.second); loadv.push_back(f.second); }
+    for (auto& pr : periodic) { per.push_back(pr.first); per.push_back(pr.second); }
+    for (auto& ui : u) for (int d = 0; d < nd; d++) us.push_back(ui(d));
+    Dump out(args("out", "ref.bin"));
+    out.d("nodes", xs); out.i("node_len", xlen); out.i("conn", cs); out.i("conn_len", clen);
+    out.i("fix", fixi); out.d("fixval", fixv); out.i("load", loadi); out.d("loadval", loadv);
+    out.i("periodic", per); out.d("initial", us);
+    return 0;
+}
+
+static int run_fem() {
+    int kind, nn, ne, nen;
+    std::vector<Vector<double> > x;
+    std::vector<std::vector<int> > elements;
+    std::vector<double> Ee;
+    double V, t;
+    BCList ufixed, qfixed;
+    int hasbody = 0, nedge = 0;
+    double bfx = 0.0, bfy = 0.0, etx = 0.0, ety = 0.0;
+    std::vector<std::vector<int> > edges;
+    if (g_args.count("csvdir")) {
+        // csvdir=<dir> kind=<k> E=<E> V=<V> t=<t>: Node.csv, Element.csv, Dirichlet.csv and
+        // Neumann.csv through the reference's ImportFromCSV.h, as sample/solid/sample_linear.cpp
+        const std::string dir = args("csvdir", ".");
+        if (!ImportNodesFromCSV(x, dir + "/Node.csv") || !ImportElementsFromCSV(elements, dir + "/Element.csv") ||
+            !ImportDirichletFromCSV(ufixed, dir + "/Dirichlet.csv") || !ImportNeumannFromCSV(qfixed, dir + "/Neumann.csv"))
+            return 2;
+        kind = (int)argd("kind", 2);
+        nn = (int)x.size();
+        ne = (int)elements.size();
+        nen = (int)elements[0].size();
+        Ee.assign(ne, argd("E", 210000.0));
+        V = argd("V", 0.3);
+        t = argd("t", 1.0);
+    } else {
+        std::ifstream in(args("mesh", "mesh.txt"));
+        if (!in) { fprintf(stderr, "cannot read mesh\n"); return 2; }
+        in >> kind >> nn >> ne >> nen;
+        const int dim = kind == 2 ? 3 : 2;
+        x.assign(nn, Vector<double>(dim));
+        for (int i = 0; i < nn; i++)
+            for (int d = 0; d < dim; d++) in >> x[i](d);
+        elements.assign(ne, std::vector<int>(nen));
+        for (int e = 0; e < ne; e++)
+            for (int q = 0; q < nen; q++) in >> elements[e][q];
+        Ee.resize(ne);
+        for (int e = 0; e < ne; e++) in >> Ee[e];
+        in >> V >> t;
+        int nfix, nload;
+        in >> nfix;
+        for (int k = 0; k < nfix; k++) { int n, d; double v; in >> n >> d >> v; ufixed.push_back({{n, d}, v}); }
+        in >> nload;
+        for (int k = 0; k < nload; k++) { int n, d; double v; in >> n >> d >> v; qfixed.push_back({{n, d}, v}); }
+        if (in >> hasbody >> bfx >> bfy >> nedge >> etx >> ety) {
+            for (int k = 0; k < nedge; k++) { int a0, a1; in >> a0 >> a1; edges.push_back({a0, a1}); }
+        } else {
+            hasbody = 0;
+            nedge = 0;
+        }
+    }
+    const int nd = kind == 1 ? 1 : (kind == 2 ? 3 : 2);
     std::vector<Vector<double> > u(nn, Vector<double>(nd)), r(nn, Vector<double>(nd));
     std::vector<std::vector<int> > nodetoglobal(nn, std::vector<int>(nd, 0));
     SetDirichlet(u, nodetoglobal, ufixed);
@@ -438,10 +500,37 @@ static int run_fem() {
         Matrix<double> Ke;
         fem_element(kind, Ke, n2e, elements[e], x, Ee[e], V, t);
         Assembling(K, F, u, Ke, nodetoglobal, n2e, elements[e]);
+        if (hasbody) {   // sample_planestrain.cpp:42-47: uniform body force per element
+            Vector<double> Fe;
+            auto fb = [&](Vector<double>) { Vector<double> f = {bfx, bfy}; return f; };
+            if (kind == 3)
+                PlaneStrainBodyForce<double, ShapeFunction3Triangle, Gauss1Triangle>(Fe, n2e, elements[e], {0, 1}, x, fb, t);
+            else
+                PlaneStrainBodyForce<double, ShapeFunction4Square, Gauss4Square>(Fe, n2e, elements[e], {0, 1}, x, fb, t);
+            Assembling(F, Fe, nodetoglobal, n2e, elements[e]);
+        }
     }
     Assembling(F, qfixed, nodetoglobal);
+    for (auto& edge : edges) {   // sample_planestrain.cpp:51-60: uniform traction per edge
+        std::vector<std::vector<std::pair<int, int> > > n2e;
+        Vector<double> Fe;
+        auto fs = [&](Vector<double>) { Vector<double> f = {etx, ety}; return f; };
+        PlaneStrainSurfaceForce<double, ShapeFunction2Line, Gauss1Line>(Fe, n2e, edge, {0, 1}, x, fs, t);
+        Assembling(F, Fe, nodetoglobal, n2e, edge);
+    }
     CSR<double> Kmod(K);
     Dump out(args("out", "ref.bin"));
+    {   // what was read: the mesh and the boundary lists in the order they were given
+        std::vector<double> xs, fixv, loadv;
+        std::vector<int> cs, fixi, loadi;
+        for (auto& xi : x) for (int d = 0; d < xi.SIZE(); d++) xs.push_back(xi(d));
+        for (auto& el : elements) cs.insert(cs.end(), el.begin(), el.end());
+        for (auto& f : ufixed) { fixi.push_back(f.first.first); fixi.push_back(f.first.second); fixv.push_back(f.second); }
+        for (auto& f : qfixed) { loadi.push_back(f.first.first); loadi.push_back(f.first.second); loadv.push_back(f.second); }
+        out.d("read_coords", xs); out.i("read_conn", cs);
+        out.i("read_fix", fixi); out.d("read_fixval", fixv);
+        out.i("read_load", loadi); out.d("read_loadval", loadv);
+    }
     std::vector<int> n2g;
     for (auto& nd2 : nodetoglobal) n2g.insert(n2g.end(), nd2.begin(), nd2.end());
     out.i("n2g", n2g);
@@ -492,6 +581,7 @@ int main(int argc, char** argv) {
     if (mode == "simp") return run_simp();
     if (mode == "conlin") return run_conlin();
     if (mode == "fem") return run_fem();
+    if (mode == "csvread") return run_csvread();
     fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

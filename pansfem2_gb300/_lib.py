@@ -36,7 +36,7 @@ EXPORTS = [
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
     "psf_fem_create", "psf_fem_destroy", "psf_fem_set_dirichlet", "psf_fem_set_loads", "psf_fem_assemble",
-    "psf_fem_get_system", "psf_fem_solve", "psf_fem_reaction",
+    "psf_fem_get_system", "psf_fem_solve", "psf_fem_reaction", "psf_fem_set_body_force", "psf_fem_set_edge_loads",
     "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
     "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv", "psf_unet_get_out_scale",
     "psf_unet_set_out_scale",
@@ -148,6 +148,8 @@ def load(path=LIB_PATH):
         "psf_fem_get_system": [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp],
         "psf_fem_solve": [vp, C.c_int, C.c_int, C.c_double, dp, C.POINTER(SolveInfo)],
         "psf_fem_reaction": [vp, dp, dp],
+        "psf_fem_set_body_force": [vp, C.c_double, C.c_double],
+        "psf_fem_set_edge_loads": [vp, C.c_int, C.POINTER(C.c_int32), C.c_double, C.c_double],
         # device pointers and a stream handle
         "psf_csr_solve_noalloc": [C.c_int, vp, vp, vp, vp, vp, C.c_int, C.c_double, vp, C.POINTER(SolveInfo)],
         # learned preconditioner network

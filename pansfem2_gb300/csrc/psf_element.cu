@@ -244,7 +244,100 @@ __global__ void fem_ke_kernel(int kind, long long ne, int nen, const int *__rest
     }
 }
 
+// PlaneStrainBodyForce (PlaneStrain.h:503-534) for a uniform force (fx, fy): Fe = sum_g
+// B^T f J t w0 w1, B the 2 x 2nen matrix of N (T3: Gauss1Triangle, Q4: Gauss4Square)
+__device__ void body_force(int kind, const double *X, double fx, double fy, double t, double *Fe) {
+    const int nen = kind == PSF_T3_PLANE_STRAIN ? 3 : 4, ng = kind == PSF_T3_PLANE_STRAIN ? 1 : 4;
+    for (int k = 0; k < 2 * nen; k++) Fe[k] = 0.0;
+    for (int g = 0; g < ng; g++) {
+        double r[2], N[4], dN[8], J2[4], w0, w1;
+        if (kind == PSF_T3_PLANE_STRAIN) {
+            r[0] = 1.0 / 3.0; r[1] = 1.0 / 3.0;
+            N[0] = r[0]; N[1] = r[1]; N[2] = 1.0 - r[0] - r[1];
+            const double d[6] = {1.0, 0.0, -1.0, 0.0, 1.0, -1.0};
+            for (int k = 0; k < 6; k++) dN[k] = d[k];
+            w0 = w1 = 1.0 / sqrt(2.0);
+        } else {
+            gauss_q4(g, r);
+            N[0] = 0.25 * (1.0 - r[0]) * (1.0 - r[1]);
+            N[1] = 0.25 * (1.0 + r[0]) * (1.0 - r[1]);
+            N[2] = 0.25 * (1.0 + r[0]) * (1.0 + r[1]);
+            N[3] = 0.25 * (1.0 - r[0]) * (1.0 + r[1]);
+            dndr_q4(r, dN);
+            w0 = w1 = 1.0;
+        }
+        mm(dN, X, J2, 2, nen, 2);
+        const double J = det2(J2);
+        for (int n = 0; n < nen; n++)
+            for (int c = 0; c < 2; c++) {
+                const double b0 = c == 0 ? N[n] : 0.0, b1 = c == 0 ? 0.0 : N[n];   // row of B^T
+                double v = 0.0;
+                v += b0 * fx;
+                v += b1 * fy;
+                Fe[2 * n + c] += v * J * t * w0 * w1;
+            }
+    }
+}
+
+// PlaneStrainSurfaceForce<ShapeFunction2Line, Gauss1Line> (PlaneStrain.h:421-452) for a
+// uniform traction (tx, ty) on a 2-node edge: Fe = B^T f dl t w0, dl the length factor
+__device__ void edge_force(const double *X, double tx, double ty, double t, double *Fe) {
+    const double r = 0.0;
+    const double N[2] = {0.5 * (1 - r), 0.5 * (1 + r)};
+    const double dN[2] = {-0.5, 0.5};
+    double d[2];
+    mm(dN, X, d, 1, 2, 2);
+    double q = 0.0;
+    q += d[0] * d[0];
+    q += d[1] * d[1];
+    const double dl = sqrt(q);
+    for (int k = 0; k < 4; k++) Fe[k] = 0.0;
+    for (int n = 0; n < 2; n++)
+        for (int c = 0; c < 2; c++) {
+            const double b0 = c == 0 ? N[n] : 0.0, b1 = c == 0 ? 0.0 : N[n];
+            double v = 0.0;
+            v += b0 * tx;
+            v += b1 * ty;
+            Fe[2 * n + c] += v * dl * t * 2.0;
+        }
+}
+
+__global__ void fem_body_kernel(int kind, long long ne, int nen, const int *__restrict__ conn,
+                                const double *__restrict__ coords, double fx, double fy, double t,
+                                double *__restrict__ Fe) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+        double X[8];
+        for (int q = 0; q < nen; q++)
+            for (int d = 0; d < 2; d++) X[q * 2 + d] = coords[(long long)conn[e * nen + q] * 2 + d];
+        body_force(kind, X, fx, fy, t, Fe + e * 2 * nen);
+    }
+}
+
+__global__ void fem_edge_kernel(int nedge, const int *__restrict__ edges, const double *__restrict__ coords, double tx,
+                                double ty, double t, double *__restrict__ Fe) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nedge; k += gridDim.x * blockDim.x) {
+        double X[4];
+        for (int q = 0; q < 2; q++)
+            for (int d = 0; d < 2; d++) X[q * 2 + d] = coords[(long long)edges[2 * k + q] * 2 + d];
+        edge_force(X, tx, ty, t, Fe + 4 * k);
+    }
+}
+
 }  // namespace
+
+psf_status fem_body_forces(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
+                           double fx, double fy, double t, double *Fe) {
+    fem_body_kernel<<<grid_for(ne, 128, 65536), 128, 0, s>>>(kind, ne, nen, conn, coords, fx, fy, t, Fe);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
+psf_status fem_edge_forces(cudaStream_t s, int nedge, const int *edges, const double *coords, double tx, double ty,
+                           double t, double *Fe) {
+    fem_edge_kernel<<<grid_for(nedge, 128, 65536), 128, 0, s>>>(nedge, edges, coords, tx, ty, t, Fe);
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
 
 psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
                                 const double *E, double V, double t, double *Ke) {

@@ -11,8 +11,9 @@
 //     is every free-free pair sharing an element (exact zeros included), columns ascending;
 //     each entry sums its element contributions from 0.0 in ascending element order (one
 //     thread per row walks the row node's elements in that order), so the values equal
-//     the reference's bit for bit; F[I] -= Ke u_fixed in the same order, then the point loads
-//     in list order (Assembling.h:151-158);
+//     the reference's bit for bit; F[I] -= Ke u_fixed and the uniform body force
+//     (PlaneStrainBodyForce) in the same order, then the point loads in list order
+//     (Assembling.h:151-158), then uniform edge tractions (PlaneStrainSurfaceForce);
 //   * the solve on the CSR (CG.h solvers of psf_solve.cu) and the reaction
 //     r = sum_e Ke_e u_e over all dofs (the samples' RemoveBoundaryConditions + Renumbering +
 //     Assembling of Ke*ElementVector, sample_planestrain.cpp:66-77).
@@ -150,11 +151,14 @@ __global__ void pattern_count_kernel(MeshArgs M, int *__restrict__ cnt, int *__r
     }
 }
 
-// indices, values (element contributions from 0.0 in ascending element order), F (the
-// fixed-dof terms in the same order, then the point loads in list order), diagonal position
+// indices, values (element contributions from 0.0 in ascending element order), F (per
+// element in that order its fixed-dof terms and its body force, then the point loads in list
+// order, then the edge tractions in edge order: the sample's sequence), diagonal position
 __global__ void assemble_rows_kernel(MeshArgs M, const double *__restrict__ Ke, const double *__restrict__ ufix,
                                      int nload, const int *__restrict__ lnode, const int *__restrict__ ldof,
-                                     const double *__restrict__ lval, const int *__restrict__ indptr,
+                                     const double *__restrict__ lval, const double *__restrict__ Fbody, int nedge,
+                                     const int *__restrict__ edges, const double *__restrict__ Fedge,
+                                     const int *__restrict__ indptr,
                                      int *__restrict__ indices, double *__restrict__ data, double *__restrict__ F,
                                      int *__restrict__ diag, int *__restrict__ err) {
     int cols[kMaxRowCols];
@@ -193,9 +197,13 @@ __global__ void assemble_rows_kernel(MeshArgs M, const double *__restrict__ Ke, 
                     }
                 }
             }
+            if (Fbody) f = __dadd_rn(f, Fbody[e * M.nk + i * M.nd + a]);   // the element's body force
         }
         for (int l = 0; l < nload; l++)
             if (lnode[l] == n && ldof[l] == a) f = __dadd_rn(f, lval[l]);
+        for (int k = 0; k < nedge; k++)   // edge tractions after the point loads, in edge order
+            for (int q = 0; q < 2; q++)
+                if (edges[2 * k + q] == n) f = __dadd_rn(f, Fedge[4 * k + 2 * q + a]);
         const int base = indptr[I];
         int dg = -1;
         for (int k = 0; k < nc; k++) {
@@ -257,6 +265,13 @@ struct FemMesh {
     int nload = 0;
     int *lnode = nullptr, *ldof = nullptr;
     double *lval = nullptr;
+    bool body = false;
+    double bfx = 0.0, bfy = 0.0;
+    double *Fbody = nullptr;       // ne x nk
+    int nedge = 0;
+    int *edges = nullptr;
+    double etx = 0.0, ety = 0.0;
+    double *Fedge = nullptr;       // nedge x 4
     std::vector<void *> allocs;
     Ctx *c = nullptr;
 };
@@ -440,6 +455,46 @@ psf_status psf_fem_set_loads(psf_fem *h, int n, const int32_t *node, const int32
     return PSF_OK;
 }
 
+psf_status psf_fem_set_body_force(psf_fem *h, double fx, double fy) {
+    using namespace psf;
+    FEM_CHECK(h);
+    FemMesh *f = &h->m;
+    if (f->kind != PSF_Q4_PLANE_STRAIN && f->kind != PSF_T3_PLANE_STRAIN) {
+        set_error("psf_fem_set_body_force: plane-strain meshes only");
+        return PSF_BAD_INPUT;
+    }
+    f->body = true;
+    f->bfx = fx;
+    f->bfy = fy;
+    return PSF_OK;
+}
+
+psf_status psf_fem_set_edge_loads(psf_fem *h, int nedge, const int32_t *edges, double tx, double ty) {
+    using namespace psf;
+    FEM_CHECK(h);
+    FemMesh *f = &h->m;
+    if (f->kind != PSF_Q4_PLANE_STRAIN && f->kind != PSF_T3_PLANE_STRAIN) {
+        set_error("psf_fem_set_edge_loads: plane-strain meshes only");
+        return PSF_BAD_INPUT;
+    }
+    if (nedge < 0 || (nedge > 0 && !edges)) { set_error("psf_fem_set_edge_loads: invalid edges"); return PSF_BAD_INPUT; }
+    for (int k = 0; k < 2 * nedge; k++)
+        if (edges[k] < 0 || edges[k] >= f->nn) { set_error("psf_fem_set_edge_loads: node out of range"); return PSF_BAD_INPUT; }
+    fem_release(f, f->edges);
+    fem_release(f, f->Fedge);
+    f->edges = nullptr;
+    f->Fedge = nullptr;
+    f->nedge = nedge;
+    f->etx = tx;
+    f->ety = ty;
+    if (nedge > 0) {
+        PSF_CHECK(fem_alloc(f, (void **)&f->edges, sizeof(int) * 2 * nedge));
+        PSF_CUDA(cudaMemcpyAsync(f->edges, edges, sizeof(int) * 2 * nedge, cudaMemcpyHostToDevice, f->c->stream));
+        PSF_CUDA(cudaStreamSynchronize(f->c->stream));
+    }
+    return PSF_OK;
+}
+
 psf_status psf_fem_assemble(psf_fem *h, const double *E, double V, double t, long long *nnz) {
     using namespace psf;
     FEM_CHECK(h);
@@ -472,9 +527,18 @@ psf_status psf_fem_assemble(psf_fem *h, const double *E, double V, double t, lon
         PSF_CHECK(fem_alloc(f, (void **)&f->diag, sizeof(int) * (f->nfree + 1)));
         PSF_CHECK(fem_alloc(f, (void **)&f->F, sizeof(double) * (f->nfree + 1)));
     }
+    if (f->body) {
+        if (!f->Fbody) PSF_CHECK(fem_alloc(f, (void **)&f->Fbody, sizeof(double) * f->ne * f->nk));
+        PSF_CHECK(fem_body_forces(s, f->kind, f->ne, f->nen, f->conn, f->coords, f->bfx, f->bfy, t, f->Fbody));
+    }
+    if (f->nedge > 0) {
+        if (!f->Fedge) PSF_CHECK(fem_alloc(f, (void **)&f->Fedge, sizeof(double) * 4 * f->nedge));
+        PSF_CHECK(fem_edge_forces(s, f->nedge, f->edges, f->coords, f->etx, f->ety, t, f->Fedge));
+    }
     assemble_rows_kernel<<<grid_for(nt, 128, 65536), 128, 0, s>>>(M, f->Ke, f->ufix, f->nload, f->lnode, f->ldof,
-                                                                  f->lval, f->indptr, f->indices, f->data, f->F,
-                                                                  f->diag, err);
+                                                                  f->lval, f->body ? f->Fbody : nullptr, f->nedge,
+                                                                  f->edges, f->Fedge, f->indptr, f->indices, f->data,
+                                                                  f->F, f->diag, err);
     PSF_CUDA(cudaGetLastError());
     int herr = 0;
     PSF_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -171,6 +171,10 @@ psf_status solve(Ctx *c, int solver, int itmax, double eps, bool warm, psf_solve
 psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward);               // psf_opt.cu
 psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho);
 psf_status generic_context(Ctx **out);   // psf_generic.cu: the process-wide internal context
+psf_status fem_body_forces(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
+                           double fx, double fy, double t, double *Fe);   // psf_element.cu
+psf_status fem_edge_forces(cudaStream_t s, int nedge, const int *edges, const double *coords, double tx, double ty,
+                           double t, double *Fe);                          // psf_element.cu
 psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
                                 const double *E, double V, double t, double *Ke);   // psf_element.cu
 psf_status heaviside_back(Ctx *c, const double *d, double *out);                            // psf_opt.cu

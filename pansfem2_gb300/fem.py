@@ -69,6 +69,14 @@ class FemMesh:
         check(self.L.psf_fem_set_loads(self.h, len(node), node.ctypes.data_as(C.POINTER(C.c_int32)),
                                        dof.ctypes.data_as(C.POINTER(C.c_int32)), ptr(value)))
 
+    def set_body_force(self, fx, fy):
+        check(self.L.psf_fem_set_body_force(self.h, float(fx), float(fy)))
+
+    def set_edge_loads(self, edges, tx, ty):
+        edges = _i32(np.asarray(edges).reshape(-1, 2))
+        check(self.L.psf_fem_set_edge_loads(self.h, len(edges), edges.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            float(tx), float(ty)))
+
     def assemble(self, E, V=0.3, t=1.0):
         E = f64(np.broadcast_to(np.asarray(E, float), (self.ne,)).copy())
         nnz = C.c_longlong()

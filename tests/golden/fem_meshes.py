@@ -9,12 +9,13 @@ Q4_PLANE_STRAIN, Q4_HEAT, H8_SOLID, T3_PLANE_STRAIN = 0, 1, 2, 3
 
 
 def planestrain_sample():
-    """sample/planestrain/sample_planestrain.cpp:20-25: 6 nodes, 4 T3, its Dirichlet list and
-    point load (its body and edge forces are not part of this path)."""
+    """sample/planestrain/sample_planestrain.cpp:20-60 in full: 6 nodes, 4 T3, its Dirichlet
+    list, point load, body force (0, -300) and edge traction (0, -200) on edges {3,4}, {4,5}."""
     coords = np.array([[0, 0], [1, 0], [2, 0], [2, 1], [1, 1], [0, 1]], float)
     conn = np.array([[0, 1, 4], [1, 2, 3], [3, 4, 1], [4, 5, 0]])
     return dict(kind=T3_PLANE_STRAIN, coords=coords, conn=conn, E=np.full(4, 210000.0), V=0.3, t=1.0,
-                fixed=[(0, 0, 0.0), (0, 1, 0.0), (5, 0, 0.0)], loads=[(3, 1, -100.0)])
+                fixed=[(0, 0, 0.0), (0, 1, 0.0), (5, 0, 0.0)], loads=[(3, 1, -100.0)],
+                body=(0.0, -300.0), edges=[(3, 4), (4, 5)], traction=(0.0, -200.0))
 
 
 def _jittered_grid(nx, ny, seed, jitter=0.2):
@@ -41,7 +42,9 @@ def q4_jitter(nx=8, ny=5, seed=1, heat=False):
         return dict(kind=Q4_HEAT, coords=coords, conn=conn, E=E, V=0.3, t=1.0, fixed=fixed, loads=loads)
     fixed = [(nid(0, j), d, 0.0) for j in range(ny + 1) for d in (0, 1)] + [(nid(nx, 0), 0, 0.01)]
     loads = [(nid(nx, j), 1, -1.0 / (ny + 1)) for j in range(ny + 1)]
-    return dict(kind=Q4_PLANE_STRAIN, coords=coords, conn=conn, E=E, V=0.3, t=1.0, fixed=fixed, loads=loads)
+    edges = [(nid(i, ny), nid(i + 1, ny)) for i in range(nx)]
+    return dict(kind=Q4_PLANE_STRAIN, coords=coords, conn=conn, E=E, V=0.3, t=1.0, fixed=fixed, loads=loads,
+                body=(0.05, -0.1), edges=edges, traction=(0.0, -0.3))
 
 
 def t3_jitter(nx=9, ny=6, seed=2):
@@ -58,7 +61,9 @@ def t3_jitter(nx=9, ny=6, seed=2):
     E = rng.uniform(0.1, 1.0, len(conn))
     fixed = [(nid(0, j), d, 0.0) for j in range(ny + 1) for d in (0, 1)] + [(nid(nx, ny), 0, -0.02)]
     loads = [(nid(i, ny), 1, -0.5) for i in range(1, nx + 1)]
-    return dict(kind=T3_PLANE_STRAIN, coords=coords, conn=conn, E=E, V=0.3, t=0.5, fixed=fixed, loads=loads)
+    edges = [(nid(nx, j), nid(nx, j + 1)) for j in range(ny)]
+    return dict(kind=T3_PLANE_STRAIN, coords=coords, conn=conn, E=E, V=0.3, t=0.5, fixed=fixed, loads=loads,
+                body=(-0.02, -0.07), edges=edges, traction=(0.1, 0.0))
 
 
 def h8_jitter(nx=3, ny=2, nz=2, seed=3):
@@ -105,3 +110,10 @@ def write_mesh(case, path):
         fh.write(f"{len(case['loads'])}\n")
         for n, d, v in case["loads"]:
             fh.write(f"{int(n)} {int(d)} {float(v)!r}\n")
+        body = case.get("body")
+        edges = case.get("edges", [])
+        tx, ty = case.get("traction", (0.0, 0.0))
+        fh.write(f"{1 if body else 0} {float(body[0]) if body else 0.0!r} {float(body[1]) if body else 0.0!r} "
+                 f"{len(edges)} {float(tx)!r} {float(ty)!r}\n")
+        for a0, a1 in edges:
+            fh.write(f"{int(a0)} {int(a1)}\n")

@@ -47,6 +47,15 @@ TEST_MAINS = ["test_CG", "test_MMA", "test_MMA_3", "test_MMA_TOY2"]
 CONLIN_PROBLEMS = {"mma": 30, "mma3": 30, "toy2": 30}
 
 
+def read_vtk_vectors(path, name):
+    """The POINT_DATA vectors called name of a legacy ASCII VTK file, as (npoints, 3)."""
+    with open(path) as fh:
+        words = fh.read().split()
+    npts = int(words[words.index("POINT_DATA") + 1])
+    k = next(i for i in range(len(words) - 1) if words[i] == "VECTORS" and words[i + 1] == name)
+    return np.array(words[k + 3:k + 3 + 3 * npts], float).reshape(npts, 3)
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     obuild.build()
@@ -82,10 +91,34 @@ def main():
                  conn=np.asarray(case["conn"], np.int32), E=np.asarray(case["E"], float),
                  Vt=np.array([case["V"], case["t"]]),
                  fixed=np.array(case["fixed"], float).reshape(-1, 3), loads=np.array(case["loads"], float).reshape(-1, 3),
+                 body=np.array(case.get("body") or (np.nan, np.nan), float),
+                 edges=np.array(case.get("edges", []), np.int32).reshape(-1, 2),
+                 traction=np.array(case.get("traction", (0.0, 0.0)), float),
                  solver=np.array([0 if solver == "scaling_cg" else 4], np.int32))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(f"{name}.npz")
     os.remove(mesh)
+    # sample/solid/sample_linear.cpp: an H8 cantilever read from the reference's CSV files by its
+    # own ImportFromCSV.h, with the displacements of its committed result_linear.vtk
+    solid = os.path.join(ref_root, "sample", "solid")
+    subprocess.run([os.path.join(REF, "ref_driver"), "fem", f"csvdir={solid}", "kind=2", "E=210000", "V=0.3",
+                    f"out={tmp}"], check=True, stdout=subprocess.DEVNULL)
+    d = read_dump(tmp)
+    nn = len(d["read_coords"]) // 3
+    d.update(kind=np.array([2], np.int32), coords=d["read_coords"].reshape(nn, 3),
+             conn=d["read_conn"].reshape(-1, 8), E=np.full(len(d["read_conn"]) // 8, 210000.0),
+             Vt=np.array([0.3, 1.0]),
+             fixed=np.column_stack([d["read_fix"].reshape(-1, 2), d["read_fixval"]]),
+             loads=np.column_stack([d["read_load"].reshape(-1, 2), d["read_loadval"]]),
+             body=np.array([np.nan, np.nan]), edges=np.zeros((0, 2), np.int32), traction=np.zeros(2),
+             solver=np.array([0], np.int32), vtk_u=read_vtk_vectors(os.path.join(solid, "result_linear.vtk"), "u"))
+    np.savez_compressed(os.path.join(HERE, "fem_solid_sample.npz"), **d)
+    print("fem_solid_sample.npz")
+    # the reference's parse of the CSV grammar cases in tests/golden/csv_grammar/
+    subprocess.run([os.path.join(REF, "ref_driver"), "csvread", f"csvdir={os.path.join(HERE, 'csv_grammar')}",
+                    "nd=2", f"out={tmp}"], check=True, stdout=subprocess.DEVNULL)
+    np.savez_compressed(os.path.join(HERE, "csv_grammar.npz"), **read_dump(tmp))
+    print("csv_grammar.npz")
     for pb, iters in CONLIN_PROBLEMS.items():
         subprocess.run([os.path.join(REF, "ref_driver"), "conlin", f"out={tmp}", f"problem={pb}", f"iters={iters}"],
                        check=True, stdout=subprocess.DEVNULL)

@@ -202,13 +202,15 @@ def test_reference_test_CG():
     assert got == ref
 
 
-FEM_NAMES = ["fem_planestrain_sample", "fem_q4_jitter", "fem_q4_heat_jitter", "fem_t3_jitter", "fem_h8_jitter"]
+FEM_NAMES = ["fem_planestrain_sample", "fem_q4_jitter", "fem_q4_heat_jitter", "fem_t3_jitter", "fem_h8_jitter",
+             "fem_solid_sample"]
 
 
 @pytest.mark.parametrize("name", FEM_NAMES)
 def test_fem_explicit_mesh_assembly_bitexact(name):
     """The general path on explicit meshes (permuted node ids, jittered coordinates, per-element
-    moduli, prescribed nonzero values): numbering, CSR pattern, values and F of the oracle
+    moduli, prescribed nonzero values, uniform body forces and edge tractions): numbering, CSR
+    pattern, values and F of the oracle
     against the reference's SetDirichlet / Renumbering / Assembling / CSR(LILCSR&) run, bit for
     bit; the element matrix of element 0 too (T3, Q4, Q4 heat, H8)."""
     g = load(name)
@@ -222,9 +224,12 @@ def test_fem_explicit_mesh_assembly_bitexact(name):
         uf[int(n) * nd + int(d)] = v
     n2g, N = O.renumber(nn, nd, fixed)
     V, t = g["Vt"]
-    ip, ix, dat, F = O.assemble(kind, g["conn"], g["coords"], g["E"], n2g, N, V, t, ufixed=uf)
+    body = None if np.isnan(g["body"]).any() else tuple(g["body"])
+    ip, ix, dat, F = O.assemble(kind, g["conn"], g["coords"], g["E"], n2g, N, V, t, ufixed=uf, body=body)
     L = g["loads"]
     F = O.neumann(F, L[:, 0].astype(int), L[:, 1].astype(int), L[:, 2], nd, n2g)
+    if len(g["edges"]):
+        F = O.edge_loads(F, g["edges"], g["coords"], g["traction"], t, n2g)
     for a, b in ((n2g, "n2g"), (ip, "indptr"), (ix, "indices"), (dat, "data"), (F, "F")):
         assert same(g[b], a), b
     X = g["coords"][g["conn"][0]]
