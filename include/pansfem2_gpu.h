@@ -71,6 +71,9 @@ psf_status psf_create(psf_ctx **ctx, int kind, int nx, int ny, int nz, double lx
                       double lz, double V, double t);
 psf_status psf_destroy(psf_ctx *ctx);
 const char *psf_last_error(void);
+/* kernel launches this host thread has made through the library so far (graph replays count
+ * their kernel nodes); the difference over a call sequence is its launch count */
+psf_status psf_kernel_launches(long long *n);
 /* sizes: elements, nodes, dofs per node, free dofs (after psf_set_dirichlet), CSR nnz (after psf_build_csr) */
 psf_status psf_sizes(const psf_ctx *ctx, int64_t *ne, int64_t *nnodes, int *ndof, int64_t *nfree,
                      int64_t *nnz);
@@ -248,6 +251,9 @@ psf_status psf_fem_set_body_force(psf_fem *fem, double fx, double fy);
 psf_status psf_fem_set_edge_loads(psf_fem *fem, int nedge, const int32_t *edges, double tx, double ty);
 /* element matrices (modulus / conductivity E[e], Poisson ratio V, thickness t) and the CSR system */
 psf_status psf_fem_assemble(psf_fem *fem, const double *E, double V, double t, long long *nnz);
+/* device time of the last psf_fem_assemble, in ms (optional pointers): the element matrices, the
+ * CSR pattern (0 when the pattern of an earlier call was reused), the values and loads */
+psf_status psf_fem_timings(psf_fem *fem, double *element_ms, double *pattern_ms, double *values_ms);
 /* host copies (optional pointers): n2g (nnodes x ndof, -1 fixed), indptr (nfree + 1), indices and
  * data (nnz), F (nfree) */
 psf_status psf_fem_get_system(psf_fem *fem, int32_t *n2g, int32_t *indptr, int32_t *indices, double *data,

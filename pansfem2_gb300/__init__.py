@@ -5,5 +5,5 @@ include/pansfem2_gpu.h).  This package is a thin Python host over that ABI;
 the C++ host mirror of the reference's template API is include/pansfem2_gb300.hpp.
 """
 from . import problems  # noqa: F401
-from ._lib import PsfError, SOLVERS, load  # noqa: F401
+from ._lib import PsfError, SOLVERS, kernel_launches, load  # noqa: F401
 from .api import Problem  # noqa: F401

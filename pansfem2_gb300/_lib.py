@@ -27,7 +27,7 @@ SOLVERS = {
 
 # every symbol declared in include/pansfem2_gpu.h
 EXPORTS = [
-    "psf_create", "psf_destroy", "psf_last_error", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
+    "psf_create", "psf_destroy", "psf_last_error", "psf_kernel_launches", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
     "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_solve",
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_sensitivity_filter",
     "psf_compliance_sensitivity",
@@ -37,6 +37,7 @@ EXPORTS = [
     "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
     "psf_fem_create", "psf_fem_destroy", "psf_fem_set_dirichlet", "psf_fem_set_loads", "psf_fem_assemble",
     "psf_fem_get_system", "psf_fem_solve", "psf_fem_reaction", "psf_fem_set_body_force", "psf_fem_set_edge_loads",
+    "psf_fem_timings",
     "psf_unet_create", "psf_unet_destroy", "psf_unet_nparams", "psf_unet_set_params", "psf_unet_get_params",
     "psf_unet_forward_host", "psf_unet_loss_grad_host", "psf_unet_conv", "psf_unet_get_out_scale",
     "psf_unet_set_out_scale",
@@ -148,6 +149,8 @@ def load(path=LIB_PATH):
         "psf_fem_get_system": [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp],
         "psf_fem_solve": [vp, C.c_int, C.c_int, C.c_double, dp, C.POINTER(SolveInfo)],
         "psf_fem_reaction": [vp, dp, dp],
+        "psf_fem_timings": [vp, dp, dp, dp],
+        "psf_kernel_launches": [C.POINTER(C.c_longlong)],
         "psf_fem_set_body_force": [vp, C.c_double, C.c_double],
         "psf_fem_set_edge_loads": [vp, C.c_int, C.POINTER(C.c_int32), C.c_double, C.c_double],
         # device pointers and a stream handle
@@ -208,3 +211,10 @@ def f64(a):
 
 def i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def kernel_launches():
+    """Kernel launches this thread has made through the library (psf_kernel_launches)."""
+    n = C.c_longlong()
+    check(load().psf_kernel_launches(C.byref(n)))
+    return n.value

@@ -796,6 +796,7 @@ struct psf_batch {
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    size_t graph_nodes = 0;   // kernel nodes of one iteration's graph
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<void *> allocs;
     std::vector<double> hout;
@@ -840,6 +841,7 @@ cudaError_t launch_phase(psf_batch *b, void (*kern)(Args), size_t smem) {
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = b->cluster > 1 ? 1 : 0;
+    ::psf::note_launch();
     return cudaLaunchKernelEx(&cfg, kern, b->a);
 }
 
@@ -1109,6 +1111,8 @@ psf_status psf_batch_begin(psf_batch *b, const psf_simp_params *prm) {
     PSF_CUDA(e);
     b->graph = g;
     PSF_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+    b->graph_nodes = 0;
+    PSF_CUDA(cudaGraphGetNodes(g, nullptr, &b->graph_nodes));
     b->hout.assign((size_t)b->ninst * psf::batch::kOut, 0.0);
     b->begun = true;
     return PSF_OK;
@@ -1118,6 +1122,7 @@ psf_status psf_batch_step(psf_batch *b, int iters, double *seconds) {
     if (!b || !b->begun || iters < 1) return PSF_BAD_INPUT;
     PSF_CUDA(cudaEventRecord(b->ev0, b->stream));
     for (int k = 0; k < iters; k++) PSF_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    ::psf::note_launch((long long)iters * (long long)b->graph_nodes);
     PSF_CUDA(cudaEventRecord(b->ev1, b->stream));
     PSF_CUDA(cudaEventSynchronize(b->ev1));
     float ms = 0.f;

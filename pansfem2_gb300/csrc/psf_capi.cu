@@ -36,6 +36,12 @@ extern "C" {
 
 const char *psf_last_error(void) { return last_error(); }
 
+psf_status psf_kernel_launches(long long *n) {
+    if (!n) { set_error("psf_kernel_launches: null output"); return PSF_BAD_INPUT; }
+    *n = launches();
+    return PSF_OK;
+}
+
 psf_status psf_create(psf_ctx **out, int kind, int nx, int ny, int nz, double lx, double ly, double lz, double V,
                       double t) {
     if (!out) { set_error("psf_create: null output"); return PSF_BAD_INPUT; }

@@ -18,6 +18,14 @@
 
 namespace psf {
 
+// Kernel launches made by this host thread.  Every launch site calls note_launch (a graph
+// replay adds its kernel nodes); the iteration and assembly reports give the difference
+// over their calls.
+inline thread_local long long g_launches = 0;
+inline void note_launch(long long n = 1) { g_launches += n; }
+inline long long launches() { return g_launches; }
+
+
 constexpr int kMaxRed = 6;                    // values reduced by one grid_sync
 constexpr long long kSpinLimit = 1ll << 23;   // polls (x >= 64 ns each): ~1 s bound
 

@@ -20,6 +20,62 @@ __device__ void mm(const double *A, const double *B, double *C, int r, int k, in
         }
 }
 
+// sum over q of a[q] * b[q * bstride] for the q where row i of A and column j of B can both be
+// nonzero, in q order, starting from the first such product (0.0 when there is none)
+template <int K, class MA, class MB>
+__device__ __forceinline__ double dot_s(const double *a, const double *b, int bstride, int i, int j) {
+    double v = 0.0;
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < K; q++)
+        if (MA::nz(i, q) && MB::nz(q, j)) {
+            const double p = a[q] * b[q * bstride];
+            v = any ? v + p : p;
+            any = true;
+        }
+    return v;
+}
+
+// The same product with the structural zeros of A and B left out, and the leading 0.0 +.
+// MA::nz(i, q) and MB::nz(q, j) say where A and B can be nonzero; after unrolling they are
+// constants, so the skipped terms cost nothing.  For finite factors the result differs from
+// the reference's sum at most in the sign of a zero: a skipped term is +-0, and adding +-0
+// leaves a nonzero sum as it is.  Every such value ends in a product and then in a sum that
+// starts from +0.0 (the element matrix), and a sum that starts from +0 is never -0 (x + (-x)
+// rounds to +0), so the element matrix is the reference's bit for bit.
+template <int R, int K, int C, class MA, class MB>
+__device__ __forceinline__ void mm_s(const double *A, const double *B, double *Out) {
+#pragma unroll
+    for (int i = 0; i < R; i++)
+#pragma unroll
+        for (int j = 0; j < C; j++) Out[i * C + j] = dot_s<K, MA, MB>(A + i * K, B + j, C, i, j);
+}
+// plane strain, Q4: B (3 x 8) rows exx, eyy, gxy over (ux0, uy0, ux1, ...); D (3 x 3)
+struct NzB2 { static __device__ constexpr bool nz(int r, int c) { return r == 2 || (c & 1) == r; } };
+struct NzBt2 { static __device__ constexpr bool nz(int r, int c) { return NzB2::nz(c, r); } };
+struct NzD2 { static __device__ constexpr bool nz(int r, int c) { return (r < 2 && c < 2) || (r == 2 && c == 2); } };
+struct NzBtD2 {
+    static __device__ constexpr bool nz(int r, int c) {
+        return (NzBt2::nz(r, 0) && NzD2::nz(0, c)) || (NzBt2::nz(r, 1) && NzD2::nz(1, c)) ||
+               (NzBt2::nz(r, 2) && NzD2::nz(2, c));
+    }
+};
+// solid, H8: B (6 x 24) rows exx, eyy, ezz, gxy, gyz, gzx over (ux0, uy0, uz0, ...); C (6 x 6)
+struct NzB3 {
+    static __device__ constexpr bool nz(int r, int c) {
+        return r < 3 ? c % 3 == r : (r == 3 ? c % 3 != 2 : (r == 4 ? c % 3 != 0 : c % 3 != 1));
+    }
+};
+struct NzBt3 { static __device__ constexpr bool nz(int r, int c) { return NzB3::nz(c, r); } };
+struct NzC3 { static __device__ constexpr bool nz(int r, int c) { return (r < 3 && c < 3) || r == c; } };
+struct NzBtC3 {
+    static __device__ constexpr bool nz(int r, int c) {
+        return (NzBt3::nz(r, 0) && NzC3::nz(0, c)) || (NzBt3::nz(r, 1) && NzC3::nz(1, c)) ||
+               (NzBt3::nz(r, 2) && NzC3::nz(2, c)) || (NzBt3::nz(r, 3) && NzC3::nz(3, c)) ||
+               (NzBt3::nz(r, 4) && NzC3::nz(4, c)) || (NzBt3::nz(r, 5) && NzC3::nz(5, c));
+    }
+};
+
 __device__ double det2(const double *v) { return v[0] * v[3] - v[1] * v[2]; }
 // Matrix::Determinant 3x3 term order (Matrix.h:333-334)
 __device__ double det3(const double *v) {
@@ -82,31 +138,44 @@ __device__ void dndr_h8(const double *r, double *d) {
     }
 }
 
-// PlaneStrainStiffness (PlaneStrain.h:20-58)
-__device__ void ke_planestrain(const double *X, double E, double V, double t, double *Ke) {
+// PlaneStrainStiffness (PlaneStrain.h:20-58): Ke = sum_g B^T D B J t w0 w1, accumulated in
+// registers and stored once.  The products skip the structural zeros of B and D (mm_s) and
+// the weights (both 1.0: x * 1.0 is x), which leaves every entry as the reference's
+__device__ void ke_planestrain(const double *X, double E, double V, double t, double *Ke_out) {
     double D[9] = {1.0 - V, V, 0.0, V, 1.0 - V, 0.0, 0.0, 0.0, 0.5 * (1.0 - 2.0 * V)};
     const double sc = E / ((1.0 - 2.0 * V) * (1.0 + V));
+#pragma unroll
     for (int k = 0; k < 9; k++) D[k] *= sc;
+    double Ke[64];
+#pragma unroll
     for (int k = 0; k < 64; k++) Ke[k] = 0.0;
+#pragma unroll 1
     for (int g = 0; g < 4; g++) {
-        double r[2], dN[8], J2[4], iv[4], dX[8], B[24], Bt[24], BtD[24], K[64];
+        double r[2], dN[8], J2[4], iv[4], dX[8], B[24], Bt[24], BtD[24];
         gauss_q4(g, r);
         dndr_q4(r, dN);
         mm(dN, X, J2, 2, 4, 2);
         const double J = det2(J2);
         inv_n(J2, 2, iv);
         mm(iv, dN, dX, 2, 2, 4);
+#pragma unroll
         for (int n = 0; n < 4; n++) {
             B[2 * n] = dX[n];          B[2 * n + 1] = 0.0;
             B[8 + 2 * n] = 0.0;        B[8 + 2 * n + 1] = dX[4 + n];
             B[16 + 2 * n] = dX[4 + n]; B[16 + 2 * n + 1] = dX[n];
         }
+#pragma unroll
         for (int i = 0; i < 8; i++)
+#pragma unroll
             for (int j = 0; j < 3; j++) Bt[i * 3 + j] = B[j * 8 + i];
-        mm(Bt, D, BtD, 8, 3, 3);
-        mm(BtD, B, K, 8, 3, 8);
-        for (int k = 0; k < 64; k++) Ke[k] += K[k] * J * t * 1.0 * 1.0;
+        mm_s<8, 3, 3, NzBt2, NzD2>(Bt, D, BtD);
+#pragma unroll
+        for (int i = 0; i < 8; i++)   // (B^T D) B entry by entry, each added to Ke at once
+#pragma unroll
+            for (int j = 0; j < 8; j++) Ke[i * 8 + j] += dot_s<3, NzBtD2, NzB2>(BtD + i * 3, B + j, 8, i, j) * J * t;
     }
+#pragma unroll
+    for (int k = 0; k < 64; k += 2) *reinterpret_cast<double2 *>(Ke_out + k) = make_double2(Ke[k], Ke[k + 1]);
 }
 
 // PlaneStrainStiffness<ShapeFunction3Triangle, Gauss1Triangle> (PlaneStrain.h:20-58 with
@@ -186,9 +255,9 @@ __device__ void ke_solid(const double *X, double E, double V, double *Ke, double
         }
         for (int i = 0; i < 24; i++)
             for (int j = 0; j < 6; j++) Bt[i * 6 + j] = B[j * 24 + i];
-        mm(Bt, C, BtC, 24, 6, 6);
-        mm(BtC, B, K, 24, 6, 24);
-        for (int k = 0; k < 576; k++) Ke[k] += K[k] * J * 1.0 * 1.0 * 1.0;
+        mm_s<24, 6, 6, NzBt3, NzC3>(Bt, C, BtC);        // structural zeros skipped, as in ke_planestrain
+        mm_s<24, 6, 24, NzBtC3, NzB3>(BtC, B, K);
+        for (int k = 0; k < 576; k++) Ke[k] += K[k] * J;   // the three weights are 1.0
     }
 }
 
@@ -220,23 +289,28 @@ __global__ void ke_element0_kernel(int kind, int nx, int ny, int nz, double lx, 
 
 // one thread per element of an explicit mesh: Ke_e (nk x nk) from the element's own node
 // coordinates (coords: dim doubles per node), modulus E[e]
-__global__ void fem_ke_kernel(int kind, long long ne, int nen, const int *__restrict__ conn,
-                              const double *__restrict__ coords, const double *__restrict__ E, double V, double t,
-                              double *__restrict__ Ke) {
-    const int dim = kind == PSF_H8_SOLID ? 3 : 2;
-    const int nd = kind == PSF_Q4_HEAT ? 1 : dim;
-    const long long nk = (long long)nen * nd;
+template <int KIND>
+__global__ void fem_ke_kernel(long long ne, const int *__restrict__ conn, const double *__restrict__ coords,
+                              const double *__restrict__ E, double V, double t, double *__restrict__ Ke) {
+    constexpr int dim = KIND == PSF_H8_SOLID ? 3 : 2;
+    constexpr int nd = KIND == PSF_Q4_HEAT ? 1 : dim;
+    constexpr int nen = KIND == PSF_H8_SOLID ? 8 : (KIND == PSF_T3_PLANE_STRAIN ? 3 : 4);
+    constexpr long long nk = (long long)nen * nd;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
-        double X[24];
-        for (int q = 0; q < nen; q++)
-            for (int d = 0; d < dim; d++) X[q * dim + d] = coords[(long long)conn[e * nen + q] * dim + d];
+        double X[nen * dim];
+#pragma unroll
+        for (int q = 0; q < nen; q++) {
+            const long long n = conn[e * nen + q];
+#pragma unroll
+            for (int d = 0; d < dim; d++) X[q * dim + d] = coords[n * dim + d];
+        }
         double *K = Ke + e * nk * nk;
-        if (kind == PSF_H8_SOLID) {
+        if constexpr (KIND == PSF_H8_SOLID) {
             double wk[1008];
             ke_solid(X, E[e], V, K, wk);
-        } else if (kind == PSF_T3_PLANE_STRAIN) {
+        } else if constexpr (KIND == PSF_T3_PLANE_STRAIN) {
             ke_planestrain_t3(X, E[e], V, t, K);
-        } else if (kind == PSF_Q4_PLANE_STRAIN) {
+        } else if constexpr (KIND == PSF_Q4_PLANE_STRAIN) {
             ke_planestrain(X, E[e], V, t, K);
         } else {
             ke_heat(X, E[e], t, K);
@@ -327,21 +401,34 @@ __global__ void fem_edge_kernel(int nedge, const int *__restrict__ edges, const 
 
 psf_status fem_body_forces(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
                            double fx, double fy, double t, double *Fe) {
-    fem_body_kernel<<<grid_for(ne, 128, 65536), 128, 0, s>>>(kind, ne, nen, conn, coords, fx, fy, t, Fe);
+    (fem_body_kernel<<<grid_for(ne, 128, 65536), 128, 0, s>>>(kind, ne, nen, conn, coords, fx, fy, t, Fe), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status fem_edge_forces(cudaStream_t s, int nedge, const int *edges, const double *coords, double tx, double ty,
                            double t, double *Fe) {
-    fem_edge_kernel<<<grid_for(nedge, 128, 65536), 128, 0, s>>>(nedge, edges, coords, tx, ty, t, Fe);
+    (fem_edge_kernel<<<grid_for(nedge, 128, 65536), 128, 0, s>>>(nedge, edges, coords, tx, ty, t, Fe), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
                                 const double *E, double V, double t, double *Ke) {
-    fem_ke_kernel<<<grid_for(ne, 64, 65536), 64, 0, s>>>(kind, ne, nen, conn, coords, E, V, t, Ke);
+    (void)nen;
+    switch (kind) {
+        case PSF_Q4_PLANE_STRAIN:
+            (fem_ke_kernel<PSF_Q4_PLANE_STRAIN><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            break;
+        case PSF_Q4_HEAT:
+            (fem_ke_kernel<PSF_Q4_HEAT><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            break;
+        case PSF_H8_SOLID:
+            (fem_ke_kernel<PSF_H8_SOLID><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            break;
+        default:
+            (fem_ke_kernel<PSF_T3_PLANE_STRAIN><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+    }
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -349,8 +436,8 @@ psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen,
 psf_status ke_element0(Ctx *c, double E, double *Ke_dev) {
     double *wk = nullptr;
     if (c->kind == PSF_H8_SOLID) PSF_CUDA(cudaMallocAsync((void **)&wk, 576 * sizeof(double), c->stream));
-    ke_element0_kernel<<<1, 32, 0, c->stream>>>(c->kind, c->nx, c->ny, c->nz, c->lx, c->ly, c->lz, E,
-                                                c->V, c->t, Ke_dev, wk);
+    (ke_element0_kernel<<<1, 32, 0, c->stream>>>(c->kind, c->nx, c->ny, c->nz, c->lx, c->ly, c->lz, E,
+                                                c->V, c->t, Ke_dev, wk), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     if (wk) PSF_CUDA(cudaFreeAsync(wk, c->stream));
     return PSF_OK;

@@ -1,6 +1,6 @@
 // psf_fem.cu -- explicit (unstructured) meshes: the reference's general assembly path.
 //
-// A mesh is node coordinates plus element connectivity, as ImportFromCSV.h:23-101 reads
+// A mesh is node coordinates plus element connectivity, as ImportFromCSV.h:22-98 reads
 // them or a sample writes them out (sample/planestrain/sample_planestrain.cpp:20-23).  On
 // the device, per call:
 //   * element matrices from each element's own coordinates (psf_element.cu: T3 / Q4 plane
@@ -10,8 +10,9 @@
 //   * Assembling into LILCSR, then CSR(LILCSR&) (Assembling.h:46-66, CSR.h:92-105): the pattern
 //     is every free-free pair sharing an element (exact zeros included), columns ascending;
 //     each entry sums its element contributions from 0.0 in ascending element order (one
-//     thread per row walks the row node's elements in that order), so the values equal
-//     the reference's bit for bit; F[I] -= Ke u_fixed and the uniform body force
+//     thread per node builds the node's sorted neighbour list once, then walks the node's
+//     elements in that order for each of its rows), so the values equal the reference's bit
+//     for bit; F[I] -= Ke u_fixed and the uniform body force
 //     (PlaneStrainBodyForce) in the same order, then the point loads in list order
 //     (Assembling.h:151-158), then uniform edge tractions (PlaneStrainSurfaceForce);
 //   * the solve on the CSR (CG.h solvers of psf_solve.cu) and the reaction
@@ -31,7 +32,7 @@ psf_status generic_context(Ctx **out);                                   // psf_
 
 namespace {
 
-constexpr int kMaxRowCols = 256;   // distinct columns of one row (2D meshes need < 40, H8 81)
+constexpr int kMaxNb = 96;   // distinct nodes sharing an element with one node (Q4 9, H8 27)
 
 __global__ void adj_count(long long ne, int nen, const int *__restrict__ conn, int *__restrict__ cnt) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ne * nen; t += (long long)gridDim.x * blockDim.x)
@@ -116,39 +117,56 @@ struct MeshArgs {
     const unsigned char *fixed;
 };
 
-// the sorted distinct free columns of the row of dof t = n * nd + a; false on overflow
-__device__ bool row_columns(const MeshArgs &M, long long n, int *cols, int &nc) {
-    nc = 0;
+// The nodes that share an element with node n, ascending, without repeats; false when there
+// are more than kMaxNb.  Renumbering (Assembling.h:175-186) numbers the free dofs node-major
+// and dof-minor, so the free dofs of these nodes, taken in this order, are the sorted distinct
+// columns of every row of node n: the rows of one node share one column list.
+__device__ bool node_neighbours(const MeshArgs &M, long long n, int *nb, int &cnt) {
+    cnt = 0;
     for (int p = M.adj_ptr[n]; p < M.adj_ptr[n + 1]; p++) {
         const long long e = M.adj[p];
         for (int j = 0; j < M.nen; j++) {
-            const long long m = M.conn[e * M.nen + j];
-            for (int b = 0; b < M.nd; b++) {
-                const int J = M.n2g[m * M.nd + b];
-                if (J < 0) continue;
-                int k = nc;   // insertion into the sorted list, skipping duplicates
-                while (k > 0 && cols[k - 1] > J) k--;
-                if (k > 0 && cols[k - 1] == J) continue;
-                if (nc >= kMaxRowCols) return false;
-                for (int q = nc; q > k; q--) cols[q] = cols[q - 1];
-                cols[k] = J;
-                nc++;
-            }
+            const int m = M.conn[e * M.nen + j];
+            int k = cnt;   // insertion into the sorted list, skipping repeats
+            while (k > 0 && nb[k - 1] > m) k--;
+            if (k > 0 && nb[k - 1] == m) continue;
+            if (cnt >= kMaxNb) return false;
+            for (int q = cnt; q > k; q--) nb[q] = nb[q - 1];
+            nb[k] = m;
+            cnt++;
         }
     }
     return true;
 }
 
+// one thread per node: the number of columns of each of its free rows
 __global__ void pattern_count_kernel(MeshArgs M, int *__restrict__ cnt, int *__restrict__ err) {
-    int cols[kMaxRowCols];
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M.nn * M.nd;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int I = M.n2g[t];
-        if (I < 0) continue;
+    int nb[kMaxNb];
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < M.nn; n += (long long)gridDim.x * blockDim.x) {
+        bool any = false;
+        for (int a = 0; a < M.nd; a++) any = any || M.n2g[n * M.nd + a] >= 0;
+        if (!any) continue;
+        int k = 0;
+        if (!node_neighbours(M, n, nb, k)) { atomicExch(err, 1); continue; }
         int nc = 0;
-        if (!row_columns(M, t / M.nd, cols, nc)) atomicExch(err, 1);
-        cnt[I] = nc;
+        for (int q = 0; q < k; q++)
+            for (int b = 0; b < M.nd; b++) nc += M.n2g[(long long)nb[q] * M.nd + b] >= 0;
+        for (int a = 0; a < M.nd; a++) {
+            const int I = M.n2g[n * M.nd + a];
+            if (I >= 0) cnt[I] = nc;
+        }
     }
+}
+
+// first position of key in the ascending list a[0..n), n when absent
+__device__ __forceinline__ int first_of(const int *__restrict__ a, int n, int key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
 }
 
 // indices, values (element contributions from 0.0 in ascending element order), F (per
@@ -157,62 +175,77 @@ __global__ void pattern_count_kernel(MeshArgs M, int *__restrict__ cnt, int *__r
 __global__ void assemble_rows_kernel(MeshArgs M, const double *__restrict__ Ke, const double *__restrict__ ufix,
                                      int nload, const int *__restrict__ lnode, const int *__restrict__ ldof,
                                      const double *__restrict__ lval, const double *__restrict__ Fbody, int nedge,
-                                     const int *__restrict__ edges, const double *__restrict__ Fedge,
-                                     const int *__restrict__ indptr,
+                                     const int *__restrict__ enode, const int *__restrict__ eslot,
+                                     const double *__restrict__ Fedge, const int *__restrict__ indptr,
                                      int *__restrict__ indices, double *__restrict__ data, double *__restrict__ F,
                                      int *__restrict__ diag, int *__restrict__ err) {
-    int cols[kMaxRowCols];
-    double vals[kMaxRowCols];
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M.nn * M.nd;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int I = M.n2g[t];
-        if (I < 0) continue;
-        const long long n = t / M.nd;
-        const int a = (int)(t % M.nd);
-        int nc = 0;
-        if (!row_columns(M, n, cols, nc)) { atomicExch(err, 1); continue; }
-        for (int k = 0; k < nc; k++) vals[k] = 0.0;
-        double f = 0.0;
-        for (int p = M.adj_ptr[n]; p < M.adj_ptr[n + 1]; p++) {
-            const long long e = M.adj[p];
-            int i = 0;
-            while (i < M.nen && M.conn[e * M.nen + i] != n) i++;
-            const double *K = Ke + e * (long long)M.nk * M.nk + (long long)(i * M.nd + a) * M.nk;
-            for (int j = 0; j < M.nen; j++) {
-                const long long m = M.conn[e * M.nen + j];
-                for (int b = 0; b < M.nd; b++) {
-                    const long long u = m * M.nd + b;
-                    const int J = M.n2g[u];
-                    const double kv = K[j * M.nd + b];
-                    if (J >= 0) {
-                        int lo = 0, hi = nc;
-                        while (lo < hi) {
-                            const int mid = (lo + hi) >> 1;
-                            if (cols[mid] < J) lo = mid + 1;
-                            else hi = mid;
+    int nb[kMaxNb], off[kMaxNb + 1];
+    double vals[kMaxNb * 3];
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < M.nn; n += (long long)gridDim.x * blockDim.x) {
+        bool any = false;
+        for (int a = 0; a < M.nd; a++) any = any || M.n2g[n * M.nd + a] >= 0;
+        if (!any) continue;
+        int k = 0;
+        if (!node_neighbours(M, n, nb, k)) { atomicExch(err, 1); continue; }
+        off[0] = 0;   // first column of each neighbour's free dofs
+        for (int q = 0; q < k; q++) {
+            int c = 0;
+            for (int b = 0; b < M.nd; b++) c += M.n2g[(long long)nb[q] * M.nd + b] >= 0;
+            off[q + 1] = off[q] + c;
+        }
+        const int nc = off[k];
+        for (int a = 0; a < M.nd; a++) {   // the rows of node n, one after the other
+            const int I = M.n2g[n * M.nd + a];
+            if (I < 0) continue;
+            for (int c = 0; c < nc; c++) vals[c] = 0.0;
+            double f = 0.0;
+            for (int p = M.adj_ptr[n]; p < M.adj_ptr[n + 1]; p++) {   // ascending element order
+                const long long e = M.adj[p];
+                int i = 0;
+                while (i < M.nen && M.conn[e * M.nen + i] != n) i++;
+                const double *K = Ke + e * (long long)M.nk * M.nk + (long long)(i * M.nd + a) * M.nk;
+                for (int j = 0; j < M.nen; j++) {
+                    const int m = M.conn[e * M.nen + j];
+                    int lo = 0, hi = k;   // m's place among the neighbours
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (nb[mid] < m) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    int c = off[lo];
+                    for (int b = 0; b < M.nd; b++) {
+                        const long long u = (long long)m * M.nd + b;
+                        const double kv = K[j * M.nd + b];
+                        if (M.n2g[u] >= 0) {
+                            vals[c] = __dadd_rn(vals[c], kv);
+                            c++;
+                        } else {
+                            f = __dsub_rn(f, __dmul_rn(kv, ufix[u]));
                         }
-                        vals[lo] = __dadd_rn(vals[lo], kv);
-                    } else {
-                        f = __dsub_rn(f, __dmul_rn(kv, ufix[u]));
                     }
                 }
+                if (Fbody) f = __dadd_rn(f, Fbody[e * M.nk + i * M.nd + a]);   // the element's body force
             }
-            if (Fbody) f = __dadd_rn(f, Fbody[e * M.nk + i * M.nd + a]);   // the element's body force
+            // point loads, then edge tractions: both lists are sorted by node, stably, so a
+            // node's entries keep their list (edge) order
+            for (int l = first_of(lnode, nload, (int)n); l < nload && lnode[l] == n; l++)
+                if (ldof[l] == a) f = __dadd_rn(f, lval[l]);
+            for (int l = first_of(enode, 2 * nedge, (int)n); l < 2 * nedge && enode[l] == n; l++)
+                f = __dadd_rn(f, Fedge[eslot[l] + a]);
+            const int base = indptr[I];
+            int dg = -1, c = 0;
+            for (int q = 0; q < k; q++)
+                for (int b = 0; b < M.nd; b++) {
+                    const int J = M.n2g[(long long)nb[q] * M.nd + b];
+                    if (J < 0) continue;
+                    indices[base + c] = J;
+                    data[base + c] = vals[c];
+                    if (J == I) dg = base + c;
+                    c++;
+                }
+            diag[I] = dg;
+            F[I] = f;
         }
-        for (int l = 0; l < nload; l++)
-            if (lnode[l] == n && ldof[l] == a) f = __dadd_rn(f, lval[l]);
-        for (int k = 0; k < nedge; k++)   // edge tractions after the point loads, in edge order
-            for (int q = 0; q < 2; q++)
-                if (edges[2 * k + q] == n) f = __dadd_rn(f, Fedge[4 * k + 2 * q + a]);
-        const int base = indptr[I];
-        int dg = -1;
-        for (int k = 0; k < nc; k++) {
-            indices[base + k] = cols[k];
-            data[base + k] = vals[k];
-            if (cols[k] == I) dg = base + k;
-        }
-        diag[I] = dg;
-        F[I] = f;
     }
 }
 
@@ -270,10 +303,13 @@ struct FemMesh {
     double *Fbody = nullptr;       // ne x nk
     int nedge = 0;
     int *edges = nullptr;
+    int *enode = nullptr, *eslot = nullptr;   // edge ends sorted by node: node, 4 k + 2 q
     double etx = 0.0, ety = 0.0;
     double *Fedge = nullptr;       // nedge x 4
     std::vector<void *> allocs;
     Ctx *c = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};   // phases of the last assembly
+    double ms[3] = {0.0, 0.0, 0.0};                             // element matrices, pattern, values
 };
 
 static psf_status fem_alloc(FemMesh *f, void **p, size_t bytes) {
@@ -294,9 +330,9 @@ static psf_status scan_ints(FemMesh *f, long long n, const int *in, int *out, in
     PSF_CHECK(fem_alloc(f, (void **)&bs, sizeof(int) * (nb + 1)));
     PSF_CHECK(fem_alloc(f, (void **)&tot, sizeof(int)));
     cudaStream_t s = f->c->stream;
-    if (nb > 0) scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(n, in, out, bs);
-    scan_sums<<<1, 32, 0, s>>>((int)nb, bs, tot);
-    if (nb > 0) scan_add<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, out, bs);
+    if (nb > 0) (scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(n, in, out, bs), ::psf::note_launch());
+    (scan_sums<<<1, 32, 0, s>>>((int)nb, bs, tot), ::psf::note_launch());
+    if (nb > 0) (scan_add<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, out, bs), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaMemcpyAsync(total, tot, sizeof(int), cudaMemcpyDeviceToHost, s));
     PSF_CUDA(cudaStreamSynchronize(s));
@@ -353,6 +389,7 @@ psf_status psf_fem_create(int kind, long long nnodes, const double *coords, long
     A(fem_alloc(f, (void **)&f->fixed, nnodes * f->nd));
     A(fem_alloc(f, (void **)&f->ufix, sizeof(double) * nnodes * f->nd));
     A(fem_alloc(f, (void **)&f->n2g, sizeof(int) * nnodes * f->nd));
+    for (auto &e : f->ev) A(cuda_status(cudaEventCreate(&e), "event"));
     int *cnt = nullptr, *pos = nullptr;
     A(fem_alloc(f, (void **)&cnt, sizeof(int) * (nnodes + 1)));
     A(fem_alloc(f, (void **)&pos, sizeof(int) * (nnodes + 1)));
@@ -366,11 +403,11 @@ psf_status psf_fem_create(int kind, long long nnodes, const double *coords, long
         A(cuda_status(cudaMemsetAsync(f->fixed, 0, nnodes * f->nd, s), "memset"));
         A(cuda_status(cudaMemsetAsync(f->ufix, 0, sizeof(double) * nnodes * f->nd, s), "memset"));
         if (st == PSF_OK) {
-            adj_count<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(nelem, nen, f->conn, cnt);
+            (adj_count<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(nelem, nen, f->conn, cnt), ::psf::note_launch());
             int total = 0;
             A(scan_ints(f, nnodes + 1, cnt, f->adj_ptr, &total));
-            adj_fill<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(nelem, nen, f->conn, f->adj_ptr, pos, f->adj);
-            adj_sort<<<grid_for(nnodes, 256, 65536), 256, 0, s>>>(nnodes, f->adj_ptr, f->adj);
+            (adj_fill<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(nelem, nen, f->conn, f->adj_ptr, pos, f->adj), ::psf::note_launch());
+            (adj_sort<<<grid_for(nnodes, 256, 65536), 256, 0, s>>>(nnodes, f->adj_ptr, f->adj), ::psf::note_launch());
             A(cuda_status(cudaGetLastError(), "adjacency"));
         }
     }
@@ -378,6 +415,8 @@ psf_status psf_fem_create(int kind, long long nnodes, const double *coords, long
     fem_release(f, pos);
     if (st != PSF_OK) {
         for (void *p : f->allocs) cudaFree(p);
+        for (auto e : f->ev)
+            if (e) cudaEventDestroy(e);
         delete h;
         return st;
     }
@@ -389,6 +428,8 @@ psf_status psf_fem_destroy(psf_fem *h) {
     if (!h) return PSF_OK;
     cudaStreamSynchronize(h->m.c->stream);
     for (void *p : h->m.allocs) cudaFree(p);
+    for (auto e : h->m.ev)
+        if (e) cudaEventDestroy(e);
     delete h;
     return PSF_OK;
 }
@@ -417,13 +458,13 @@ psf_status psf_fem_set_dirichlet(psf_fem *h, int n, const int32_t *node, const i
         PSF_CUDA(cudaMemcpyAsync(dn, node, sizeof(int) * n, cudaMemcpyHostToDevice, s));
         PSF_CUDA(cudaMemcpyAsync(dd, dof, sizeof(int) * n, cudaMemcpyHostToDevice, s));
         if (value) PSF_CUDA(cudaMemcpyAsync(dv, value, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-        mark_fixed_kernel<<<1, 32, 0, s>>>(n, dn, dd, value ? dv : nullptr, f->nd, f->fixed, f->ufix);
+        (mark_fixed_kernel<<<1, 32, 0, s>>>(n, dn, dd, value ? dv : nullptr, f->nd, f->fixed, f->ufix), ::psf::note_launch());
     }
-    free_flags_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->fixed, flags);
+    (free_flags_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->fixed, flags), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     int total = 0;
     PSF_CHECK(scan_ints(f, nt, flags, f->n2g, &total));
-    numbering_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->fixed, f->n2g);
+    (numbering_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->fixed, f->n2g), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaStreamSynchronize(s));
     for (void *p : {(void *)dn, (void *)dd, (void *)dv, (void *)flags}) fem_release(f, p);
@@ -439,6 +480,18 @@ psf_status psf_fem_set_loads(psf_fem *h, int n, const int32_t *node, const int32
     FEM_CHECK(h);
     FemMesh *f = &h->m;
     if (n < 0 || (n > 0 && (!node || !dof || !value))) { set_error("psf_fem_set_loads: invalid arrays"); return PSF_BAD_INPUT; }
+    for (int k = 0; k < n; k++)
+        if (node[k] < 0 || node[k] >= f->nn || dof[k] < 0 || dof[k] >= f->nd) {
+            set_error("psf_fem_set_loads: (node, dof) out of range");
+            return PSF_BAD_INPUT;
+        }
+    // sorted by node, stably: the assembly walks a node's loads in list order
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return node[x] < node[y]; });
+    std::vector<int> sn(n), sd(n);
+    std::vector<double> sv(n);
+    for (int k = 0; k < n; k++) { sn[k] = node[order[k]]; sd[k] = dof[order[k]]; sv[k] = value[order[k]]; }
     for (void *p : {(void *)f->lnode, (void *)f->ldof, (void *)f->lval}) fem_release(f, p);
     f->lnode = nullptr; f->ldof = nullptr; f->lval = nullptr;
     PSF_CHECK(fem_alloc(f, (void **)&f->lnode, sizeof(int) * (n + 1)));
@@ -446,9 +499,9 @@ psf_status psf_fem_set_loads(psf_fem *h, int n, const int32_t *node, const int32
     PSF_CHECK(fem_alloc(f, (void **)&f->lval, sizeof(double) * (n + 1)));
     cudaStream_t s = f->c->stream;
     if (n > 0) {
-        PSF_CUDA(cudaMemcpyAsync(f->lnode, node, sizeof(int) * n, cudaMemcpyHostToDevice, s));
-        PSF_CUDA(cudaMemcpyAsync(f->ldof, dof, sizeof(int) * n, cudaMemcpyHostToDevice, s));
-        PSF_CUDA(cudaMemcpyAsync(f->lval, value, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        PSF_CUDA(cudaMemcpyAsync(f->lnode, sn.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        PSF_CUDA(cudaMemcpyAsync(f->ldof, sd.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        PSF_CUDA(cudaMemcpyAsync(f->lval, sv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     }
     PSF_CUDA(cudaStreamSynchronize(s));
     f->nload = n;
@@ -480,17 +533,28 @@ psf_status psf_fem_set_edge_loads(psf_fem *h, int nedge, const int32_t *edges, d
     if (nedge < 0 || (nedge > 0 && !edges)) { set_error("psf_fem_set_edge_loads: invalid edges"); return PSF_BAD_INPUT; }
     for (int k = 0; k < 2 * nedge; k++)
         if (edges[k] < 0 || edges[k] >= f->nn) { set_error("psf_fem_set_edge_loads: node out of range"); return PSF_BAD_INPUT; }
-    fem_release(f, f->edges);
-    fem_release(f, f->Fedge);
+    for (void *p : {(void *)f->edges, (void *)f->Fedge, (void *)f->enode, (void *)f->eslot}) fem_release(f, p);
     f->edges = nullptr;
     f->Fedge = nullptr;
+    f->enode = nullptr;
+    f->eslot = nullptr;
     f->nedge = nedge;
     f->etx = tx;
     f->ety = ty;
     if (nedge > 0) {
+        // the edge ends sorted by node, stably, so a node's tractions keep the edge order
+        std::vector<int> order(2 * (size_t)nedge), en(2 * (size_t)nedge), es(2 * (size_t)nedge);
+        for (int k = 0; k < 2 * nedge; k++) order[k] = k;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return edges[x] < edges[y]; });
+        for (int k = 0; k < 2 * nedge; k++) { en[k] = edges[order[k]]; es[k] = 2 * order[k]; }   // 4 e + 2 q
         PSF_CHECK(fem_alloc(f, (void **)&f->edges, sizeof(int) * 2 * nedge));
-        PSF_CUDA(cudaMemcpyAsync(f->edges, edges, sizeof(int) * 2 * nedge, cudaMemcpyHostToDevice, f->c->stream));
-        PSF_CUDA(cudaStreamSynchronize(f->c->stream));
+        PSF_CHECK(fem_alloc(f, (void **)&f->enode, sizeof(int) * 2 * nedge));
+        PSF_CHECK(fem_alloc(f, (void **)&f->eslot, sizeof(int) * 2 * nedge));
+        cudaStream_t s = f->c->stream;
+        PSF_CUDA(cudaMemcpyAsync(f->edges, edges, sizeof(int) * 2 * nedge, cudaMemcpyHostToDevice, s));
+        PSF_CUDA(cudaMemcpyAsync(f->enode, en.data(), sizeof(int) * 2 * nedge, cudaMemcpyHostToDevice, s));
+        PSF_CUDA(cudaMemcpyAsync(f->eslot, es.data(), sizeof(int) * 2 * nedge, cudaMemcpyHostToDevice, s));
+        PSF_CUDA(cudaStreamSynchronize(s));
     }
     return PSF_OK;
 }
@@ -503,9 +567,10 @@ psf_status psf_fem_assemble(psf_fem *h, const double *E, double V, double t, lon
     if (!f->have_bc) { set_error("psf_fem_assemble: call psf_fem_set_dirichlet first"); return PSF_BAD_INPUT; }
     cudaStream_t s = f->c->stream;
     PSF_CUDA(cudaMemcpyAsync(f->E, E, sizeof(double) * f->ne, cudaMemcpyHostToDevice, s));
+    PSF_CUDA(cudaEventRecord(f->ev[0], s));
     PSF_CHECK(fem_element_matrices(s, f->kind, f->ne, f->nen, f->conn, f->coords, f->E, V, t, f->Ke));
+    PSF_CUDA(cudaEventRecord(f->ev[1], s));
     const MeshArgs M = mesh_args(f);
-    const long long nt = f->nn * f->nd;
     int *err = nullptr;
     PSF_CHECK(fem_alloc(f, (void **)&err, sizeof(int)));
     PSF_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
@@ -515,7 +580,7 @@ psf_status psf_fem_assemble(psf_fem *h, const double *E, double V, double t, lon
         int *cnt = nullptr;
         PSF_CHECK(fem_alloc(f, (void **)&cnt, sizeof(int) * (f->nfree + 1)));
         PSF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (f->nfree + 1), s));
-        pattern_count_kernel<<<grid_for(nt, 128, 65536), 128, 0, s>>>(M, cnt, err);
+        (pattern_count_kernel<<<grid_for(f->nn, 128, 65536), 128, 0, s>>>(M, cnt, err), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
         PSF_CHECK(fem_alloc(f, (void **)&f->indptr, sizeof(int) * (f->nfree + 1)));
         int total = 0;
@@ -527,6 +592,7 @@ psf_status psf_fem_assemble(psf_fem *h, const double *E, double V, double t, lon
         PSF_CHECK(fem_alloc(f, (void **)&f->diag, sizeof(int) * (f->nfree + 1)));
         PSF_CHECK(fem_alloc(f, (void **)&f->F, sizeof(double) * (f->nfree + 1)));
     }
+    PSF_CUDA(cudaEventRecord(f->ev[2], s));
     if (f->body) {
         if (!f->Fbody) PSF_CHECK(fem_alloc(f, (void **)&f->Fbody, sizeof(double) * f->ne * f->nk));
         PSF_CHECK(fem_body_forces(s, f->kind, f->ne, f->nen, f->conn, f->coords, f->bfx, f->bfy, t, f->Fbody));
@@ -535,18 +601,35 @@ psf_status psf_fem_assemble(psf_fem *h, const double *E, double V, double t, lon
         if (!f->Fedge) PSF_CHECK(fem_alloc(f, (void **)&f->Fedge, sizeof(double) * 4 * f->nedge));
         PSF_CHECK(fem_edge_forces(s, f->nedge, f->edges, f->coords, f->etx, f->ety, t, f->Fedge));
     }
-    assemble_rows_kernel<<<grid_for(nt, 128, 65536), 128, 0, s>>>(M, f->Ke, f->ufix, f->nload, f->lnode, f->ldof,
+    (assemble_rows_kernel<<<grid_for(f->nn, 128, 65536), 128, 0, s>>>(M, f->Ke, f->ufix, f->nload, f->lnode, f->ldof,
                                                                   f->lval, f->body ? f->Fbody : nullptr, f->nedge,
-                                                                  f->edges, f->Fedge, f->indptr, f->indices, f->data,
-                                                                  f->F, f->diag, err);
+                                                                  f->enode, f->eslot, f->Fedge, f->indptr, f->indices,
+                                                                  f->data,
+                                                                  f->F, f->diag, err), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
+    PSF_CUDA(cudaEventRecord(f->ev[3], s));
     int herr = 0;
     PSF_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     PSF_CUDA(cudaStreamSynchronize(s));
     fem_release(f, err);
-    if (herr) { set_error("psf_fem_assemble: a row has more than 256 distinct columns"); return PSF_BAD_INPUT; }
+    for (int k = 0; k < 3; k++) {
+        float ms = 0.0f;
+        PSF_CUDA(cudaEventElapsedTime(&ms, f->ev[k], f->ev[k + 1]));
+        f->ms[k] = ms;
+    }
+    if (herr) { set_error("psf_fem_assemble: a node shares elements with more than 96 other nodes"); return PSF_BAD_INPUT; }
     f->have_sys = true;
     if (nnz) *nnz = f->nnz;
+    return PSF_OK;
+}
+
+psf_status psf_fem_timings(psf_fem *h, double *element_ms, double *pattern_ms, double *values_ms) {
+    using namespace psf;
+    FEM_CHECK(h);
+    if (!h->m.have_sys) { set_error("psf_fem_timings: assemble first"); return PSF_BAD_INPUT; }
+    if (element_ms) *element_ms = h->m.ms[0];
+    if (pattern_ms) *pattern_ms = h->m.ms[1];
+    if (values_ms) *values_ms = h->m.ms[2];
     return PSF_OK;
 }
 
@@ -589,7 +672,7 @@ psf_status psf_fem_solve(psf_fem *h, int solver, int itmax, double eps, double *
     psf_status st = pcg_csr_any(c, n, f->indptr, f->indices, f->diag, f->data, f->F, x, w,
                                 solver == PSF_SOLVE_CSR_JACOBI_F64 ? 1 : 0, itmax, eps, &it, &rr, &bb, &conv);
     if (st == PSF_OK) {
-        scatter_u_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->n2g, x, f->ufix, u);
+        (scatter_u_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->n2g, x, f->ufix, u), ::psf::note_launch());
         st = cuda_status(cudaGetLastError(), "scatter");
     }
     if (st == PSF_OK) st = cuda_status(cudaMemcpyAsync(u_nodal, u, sizeof(double) * nt, cudaMemcpyDeviceToHost, s), "copy");
@@ -621,7 +704,7 @@ psf_status psf_fem_reaction(psf_fem *h, const double *u_nodal, double *r_nodal) 
     PSF_CHECK(fem_alloc(f, (void **)&u, sizeof(double) * nt));
     PSF_CHECK(fem_alloc(f, (void **)&r, sizeof(double) * nt));
     PSF_CUDA(cudaMemcpyAsync(u, u_nodal, sizeof(double) * nt, cudaMemcpyHostToDevice, s));
-    reaction_kernel<<<grid_for(nt, 128, 65536), 128, 0, s>>>(mesh_args(f), f->Ke, u, r);
+    (reaction_kernel<<<grid_for(nt, 128, 65536), 128, 0, s>>>(mesh_args(f), f->Ke, u, r), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaMemcpyAsync(r_nodal, r, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
     PSF_CUDA(cudaStreamSynchronize(s));

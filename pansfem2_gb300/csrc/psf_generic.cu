@@ -101,7 +101,7 @@ psf_status psf_csr_spmv(int n, const int32_t *indptr, const int32_t *indices, co
     PSF_CUDA(cudaMemcpyAsync(di, indices, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dd, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    spmv_rows<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, dp, di, dd, dx, dy);
+    (spmv_rows<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, dp, di, dd, dx, dy), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     for (void *p : {(void *)dp, (void *)di, (void *)dd, (void *)dx, (void *)dy}) PSF_CUDA(cudaFreeAsync(p, s));
@@ -135,7 +135,7 @@ psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, c
     PSF_CUDA(cudaMemcpyAsync(di, indices, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dd, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    diag_positions<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, dp, di, dg);
+    (diag_positions<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, dp, di, dg), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     c->ksec = 0.0;
     c->klaunch = 0;
@@ -194,7 +194,7 @@ psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const 
     PSF_CUDA(cudaMemcpyAsync(di, idx, sizeof(int) * m, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dw, w, sizeof(double) * m, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dinp, in, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    list_filter_kernel<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, dp, di, dw, dinp, dout);
+    (list_filter_kernel<<<grid_for(n, 256, 65536), 256, 0, s>>>(n, dp, di, dw, dinp, dout), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     for (void *p : {(void *)dp, (void *)di, (void *)dw, (void *)dinp, (void *)dout}) PSF_CUDA(cudaFreeAsync(p, s));

@@ -561,10 +561,10 @@ psf_status learned_attach(Ctx *c, unet::Net *net, int pre_mg, int nu_pre, int nu
 // per-solve inputs of the preconditioner that depend on the design: D^-1/2 and the density feature
 static psf_status lp_refresh(Ctx *c, Learned *L) {
     const int gb = 4 * std::max(c->num_sms, 1);
-    isd_kernel<<<gb, 256, 0, c->stream>>>(c->ndofs, c->Dl1f, c->fixed, L->isd);
+    (isd_kernel<<<gb, 256, 0, c->stream>>>(c->ndofs, c->Dl1f, c->fixed, L->isd), ::psf::note_launch());
     const double E1 = c->simp_ready && c->prm.E1 > 0 ? c->prm.E1 : 1.0;
     L->inv_e1 = (float)(1.0 / E1);
-    rho_node_kernel<<<gb, 256, 0, c->stream>>>(c->nx, c->ny, c->Epad, E1, L->rho);
+    (rho_node_kernel<<<gb, 256, 0, c->stream>>>(c->nx, c->ny, c->Epad, E1, L->rho), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -581,10 +581,10 @@ static psf_status lp_pre(Ctx *c, Learned *L, const double *r, const int *fl, flo
     if (L->pre_mg) return mg_apply(c, r, L->r32, L->xa, fl);
     const Geo g = lp_geo(c);
     const KeT<float> Kf = lp_ke<float>(c);
-    lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, r, c->Dl1f, c->fixed, L->r32, L->xa, fl);
+    (lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, r, c->Dl1f, c->fixed, L->r32, L->xa, fl), ::psf::note_launch());
     for (int k = 1; k < L->nu_pre; k++) {
-        lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, *cur,
-                                                               *oth, fl);
+        (lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, *cur,
+                                                               *oth, fl), ::psf::note_launch());
         std::swap(*cur, *oth);
     }
     PSF_CUDA(cudaGetLastError());
@@ -600,24 +600,24 @@ static psf_status lp_precond(Ctx *c, Learned *L, const double *r, double *z, con
     float *cur, *oth;
     PSF_CHECK(lp_pre<KIND>(c, L, r, fl, &cur, &oth));
     if (L->use_net) {
-        lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
-                                                               L->part, fl);
-        nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho,
-                                                              L->nnin, L->sc, fl, c->ny, c->Epadf, L->inv_e1);
+        (lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
+                                                               L->part, fl), ::psf::note_launch());
+        (nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho,
+                                                              L->nnin, L->sc, fl, c->ny, c->Epadf, L->inv_e1), ::psf::note_launch());
         L->net->stream = st;
         L->net->skip = fl;
         PSF_CHECK(L->net->forward(1, L->nnin));
-        nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc,
-                                                               L->net->out_scale, L->dcorr, fl);
-        nn_step_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->dcorr, L->r1, L->part, fl);
-        nn_add_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, L->part, L->dcorr, cur, L->sc, fl);
+        (nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc,
+                                                               L->net->out_scale, L->dcorr, fl), ::psf::note_launch());
+        (nn_step_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->dcorr, L->r1, L->part, fl), ::psf::note_launch());
+        (nn_add_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, L->part, L->dcorr, cur, L->sc, fl), ::psf::note_launch());
     }
     for (int k = 1; k < L->nu_post; k++) {
-        lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl);
+        (lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl), ::psf::note_launch());
         std::swap(cur, oth);
     }
-    lp_last_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur,
-                                                          L->nu_post > 0 ? 1 : 0, z, qprev, L->part, fl);
+    (lp_last_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur,
+                                                          L->nu_post > 0 ? 1 : 0, z, qprev, L->part, fl), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -631,11 +631,11 @@ static psf_status lp_iteration(Ctx *c, Learned *L, double *x, double *r, double 
     const long long nd = c->ndofs;
     const int *fl = L->flags;
     PSF_CHECK(lp_precond<KIND>(c, L, r, z, q, fl));
-    fcg_dir_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, z, p, L->sc, fl);
-    fcg_op_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, p, q, r, L->part, fl);
+    (fcg_dir_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, z, p, L->sc, fl), ::psf::note_launch());
+    (fcg_op_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, p, q, r, L->part, fl), ::psf::note_launch());
     // the step writes |r|^2 partials into the upper half so that the (p.q, r.p) partials stay readable
-    fcg_step_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, p, q, x, r, L->part + 2 * kLpBlocks, L->sc, fl);
-    fcg_check_kernel<<<1, 32, 0, st>>>(L->part + 2 * kLpBlocks, L->sc, L->flags);
+    (fcg_step_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, p, q, x, r, L->part + 2 * kLpBlocks, L->sc, fl), ::psf::note_launch());
+    (fcg_check_kernel<<<1, 32, 0, st>>>(L->part + 2 * kLpBlocks, L->sc, L->flags), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -704,12 +704,13 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     PSF_CUDA(cudaEventRecord(c->evk0, st));
     for (int pass = 0; pass < 3 && total < limit; pass++) {
         passes++;
-        lp_residual_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, c->Fn, x, r, L->part);
-        lp_start_kernel<<<1, 32, 0, st>>>(L->part, eps, limit - total, L->sc, L->flags);
+        (lp_residual_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, c->Fn, x, r, L->part), ::psf::note_launch());
+        (lp_start_kernel<<<1, 32, 0, st>>>(L->part, eps, limit - total, L->sc, L->flags), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
         for (;;) {
             for (int k = 0; k < 2; k++) PSF_CUDA(cudaGraphLaunch(L->exec, st));
             glaunch += 2;
+            note_launch(2 * (long long)L->graph_nodes);
             PSF_CUDA(cudaMemcpyAsync(L->hflags, L->flags, sizeof(int) * F_N, cudaMemcpyDeviceToHost, st));
             PSF_CUDA(cudaStreamSynchronize(st));
             if (L->hflags[F_DONE]) break;
@@ -1037,11 +1038,11 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     float *cur, *oth;
     if (L->pre_mg) PSF_CHECK(mg_prepare(c));
     PSF_CHECK(lp_pre<KIND>(c, L, r, L->flags, &cur, &oth));
-    lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
-                                                           L->part, L->flags);
-    nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho, in_out,
-                                                          L->sc, L->flags, c->ny, c->Epadf, L->inv_e1);
-    f32_to_f64_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->r1, rhs64);
+    (lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
+                                                           L->part, L->flags), ::psf::note_launch());
+    (nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho, in_out,
+                                                          L->sc, L->flags, c->ny, c->Epadf, L->inv_e1), ::psf::note_launch());
+    (f32_to_f64_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->r1, rhs64), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     // e = K^-1 r1 with the multigrid FCG to 1e-8 (its right-hand side is the context's nodal load vector)
     double *Fn_saved = c->Fn;
@@ -1052,11 +1053,11 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     if (s == PSF_NOT_CONVERGED) return PSF_NOT_CONVERGED;   // the caller skips this pair
     if (s != PSF_OK) return s;
     PSF_CUDA(cudaMemcpyAsync(e64, c->un, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st));
-    tgt_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, e64, L->isd, L->sc, tgt_out, mask_out, L->part);
-    mask_scale_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes * 2, L->part, mask_out);
-    pair_extra_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, L->r1, L->isd, L->sc, tgt_out,
-                                                        ts->rhat + slot * P * 2, ts->isd + slot * P * 2, L->part);
-    fold_to_kernel<<<1, 32, 0, st>>>(L->part, ts->cden + slot);
+    (tgt_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, e64, L->isd, L->sc, tgt_out, mask_out, L->part), ::psf::note_launch());
+    (mask_scale_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes * 2, L->part, mask_out), ::psf::note_launch());
+    (pair_extra_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, L->r1, L->isd, L->sc, tgt_out,
+                                                        ts->rhat + slot * P * 2, ts->isd + slot * P * 2, L->part), ::psf::note_launch());
+    (fold_to_kernel<<<1, 32, 0, st>>>(L->part, ts->cden + slot), ::psf::note_launch());
     PSF_CUDA(cudaMemcpyAsync(ts->epad + slot * Pe, c->Epadf, sizeof(float) * Pe, cudaMemcpyDeviceToDevice, st));
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -1195,8 +1196,8 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
     if (ts->scale_n != ts->n || !(ts->out_scale > 0.0)) {
         double *part = nullptr;
         PSF_CUDA(cudaMalloc(&part, sizeof(double) * 2 * psf::kLpBlocks));
-        psf::tgt_rms_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>((long long)ts->n * P * 2, ts->tgt, ts->mask,
-                                                                        part);
+        (psf::tgt_rms_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>((long long)ts->n * P * 2, ts->tgt, ts->mask,
+                                                                        part), ::psf::note_launch());
         std::vector<double> h(2 * psf::kLpBlocks);
         cudaError_t e = cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1226,8 +1227,8 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
             s = psf::cuda_status(cudaMemcpyAsync(net.t[0] + b * P * 8, ts->in + i * P * 8, sizeof(psf::unet::bf16) * P * 8,
                                                  cudaMemcpyDeviceToDevice, st), "copy");
             if (s == PSF_OK) {
-                psf::scale_copy_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
-                    (long long)P * 2, ts->tgt + i * P * 2, (float)(1.0 / ts->out_scale), tgt + b * P * 2);
+                (psf::scale_copy_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (long long)P * 2, ts->tgt + i * P * 2, (float)(1.0 / ts->out_scale), tgt + b * P * 2), ::psf::note_launch());
                 s = psf::cuda_status(cudaGetLastError(), "scale_copy_kernel");
             }
             if (s == PSF_OK)
@@ -1256,28 +1257,28 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
         if (s == PSF_OK && loss_mode == 1) {
             const int nx = ts->H - 1, ny = ts->W - 1;
             if (ts->kind == PSF_Q4_HEAT)
-                psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                (psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                     nx, ny, Kf, batch, net.out32, rhat, isdb, epad, cden, net.out_scale, net.g[psf::unet::kTensors - 1],
-                    epart);
+                    epart), ::psf::note_launch());
             else
-                psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                (psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                     nx, ny, Kf, batch, net.out32, rhat, isdb, epad, cden, net.out_scale, net.g[psf::unet::kTensors - 1],
-                    epart);
-            psf::energy_loss_kernel<<<1, 32, 0, st>>>(epart, batch, dl + k);
+                    epart), ::psf::note_launch());
+            (psf::energy_loss_kernel<<<1, 32, 0, st>>>(epart, batch, dl + k), ::psf::note_launch());
             s = psf::cuda_status(cudaGetLastError(), "energy loss");
         }
         if (s == PSF_OK && loss_mode == 2) {
             const int nx = ts->H - 1, ny = ts->W - 1;
             float *ky = tgt;   // the MSE target buffer is free in this mode
             if (ts->kind == PSF_Q4_HEAT)
-                psf::angle_ab_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
-                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, net.out_scale, ky, epart);
+                (psf::angle_ab_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, net.out_scale, ky, epart), ::psf::note_launch());
             else
-                psf::angle_ab_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
-                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, net.out_scale, ky, epart);
-            psf::angle_grad_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                (psf::angle_ab_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    nx, ny, Kf, batch, net.out32, rhat, isdb, epad, net.out_scale, ky, epart), ::psf::note_launch());
+            (psf::angle_grad_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                 (long long)P, batch, epart, cden, rhat, ky, isdb, net.out_scale, net.g[psf::unet::kTensors - 1],
-                dl + k);
+                dl + k), ::psf::note_launch());
             s = psf::cuda_status(cudaGetLastError(), "scale-free energy loss");
         }
         if (s == PSF_OK) s = net.backward(batch, nullptr);
@@ -1400,26 +1401,26 @@ psf_status psf_learned_eval(psf_unet *u, psf_trainset *ts, int first, int count,
             float *gsc = net.g[psf::unet::kTensors - 1];   // scratch: the output gradient is not needed
             if (mode == 1) {
                 if (ts->kind == PSF_Q4_HEAT)
-                    psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (psf::energy_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                         nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
-                        ts->epad + j * Pe, ts->cden + j, net.out_scale, gsc, part);
+                        ts->epad + j * Pe, ts->cden + j, net.out_scale, gsc, part), ::psf::note_launch());
                 else
-                    psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (psf::energy_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                         nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
-                        ts->epad + j * Pe, ts->cden + j, net.out_scale, gsc, part);
-                psf::energy_loss_kernel<<<1, 32, 0, st>>>(part, 1, dl + i0 + b);
+                        ts->epad + j * Pe, ts->cden + j, net.out_scale, gsc, part), ::psf::note_launch());
+                (psf::energy_loss_kernel<<<1, 32, 0, st>>>(part, 1, dl + i0 + b), ::psf::note_launch());
             } else {
                 if (ts->kind == PSF_Q4_HEAT)
-                    psf::angle_ab_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (psf::angle_ab_kernel<PSF_Q4_HEAT><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                         nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
-                        ts->epad + j * Pe, net.out_scale, ky, part);
+                        ts->epad + j * Pe, net.out_scale, ky, part), ::psf::note_launch());
                 else
-                    psf::angle_ab_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                    (psf::angle_ab_kernel<PSF_Q4_PLANE_STRAIN><<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                         nx, ny, Kf, 1, net.out32 + b * P * 2, ts->rhat + j * P * 2, ts->isd + j * P * 2,
-                        ts->epad + j * Pe, net.out_scale, ky, part);
-                psf::angle_grad_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
+                        ts->epad + j * Pe, net.out_scale, ky, part), ::psf::note_launch());
+                (psf::angle_grad_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
                     (long long)P, 1, part, ts->cden + j, ts->rhat + j * P * 2, ky, ts->isd + j * P * 2, net.out_scale,
-                    gsc, dl + i0 + b);
+                    gsc, dl + i0 + b), ::psf::note_launch());
             }
             s = psf::cuda_status(cudaGetLastError(), "energy loss");
         }

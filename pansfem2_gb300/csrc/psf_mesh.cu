@@ -40,6 +40,7 @@ psf_status read_sync_status(Ctx *c) {
 psf_status launch_coop(Ctx *c, const void *fn, int blocks, int threads, void **args, size_t smem) {
     PSF_CHECK(reset_sync(c));
     PSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, smem, c->stream));
+    note_launch();
     return PSF_OK;
 }
 
@@ -121,9 +122,9 @@ static psf_status exclusive_scan(Ctx *c, const int *in, long long n, int *out, l
     PSF_CUDA(cudaMallocAsync((void **)&ovf, sizeof(int), c->stream));
     tot_d = sums + nb;
     PSF_CUDA(cudaMemsetAsync(ovf, 0, sizeof(int), c->stream));
-    scan_tile_sums<<<nb, kScanThreads, 0, c->stream>>>(in, n, sums);
-    scan_sums<<<1, 1024, 0, c->stream>>>(sums, nb, tot_d);
-    scan_write<<<nb, kScanThreads, 0, c->stream>>>(in, n, sums, out, ovf);
+    (scan_tile_sums<<<nb, kScanThreads, 0, c->stream>>>(in, n, sums), ::psf::note_launch());
+    (scan_sums<<<1, 1024, 0, c->stream>>>(sums, nb, tot_d), ::psf::note_launch());
+    (scan_write<<<nb, kScanThreads, 0, c->stream>>>(in, n, sums, out, ovf), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     long long tot = 0;
     int o = 0;
@@ -456,20 +457,20 @@ psf_status set_dirichlet(Ctx *c, int n, const int *node, const int *dof, const d
             PSF_CUDA(cudaMallocAsync((void **)&dv, sizeof(double) * n, c->stream));
             PSF_CUDA(cudaMemcpyAsync(dv, value, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
         }
-        mark_fixed<<<grid_for(n, 256), 256, 0, c->stream>>>(dn, dd, dv, n, c->ndof, c->fixed, c->ufixed);
+        (mark_fixed<<<grid_for(n, 256), 256, 0, c->stream>>>(dn, dd, dv, n, c->ndof, c->fixed, c->ufixed), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
     }
     int *flag = nullptr, *prefix = nullptr;
     PSF_CUDA(cudaMallocAsync((void **)&flag, sizeof(int) * c->ndofs, c->stream));
     PSF_CUDA(cudaMallocAsync((void **)&prefix, sizeof(int) * c->ndofs, c->stream));
-    free_flags<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->fixed, c->ndofs, flag);
+    (free_flags<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->fixed, c->ndofs, flag), ::psf::note_launch());
     long long nfree = 0;
     PSF_CHECK(exclusive_scan(c, flag, c->ndofs, prefix, &nfree));
     c->nfree = nfree;
     if (c->g2n) { cudaFreeAsync(c->g2n, c->stream); c->g2n = nullptr; }
     PSF_CUDA(cudaMallocAsync((void **)&c->g2n, sizeof(int) * (nfree > 0 ? nfree : 1), c->stream));
-    write_numbering<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->fixed, prefix, c->ndofs, c->n2g,
-                                                                            c->g2n);
+    (write_numbering<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->fixed, prefix, c->ndofs, c->n2g,
+                                                                            c->g2n), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaFreeAsync(flag, c->stream));
     PSF_CUDA(cudaFreeAsync(prefix, c->stream));
@@ -500,7 +501,7 @@ psf_status build_pattern(Ctx *c) {
     PSF_CUDA(cudaMallocAsync((void **)&c->indptr, sizeof(int) * (c->nfree + 1), c->stream));
     PSF_CUDA(cudaMallocAsync((void **)&c->diag, sizeof(int) * (c->nfree + 1), c->stream));
     PSF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (c->nfree + 1), c->stream));
-    pattern_count<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(g, c->n2g, c->g2n, c->nfree, cnt);
+    (pattern_count<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(g, c->n2g, c->g2n, c->nfree, cnt), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     long long nnz = 0;
     PSF_CHECK(exclusive_scan(c, cnt, c->nfree + 1, c->indptr, &nnz));
@@ -510,8 +511,8 @@ psf_status build_pattern(Ctx *c) {
     if (c->data) { cudaFreeAsync(c->data, c->stream); c->data = nullptr; }
     PSF_CUDA(cudaMallocAsync((void **)&c->indices, sizeof(int) * (nnz > 0 ? nnz : 1), c->stream));
     PSF_CUDA(cudaMallocAsync((void **)&c->data, sizeof(double) * (nnz > 0 ? nnz : 1), c->stream));
-    pattern_fill<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(g, c->n2g, c->g2n, c->nfree, c->indptr,
-                                                                         c->indices, c->diag);
+    (pattern_fill<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(g, c->n2g, c->g2n, c->nfree, c->indptr,
+                                                                         c->indices, c->diag), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaStreamSynchronize(c->stream));
     c->have_csr = true;
@@ -532,7 +533,7 @@ psf_status build_rhs(Ctx *c) {
         PSF_CUDA(cudaMemcpyAsync(dn, c->load_node.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
         PSF_CUDA(cudaMemcpyAsync(dd, c->load_dof.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
         PSF_CUDA(cudaMemcpyAsync(dv, c->load_val.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-        loads_nodal<<<grid_for(n, 256), 256, 0, c->stream>>>(dn, dd, dv, n, c->ndof, c->n2g, c->Fn);
+        (loads_nodal<<<grid_for(n, 256), 256, 0, c->stream>>>(dn, dd, dv, n, c->ndof, c->n2g, c->Fn), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
         PSF_CUDA(cudaFreeAsync(dn, c->stream));
         PSF_CUDA(cudaFreeAsync(dd, c->stream));
@@ -546,9 +547,9 @@ psf_status set_moduli(Ctx *c, const double *E_dev) {
     if (E_dev != c->E)
         PSF_CUDA(cudaMemcpyAsync(c->E, E_dev, sizeof(double) * c->ne, cudaMemcpyDeviceToDevice, c->stream));
     Grid g = grid_of(c);
-    moduli_pad<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(g, c->ne, c->E, c->Ef, c->Epad, c->Epadf);
-    nodal_diag<<<grid_for(c->nnodes, 256, 65536), 256, 0, c->stream>>>(g, c->nnodes, c->Epad, (const Ke64 *)c->Ke0,
-                                                                         c->n2g, c->Dn, c->Dnf, c->Dl1f);
+    (moduli_pad<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(g, c->ne, c->E, c->Ef, c->Epad, c->Epadf), ::psf::note_launch());
+    (nodal_diag<<<grid_for(c->nnodes, 256, 65536), 256, 0, c->stream>>>(g, c->nnodes, c->Epad, (const Ke64 *)c->Ke0,
+                                                                         c->n2g, c->Dn, c->Dnf, c->Dl1f), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -560,31 +561,31 @@ psf_status assemble_values(Ctx *c, const double *E_dev) {
     Grid g = grid_of(c);
     const int lift = c->nonzero_ufixed ? 1 : 0;
     if (g.is3d)
-        assemble_rows<1><<<grid_for(c->nfree, 128, 65536), 128, 0, c->stream>>>(
-            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F);
+        (assemble_rows<1><<<grid_for(c->nfree, 128, 65536), 128, 0, c->stream>>>(
+            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F), ::psf::note_launch());
     else
-        assemble_rows<0><<<grid_for(c->nfree, 128, 65536), 128, 0, c->stream>>>(
-            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F);
+        (assemble_rows<0><<<grid_for(c->nfree, 128, 65536), 128, 0, c->stream>>>(
+            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     c->have_values = true;
     return PSF_OK;
 }
 
 psf_status spmv_csr64(Ctx *c, const double *x, double *y) {
-    spmv_csr64_kernel<<<grid_for(c->nfree * 4, 256, c->num_sms * 16), 256, 0, c->stream>>>(
-        c->nfree, c->indptr, c->indices, c->data, x, y);
+    (spmv_csr64_kernel<<<grid_for(c->nfree * 4, 256, c->num_sms * 16), 256, 0, c->stream>>>(
+        c->nfree, c->indptr, c->indices, c->data, x, y), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status gather_reduced(Ctx *c, const double *nodal, double *red) {
-    gather_kernel<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(c->g2n, c->nfree, nodal, red);
+    (gather_kernel<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(c->g2n, c->nfree, nodal, red), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status scatter_reduced(Ctx *c, const double *red, double *nodal) {
-    scatter_kernel<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->n2g, c->ndofs, red, nodal);
+    (scatter_kernel<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->n2g, c->ndofs, red, nodal), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }

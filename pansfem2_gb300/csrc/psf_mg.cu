@@ -1243,17 +1243,17 @@ static psf_status mg_setup_t(Ctx *c, MgHier *H) {
     KeF Ke = kef_of(c);
     for (int l = 1; l < H->nlev; l++) {
         MgLev &F = H->L[l - 1], &Cc = H->L[l];
-        coarse_fixed_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(F, Cc);
-        galerkin_kernel<KIND><<<grid_for(Cc.ne, 64, 65536), 64, 0, c->stream>>>(F, Cc, l - 1, Ke);
-        coarse_stencil_kernel<KIND><<<grid_for(Cc.nnodes, 128, 65536), 128, 0, c->stream>>>(Cc);
+        (coarse_fixed_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(F, Cc), ::psf::note_launch());
+        (galerkin_kernel<KIND><<<grid_for(Cc.ne, 64, 65536), 64, 0, c->stream>>>(F, Cc, l - 1, Ke), ::psf::note_launch());
+        (coarse_stencil_kernel<KIND><<<grid_for(Cc.nnodes, 128, 65536), 128, 0, c->stream>>>(Cc), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
     }
     MgLev &Lc = H->L[H->nlev - 1];
     const int n = H->nc;
     PSF_CUDA(cudaMemsetAsync(H->Ac, 0, sizeof(double) * (size_t)n * n, c->stream));
-    coarse_dense_kernel<KIND><<<grid_for(Lc.ne, 128, 4096), 128, 0, c->stream>>>(Lc, H->Ac, n);
-    dense_fix_identity<<<grid_for(n, 128), 128, 0, c->stream>>>(H->Ac, Lc.fixed, n);
-    gauss_jordan_kernel<<<1, 1024, 0, c->stream>>>(H->Ac, n);
+    (coarse_dense_kernel<KIND><<<grid_for(Lc.ne, 128, 4096), 128, 0, c->stream>>>(Lc, H->Ac, n), ::psf::note_launch());
+    (dense_fix_identity<<<grid_for(n, 128), 128, 0, c->stream>>>(H->Ac, Lc.fixed, n), ::psf::note_launch());
+    (gauss_jordan_kernel<<<1, 1024, 0, c->stream>>>(H->Ac, n), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     // the solver kernels may use up to kMaxDynSmem of dynamic shared memory (block 0's levels);
     // set here, outside any stream capture of their launches

@@ -97,7 +97,7 @@ extern "C" psf_status psf_csr_solve_noalloc(int n, const int32_t *d_indptr, cons
     double *partials = (double *)(base + kOffPart);
     GridSync *gs = (GridSync *)(base + kOffSync);
     double *out = (double *)(base + kOffOut);
-    noalloc_diag<<<grid_for(n, 256, 4096), 256, 0, s>>>(n, d_indptr, d_indices, diag);
+    (noalloc_diag<<<grid_for(n, 256, 4096), 256, 0, s>>>(n, d_indptr, d_indices, diag), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CHECK(pcg_csr_launch_raw(s, n, d_indptr, d_indices, diag, d_data, d_b, d_x, w, itmax, eps, gs, partials,
                                  kNoallocMaxBlocks, out));

@@ -547,7 +547,7 @@ psf_status filter_setup(Ctx *c, double R) {
     psf_status st = make_stencil(c, S);
     if (st != PSF_OK) { delete S; return st; }
     c->filt_n = S->n;
-    wsum_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, c->filt_wsum);
+    (wsum_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, c->filt_wsum), ::psf::note_launch());
     delete S;
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -577,8 +577,8 @@ psf_status sensitivity_filter(Ctx *c, const double *s, const double *d, int mode
     Stencil *S = new Stencil;
     psf_status st = get_stencil(c, S);
     if (st == PSF_OK) {
-        sens_filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, s, d, c->filt_wsum, mode,
-                                                                                out);
+        (sens_filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, s, d, c->filt_wsum, mode,
+                                                                                out), ::psf::note_launch());
         if (cudaGetLastError() != cudaSuccess) st = PSF_CUDA_ERROR;
     }
     delete S;
@@ -604,7 +604,7 @@ __global__ void heaviside_project_kernel(long long n, double beta, double *__res
 // rho = H(filter(s)); dH = H'(filter(s)) is kept for heaviside_back
 psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho) {
     PSF_CHECK(filter_apply(c, s, rho, false));
-    heaviside_project_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, beta, rho, c->dH);
+    (heaviside_project_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, beta, rho, c->dH), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -612,7 +612,7 @@ psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho) 
 // filtered sensitivity through the projection (HeavisideFilter.h:81-97):
 // out_i = sum_j w_ij d_j dH_j / wsum_i
 psf_status heaviside_back(Ctx *c, const double *d, double *out) {
-    mul_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, d, c->dH, c->tmp_ne);
+    (mul_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, d, c->dH, c->tmp_ne), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return filter_apply(c, c->tmp_ne, out, true);
 }
@@ -622,7 +622,7 @@ psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward) {
     Stencil *S = new Stencil;
     psf_status st = get_stencil(c, S);
     if (st == PSF_OK) {
-        filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, in, c->filt_wsum, out);
+        (filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, in, c->filt_wsum, out), ::psf::note_launch());
         if (cudaGetLastError() != cudaSuccess) st = PSF_CUDA_ERROR;
     }
     delete S;
@@ -637,22 +637,22 @@ psf_status filter_moduli(Ctx *c, const double *s, double *rho, double *E, double
     if (st != PSF_OK) { delete S; return st; }
     const int nb = grid_for(c->ne, 256, c->num_sms * 8);
     const double vscale = scale1 / (vf * (double)c->ne);
-    filter_moduli_kernel<<<nb, 256, 0, c->stream>>>(*S, c->ne, s, c->filt_wsum, E1, E0, p, vscale, rho, E, c->partials,
-                                                    c->heav, c->beta, c->dH);
+    (filter_moduli_kernel<<<nb, 256, 0, c->stream>>>(*S, c->ne, s, c->filt_wsum, E1, E0, p, vscale, rho, E, c->partials,
+                                                    c->heav, c->beta, c->dH), ::psf::note_launch());
     delete S;
-    sum_partials<<<1, 32, 0, c->stream>>>(c->partials, nb, 1.0, -1.0 * scale1, g_dev);
+    (sum_partials<<<1, 32, 0, c->stream>>>(c->partials, nb, 1.0, -1.0 * scale1, g_dev), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status moduli_from_rho(Ctx *c, const double *rho, double E1, double E0, double p, double *E_dev) {
-    moduli_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, rho, E1, E0, p, E_dev);
+    (moduli_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, rho, E1, E0, p, E_dev), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status fill(Ctx *c, double *x, long long n, double v) {
-    fill_kernel<<<grid_for(n, 256, 65536), 256, 0, c->stream>>>(n, v, x);
+    (fill_kernel<<<grid_for(n, 256, 65536), 256, 0, c->stream>>>(n, v, x), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -665,19 +665,19 @@ psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, doub
     const int nb = grid_for(c->ne, 256, c->num_sms * 8);
     switch (c->kind) {
     case PSF_Q4_PLANE_STRAIN:
-        sens_kernel<0><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials);
+        (sens_kernel<0><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials), ::psf::note_launch());
         break;
     case PSF_Q4_HEAT:
-        sens_kernel<1><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials);
+        (sens_kernel<1><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials), ::psf::note_launch());
         break;
     default:
-        sens_kernel<2><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials);
+        (sens_kernel<2><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials), ::psf::note_launch());
         break;
     }
     delete K;
     PSF_CUDA(cudaGetLastError());
     // f = scale0 * sum_e E_e q_e
-    sum_partials<<<1, 32, 0, c->stream>>>(c->partials, nb, scale0, 0.0, f_dev);
+    (sum_partials<<<1, 32, 0, c->stream>>>(c->partials, nb, scale0, 0.0, f_dev), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }

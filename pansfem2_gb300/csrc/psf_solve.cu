@@ -393,9 +393,9 @@ static psf_status ebe_apply_t(Ctx *c, const T *x, T *y, const T *Ep) {
     KeT<T> Ke = ke_param<T>(c);
     const int nb = grid_for(c->nnodes, 256, c->num_sms * 8);
     switch (c->kind) {
-    case PSF_Q4_PLANE_STRAIN: ebe_apply_kernel<T, 0><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y); break;
-    case PSF_Q4_HEAT: ebe_apply_kernel<T, 1><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y); break;
-    default: ebe_apply_kernel<T, 2><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y); break;
+    case PSF_Q4_PLANE_STRAIN: (ebe_apply_kernel<T, 0><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch()); break;
+    case PSF_Q4_HEAT: (ebe_apply_kernel<T, 1><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch()); break;
+    default: (ebe_apply_kernel<T, 2><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch()); break;
     }
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -410,11 +410,11 @@ static psf_status residual64(Ctx *c, const double *b, const double *x, double *r
     KeT<double> Ke = ke_param<double>(c);
     const int nb = grid_for(c->nnodes, 256, c->num_sms * 4);
     switch (c->kind) {
-    case PSF_Q4_PLANE_STRAIN: residual64_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials); break;
-    case PSF_Q4_HEAT: residual64_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials); break;
-    default: residual64_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials); break;
+    case PSF_Q4_PLANE_STRAIN: (residual64_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials), ::psf::note_launch()); break;
+    case PSF_Q4_HEAT: (residual64_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials), ::psf::note_launch()); break;
+    default: (residual64_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials), ::psf::note_launch()); break;
     }
-    finalize_sums<<<1, 64, 0, c->stream>>>(c->partials, nb, 2, c->scal + 8);
+    (finalize_sums<<<1, 64, 0, c->stream>>>(c->partials, nb, 2, c->scal + 8), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     double h[2];
     PSF_CUDA(cudaMemcpyAsync(h, c->scal + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -703,6 +703,7 @@ psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr,
     PSF_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), s));
     void *args[] = {&a};
     PSF_CUDA(cudaLaunchCooperativeKernel((const void *)pcg_csr_kernel, dim3(blocks), dim3(256), args, 0, s));
+    note_launch();
     return PSF_OK;
 }
 
@@ -715,7 +716,7 @@ static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr,
 psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_mg.cu
 
 static psf_status sum_partials_host(Ctx *c, int nb, double *out) {
-    finalize_sums<<<1, 32, 0, c->stream>>>(c->partials, nb, 1, c->scal + 8);
+    (finalize_sums<<<1, 32, 0, c->stream>>>(c->partials, nb, 1, c->scal + 8), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaMemcpyAsync(out, c->scal + 8, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PSF_CUDA(cudaStreamSynchronize(c->stream));
@@ -757,20 +758,20 @@ static psf_status outer_fcg64(Ctx *c, int solver, int itmax, double eps, bool wa
         PSF_CHECK(inner_solve(c, solver, r, 1.0 / rn, std::min(inner_cap, itmax - total), inner_tol, &it));
         total += it;
         double zq = 0, pr = 0, pq = 0, rr = 0;
-        fcg_z_kernel<<<nb, 256, 0, c->stream>>>(n, rn, c->w32[5], q, z, c->partials);
+        (fcg_z_kernel<<<nb, 256, 0, c->stream>>>(n, rn, c->w32[5], q, z, c->partials), ::psf::note_launch());
         PSF_CHECK(sum_partials_host(c, nb, &zq));
         const double beta = outer > 0 ? zq / pq_prev : 0.0;
-        fcg_p_kernel<<<nb, 256, 0, c->stream>>>(n, beta, z, r, p, c->partials);
+        (fcg_p_kernel<<<nb, 256, 0, c->stream>>>(n, beta, z, r, p, c->partials), ::psf::note_launch());
         PSF_CHECK(sum_partials_host(c, nb, &pr));
         switch (c->kind) {
-        case PSF_Q4_PLANE_STRAIN: fcg_q_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials); break;
-        case PSF_Q4_HEAT: fcg_q_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials); break;
-        default: fcg_q_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials); break;
+        case PSF_Q4_PLANE_STRAIN: (fcg_q_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials), ::psf::note_launch()); break;
+        case PSF_Q4_HEAT: (fcg_q_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials), ::psf::note_launch()); break;
+        default: (fcg_q_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials), ::psf::note_launch()); break;
         }
         PSF_CHECK(sum_partials_host(c, nb, &pq));
         if (!(pq > 0.0)) break;   // direction of no energy: nothing more to gain
         const double alpha = pr / pq;
-        fcg_update_kernel<<<nb, 256, 0, c->stream>>>(n, alpha, p, q, x, r, c->partials);
+        (fcg_update_kernel<<<nb, 256, 0, c->stream>>>(n, alpha, p, q, x, r, c->partials), ::psf::note_launch());
         PSF_CHECK(sum_partials_host(c, nb, &rr));
         rn = sqrt(rr);
         pq_prev = pq;

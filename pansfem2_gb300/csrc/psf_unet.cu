@@ -313,7 +313,7 @@ static cudaError_t launch_conv_n(const ConvArgs &a, cudaStream_t st) {
     const long long P = (long long)a.batch * a.hout * a.wout;
     const unsigned grid = (unsigned)((P + 127) / 128);
     if (grid == 0) return cudaSuccess;
-    conv_mma_kernel<N><<<grid, 128, S::BYTES, st>>>(a);
+    (conv_mma_kernel<N><<<grid, 128, S::BYTES, st>>>(a), ::psf::note_launch());
     return cudaGetLastError();
 }
 
@@ -731,11 +731,11 @@ psf_status Net::pack() {
     for (int l = 0; l < kLayers; l++) {
         const LayerDesc &y = L[l];
         const int coutp = pad16(y.cout);
-        pack_kernel<<<gsz((long long)nchunk_f[l] * 64 * coutp), 256, 0, stream>>>(
-            params + y.woff, y.cout, y.cin, coutp, y.cin, nchunk_f[l], 0, wf[l]);
+        (pack_kernel<<<gsz((long long)nchunk_f[l] * 64 * coutp), 256, 0, stream>>>(
+            params + y.woff, y.cout, y.cin, coutp, y.cin, nchunk_f[l], 0, wf[l]), ::psf::note_launch());
         if (wb[l])
-            pack_kernel<<<gsz((long long)nchunk_b[l] * 64 * y.cin), 256, 0, stream>>>(
-                params + y.woff, y.cout, y.cin, y.cin, coutp, nchunk_b[l], 1, wb[l]);
+            (pack_kernel<<<gsz((long long)nchunk_b[l] * 64 * y.cin), 256, 0, stream>>>(
+                params + y.woff, y.cout, y.cin, y.cin, coutp, nchunk_b[l], 1, wb[l]), ::psf::note_launch());
     }
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -756,8 +756,8 @@ psf_status Net::forward(int B, const bf16 *input) {
             const int dst = l == 8 ? 6 : (l == 10 ? 4 : 2);
             const int lc = lev[src], lf = lev[dst];
             const long long n = (long long)B * H[lf] * W[lf] * (C[src] / 8);
-            upsample_kernel<<<gsz(n), 256, 0, stream>>>(tin[src], C[src], H[lc], W[lc], t[dst], C[dst],
-                                                        C[dst] - C[src], H[lf], W[lf], B, skip);
+            (upsample_kernel<<<gsz(n), 256, 0, stream>>>(tin[src], C[src], H[lc], W[lc], t[dst], C[dst],
+                                                        C[dst] - C[src], H[lf], W[lf], B, skip), ::psf::note_launch());
         }
         ConvArgs a{};
         a.x = tin[y.in];
@@ -802,9 +802,9 @@ psf_status Net::backward(int B, const bf16 *input) {
         const long long Pout = (long long)B * H[y.level] * W[y.level];
         // pre-activation gradient (bf16, dense coutp channels)
         const bool last = l == kLayers - 1;
-        relu_grad_kernel<<<gsz(Pout * coutp), 256, 0, stream>>>(
+        (relu_grad_kernel<<<gsz(Pout * coutp), 256, 0, stream>>>(
             g[y.out], last ? 2 : y.out_cs, last ? 0 : y.out_c0, last ? nullptr : t[y.out], y.out_cs, y.out_c0,
-            y.relu, y.cout, coutp, Pout, gpre);
+            y.relu, y.cout, coutp, Pout, gpre), ::psf::note_launch());
         // weight and bias gradients
         const int tx = (y.cout + 31) / 32, ty = (y.cin + 31) / 32;
         int nsplit = (int)std::min<long long>(std::max(1, 608 / (tx * ty)), (Pout + 255) / 256);
@@ -826,12 +826,12 @@ psf_status Net::backward(int B, const bf16 *input) {
         d.chunk = ((Pout + nsplit - 1) / nsplit + 31) / 32 * 32;
         nsplit = (int)((Pout + d.chunk - 1) / d.chunk);
         d.part = part;
-        dw_kernel<<<dim3(tx, ty, nsplit), 128, 0, stream>>>(d);
+        (dw_kernel<<<dim3(tx, ty, nsplit), 128, 0, stream>>>(d), ::psf::note_launch());
         const long long nw = (long long)y.cout * 9 * y.cin;
-        reduce_parts_kernel<<<gsz(nw), 256, 0, stream>>>(part, nsplit, nw, grads + y.woff);
+        (reduce_parts_kernel<<<gsz(nw), 256, 0, stream>>>(part, nsplit, nw, grads + y.woff), ::psf::note_launch());
         float *bpart = part + (size_t)kDwSplitMax * nw;
-        bias_grad_kernel<<<nsplit, 128, 0, stream>>>(gpre, coutp, y.cout, Pout, d.chunk, bpart);
-        reduce_parts_kernel<<<1, 128, 0, stream>>>(bpart, nsplit, y.cout, grads + y.boff);
+        (bias_grad_kernel<<<nsplit, 128, 0, stream>>>(gpre, coutp, y.cout, Pout, d.chunk, bpart), ::psf::note_launch());
+        (reduce_parts_kernel<<<1, 128, 0, stream>>>(bpart, nsplit, y.cout, grads + y.boff), ::psf::note_launch());
         // data gradient into the input tensor's gradient (accumulating where a skip tensor has two consumers)
         if (l > 0) {
             ConvArgs a{};
@@ -864,8 +864,8 @@ psf_status Net::backward(int B, const bf16 *input) {
             const int src = l == 12 ? 12 : (l == 10 ? 10 : 8);
             const int lf = lev[cat], lc = lev[src];
             const long long n = (long long)B * H[lc] * W[lc] * C[src];
-            restrict_kernel<<<gsz(n), 256, 0, stream>>>(g[cat], C[cat], C[cat] - C[src], H[lf], W[lf], g[src],
-                                                        C[src], H[lc], W[lc], B);
+            (restrict_kernel<<<gsz(n), 256, 0, stream>>>(g[cat], C[cat], C[cat] - C[src], H[lf], W[lf], g[src],
+                                                        C[src], H[lc], W[lc], B), ::psf::note_launch());
         }
     }
     PSF_CUDA(cudaGetLastError());
@@ -874,9 +874,9 @@ psf_status Net::backward(int B, const bf16 *input) {
 
 psf_status Net::loss_grad(int B, const float *tgt, const float *mask, double *d_loss, double *d_rel) {
     const long long n = npix_b(B, 0) * 2;
-    loss_partial_kernel<<<kLossBlocks, 256, 0, stream>>>(out32, tgt, mask, n, dloss);
-    loss_grad_kernel<<<gsz(n), 256, 0, stream>>>(out32, tgt, mask, n, dloss, g[kTensors - 1],
-                                                  d_loss ? d_loss : dloss + 3 * kLossBlocks, d_rel);
+    (loss_partial_kernel<<<kLossBlocks, 256, 0, stream>>>(out32, tgt, mask, n, dloss), ::psf::note_launch());
+    (loss_grad_kernel<<<gsz(n), 256, 0, stream>>>(out32, tgt, mask, n, dloss, g[kTensors - 1],
+                                                  d_loss ? d_loss : dloss + 3 * kLossBlocks, d_rel), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -885,8 +885,8 @@ psf_status Net::adam(float lr) {
     step_count++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float bc1 = 1.0f - powf(b1, (float)step_count), bc2 = 1.0f - powf(b2, (float)step_count);
-    adam_kernel<<<gsz(nparams), 256, 0, stream>>>(params, grads, adam_m, adam_v, nparams, lr, b1, b2, 1e-8f, bc1,
-                                                  bc2);
+    (adam_kernel<<<gsz(nparams), 256, 0, stream>>>(params, grads, adam_m, adam_v, nparams, lr, b1, b2, 1e-8f, bc1,
+                                                  bc2), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return pack();
 }
@@ -908,7 +908,7 @@ psf_status Net::upload_input(int B, const float *host_in) {
     PSF_CUDA(cudaMalloc(&tmp, sizeof(float) * n));
     cudaError_t e = cudaMemcpyAsync(tmp, host_in, sizeof(float) * n, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) {
-        f32_to_bf16_kernel<<<gsz(n), 256, 0, stream>>>(tmp, n, t[0]);
+        (f32_to_bf16_kernel<<<gsz(n), 256, 0, stream>>>(tmp, n, t[0]), ::psf::note_launch());
         e = cudaStreamSynchronize(stream);
     }
     cudaFree(tmp);
@@ -1059,8 +1059,8 @@ psf_status psf_unet_conv(int mode, int N, int cin, int hin, int win, int hout, i
         ck(cudaMemset(err, 0, 4));
     }
     if (s == PSF_OK) {
-        f32_to_bf16_kernel<<<gsz((long long)nx), 256>>>(fx, (long long)nx, bx);
-        pack_kernel<<<gsz((long long)nchunks * 64 * N), 256>>>(fw, N, cin, N, cin, nchunks, 0, bw);
+        (f32_to_bf16_kernel<<<gsz((long long)nx), 256>>>(fx, (long long)nx, bx), ::psf::note_launch());
+        (pack_kernel<<<gsz((long long)nchunks * 64 * N), 256>>>(fw, N, cin, N, cin, nchunks, 0, bw), ::psf::note_launch());
         ConvArgs a{};
         a.x = bx;
         a.x_cs = cin;

@@ -84,6 +84,12 @@ class FemMesh:
         self.nnz = nnz.value
         return self.nnz
 
+    def timings(self):
+        """Device milliseconds of the last assemble: element matrices, pattern, values."""
+        t = [C.c_double() for _ in range(3)]
+        check(self.L.psf_fem_timings(self.h, *[C.byref(x) for x in t]))
+        return [x.value for x in t]
+
     def system(self):
         """(n2g, indptr, indices, data, F) of the assembled free-dof system."""
         n2g = np.zeros(self.nnodes * self.ndof, np.int32)

@@ -152,3 +152,29 @@ def fixed_mask(pr):
     m = np.zeros(nn * nd, np.uint8)
     m[np.asarray(pr["fix_node"], np.int64) * nd + np.asarray(pr["fix_dof"], np.int64)] = 1
     return m
+
+
+def jittered_q4_mesh(nx=1024, ny=512, seed=0, jitter=0.2):
+    """An explicit Q4 plane-strain mesh for the general assembly path: an nx x ny grid with
+    every node moved by up to `jitter` of a cell and the node ids permuted (so neighbours are
+    far apart in memory, as in meshes read from files), per-element moduli uniform in
+    [0.1, 1], the left edge clamped, a downward point load at the top right corner, a
+    uniform body force and a uniform traction on the top edge.  Returns a dict of the
+    arrays FemMesh takes."""
+    rng = np.random.default_rng(seed)
+    nn = (nx + 1) * (ny + 1)
+    perm = rng.permutation(nn).astype(np.int32)
+    i, j = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), indexing="ij")
+    grid = np.stack([i, j], -1).reshape(-1, 2).astype(float)
+    coords = np.empty_like(grid)
+    coords[perm] = grid + rng.uniform(-jitter, jitter, grid.shape)
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    nid = lambda a, b: perm[a * (ny + 1) + b]  # noqa: E731
+    conn = np.stack([nid(I, J), nid(I + 1, J), nid(I + 1, J + 1), nid(I, J + 1)], -1).reshape(-1, 4)
+    left = nid(np.zeros(ny + 1, int), np.arange(ny + 1))
+    fixed = np.column_stack([np.repeat(left, 2), np.tile([0, 1], ny + 1), np.zeros(2 * (ny + 1))])
+    loads = np.array([[nid(nx, ny), 1, -1.0]])
+    top = nid(np.arange(nx + 1), np.full(nx + 1, ny))
+    edges = np.column_stack([top[:-1], top[1:]]).astype(np.int32)
+    return dict(kind=0, coords=coords, conn=conn.astype(np.int32), E=rng.uniform(0.1, 1.0, nx * ny), V=0.3, t=1.0,
+                fixed=fixed, loads=loads, body=(0.0, -1e-3), edges=edges, traction=(0.0, -1e-2))

@@ -153,3 +153,88 @@ def test_solid_sample_cpp(fem, tmp_path):
     u = np.array([[float(v) for v in r[2:5]] for r in rows]).reshape(-1)
     assert int(out.split()[1]) == len(g["F"])
     _check_solid(u, g)
+
+
+def _oracle_system(kind, coords, conn, E, V, t, fixed, loads, body=None, edges=None, traction=None):
+    from oracle import pyoracle as O
+    nd = {0: 2, 1: 1, 2: 3, 3: 2}[kind]
+    nn = len(coords)
+    fx = np.zeros(nn * nd, np.uint8)
+    uf = np.zeros(nn * nd)
+    for n, d, v in fixed:
+        fx[int(n) * nd + int(d)] = 1
+        uf[int(n) * nd + int(d)] = v
+    n2g, N = O.renumber(nn, nd, fx)
+    ip, ix, dat, F = O.assemble(kind, conn, coords, E, n2g, N, V, t, ufixed=uf, body=body)
+    F = O.neumann(F, loads[:, 0].astype(int), loads[:, 1].astype(int), loads[:, 2], nd, n2g)
+    if edges is not None and len(edges):
+        F = O.edge_loads(F, edges, coords, traction, t, n2g)
+    return n2g, ip, ix, dat, F
+
+
+def _gpu_system(fem, kind, coords, conn, E, V, t, fixed, loads, body=None, edges=None, traction=None):
+    with fem.FemMesh(kind, coords, conn) as m:
+        m.set_dirichlet(fixed[:, 0].astype(int), fixed[:, 1].astype(int), fixed[:, 2])
+        m.set_loads(loads[:, 0].astype(int), loads[:, 1].astype(int), loads[:, 2])
+        if body is not None:
+            m.set_body_force(*body)
+        if edges is not None and len(edges):
+            m.set_edge_loads(edges, *traction)
+        m.assemble(E, V, t)
+        return m.system()
+
+
+def test_midsize_q4_mesh_against_the_oracle(fem):
+    """256x128 jittered Q4 mesh with permuted node ids (66k dofs, 1.2M stored entries), body
+    force, top-edge tractions and a point load: the whole system bit-exact with the oracle."""
+    from pansfem2_gb300 import problems as PB
+    m = PB.jittered_q4_mesh(256, 128, seed=7)
+    args = (0, m["coords"], m["conn"], m["E"], m["V"], m["t"], m["fixed"], m["loads"], m["body"], m["edges"],
+            m["traction"])
+    for a, b, name in zip(_gpu_system(fem, *args), _oracle_system(*args), ("n2g", "indptr", "indices", "data", "F")):
+        assert np.array_equal(a, b), name
+
+
+def test_midsize_h8_mesh_against_the_oracle(fem):
+    """12x10x8 jittered H8 mesh with permuted node ids, per-element moduli, a clamped face with
+    a prescribed nonzero value and point loads: bit-exact with the oracle (rows of up to 81
+    columns, nodes with 26 neighbours)."""
+    rng = np.random.default_rng(11)
+    nx, ny, nz = 12, 10, 8
+    nn = (nx + 1) * (ny + 1) * (nz + 1)
+    perm = rng.permutation(nn)
+    i, j, k = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    grid = np.stack([i, j, k], -1).reshape(-1, 3).astype(float)
+    coords = np.empty_like(grid)
+    coords[perm] = grid + rng.uniform(-0.2, 0.2, grid.shape)
+    nid = lambda a, b, c: perm[(a * (ny + 1) + b) * (nz + 1) + c]  # noqa: E731
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    conn = np.stack([nid(I, J, K), nid(I + 1, J, K), nid(I + 1, J + 1, K), nid(I, J + 1, K),
+                     nid(I, J, K + 1), nid(I + 1, J, K + 1), nid(I + 1, J + 1, K + 1), nid(I, J + 1, K + 1)],
+                    -1).reshape(-1, 8).astype(np.int32)
+    E = rng.uniform(0.2, 1.0, len(conn))
+    face = [nid(0, b, c) for b in range(ny + 1) for c in range(nz + 1)]
+    fixed = np.array([(n, d, 0.0) for n in face for d in range(3)] + [(nid(nx, 0, 0), 2, 0.01)], float)
+    loads = np.array([(nid(nx, b, nz), 2, -0.1) for b in range(ny + 1)], float)
+    args = (2, coords, conn, E, 0.3, 1.0, fixed, loads)
+    for a, b, name in zip(_gpu_system(fem, *args), _oracle_system(*args), ("n2g", "indptr", "indices", "data", "F")):
+        assert np.array_equal(a, b), name
+
+
+def test_kernel_launch_counter(fem):
+    """psf_kernel_launches counts every launch: the first assembly of an H8 mesh runs the element
+    kernel, the pattern count, a three-kernel scan and the values kernel; a second one reuses
+    the pattern."""
+    from pansfem2_gb300 import _lib
+    g = load("fem_h8_jitter")
+    with _mesh(fem, g) as m:
+        V, t = g["Vt"]
+        l0 = _lib.kernel_launches()
+        m.assemble(g["E"], V, t)
+        assert _lib.kernel_launches() - l0 == 2
+    with fem.FemMesh(int(g["kind"][0]), g["coords"], g["conn"]) as m:
+        fx = g["fixed"]
+        m.set_dirichlet(fx[:, 0].astype(int), fx[:, 1].astype(int), fx[:, 2])
+        l0 = _lib.kernel_launches()
+        m.assemble(g["E"], *g["Vt"])
+        assert _lib.kernel_launches() - l0 == 6
