@@ -101,6 +101,21 @@ def bytes_per_krylov_iteration(solver, pr, nnz, nfree):
     return 4 * ne + 8 * ndofs + 11 * 4 * ndofs
 
 
+def max_over_ranks(values, world, device=None):
+    """The elementwise maximum of this rank's timings over all ranks of the default process
+    group (NCCL on the GPUs, gloo in the CPU tests); the values themselves for one rank.
+    Every replica does the same work, so the slowest rank sets the job's time."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    if device is None:
+        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -362,10 +377,7 @@ def bench_heat_batch(args, rank, world):
             B.step(1)
             r = B.results()
         e2e_t = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([dev_t, e2e_t], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_t, e2e_t = float(t[0]), float(t[1])
+    dev_t, e2e_t = max_over_ranks([dev_t, e2e_t], world)
     n = len(insts)
     value = world * n * args.steps / dev_t
     # algorithmic bytes of the solve kernel: per node and FCG iteration ~250 B (FP64 Krylov vectors 112 B,
@@ -522,6 +534,9 @@ def bench_fem(args, rank, world):
     oracle's assembly of the same mesh on one host core."""
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     from pansfem2_gb300 import _lib
     from pansfem2_gb300 import fem as FM
@@ -560,8 +575,8 @@ def bench_fem(args, rank, world):
         hb = 8 * len(m["E"]) + fx.size * 4 + ld.size * 4 + m["edges"].size * 4
         hd = sum(a.nbytes for a in sysm)
     ms = ph.mean(0)
-    dev_s = ms.sum() / 1e3
-    value = 1.0 / dev_s
+    dev_s, e2e_s = max_over_ranks([ms.sum() / 1e3, float(np.mean(e2e_t))], world)   # replicas: the slowest
+    value = world / dev_s
     ne, nn = len(m["conn"]), len(m["coords"])
     by = fem_assembly_bytes(ne, nn, nfree, nnz)
     names = ["element", "pattern", "values"]
@@ -586,9 +601,9 @@ def bench_fem(args, rank, world):
            "roofline": {"kernel": ["fem_ke_kernel", "pattern_count_kernel", "assemble_rows_kernel"][k],
                         "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                         "peak_source": src, "algorithmic_bytes": by[names[k]], "traffic": tr},
-           "e2e": {"value": 1.0 / float(np.mean(e2e_t)), "unit": "assemblies/s", "h2d_bytes_per_step": int(hb),
+           "e2e": {"value": world / e2e_s, "unit": "assemblies/s", "h2d_bytes_per_step": int(hb),
                    "d2h_bytes_per_step": int(hd)}}
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import build as ob
         from oracle import pyoracle as O
         ob.build()
@@ -609,6 +624,8 @@ def bench_fem(args, rank, world):
                                "bitexact_vs_gpu": same}
     if rank == 0:
         print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def ncpus():
@@ -697,10 +714,7 @@ def main():
         clk.window(*prob.t_region)
     barrier()
     dev_t = sum(sum(i["phase_seconds"]) for i in infos)
-    if world > 1:
-        t = torch.tensor([dev_t], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_t = float(t.item())
+    dev_t, = max_over_ranks([dev_t], world)
     value = world * args.steps / dev_t
     prob._sizes()
     ne, ndofs, nnz, nfree = prob.ne, prob.nnodes * prob.ndof, prob.nnz or 0, prob.nfree
@@ -752,10 +766,7 @@ def main():
         einfos, ewall, h2d, d2h, designs = run_e2e(pr, args.solver, args.warmup, args.steps, args.eps,
                                                    bool(args.warm_start), sample_at=sample_at)
         barrier()
-        if world > 1:
-            t = torch.tensor([ewall], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ewall = float(t.item())
+        ewall, = max_over_ranks([ewall], world)
         out["e2e"] = {"value": world * args.steps / ewall, "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h}
 
