@@ -401,14 +401,18 @@ __global__ void fem_edge_kernel(int nedge, const int *__restrict__ edges, const 
 
 psf_status fem_body_forces(cudaStream_t s, int kind, long long ne, int nen, const int *conn, const double *coords,
                            double fx, double fy, double t, double *Fe) {
-    (fem_body_kernel<<<grid_for(ne, 128, 65536), 128, 0, s>>>(kind, ne, nen, conn, coords, fx, fy, t, Fe), ::psf::note_launch());
+    (fem_body_kernel<<<grid_for(ne, 128, 65536), 128, 0, s>>>(
+         kind, ne, nen, conn, coords, fx, fy, t, Fe),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status fem_edge_forces(cudaStream_t s, int nedge, const int *edges, const double *coords, double tx, double ty,
                            double t, double *Fe) {
-    (fem_edge_kernel<<<grid_for(nedge, 128, 65536), 128, 0, s>>>(nedge, edges, coords, tx, ty, t, Fe), ::psf::note_launch());
+    (fem_edge_kernel<<<grid_for(nedge, 128, 65536), 128, 0, s>>>(
+         nedge, edges, coords, tx, ty, t, Fe),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -418,16 +422,24 @@ psf_status fem_element_matrices(cudaStream_t s, int kind, long long ne, int nen,
     (void)nen;
     switch (kind) {
         case PSF_Q4_PLANE_STRAIN:
-            (fem_ke_kernel<PSF_Q4_PLANE_STRAIN><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            (fem_ke_kernel<PSF_Q4_PLANE_STRAIN><<<grid_for(ne, 64, 65536), 64, 0, s>>>(
+                 ne, conn, coords, E, V, t, Ke),
+             ::psf::note_launch());
             break;
         case PSF_Q4_HEAT:
-            (fem_ke_kernel<PSF_Q4_HEAT><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            (fem_ke_kernel<PSF_Q4_HEAT><<<grid_for(ne, 64, 65536), 64, 0, s>>>(
+                 ne, conn, coords, E, V, t, Ke),
+             ::psf::note_launch());
             break;
         case PSF_H8_SOLID:
-            (fem_ke_kernel<PSF_H8_SOLID><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            (fem_ke_kernel<PSF_H8_SOLID><<<grid_for(ne, 64, 65536), 64, 0, s>>>(
+                 ne, conn, coords, E, V, t, Ke),
+             ::psf::note_launch());
             break;
         default:
-            (fem_ke_kernel<PSF_T3_PLANE_STRAIN><<<grid_for(ne, 64, 65536), 64, 0, s>>>(ne, conn, coords, E, V, t, Ke), ::psf::note_launch());
+            (fem_ke_kernel<PSF_T3_PLANE_STRAIN><<<grid_for(ne, 64, 65536), 64, 0, s>>>(
+                 ne, conn, coords, E, V, t, Ke),
+             ::psf::note_launch());
     }
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;

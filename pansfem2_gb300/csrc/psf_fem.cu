@@ -428,10 +428,14 @@ psf_status psf_fem_create(int kind, long long nnodes, const double *coords, long
         A(cuda_status(cudaMemsetAsync(f->fixed, 0, nnodes * f->nd, s), "memset"));
         A(cuda_status(cudaMemsetAsync(f->ufix, 0, sizeof(double) * nnodes * f->nd, s), "memset"));
         if (st == PSF_OK) {
-            (adj_count<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(nelem, nen, f->conn, cnt), ::psf::note_launch());
+            (adj_count<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(
+                 nelem, nen, f->conn, cnt),
+             ::psf::note_launch());
             int total = 0;
             A(scan_ints(f, nnodes + 1, cnt, f->adj_ptr, &total));
-            (adj_fill<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(nelem, nen, f->conn, f->adj_ptr, pos, f->adj), ::psf::note_launch());
+            (adj_fill<<<grid_for(nelem * nen, 256, 65536), 256, 0, s>>>(
+                 nelem, nen, f->conn, f->adj_ptr, pos, f->adj),
+             ::psf::note_launch());
             (adj_sort<<<grid_for(nnodes, 256, 65536), 256, 0, s>>>(nnodes, f->adj_ptr, f->adj), ::psf::note_launch());
             A(cuda_status(cudaGetLastError(), "adjacency"));
         }
@@ -483,7 +487,9 @@ psf_status psf_fem_set_dirichlet(psf_fem *h, int n, const int32_t *node, const i
         PSF_CUDA(cudaMemcpyAsync(dn, node, sizeof(int) * n, cudaMemcpyHostToDevice, s));
         PSF_CUDA(cudaMemcpyAsync(dd, dof, sizeof(int) * n, cudaMemcpyHostToDevice, s));
         if (value) PSF_CUDA(cudaMemcpyAsync(dv, value, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-        (mark_fixed_kernel<<<1, 32, 0, s>>>(n, dn, dd, value ? dv : nullptr, f->nd, f->fixed, f->ufix), ::psf::note_launch());
+        (mark_fixed_kernel<<<1, 32, 0, s>>>(
+             n, dn, dd, value ? dv : nullptr, f->nd, f->fixed, f->ufix),
+         ::psf::note_launch());
     }
     (free_flags_kernel<<<grid_for(nt, 256, 65536), 256, 0, s>>>(nt, f->fixed, flags), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());

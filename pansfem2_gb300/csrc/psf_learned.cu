@@ -581,7 +581,9 @@ static psf_status lp_pre(Ctx *c, Learned *L, const double *r, const int *fl, flo
     if (L->pre_mg) return mg_apply(c, r, L->r32, L->xa, fl);
     const Geo g = lp_geo(c);
     const KeT<float> Kf = lp_ke<float>(c);
-    (lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, r, c->Dl1f, c->fixed, L->r32, L->xa, fl), ::psf::note_launch());
+    (lp_first_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(
+         c->ndofs, r, c->Dl1f, c->fixed, L->r32, L->xa, fl),
+     ::psf::note_launch());
     for (int k = 1; k < L->nu_pre; k++) {
         (lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, *cur,
                                                                *oth, fl), ::psf::note_launch());
@@ -603,21 +605,29 @@ static psf_status lp_precond(Ctx *c, Learned *L, const double *r, double *z, con
         (lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
                                                                L->part, fl), ::psf::note_launch());
         (nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho,
-                                                              L->nnin, L->sc, fl, c->ny, c->Epadf, L->inv_e1), ::psf::note_launch());
+                                                              L->nnin, L->sc, fl, c->ny, c->Epadf, L->inv_e1),
+                                                              ::psf::note_launch());
         L->net->stream = st;
         L->net->skip = fl;
         PSF_CHECK(L->net->forward(1, L->nnin));
         (nn_apply_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, L->net->out32, L->isd, L->sc,
                                                                L->net->out_scale, L->dcorr, fl), ::psf::note_launch());
-        (nn_step_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->dcorr, L->r1, L->part, fl), ::psf::note_launch());
-        (nn_add_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->ndofs, L->part, L->dcorr, cur, L->sc, fl), ::psf::note_launch());
+        (nn_step_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(
+             g, Kf, c->Epadf, c->fixed, L->dcorr, L->r1, L->part, fl),
+         ::psf::note_launch());
+        (nn_add_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(
+             c->ndofs, L->part, L->dcorr, cur, L->sc, fl),
+         ::psf::note_launch());
     }
     for (int k = 1; k < L->nu_post; k++) {
-        (lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl), ::psf::note_launch());
+        (lp_sweep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(
+             g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur, oth, fl),
+         ::psf::note_launch());
         std::swap(cur, oth);
     }
     (lp_last_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->Dl1f, c->fixed, L->r32, cur,
-                                                          L->nu_post > 0 ? 1 : 0, z, qprev, L->part, fl), ::psf::note_launch());
+                                                          L->nu_post > 0 ? 1 : 0, z, qprev, L->part, fl),
+                                                          ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -632,9 +642,13 @@ static psf_status lp_iteration(Ctx *c, Learned *L, double *x, double *r, double 
     const int *fl = L->flags;
     PSF_CHECK(lp_precond<KIND>(c, L, r, z, q, fl));
     (fcg_dir_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, z, p, L->sc, fl), ::psf::note_launch());
-    (fcg_op_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, p, q, r, L->part, fl), ::psf::note_launch());
+    (fcg_op_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(
+         g, Kd, c->Epad, c->fixed, p, q, r, L->part, fl),
+     ::psf::note_launch());
     // the step writes |r|^2 partials into the upper half so that the (p.q, r.p) partials stay readable
-    (fcg_step_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->part, p, q, x, r, L->part + 2 * kLpBlocks, L->sc, fl), ::psf::note_launch());
+    (fcg_step_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(
+         nd, L->part, p, q, x, r, L->part + 2 * kLpBlocks, L->sc, fl),
+     ::psf::note_launch());
     (fcg_check_kernel<<<1, 32, 0, st>>>(L->part + 2 * kLpBlocks, L->sc, L->flags), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -704,7 +718,9 @@ static psf_status learned_solve_t(Ctx *c, int itmax, double eps, bool warm, psf_
     PSF_CUDA(cudaEventRecord(c->evk0, st));
     for (int pass = 0; pass < 3 && total < limit; pass++) {
         passes++;
-        (lp_residual_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kd, c->Epad, c->fixed, c->Fn, x, r, L->part), ::psf::note_launch());
+        (lp_residual_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(
+             g, Kd, c->Epad, c->fixed, c->Fn, x, r, L->part),
+         ::psf::note_launch());
         (lp_start_kernel<<<1, 32, 0, st>>>(L->part, eps, limit - total, L->sc, L->flags), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
         for (;;) {
@@ -1041,7 +1057,8 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     (lp_resid_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(g, Kf, c->Epadf, c->fixed, L->r32, cur, L->isd, L->r1,
                                                            L->part, L->flags), ::psf::note_launch());
     (nn_prep_kernel<KIND><<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->nfree, L->part, L->r1, L->isd, L->rho, in_out,
-                                                          L->sc, L->flags, c->ny, c->Epadf, L->inv_e1), ::psf::note_launch());
+                                                          L->sc, L->flags, c->ny, c->Epadf, L->inv_e1),
+                                                          ::psf::note_launch());
     (f32_to_f64_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(nd, L->r1, rhs64), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     // e = K^-1 r1 with the multigrid FCG to 1e-8 (its right-hand side is the context's nodal load vector)
@@ -1053,10 +1070,13 @@ static psf_status harvest_pair(Ctx *c, Learned *L, const double *r, double *rhs6
     if (s == PSF_NOT_CONVERGED) return PSF_NOT_CONVERGED;   // the caller skips this pair
     if (s != PSF_OK) return s;
     PSF_CUDA(cudaMemcpyAsync(e64, c->un, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st));
-    (tgt_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, e64, L->isd, L->sc, tgt_out, mask_out, L->part), ::psf::note_launch());
+    (tgt_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(
+         c->nnodes, c->ndof, e64, L->isd, L->sc, tgt_out, mask_out, L->part),
+     ::psf::note_launch());
     (mask_scale_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes * 2, L->part, mask_out), ::psf::note_launch());
     (pair_extra_kernel<<<kLpBlocks, kLpThreads, 0, st>>>(c->nnodes, c->ndof, L->r1, L->isd, L->sc, tgt_out,
-                                                        ts->rhat + slot * P * 2, ts->isd + slot * P * 2, L->part), ::psf::note_launch());
+                                                        ts->rhat + slot * P * 2, ts->isd + slot * P * 2, L->part),
+                                                        ::psf::note_launch());
     (fold_to_kernel<<<1, 32, 0, st>>>(L->part, ts->cden + slot), ::psf::note_launch());
     PSF_CUDA(cudaMemcpyAsync(ts->epad + slot * Pe, c->Epadf, sizeof(float) * Pe, cudaMemcpyDeviceToDevice, st));
     PSF_CUDA(cudaGetLastError());
@@ -1228,7 +1248,8 @@ psf_status psf_learned_train(psf_unet *u, psf_trainset *ts, int steps, int batch
                                                  cudaMemcpyDeviceToDevice, st), "copy");
             if (s == PSF_OK) {
                 (psf::scale_copy_kernel<<<psf::kLpBlocks, psf::kLpThreads, 0, st>>>(
-                    (long long)P * 2, ts->tgt + i * P * 2, (float)(1.0 / ts->out_scale), tgt + b * P * 2), ::psf::note_launch());
+                    (long long)P * 2, ts->tgt + i * P * 2, (float)(1.0 / ts->out_scale), tgt + b * P * 2),
+                    ::psf::note_launch());
                 s = psf::cuda_status(cudaGetLastError(), "scale_copy_kernel");
             }
             if (s == PSF_OK)

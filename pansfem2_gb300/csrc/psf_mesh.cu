@@ -457,7 +457,9 @@ psf_status set_dirichlet(Ctx *c, int n, const int *node, const int *dof, const d
             PSF_CUDA(cudaMallocAsync((void **)&dv, sizeof(double) * n, c->stream));
             PSF_CUDA(cudaMemcpyAsync(dv, value, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
         }
-        (mark_fixed<<<grid_for(n, 256), 256, 0, c->stream>>>(dn, dd, dv, n, c->ndof, c->fixed, c->ufixed), ::psf::note_launch());
+        (mark_fixed<<<grid_for(n, 256), 256, 0, c->stream>>>(
+             dn, dd, dv, n, c->ndof, c->fixed, c->ufixed),
+         ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
     }
     int *flag = nullptr, *prefix = nullptr;
@@ -501,7 +503,9 @@ psf_status build_pattern(Ctx *c) {
     PSF_CUDA(cudaMallocAsync((void **)&c->indptr, sizeof(int) * (c->nfree + 1), c->stream));
     PSF_CUDA(cudaMallocAsync((void **)&c->diag, sizeof(int) * (c->nfree + 1), c->stream));
     PSF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (c->nfree + 1), c->stream));
-    (pattern_count<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(g, c->n2g, c->g2n, c->nfree, cnt), ::psf::note_launch());
+    (pattern_count<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(
+         g, c->n2g, c->g2n, c->nfree, cnt),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     long long nnz = 0;
     PSF_CHECK(exclusive_scan(c, cnt, c->nfree + 1, c->indptr, &nnz));
@@ -533,7 +537,9 @@ psf_status build_rhs(Ctx *c) {
         PSF_CUDA(cudaMemcpyAsync(dn, c->load_node.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
         PSF_CUDA(cudaMemcpyAsync(dd, c->load_dof.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
         PSF_CUDA(cudaMemcpyAsync(dv, c->load_val.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-        (loads_nodal<<<grid_for(n, 256), 256, 0, c->stream>>>(dn, dd, dv, n, c->ndof, c->n2g, c->Fn), ::psf::note_launch());
+        (loads_nodal<<<grid_for(n, 256), 256, 0, c->stream>>>(
+             dn, dd, dv, n, c->ndof, c->n2g, c->Fn),
+         ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
         PSF_CUDA(cudaFreeAsync(dn, c->stream));
         PSF_CUDA(cudaFreeAsync(dd, c->stream));
@@ -547,9 +553,12 @@ psf_status set_moduli(Ctx *c, const double *E_dev) {
     if (E_dev != c->E)
         PSF_CUDA(cudaMemcpyAsync(c->E, E_dev, sizeof(double) * c->ne, cudaMemcpyDeviceToDevice, c->stream));
     Grid g = grid_of(c);
-    (moduli_pad<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(g, c->ne, c->E, c->Ef, c->Epad, c->Epadf), ::psf::note_launch());
+    (moduli_pad<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(
+         g, c->ne, c->E, c->Ef, c->Epad, c->Epadf),
+     ::psf::note_launch());
     (nodal_diag<<<grid_for(c->nnodes, 256, 65536), 256, 0, c->stream>>>(g, c->nnodes, c->Epad, (const Ke64 *)c->Ke0,
-                                                                         c->n2g, c->Dn, c->Dnf, c->Dl1f), ::psf::note_launch());
+                                                                         c->n2g, c->Dn, c->Dnf, c->Dl1f),
+                                                                         ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -562,10 +571,12 @@ psf_status assemble_values(Ctx *c, const double *E_dev) {
     const int lift = c->nonzero_ufixed ? 1 : 0;
     if (g.is3d)
         (assemble_rows<1><<<grid_for(c->nfree, 128, 65536), 128, 0, c->stream>>>(
-            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F), ::psf::note_launch());
+            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F),
+            ::psf::note_launch());
     else
         (assemble_rows<0><<<grid_for(c->nfree, 128, 65536), 128, 0, c->stream>>>(
-            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F), ::psf::note_launch());
+            g, c->n2g, c->g2n, c->nfree, c->indptr, c->E, (const Ke64 *)c->Ke0, c->data, c->ufixed, lift, c->F),
+            ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     c->have_values = true;
     return PSF_OK;
@@ -579,13 +590,17 @@ psf_status spmv_csr64(Ctx *c, const double *x, double *y) {
 }
 
 psf_status gather_reduced(Ctx *c, const double *nodal, double *red) {
-    (gather_kernel<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(c->g2n, c->nfree, nodal, red), ::psf::note_launch());
+    (gather_kernel<<<grid_for(c->nfree, 256, 65536), 256, 0, c->stream>>>(
+         c->g2n, c->nfree, nodal, red),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
 
 psf_status scatter_reduced(Ctx *c, const double *red, double *nodal) {
-    (scatter_kernel<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->n2g, c->ndofs, red, nodal), ::psf::note_launch());
+    (scatter_kernel<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(
+         c->n2g, c->ndofs, red, nodal),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }

@@ -1243,8 +1243,12 @@ static psf_status mg_setup_t(Ctx *c, MgHier *H) {
     KeF Ke = kef_of(c);
     for (int l = 1; l < H->nlev; l++) {
         MgLev &F = H->L[l - 1], &Cc = H->L[l];
-        (coarse_fixed_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(F, Cc), ::psf::note_launch());
-        (galerkin_kernel<KIND><<<grid_for(Cc.ne, 64, 65536), 64, 0, c->stream>>>(F, Cc, l - 1, Ke), ::psf::note_launch());
+        (coarse_fixed_kernel<KIND><<<grid_for(Cc.nnodes, 256, 65536), 256, 0, c->stream>>>(
+             F, Cc),
+         ::psf::note_launch());
+        (galerkin_kernel<KIND><<<grid_for(Cc.ne, 64, 65536), 64, 0, c->stream>>>(
+             F, Cc, l - 1, Ke),
+         ::psf::note_launch());
         (coarse_stencil_kernel<KIND><<<grid_for(Cc.nnodes, 128, 65536), 128, 0, c->stream>>>(Cc), ::psf::note_launch());
         PSF_CUDA(cudaGetLastError());
     }

@@ -604,7 +604,9 @@ __global__ void heaviside_project_kernel(long long n, double beta, double *__res
 // rho = H(filter(s)); dH = H'(filter(s)) is kept for heaviside_back
 psf_status heaviside_forward(Ctx *c, double beta, const double *s, double *rho) {
     PSF_CHECK(filter_apply(c, s, rho, false));
-    (heaviside_project_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, beta, rho, c->dH), ::psf::note_launch());
+    (heaviside_project_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(
+         c->ne, beta, rho, c->dH),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -622,7 +624,9 @@ psf_status filter_apply(Ctx *c, const double *in, double *out, bool backward) {
     Stencil *S = new Stencil;
     psf_status st = get_stencil(c, S);
     if (st == PSF_OK) {
-        (filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, in, c->filt_wsum, out), ::psf::note_launch());
+        (filter_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(
+             *S, c->ne, in, c->filt_wsum, out),
+         ::psf::note_launch());
         if (cudaGetLastError() != cudaSuccess) st = PSF_CUDA_ERROR;
     }
     delete S;
@@ -646,7 +650,9 @@ psf_status filter_moduli(Ctx *c, const double *s, double *rho, double *E, double
 }
 
 psf_status moduli_from_rho(Ctx *c, const double *rho, double E1, double E0, double p, double *E_dev) {
-    (moduli_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(c->ne, rho, E1, E0, p, E_dev), ::psf::note_launch());
+    (moduli_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(
+         c->ne, rho, E1, E0, p, E_dev),
+     ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -665,13 +671,19 @@ psf_status compliance_sens(Ctx *c, const double *rho, double E1, double E0, doub
     const int nb = grid_for(c->ne, 256, c->num_sms * 8);
     switch (c->kind) {
     case PSF_Q4_PLANE_STRAIN:
-        (sens_kernel<0><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials), ::psf::note_launch());
+        (sens_kernel<0><<<nb, 256, 0, c->stream>>>(
+             c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials),
+         ::psf::note_launch());
         break;
     case PSF_Q4_HEAT:
-        (sens_kernel<1><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials), ::psf::note_launch());
+        (sens_kernel<1><<<nb, 256, 0, c->stream>>>(
+             c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials),
+         ::psf::note_launch());
         break;
     default:
-        (sens_kernel<2><<<nb, 256, 0, c->stream>>>(c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials), ::psf::note_launch());
+        (sens_kernel<2><<<nb, 256, 0, c->stream>>>(
+             c->nx, c->ny, c->nz, c->ne, *K, c->un, rho, c->E, scale0, p, E1, E0, dfdrho, c->partials),
+         ::psf::note_launch());
         break;
     }
     delete K;

@@ -393,9 +393,15 @@ static psf_status ebe_apply_t(Ctx *c, const T *x, T *y, const T *Ep) {
     KeT<T> Ke = ke_param<T>(c);
     const int nb = grid_for(c->nnodes, 256, c->num_sms * 8);
     switch (c->kind) {
-    case PSF_Q4_PLANE_STRAIN: (ebe_apply_kernel<T, 0><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch()); break;
-    case PSF_Q4_HEAT: (ebe_apply_kernel<T, 1><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch()); break;
-    default: (ebe_apply_kernel<T, 2><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch()); break;
+    case PSF_Q4_PLANE_STRAIN:
+        (ebe_apply_kernel<T, 0><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch());
+        break;
+    case PSF_Q4_HEAT:
+        (ebe_apply_kernel<T, 1><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch());
+        break;
+    default:
+        (ebe_apply_kernel<T, 2><<<nb, 256, 0, c->stream>>>(g, Ke, Ep, c->fixed, x, y), ::psf::note_launch());
+        break;
     }
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -410,9 +416,21 @@ static psf_status residual64(Ctx *c, const double *b, const double *x, double *r
     KeT<double> Ke = ke_param<double>(c);
     const int nb = grid_for(c->nnodes, 256, c->num_sms * 4);
     switch (c->kind) {
-    case PSF_Q4_PLANE_STRAIN: (residual64_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials), ::psf::note_launch()); break;
-    case PSF_Q4_HEAT: (residual64_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials), ::psf::note_launch()); break;
-    default: (residual64_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, b, x, r, c->partials), ::psf::note_launch()); break;
+    case PSF_Q4_PLANE_STRAIN:
+        (residual64_kernel<0><<<nb, 256, 0, c->stream>>>(
+             g, Ke, c->Epad, c->fixed, b, x, r, c->partials),
+         ::psf::note_launch());
+        break;
+    case PSF_Q4_HEAT:
+        (residual64_kernel<1><<<nb, 256, 0, c->stream>>>(
+             g, Ke, c->Epad, c->fixed, b, x, r, c->partials),
+         ::psf::note_launch());
+        break;
+    default:
+        (residual64_kernel<2><<<nb, 256, 0, c->stream>>>(
+             g, Ke, c->Epad, c->fixed, b, x, r, c->partials),
+         ::psf::note_launch());
+        break;
     }
     (finalize_sums<<<1, 64, 0, c->stream>>>(c->partials, nb, 2, c->scal + 8), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
@@ -764,9 +782,21 @@ static psf_status outer_fcg64(Ctx *c, int solver, int itmax, double eps, bool wa
         (fcg_p_kernel<<<nb, 256, 0, c->stream>>>(n, beta, z, r, p, c->partials), ::psf::note_launch());
         PSF_CHECK(sum_partials_host(c, nb, &pr));
         switch (c->kind) {
-        case PSF_Q4_PLANE_STRAIN: (fcg_q_kernel<0><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials), ::psf::note_launch()); break;
-        case PSF_Q4_HEAT: (fcg_q_kernel<1><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials), ::psf::note_launch()); break;
-        default: (fcg_q_kernel<2><<<nb, 256, 0, c->stream>>>(g, Ke, c->Epad, c->fixed, p, q, c->partials), ::psf::note_launch()); break;
+        case PSF_Q4_PLANE_STRAIN:
+            (fcg_q_kernel<0><<<nb, 256, 0, c->stream>>>(
+                 g, Ke, c->Epad, c->fixed, p, q, c->partials),
+             ::psf::note_launch());
+            break;
+        case PSF_Q4_HEAT:
+            (fcg_q_kernel<1><<<nb, 256, 0, c->stream>>>(
+                 g, Ke, c->Epad, c->fixed, p, q, c->partials),
+             ::psf::note_launch());
+            break;
+        default:
+            (fcg_q_kernel<2><<<nb, 256, 0, c->stream>>>(
+                 g, Ke, c->Epad, c->fixed, p, q, c->partials),
+             ::psf::note_launch());
+            break;
         }
         PSF_CHECK(sum_partials_host(c, nb, &pq));
         if (!(pq > 0.0)) break;   // direction of no energy: nothing more to gain

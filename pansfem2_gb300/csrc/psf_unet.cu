@@ -876,7 +876,8 @@ psf_status Net::loss_grad(int B, const float *tgt, const float *mask, double *d_
     const long long n = npix_b(B, 0) * 2;
     (loss_partial_kernel<<<kLossBlocks, 256, 0, stream>>>(out32, tgt, mask, n, dloss), ::psf::note_launch());
     (loss_grad_kernel<<<gsz(n), 256, 0, stream>>>(out32, tgt, mask, n, dloss, g[kTensors - 1],
-                                                  d_loss ? d_loss : dloss + 3 * kLossBlocks, d_rel), ::psf::note_launch());
+                                                  d_loss ? d_loss : dloss + 3 * kLossBlocks, d_rel),
+                                                  ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
 }
@@ -1060,7 +1061,9 @@ psf_status psf_unet_conv(int mode, int N, int cin, int hin, int win, int hout, i
     }
     if (s == PSF_OK) {
         (f32_to_bf16_kernel<<<gsz((long long)nx), 256>>>(fx, (long long)nx, bx), ::psf::note_launch());
-        (pack_kernel<<<gsz((long long)nchunks * 64 * N), 256>>>(fw, N, cin, N, cin, nchunks, 0, bw), ::psf::note_launch());
+        (pack_kernel<<<gsz((long long)nchunks * 64 * N), 256>>>(
+             fw, N, cin, N, cin, nchunks, 0, bw),
+         ::psf::note_launch());
         ConvArgs a{};
         a.x = bx;
         a.x_cs = cin;

@@ -163,9 +163,21 @@ psf_status export_vtk(Ctx *c, const char *path, int async) {
     for (int q = 0; q < nk * nk; q++) Ke.v[q] = c->Ke0_host[q];
     const int grid = grid_for(c->nnodes, 256, 4 * std::max(c->num_sms, 1));
     switch (c->kind) {
-        case PSF_Q4_PLANE_STRAIN: (reaction_kernel<PSF_Q4_PLANE_STRAIN><<<grid, 256, 0, c->stream>>>(g, Ke, c->Epad, c->un, V->d_r), ::psf::note_launch()); break;
-        case PSF_Q4_HEAT: (reaction_kernel<PSF_Q4_HEAT><<<grid, 256, 0, c->stream>>>(g, Ke, c->Epad, c->un, V->d_r), ::psf::note_launch()); break;
-        default: (reaction_kernel<PSF_H8_SOLID><<<grid, 256, 0, c->stream>>>(g, Ke, c->Epad, c->un, V->d_r), ::psf::note_launch()); break;
+        case PSF_Q4_PLANE_STRAIN:
+            (reaction_kernel<PSF_Q4_PLANE_STRAIN><<<grid, 256, 0, c->stream>>>(
+                 g, Ke, c->Epad, c->un, V->d_r),
+             ::psf::note_launch());
+            break;
+        case PSF_Q4_HEAT:
+            (reaction_kernel<PSF_Q4_HEAT><<<grid, 256, 0, c->stream>>>(
+                 g, Ke, c->Epad, c->un, V->d_r),
+             ::psf::note_launch());
+            break;
+        default:
+            (reaction_kernel<PSF_H8_SOLID><<<grid, 256, 0, c->stream>>>(
+                 g, Ke, c->Epad, c->un, V->d_r),
+             ::psf::note_launch());
+            break;
     }
     PSF_CUDA(cudaGetLastError());
     PSF_CUDA(cudaMemcpyAsync(V->h_rho, c->rho, sizeof(double) * c->ne, cudaMemcpyDeviceToHost, c->stream));
