@@ -656,6 +656,9 @@ def main():
     ap.add_argument("--train-steps", type=int, default=3000, help="learned2d: Adam steps")
     ap.add_argument("--instances", type=int, default=256, help="heat_batch: number of instances")
     ap.add_argument("--eps", type=float, default=1e-8, help="relative residual of every solve")
+    ap.add_argument("--optimizer", default=None, choices=["oc", "mma", "conlin"],
+                    help="mbb2d/h8: the optimiser (default: MMA for mbb2d, OC for h8)")
+    ap.add_argument("--heaviside", action="store_true", help="mbb2d/h8: HeavisideFilter with beta continuation")
     ap.add_argument("--nx", type=int, default=None)
     ap.add_argument("--ny", type=int, default=None)
     ap.add_argument("--nz", type=int, default=None)
@@ -671,6 +674,12 @@ def main():
     if args.workload == "fem_q4":
         return bench_fem(args, rank, world)
     pr, desc = workload(args.workload, args.nx, args.ny, args.nz)
+    if args.optimizer is not None:   # the reference's other optimisers on the same problem
+        pr["optimizer"] = {"oc": 0, "mma": 1, "conlin": 2}[args.optimizer]
+        desc = desc.replace("MMA", args.optimizer.upper()).replace(", OC,", f", {args.optimizer.upper()},")
+    if args.heaviside:   # HeavisideFilter with the samples' beta continuation (0.5, x2 every 40)
+        pr.update(heaviside=1, beta=0.5, beta_every=40, beta_mult=2.0)
+        desc += ", Heaviside projection (beta 0.5, x2 every 40 iterations)"
     from pansfem2_gb300 import problems as PB
     ne_w, nn_w, nd_w = PB.counts(pr)
     config = {"workload": desc, "dofs": nn_w * nd_w, "elements": ne_w,
