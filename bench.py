@@ -243,14 +243,23 @@ def run_e2e(pr, solver, warmup, steps, cg_eps, warm_start, sample_at=()):
     return infos, wall, 8 * ne, 16 * ne, designs
 
 
-def fp64_at_designs(pr, solver, designs, cg_eps):
+def fp64_at_designs(pr, solver, designs, cg_eps, first_iter=0):
     """One SIMP iteration of the plain FP64 PCG path (cold-started solves, as that path
     runs) from each given design: device seconds of the iteration (CUDA events of its
-    phases), its compliance and its Krylov count."""
+    phases), its compliance and its Krylov count.  Design k entered iteration first_iter + k
+    of the trajectory; with the Heaviside filter the fresh problem gets the projection
+    sharpness beta of that iteration (the continuation multiplies beta at iterations 0,
+    beta_every, 2 beta_every, ...), so both solvers see the same densities."""
     import pansfem2_gb300 as P
     out = {}
     for k, s0 in sorted(designs.items()):
-        with P.Problem(pr) as prob:
+        prk = dict(pr)
+        if prk.get("heaviside") and int(prk.get("beta_every", 40)) > 0:
+            it = first_iter + k
+            prk["beta"] = float(prk.get("beta", 0.5)) * float(prk.get("beta_mult", 2.0)) ** (
+                it // int(prk.get("beta_every", 40)) + 1)
+            prk["beta_every"] = 0
+        with P.Problem(prk) as prob:
             prob.setup_bc()
             prob.simp_begin(solver=solver, cg_eps=cg_eps, warm_start=False, s0=s0)
             info = prob.simp_step()
@@ -650,6 +659,7 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 GPU PCG comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-vtk", action="store_true", help="skip the VTK export of the final state")
     ap.add_argument("--warm-start", type=int, default=1)
     ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch", "c1", "learned2d", "fem_q4"])
     ap.add_argument("--pairs", type=int, default=4000, help="learned2d: training pairs")
@@ -730,6 +740,23 @@ def main():
     value = world * args.steps / dev_t
     prob._sizes()
     ne, ndofs, nnz, nfree = prob.ne, prob.nnodes * prob.ndof, prob.nnz or 0, prob.nfree
+    # ---- one VTK export of the final state (the samples' ExportToVTK.h file), outside the timed
+    #      region: the call returns after the device work and the copy are queued; a host thread
+    #      formats and writes the file
+    vtk_info = None
+    if not args.no_vtk and rank == 0:
+        import tempfile
+        try:
+            with tempfile.TemporaryDirectory() as td:
+                path = os.path.join(td, "state.vtk")
+                t0 = time.perf_counter()
+                prob.export_vtk(path, async_=True)
+                t_call = time.perf_counter() - t0
+                prob.export_wait()
+                t_all = time.perf_counter() - t0
+                vtk_info = {"call_ms": 1e3 * t_call, "file_ms": 1e3 * t_all, "bytes": os.path.getsize(path)}
+        except Exception as e:   # reported, not fatal to the bench line
+            vtk_info = {"error": str(e)[:200]}
     prob.close()
 
     # roofline of the dominant kernel (the Krylov kernel)
@@ -767,8 +794,11 @@ def main():
                        "algorithmic_bytes_per_launch": bpi * kit / max(klaunch, 1),
                        "traffic_unit": "DRAM bytes per launch (read + write)",
                        "peak_source": peak_kind}
-    # launches of our kernels in the timed region: per step ~12 fixed kernels + Krylov launches + residual kernels
+    # launches of our kernels in the timed region, counted by the library
     out["gpu_launches"] = int(prob.launches)
+
+    if vtk_info is not None:
+        out["vtk_export"] = vtk_info
 
     # ---- e2e through host buffers
     if not args.no_e2e:
@@ -794,7 +824,7 @@ def main():
             sample_at = sorted({(i * args.steps) // nsamp for i in range(nsamp)} | {args.steps - 1})
             _, _, _, _, designs = run_e2e(pr, args.solver, args.warmup, args.steps, args.eps,
                                           bool(args.warm_start), sample_at=sample_at)
-        res = fp64_at_designs(pr, bsolver, designs, args.eps)
+        res = fp64_at_designs(pr, bsolver, designs, args.eps, first_iter=args.warmup)
         bt = float(np.mean([r["t"] for r in res.values()]))
         klast = max(res)
         out["fp64_gpu_pcg"] = {"solver": bsolver, "value": 1.0 / bt, "unit": UNIT,
