@@ -757,6 +757,30 @@ def main():
                 vtk_info = {"call_ms": 1e3 * t_call, "file_ms": 1e3 * t_all, "bytes": os.path.getsize(path)}
         except Exception as e:   # reported, not fatal to the bench line
             vtk_info = {"error": str(e)[:200]}
+    # ---- the reference's filter entry points on host arrays of this size (copies included),
+    #      median of 5 calls each, outside the timed region
+    entry_ms = None
+    if rank == 0:
+        try:
+            s = prob.fields()["s"]
+            prob.filter_setup()
+            d = -np.abs(np.sin(np.arange(prob.ne) * 0.37)) - 0.1
+            calls = {"DensityFilter.GetFilteredVariables": lambda: prob.filter_forward(s),
+                     "DensityFilter.GetFilteredSensitivitis": lambda: prob.filter_backward(d),
+                     "SensitivityFilter": lambda: prob.sensitivity_filter(s, d, 0),
+                     "SensitivityFilter2": lambda: prob.sensitivity_filter(s, d, 1),
+                     "HeavisideFilter.GetFilteredVariables": lambda: prob.heaviside_forward(4.0, s)}
+            entry_ms = {}
+            for name, fn in calls.items():
+                fn()
+                ts = []
+                for _ in range(5):
+                    t0 = time.perf_counter()
+                    fn()
+                    ts.append(1e3 * (time.perf_counter() - t0))
+                entry_ms[name] = float(np.median(ts))
+        except Exception as e:
+            entry_ms = {"error": str(e)[:200]}
     prob.close()
 
     # roofline of the dominant kernel (the Krylov kernel)
@@ -799,6 +823,8 @@ def main():
 
     if vtk_info is not None:
         out["vtk_export"] = vtk_info
+    if entry_ms is not None:
+        out["filter_entry_points_ms"] = entry_ms
 
     # ---- e2e through host buffers
     if not args.no_e2e:
