@@ -243,6 +243,15 @@ def run_e2e(pr, solver, warmup, steps, cg_eps, warm_start, sample_at=()):
     return infos, wall, 8 * ne, 16 * ne, designs
 
 
+def heaviside_beta_at(pr, it):
+    """The projection sharpness iteration `it` of a SIMP run uses: psf_simp_step multiplies
+    beta by beta_mult at the start of every iteration k with k % beta_every == 0, k = 0, 1, ..."""
+    beta, every = float(pr.get("beta", 0.5)), int(pr.get("beta_every", 40))
+    if every <= 0:
+        return beta
+    return beta * float(pr.get("beta_mult", 2.0)) ** (it // every + 1)
+
+
 def fp64_at_designs(pr, solver, designs, cg_eps, first_iter=0):
     """One SIMP iteration of the plain FP64 PCG path (cold-started solves, as that path
     runs) from each given design: device seconds of the iteration (CUDA events of its
@@ -254,10 +263,8 @@ def fp64_at_designs(pr, solver, designs, cg_eps, first_iter=0):
     out = {}
     for k, s0 in sorted(designs.items()):
         prk = dict(pr)
-        if prk.get("heaviside") and int(prk.get("beta_every", 40)) > 0:
-            it = first_iter + k
-            prk["beta"] = float(prk.get("beta", 0.5)) * float(prk.get("beta_mult", 2.0)) ** (
-                it // int(prk.get("beta_every", 40)) + 1)
+        if prk.get("heaviside"):
+            prk["beta"] = heaviside_beta_at(pr, first_iter + k)
             prk["beta_every"] = 0
         with P.Problem(prk) as prob:
             prob.setup_bc()
