@@ -845,7 +845,7 @@ def main():
         out["e2e"] = {"value": world * args.steps / ewall, "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h}
 
-    # ---- plain FP64 GPU PCG (the spec denominator) at designs sampled evenly from the
+    # ---- plain FP64 GPU PCG (the metric's denominator) at designs sampled evenly from the
     #      timed iterations.  That path cold-starts every solve, so one iteration's cost depends
     #      on its design only: the mean over the samples is its rate over the same iterations.
     if not args.no_compare:
