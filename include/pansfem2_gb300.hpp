@@ -418,6 +418,17 @@ private:
 // files the value fields are the dofs 0, 1, ... and "free" skips one.  Numbers go through
 // std::stod / std::stoi, which throw on a bad field, as in the reference.
 namespace detail {
+// entry d and length of a node row: std::vector<T> (operator[], size) or the reference's
+// Vector<T> (operator(), SIZE)
+template <class V>
+auto entry(V &v, int d, int) -> decltype(v[d]) { return v[d]; }
+template <class V>
+auto entry(V &v, int d, long) -> decltype(v(d)) { return v(d); }
+template <class V>
+auto length(const V &v, int) -> decltype((int)v.size()) { return (int)v.size(); }
+template <class V>
+auto length(const V &v, long) -> decltype((int)v.SIZE()) { return (int)v.SIZE(); }
+
 template <class Record>
 bool csv_records(const std::string &fname, const char *what, Record record) {
     std::ifstream in(fname);
@@ -483,9 +494,9 @@ bool ImportInitialFromCSV(std::vector<Node> &u, std::string fname) {
     return detail::csv_records(fname, "Initial Condition", [&](const std::string &id, std::istringstream &fields) {
         const int node = std::stoi(id);
         std::string v = id;
-        for (int dof = 0; dof < (int)u[node].size(); dof++) {
+        for (int dof = 0; dof < detail::length(u[node], 0); dof++) {
             std::getline(fields, v, ',');
-            if (v != "free") u[node][dof] = std::stod(v);
+            if (v != "free") detail::entry(u[node], dof, 0) = std::stod(v);
         }
     });
 }
@@ -511,7 +522,7 @@ public:
         std::vector<double> xs;
         std::vector<int32_t> conn;
         for (auto &xi : x)
-            for (int d = 0; d < dim; d++) xs.push_back(xi[d]);
+            for (int d = 0; d < dim; d++) xs.push_back(detail::entry(const_cast<Node &>(xi), d, 0));
         const int nen = elements.empty() ? 0 : (int)elements[0].size();
         for (auto &el : elements) {
             if ((int)el.size() != nen) throw std::runtime_error("pansfem2_gb300: elements of different sizes");
