@@ -46,11 +46,15 @@ def test_python_reader_matches_the_reference_on_the_grammar_cases():
     assert np.array_equal(u.reshape(-1), g["initial"])
 
 
-def test_cpp_reader_matches_the_reference_on_the_grammar_cases(tmp_path):
+@pytest.mark.parametrize("rows", ["std_vector", "reference_vector"])
+def test_cpp_reader_matches_the_reference_on_the_grammar_cases(tmp_path, rows):
+    """With std::vector<double> node rows, and with rows that have only the reference
+    Vector<T>'s operator() and SIZE()."""
     if shutil.which("g++") is None:
         pytest.skip("no g++")
     exe = str(tmp_path / "csv_check")
-    subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+    flags = ["-DVECTOR_ROWS"] if rows == "reference_vector" else []
+    subprocess.run(["g++", "-O1", "-std=c++17", *flags, "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "csv_check.cpp"), "-o", exe], check=True)
     out = subprocess.run([exe, GRAMMAR, "2"], check=True, capture_output=True, text=True).stdout
     got = {}
