@@ -97,3 +97,31 @@ def test_reference_sample_files():
     assert np.array_equal(i, g["read_fix"]) and np.array_equal(v, g["read_fixval"])
     i, v = _pairs(csvio.import_neumann_from_csv(os.path.join(SOLID, "Neumann.csv")))
     assert np.array_equal(i, g["read_load"]) and np.array_equal(v, g["read_loadval"])
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="the reference's headers are not present")
+def test_mirror_accepts_the_reference_vector_type(tmp_path):
+    """The reference's own Vector<double> rows (as ImportNodesFromCSV and Delaunay::GenerateNodes
+    return them) go into the mirror's readers and FemMesh unchanged: a compile check against
+    the reference's Vector.h (no device call)."""
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    src = tmp_path / "refvec.cpp"
+    src.write_text("""
+#include <string>
+#include <vector>
+#include "src/LinearAlgebra/Models/Vector.h"
+#include "pansfem2_gb300.hpp"
+int run(const std::string &p) {
+    std::vector<PANSFEM2::Vector<double> > x;
+    PANSFEM2_GB300::ImportNodesFromCSV(x, p + "Node.csv");
+    std::vector<std::vector<int> > el;
+    PANSFEM2_GB300::ImportElementsFromCSV(el, p + "Element.csv");
+    std::vector<PANSFEM2::Vector<double> > u(x.size(), PANSFEM2::Vector<double>(3));
+    PANSFEM2_GB300::ImportInitialFromCSV(u, p + "Initial.csv");
+    PANSFEM2_GB300::FemMesh m(PSF_H8_SOLID, x, el);
+    return (int)m.nnodes();
+}
+""")
+    subprocess.run(["g++", "-std=c++17", "-w", "-I", os.path.join(ROOT, "include"), "-I", "/root/reference",
+                    "-c", str(src), "-o", str(tmp_path / "refvec.o")], check=True)
