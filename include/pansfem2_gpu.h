@@ -287,19 +287,32 @@ psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const 
  * when they solve: a host whose pool allocator owns the device heap, a
  * real-time or embedded loop that forbids allocation after start-up, a host
  * whose allocator belongs to another framework.  Inputs and outputs are DEVICE
- * pointers (CSR arrays of n rows, b, x); the call makes no cudaMalloc /
- * cudaFree and calls no allocating library routine.  Its scratch lives in one
- * fixed file-scope device array sized for PSF_NOALLOC_MAX_ROWS rows (about
- * 11.6 MB, held by every GPU that loads the library until the process exits);
- * larger n is rejected with PSF_BAD_INPUT.  The first call on a device looks
- * up that array's device address (once per device, with the device current):
- * make that first call before any stream capture.  Every call reuses the same
+ * pointers (CSR arrays of n rows and nnz stored entries, b, x); the call makes
+ * no cudaMalloc / cudaFree and calls no allocating library routine.  Its
+ * scratch lives in one fixed file-scope device array sized for
+ * PSF_NOALLOC_MAX_ROWS rows (about 11.6 MB); larger n is rejected with
+ * PSF_BAD_INPUT.
+ *
+ * Set-up: the driver allocates that array, and the code of the kernels the
+ * solve launches, when it loads their modules, which with lazy module loading
+ * (the CUDA default) happens at their first use on a device.  A call with
+ * n == 0 (all pointers may be NULL) does only that set-up on the current device
+ * and returns PSF_OK: make it once per device at start-up, before the host's
+ * pool claims the device heap and before any stream capture.  Without it the
+ * first solve on a device does the set-up itself.  Every GPU that loads the
+ * library's modules holds the array until the process exits.
+ *
+ * The matrix is checked on the device before any kernel indexes through it:
+ * indptr[0] == 0, indptr non-decreasing, indptr[n] == nnz, column indices in
+ * [0, n); a malformed matrix returns PSF_BAD_INPUT.  Every call reuses the same
  * array, so calls that overlap on the GPU (other streams, other host threads)
  * race: order them on one stream or synchronise between them.  stream may be
- * NULL (the default stream).  Returns PSF_NOT_CONVERGED with the last iterate
- * after itmax iterations. */
+ * NULL (the default stream).  The call returns after its work is done.
+ * info->rel_residual is the FP64 true residual |b - A x| / |b| of the result,
+ * info->rel_residual_recurrence the CG recurrence's.  Returns
+ * PSF_NOT_CONVERGED with the last iterate after itmax iterations. */
 #define PSF_NOALLOC_MAX_ROWS 262144
-psf_status psf_csr_solve_noalloc(int n, const int32_t *d_indptr, const int32_t *d_indices,
+psf_status psf_csr_solve_noalloc(int n, int64_t nnz, const int32_t *d_indptr, const int32_t *d_indices,
                                  const double *d_data, const double *d_b, double *d_x, int itmax,
                                  double eps, void *stream, psf_solve_info *info);
 

@@ -13,6 +13,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# where the PANSFEM2 source tree lies, if anywhere (the reference harness and the golden
+# fixtures are built from it; nothing at run time needs it)
+REFERENCE_ROOT = os.environ.get("PANSFEM2_REF", "/root/reference")
 OUT = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "psf_oracle.c")
 USRC = os.path.join(HERE, "unet_oracle.c")
@@ -40,9 +43,14 @@ def build(verbose=False):
     return OUT
 
 
-def build_reference(ref_root="/root/reference"):
+def reference_present(ref_root=None):
+    return os.path.isdir(os.path.join(ref_root or REFERENCE_ROOT, "src"))
+
+
+def build_reference(ref_root=None):
     """Builds oracle/_ref/ from the reference sources when they are present."""
-    if not os.path.isdir(os.path.join(ref_root, "src")):
+    ref_root = ref_root or REFERENCE_ROOT
+    if not reference_present(ref_root):
         return False
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), ref_root])
     return True

@@ -1,9 +1,9 @@
 #!/bin/sh
 # Builds the reference-side harness from the PANSFEM2 sources where they lie
 # (header-only C++; nothing is copied).  Outputs go to oracle/_ref/ only.
-# Usage: oracle/build_ref.sh [path-to-PANSFEM2]   (default /root/reference)
+# Usage: oracle/build_ref.sh [path-to-PANSFEM2]   (default $PANSFEM2_REF, else /root/reference)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${PANSFEM2_REF:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

@@ -154,7 +154,8 @@ def load(path=LIB_PATH):
         "psf_fem_set_body_force": [vp, C.c_double, C.c_double],
         "psf_fem_set_edge_loads": [vp, C.c_int, C.POINTER(C.c_int32), C.c_double, C.c_double],
         # device pointers and a stream handle
-        "psf_csr_solve_noalloc": [C.c_int, vp, vp, vp, vp, vp, C.c_int, C.c_double, vp, C.POINTER(SolveInfo)],
+        "psf_csr_solve_noalloc": [C.c_int, C.c_int64, vp, vp, vp, vp, vp, C.c_int, C.c_double, vp,
+                                  C.POINTER(SolveInfo)],
         # learned preconditioner network
         "psf_unet_create": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)],
         "psf_unet_destroy": [vp],

@@ -46,6 +46,7 @@ struct Inst {
     long long me[kLev];      // per-level element offsets (coarse element matrices, levels >= 1)
     long long mv[kLev];      // per-level node offsets (multigrid vectors, all levels)
     long long ainv;          // offset of the coarsest dense inverse
+    long long c0;            // offset of the OC bisection's chunk sums (2 sets of ceil(n^2 / kChunk))
     double vf;
 };
 
@@ -56,6 +57,7 @@ struct Args {
     // level-0 element arrays
     double *s, *rho, *E, *dfdrho, *dfds, *dgds, *snew, *wsum;
     double *vw;              // volume weight of each design variable: sum over e in N(j) of w_ej / wsum_e
+    double *ocs;             // OC bisection chunk sums (per instance at Inst::c0)
     double *Bp;              // per OC call: x_j (-dfdx_j / dgdx_j)^iota
     float *Ef;
     float2 *Ew;              // E as double words (the Krylov operator)
@@ -725,51 +727,67 @@ __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ A
     }
 }
 
-// OC (OC.h:76-107) with the samples' filtered-volume constraint, bisection inside the block.
-// The trial design is x (-dfdx / (dgdx lambda))^iota = [x (-dfdx / dgdx)^iota] lambda^-iota, so the
-// per-element power is taken once per update and a bisection step costs a multiplication and a
-// clamp per element; the filtered volume sum_e (sum_j w_ej x_j) / wsum_e is sum_j vw_j x_j with the
-// weights vw precomputed.
+// OC (OC.h:76-107) with the samples' filtered-volume constraint, bisection inside the team.
+// The trial design x (-dfdx / (dgdx lambda))^iota is formed as [x (-dfdx / dgdx)^iota] lambda^-iota,
+// so the per-element power is taken once per update and a bisection step costs a multiplication
+// and a clamp per element; the filtered volume sum_e (sum_j w_ej x_j) / wsum_e is sum_j vw_j x_j
+// with the weights vw precomputed.  The volume is summed in the canonical chunk order
+// (psf_common.cuh), and the element arithmetic is the single-problem OC kernel's (psf_opt.cu
+// oc_fact_kernel): both paths take the same bisection branches on the same inputs, whatever
+// the team size.
 __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Args A) {
-    __shared__ double sm[32];
+    __shared__ double s_tot;
     const Team T = team(A);
     const Inst &I = A.inst[T.idx];
-    int par = 0;
     const int n = I.n;
     const long long ne = (long long)n * n;
+    const long long nc = (ne + kChunk - 1) / kChunk;
+    const int lane = threadIdx.x & 31;
+    const long long gw = T.tid >> 5, nw = T.nt >> 5;
     double *x = A.s + I.e0, *xn = A.snew + I.e0, *Bp = A.Bp + I.e0;
     const double *dfdx = A.dfds + I.e0, *dgdx = A.dgds + I.e0, *vw = A.vw + I.e0;
-    for (long long e = T.tid; e < ne; e += T.nt) {
-        const double b = -dfdx[e] / dgdx[e];
-        Bp[e] = x[e] * (A.iota == 0.5 ? sqrt(b) : pow(b, A.iota));
-    }
-    tsync(T);
+    for (long long c = gw; c < nc; c += nw)
+        for (long long e = c * kChunk + lane; e < ne && e < (c + 1) * kChunk; e += 32) {
+            const double b = -dfdx[e] / dgdx[e];
+            Bp[e] = x[e] * (A.iota == 0.5 ? sqrt(b) : pow(b, A.iota));
+        }
     const double vscale = 1.0 / (I.vf * (double)ne);
     double l0 = A.lmin, l1 = A.lmax, lambda = 0.0;
     int steps = 0;
     while ((l1 - l0) / (l1 + l0) > A.leps && steps < 4000) {
         lambda = 0.5 * (l1 + l0);
+        double *cs = A.ocs + I.c0 + (steps & 1) * nc;
         steps++;
         const double li = A.iota == 0.5 ? 1.0 / sqrt(lambda) : pow(lambda, -A.iota);
-        double vol = 0.0;
-        for (long long e = T.tid; e < ne; e += T.nt) {
-            const double xe = x[e];
-            double v = Bp[e] * li;
-            const double lo0 = (1.0 - A.move) * xe, hi0 = (1.0 + A.move) * xe;
-            const double lo = (0.0 < lo0) ? lo0 : 0.0;
-            const double hi = (hi0 < 1.0) ? hi0 : 1.0;
-            if (v < lo) v = lo;
-            else if (v > hi) v = hi;
-            xn[e] = v;
-            vol += vw[e] * v;
+        for (long long c = gw; c < nc; c += nw) {
+            double acc = 0.0;
+            for (long long e = c * kChunk + lane; e < ne && e < (c + 1) * kChunk; e += 32) {
+                const double xe = x[e];
+                double v = Bp[e] * li;
+                const double lo0 = (1.0 - A.move) * xe, hi0 = (1.0 + A.move) * xe;
+                const double lo = (0.0 < lo0) ? lo0 : 0.0;
+                const double hi = (hi0 < 1.0) ? hi0 : 1.0;
+                if (v < lo) v = lo;
+                else if (v > hi) v = hi;
+                xn[e] = v;
+                acc += vw[e] * v;
+            }
+            acc = warp_xor_sum(acc);
+            if (lane == 0) cs[c] = acc;
         }
-        vol = tsum(A, T, vol, sm, par);
-        const double g = vol * vscale - 1.0;
+        tsync(T);
+        if (threadIdx.x < 32) {
+            const double tot = warp_canonical_sum(cs, nc);
+            if (threadIdx.x == 0) s_tot = tot;
+        }
+        __syncthreads();
+        const double g = s_tot * vscale - 1.0;
         if (g > 0.0) l0 = lambda;
         else l1 = lambda;
+        __syncthreads();   // s_tot is rewritten by the next step
     }
-    tsync(T);
-    for (long long e = T.tid; e < ne; e += T.nt) x[e] = xn[e];
+    for (long long c = gw; c < nc; c += nw)
+        for (long long e = c * kChunk + lane; e < ne && e < (c + 1) * kChunk; e += 32) x[e] = xn[e];
     if (T.tid == 0) {
         double *o = A.out + (long long)T.idx * kOut;
         o[O_LAMBDA] = lambda;
@@ -880,7 +898,7 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     b->threads = threads;
     b->cluster = cluster;
     b->hinst.resize(ninst);
-    size_t ne = 0, nv = 0, mgn = 0, mge = 0, ai = 0;
+    size_t ne = 0, nv = 0, mgn = 0, mge = 0, ai = 0, ocs = 0;
     int ncmax = 0;
     for (int k = 0; k < ninst; k++) {
         Inst &I = b->hinst[k];
@@ -916,6 +934,8 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
         }
         I.ainv = (long long)ai;
         ai += (size_t)I.nc * I.nc;
+        I.c0 = (long long)ocs;
+        ocs += 2 * (((size_t)I.n * I.n + psf::kChunk - 1) / psf::kChunk);
         ncmax = std::max(ncmax, I.nc);
     }
     b->ne_tot = ne;
@@ -954,6 +974,7 @@ psf_status psf_batch_create(int ninst, const int *side, const int *edge, const i
     ck(balloc(b, &a.Ainv, ai));
     ck(balloc(b, &a.out, (size_t)ninst * psf::batch::kOut));
     ck(balloc(b, &a.red, (size_t)ninst * 2 * psf::batch::kMaxCluster));
+    ck(balloc(b, &a.ocs, ocs));
     if (s != PSF_OK) {
         batch_free(b);
         return s;

@@ -98,6 +98,9 @@ psf_status psf_create(psf_ctx **out, int kind, int nx, int ny, int nz, double lx
     A(dzalloc(c, &c->partials, (size_t)(kMaxRed + 2) * 8192));
     A(dzalloc(c, &c->scal, 64));
     A(dzalloc(c, &c->filt_wsum, c->ne));
+    A(dzalloc(c, &c->filt_vw, c->ne));
+    A(dzalloc(c, &c->oc_bp, c->ne));
+    A(dzalloc(c, &c->oc_cs, 2 * ((c->ne + kChunk - 1) / kChunk)));
     for (double **p : {&c->s, &c->rho, &c->dfdrho, &c->dgdrho, &c->dfds, &c->dgds, &c->snew}) A(dzalloc(c, p, c->ne));
     if (st == PSF_OK) st = ke_element0(c, 1.0, c->Ke0);
     if (st == PSF_OK) {

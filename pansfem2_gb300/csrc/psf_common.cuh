@@ -173,6 +173,27 @@ __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV >
     return s_ok && ld_volatile_int(&gs->status) == 0;
 }
 
+// ------------------------------------------------------------------ canonical sums
+// A sum over n terms whose rounding does not depend on the launch shape: the terms are cut
+// into chunks of kChunk consecutive indices; a chunk's sum is formed by one warp (lane l adds
+// terms l, l+32, ... of the chunk in order, then an xor butterfly, which leaves the same value
+// in every lane because each pairwise addition is commutative), and the chunk sums are added
+// by one warp in the same way.  Kernels with different grids, block sizes or thread-block
+// clusters (the single-problem and the batched OC bisection) therefore agree bit for bit.
+constexpr int kChunk = 256;
+__device__ __forceinline__ double warp_xor_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// sum of nv values v[0..nv) by one warp (all lanes return it)
+__device__ __forceinline__ double warp_canonical_sum(const double *v, long long nv) {
+    const int lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for (long long t = lane; t < nv; t += 32) acc += __ldcg(v + t);
+    return warp_xor_sum(acc);
+}
+
 // reduced values of the last grid_sync, read past L1 (the slot is rewritten every phase)
 __device__ __forceinline__ double gs_result(const GridSync *gs, int k) { return __ldcg(&gs->result[k]); }
 __device__ __forceinline__ double gs_result_max(const GridSync *gs) { return __ldcg(&gs->result_max); }

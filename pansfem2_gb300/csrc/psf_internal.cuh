@@ -85,6 +85,9 @@ struct Ctx {
     int *filt_off = nullptr;     // offsets (di, dj, dk) x filt_n
     double *filt_w = nullptr;    // weights
     double *filt_wsum = nullptr; // per-element weight sum (in-bounds entries)
+    double *filt_vw = nullptr;   // per-element volume weight sum over e in N(j) of w_ej / wsum_e (OC)
+    double *oc_bp = nullptr;     // OC: x (-dfdx / dgdx)^iota per element
+    double *oc_cs = nullptr;     // OC: two sets of canonical chunk sums
     double R = 0;
 
     // SIMP state

@@ -192,6 +192,8 @@ struct OcArgs {
     long long n;
     double *x, *xnew, *rho;
     const double *dfdx, *dgdx, *wsum;
+    const double *vw;   // volume weights sum over e in N(j) of w_ej / wsum_e (oc_fact_kernel)
+    double *bp, *cs;    // x (-dfdx / dgdx)^iota per element; two sets of chunk sums (oc_fact_kernel)
     double iota, lmin, lmax, leps, move, vscale, scale1;
     int heav;
     double beta;
@@ -240,6 +242,86 @@ __global__ void __launch_bounds__(256) oc_kernel(const __grid_constant__ Stencil
     if (tid == 0) {
         A.out[0] = lambda;
         A.out[1] = steps;
+    }
+}
+
+// OC without the Heaviside projection: the same bisection with the trial design formed as
+// [x (-dfdx / dgdx)^iota] lambda^-iota (the power once per update) and the filtered volume
+// sum_e (sum_j w_ej x_j) / wsum_e reordered as sum_j vw_j x_j, summed in the canonical chunk
+// order (psf_common.cuh).  Each warp owns whole chunks, so a step is one pass and one grid
+// barrier; the chunk sums alternate between two sets, so a set is rewritten only after a
+// later barrier.  The batched OC (psf_batch.cu oc_batch) uses the same arithmetic and order,
+// so both take the same bisection branches on the same inputs.  Against the reference's
+// expression the trial designs differ by rounding only.
+__global__ void __launch_bounds__(256) oc_fact_kernel(OcArgs A) {
+    __shared__ double s_tot;
+    const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long gw = gtid >> 5, nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long n = A.n, nc = (n + kChunk - 1) / kChunk;
+    for (long long c = gw; c < nc; c += nw)
+        for (long long e = c * kChunk + lane; e < n && e < (c + 1) * kChunk; e += 32) {
+            const double b = -A.dfdx[e] / A.dgdx[e];
+            A.bp[e] = A.x[e] * (A.iota == 0.5 ? sqrt(b) : pow(b, A.iota));
+        }
+    double l0 = A.lmin, l1 = A.lmax, lambda = 0.0;
+    int steps = 0;
+    while ((l1 - l0) / (l1 + l0) > A.leps && steps < 4000) {
+        lambda = 0.5 * (l1 + l0);
+        double *cs = A.cs + (steps & 1) * nc;
+        steps++;
+        const double li = A.iota == 0.5 ? 1.0 / sqrt(lambda) : pow(lambda, -A.iota);
+        for (long long c = gw; c < nc; c += nw) {
+            double acc = 0.0;
+            for (long long e = c * kChunk + lane; e < n && e < (c + 1) * kChunk; e += 32) {
+                const double xe = A.x[e];
+                double v = A.bp[e] * li;
+                const double lo0 = (1.0 - A.move) * xe, hi0 = (1.0 + A.move) * xe;
+                const double lo = (0.0 < lo0) ? lo0 : 0.0;      // std::max(T(), (1 - move) x)
+                const double hi = (hi0 < 1.0) ? hi0 : 1.0;      // std::min(1.0, (1 + move) x)
+                if (v < lo) v = lo;
+                else if (v > hi) v = hi;
+                A.xnew[e] = v;
+                acc += A.vw[e] * v;
+            }
+            acc = warp_xor_sum(acc);
+            if (lane == 0) cs[c] = acc;
+        }
+        if (!grid_barrier(A.gs, A.partials)) return;
+        if (threadIdx.x < 32) {
+            const double tot = warp_canonical_sum(cs, nc);
+            if (threadIdx.x == 0) s_tot = tot;
+        }
+        __syncthreads();
+        const double g = s_tot * A.vscale - 1.0 * A.scale1;
+        if (g > 0.0) l0 = lambda;
+        else l1 = lambda;
+    }
+    for (long long c = gw; c < nc; c += nw)
+        for (long long e = c * kChunk + lane; e < n && e < (c + 1) * kChunk; e += 32) A.x[e] = A.xnew[e];
+    if (gtid == 0) {
+        A.out[0] = lambda;
+        A.out[1] = steps;
+    }
+}
+
+// volume weights vw_j = sum over the in-grid stencil entries q of w_q / wsum_{j + q} (the
+// stencil is symmetric, so this sums w_ej / wsum_e over the elements e whose filter holds j),
+// in stencil order
+__global__ void volume_weights_kernel(const __grid_constant__ Stencil S, long long ne, const double *__restrict__ wsum,
+                                      double *__restrict__ vw) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        elem_ijk(S, e, i, j, k);
+        double acc = 0.0;
+        for (int o = 0; o < S.n; o++) {
+            const int a = i + S.di[o], b = j + S.dj[o], q = k + S.dk[o];
+            if (a < 0 || a >= S.nx || b < 0 || b >= S.ny) continue;
+            if (S.is3d && (q < 0 || q >= S.nz)) continue;
+            const long long m = S.is3d ? ((long long)S.ny * a + b) * S.nz + q : (long long)S.ny * a + b;
+            acc += S.w[o] / wsum[m];
+        }
+        vw[e] = acc;
     }
 }
 
@@ -548,6 +630,8 @@ psf_status filter_setup(Ctx *c, double R) {
     if (st != PSF_OK) { delete S; return st; }
     c->filt_n = S->n;
     (wsum_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, c->filt_wsum), ::psf::note_launch());
+    (volume_weights_kernel<<<grid_for(c->ne, 256, 65536), 256, 0, c->stream>>>(*S, c->ne, c->filt_wsum, c->filt_vw),
+     ::psf::note_launch());
     delete S;
     PSF_CUDA(cudaGetLastError());
     return PSF_OK;
@@ -731,10 +815,20 @@ psf_status oc_update(Ctx *c, double *x, const double *dfdx, const double *dgdx, 
     A.gs = c->gs;
     A.partials = c->partials;
     A.out = c->scal + 4;
-    const int blocks = coop_blocks_for(c, (const void *)oc_kernel, 256, c->ne);
-    if (!blocks) { delete S; set_error("OC kernel does not fit"); return PSF_CUDA_ERROR; }
-    void *args[] = {S, &A};
-    st = launch_coop(c, (const void *)oc_kernel, blocks, 256, args);
+    A.vw = c->filt_vw;
+    A.bp = c->oc_bp;
+    A.cs = c->oc_cs;
+    if (c->heav) {
+        const int blocks = coop_blocks_for(c, (const void *)oc_kernel, 256, c->ne);
+        if (!blocks) { delete S; set_error("OC kernel does not fit"); return PSF_CUDA_ERROR; }
+        void *args[] = {S, &A};
+        st = launch_coop(c, (const void *)oc_kernel, blocks, 256, args);
+    } else {
+        const int blocks = coop_blocks_for(c, (const void *)oc_fact_kernel, 256, c->ne);
+        if (!blocks) { delete S; set_error("OC kernel does not fit"); return PSF_CUDA_ERROR; }
+        void *args[] = {&A};
+        st = launch_coop(c, (const void *)oc_fact_kernel, blocks, 256, args);
+    }
     delete S;
     PSF_CHECK(st);
     PSF_CHECK(read_sync_status(c));

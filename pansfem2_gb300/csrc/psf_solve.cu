@@ -725,6 +725,13 @@ psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr,
     return PSF_OK;
 }
 
+// loads the module of the persistent PCG kernel (its code and static data), without a launch
+psf_status pcg_csr_load_module() {
+    cudaFuncAttributes fa;
+    PSF_CUDA(cudaFuncGetAttributes(&fa, pcg_csr_kernel));
+    return PSF_OK;
+}
+
 static psf_status pcg_csr(Ctx *c, int itmax, double eps, int *iters, double *rr, double *bb, int *conv) {
     // 5 reduced-length buffers carved from the nodal scratch
     return pcg_csr_any(c, c->nfree, c->indptr, c->indices, c->diag, c->data, c->F, c->u, c->w64[0], 1, itmax, eps,

@@ -57,7 +57,8 @@ def read_vtk_vectors(path, name):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    from oracle.build import REFERENCE_ROOT
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else REFERENCE_ROOT
     obuild.build()
     if not obuild.build_reference(ref_root):
         raise SystemExit(f"reference tree not found at {ref_root}")

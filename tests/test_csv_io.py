@@ -10,12 +10,13 @@ import subprocess
 import numpy as np
 import pytest
 
+from oracle.build import REFERENCE_ROOT
 from pansfem2_gb300 import csvio
 from tests.cases import load
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GRAMMAR = os.path.join(ROOT, "tests", "golden", "csv_grammar")
-SOLID = "/root/reference/sample/solid"
+SOLID = os.path.join(REFERENCE_ROOT, "sample", "solid")
 
 
 def _flat(rows):
@@ -99,7 +100,8 @@ def test_reference_sample_files():
     assert np.array_equal(i, g["read_load"]) and np.array_equal(v, g["read_loadval"])
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="the reference's headers are not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE_ROOT, "src")),
+                    reason="the reference's headers are not present")
 def test_mirror_accepts_the_reference_vector_type(tmp_path):
     """The reference's own Vector<double> rows (as ImportNodesFromCSV and Delaunay::GenerateNodes
     return them) go into the mirror's readers and FemMesh unchanged: a compile check against
@@ -123,5 +125,5 @@ int run(const std::string &p) {
     return (int)m.nnodes();
 }
 """)
-    subprocess.run(["g++", "-std=c++17", "-w", "-I", os.path.join(ROOT, "include"), "-I", "/root/reference",
+    subprocess.run(["g++", "-std=c++17", "-w", "-I", os.path.join(ROOT, "include"), "-I", REFERENCE_ROOT,
                     "-c", str(src), "-o", str(tmp_path / "refvec.o")], check=True)

@@ -1,7 +1,11 @@
 """Batched heat-conduction SIMP on the GPU against the same instances run one
-by one through the single-problem path (and one against the oracle): per
-instance compliance within 1e-6 at each of 8 iterations, densities of the last
-iteration (mean abs < 1e-4), every solve at the FP64 true residual."""
+by one through the single-problem path and against the oracle: per instance
+compliance within 1e-6 at each of 8 iterations, densities and designs of the
+last iteration within 1e-6 max-abs, every solve at the FP64 true residual.
+The OC bisection of both GPU paths forms the same trial designs and sums the
+filtered volume in the same launch-independent order, so they take the same
+bisection branches; the solves go to 1e-11 so that the inputs of the
+bisection agree far below its branch margins."""
 import numpy as np
 import pytest
 
@@ -16,6 +20,7 @@ INSTANCES = [dict(side=16, edge=0, patch_w=1, patch_i0=7, vf=0.4),
              dict(side=64, edge=0, patch_w=6, patch_i0=58, vf=0.45),
              dict(side=32, edge=1, patch_w=3, patch_i0=14, vf=0.42)]
 ITERS = 8
+EPS = 1e-11
 
 
 @pytest.fixture(scope="module")
@@ -34,7 +39,7 @@ def batched(gpu, request):
     from pansfem2_gb300.batch import HeatBatch
     threads, cluster = request.param
     with HeatBatch(INSTANCES, threads=threads, cluster=cluster) as B:
-        B.begin(cg_eps=1e-10, cg_itmax=5000, warm_start=True)
+        B.begin(cg_eps=EPS, cg_itmax=5000, warm_start=True)
         fs, res = [], []
         for _ in range(ITERS):
             B.step(1)
@@ -42,33 +47,36 @@ def batched(gpu, request):
             fs.append(r["f"].copy())
             res.append(r["res"].copy())
             assert (r["conv"] == 1).all(), r
-        rho = [B.fields(k)["rho"] for k in range(len(INSTANCES))]
+        rho = [B.fields(k) for k in range(len(INSTANCES))]
         probs = [B.problem(k) for k in range(len(INSTANCES))]
     return np.array(fs), np.array(res), rho, probs
 
 
 def test_batch_residuals(batched):
     _, res, _, _ = batched
-    assert res.max() < 1e-10
+    assert res.max() < EPS
 
 
 @pytest.mark.parametrize("k", range(len(INSTANCES)))
 def test_batch_matches_single_problem_path(gpu, batched, k):
-    fs, _, rho, probs = batched
+    fs, _, fl, probs = batched
     with gpu.Problem(probs[k]) as P:
         P.setup_bc()
-        P.simp_begin(solver="ir_mg_f32", cg_eps=1e-10)
+        P.simp_begin(solver="ir_mg_f32", cg_eps=EPS)
         for it in range(ITERS):
             info = P.simp_step()
             assert abs(info["f"] - fs[it, k]) <= 1e-6 * abs(info["f"]), (k, it, info["f"], fs[it, k])
-        # densities of the last iteration: the OC bisection takes its branch on the sign of the volume
-        # constraint, and where g is within rounding of 0 the two summation orders may take different
-        # branches (lambda then differs by the bisection tolerance); the compliance above is unaffected
-        d = np.abs(P.fields()["rho"] - rho[k])
-        assert d.mean() < 1e-4 and d.max() < 5e-2, (d.mean(), d.max())
+        single = P.fields()
+    d_rho = float(np.max(np.abs(single["rho"] - fl[k]["rho"])))
+    d_s = float(np.max(np.abs(single["s"] - fl[k]["s"])))
+    assert d_rho <= 1e-6 and d_s <= 1e-6, (k, d_rho, d_s)
 
 
-def test_batch_matches_oracle(batched):
-    fs, _, _, probs = batched
-    ref = O.simp_run(dict(probs[0], cg_eps=1e-10), ITERS)
-    assert np.max(np.abs(ref["f"] - fs[:, 0]) / np.abs(ref["f"])) < 1e-6
+@pytest.mark.parametrize("k", range(len(INSTANCES)))
+def test_batch_matches_oracle(batched, k):
+    fs, _, fl, probs = batched
+    ref = O.simp_run(dict(probs[k], cg_eps=EPS), ITERS, fields=True)
+    assert np.max(np.abs(ref["f"] - fs[:, k]) / np.abs(ref["f"])) < 1e-6
+    d_rho = float(np.max(np.abs(ref["rho"][ITERS - 1] - fl[k]["rho"])))
+    d_s = float(np.max(np.abs(ref["s_after"][ITERS - 1] - fl[k]["s"])))
+    assert d_rho <= 1e-6 and d_s <= 1e-6, (k, d_rho, d_s)
