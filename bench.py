@@ -56,8 +56,9 @@ def workload(name="mbb2d", nx=None, ny=None, nz=None):
 
 
 def mg_levels(pr, coarse_dofs=40):
-    """Node counts of the multigrid hierarchy (halving every axis while all are
-    even, until a level has <= coarse_dofs dofs), as psf_mg.cu builds it."""
+    """Node counts of the multigrid hierarchy (every axis coarsened to ceil(n/2)
+    elements while all have at least 2, until a level has <= coarse_dofs dofs),
+    as psf_mg.cu builds it."""
     from pansfem2_gb300 import problems as PB
     nd = PB.counts(pr)[2]
     dims = [pr["nx"], pr["ny"]] + ([pr["nz"]] if pr["kind"] == PB.H8_SOLID else [])
@@ -66,9 +67,9 @@ def mg_levels(pr, coarse_dofs=40):
     while True:
         if len(levels) > 1 and levels[-1] * nd <= coarse_dofs:
             break
-        if any(x % 2 or x < 2 for x in dims):
+        if any(x < 2 for x in dims):
             break
-        dims = [x // 2 for x in dims]
+        dims = [(x + 1) // 2 for x in dims]
         levels.append(nodes(dims))
     return levels
 
@@ -402,10 +403,18 @@ def bench_heat_batch(args, rank, world):
         with HeatBatch(insts, threads=threads, cluster=cluster) as B:
             B.begin(cg_eps=1e-8)
             B.step(args.warmup)
+            done = B.results()["done"]
             l0 = P.kernel_launches()
             t0 = time.perf_counter()
-            t_first = B.step(1)                      # the first timed iteration, also timed alone
-            dev_t = t_first + (B.step(args.steps - 1) if args.steps > 1 else 0.0)
+            # one replay per iteration; an instance counts for the iterations it entered
+            # unconverged (a converged one keeps its design, as the samples leave their loop)
+            dev_t, active, t_first = 0.0, 0, None
+            for _ in range(args.steps):
+                active += int(np.sum(done == 0))
+                t = B.step(1)
+                t_first = t if t_first is None else t_first   # the first timed iteration alone
+                dev_t += t
+                done = B.results()["done"]
             clk.window(t0, time.perf_counter())
             nlaunch = P.kernel_launches() - l0
             res = B.results()
@@ -421,7 +430,7 @@ def bench_heat_batch(args, rank, world):
         e2e_t = time.perf_counter() - t0
     dev_t, e2e_t = max_over_ranks([dev_t, e2e_t], world)
     n = len(insts)
-    value = world * n * args.steps / dev_t
+    value = world * active / dev_t
     # algorithmic bytes of the solve kernel: per node and FCG iteration ~250 B (FP64 Krylov vectors 112 B,
     # FP32 level-0 V(2,2) 100 B, coarse levels ~1/3 of level 0)
     its = res["iters"]
@@ -435,14 +444,15 @@ def bench_heat_batch(args, rank, world):
            "config": dict(config, threads_per_cta=threads, ctas_per_instance=cluster),
            "clocks": clk.summary(), "gpu_launches": int(nlaunch),   # the graph's kernel nodes per replay
            "autotune": {"batch_threads_x_cluster": tune_times},
-           "detail": {"solve_iterations_mean": float(np.mean(its)), "solve_iterations_max": int(np.max(its)),
+           "detail": {"active_instance_iterations": active, "converged_at_end": int(np.sum(res["done"] != 0)),
+                      "solve_iterations_mean": float(np.mean(its)), "solve_iterations_max": int(np.max(its)),
                       "true_residual_max": float(np.max(res["res"])), "all_converged": bool((res["conv"] == 1).all())},
            "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
                         "traffic": None, "kernel": "solve_batch (one CTA per instance)",
                         "bytes_last_iteration_solve": bytes_solve, "peak_source": peak_kind,
                         "note": "achieved = bytes of the last iteration's solves / (device time per iteration), "
                                 "an upper bound on the solve kernel's share"},
-           "e2e": {"value": world * n * args.steps / e2e_t, "unit": "instance-iterations/s", "h2d_bytes_per_step": 0,
+           "e2e": {"value": world * active / e2e_t, "unit": "instance-iterations/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 8 * 8 * n}}
     out["roofline"]["achieved"] = bytes_solve / (dev_t / args.steps) / 1e9
     out["roofline"]["frac"] = out["roofline"]["achieved"] / peak

@@ -74,6 +74,16 @@ const char *psf_last_error(void);
 /* kernel launches this host thread has made through the library so far (graph replays count
  * their kernel nodes); the difference over a call sequence is its launch count */
 psf_status psf_kernel_launches(long long *n);
+/* Launch shape of a persistent kernel family of this context (no counterpart in the
+ * reference; the autotuner pansfem2_gb300/autotune.py times candidates on the workload and
+ * sets the fastest).  kernel = PSF_KERNEL_PCG_CSR: a = lanes per CSR row (4, 8, 16),
+ * b = threads per block (256, 512, 1024), c = blocks per SM (1-8).  kernel = PSF_KERNEL_OPT
+ * (the OC / MMA / CONLIN kernels, 256 threads): c = blocks per SM (1-8), a and b ignored.
+ * Blocks per SM are capped by what fits.  Results agree to rounding across shapes. */
+#define PSF_KERNEL_PCG_CSR 0
+#define PSF_KERNEL_OPT 1
+psf_status psf_set_launch_shape(psf_ctx *ctx, int kernel, int a, int b, int c);
+psf_status psf_get_launch_shape(const psf_ctx *ctx, int kernel, int *a, int *b, int *c);
 /* sizes: elements, nodes, dofs per node, free dofs (after psf_set_dirichlet), CSR nnz (after psf_build_csr) */
 psf_status psf_sizes(const psf_ctx *ctx, int64_t *ne, int64_t *nnodes, int *ndof, int64_t *nfree,
                      int64_t *nnz);
@@ -290,7 +300,7 @@ psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const 
  * pointers (CSR arrays of n rows and nnz stored entries, b, x); the call makes
  * no cudaMalloc / cudaFree and calls no allocating library routine.  Its
  * scratch lives in one fixed file-scope device array sized for
- * PSF_NOALLOC_MAX_ROWS rows (about 11.6 MB); larger n is rejected with
+ * PSF_NOALLOC_MAX_ROWS rows (about 15.8 MB); larger n is rejected with
  * PSF_BAD_INPUT.
  *
  * Set-up: the driver allocates that array, and the code of the kernels the
@@ -424,8 +434,10 @@ psf_status psf_batch_destroy(psf_batch *batch);
 psf_status psf_batch_begin(psf_batch *batch, const psf_simp_params *prm);
 /* iters SIMP iterations of every instance (graph replays); device seconds */
 psf_status psf_batch_step(psf_batch *batch, int iters, double *seconds);
-/* per instance 8 values: f, g, OC lambda, solver iterations, FP64 relative
- * residual, converged, refinement passes, bisection steps */
+/* per instance 10 values: f, g, OC lambda, solver iterations, FP64 relative
+ * residual, solve converged, refinement passes, bisection steps, the compliance of
+ * the last update, done (IsConvergence held, OC.h:67-73: the instance's design is
+ * no longer updated, as the samples leave their loop there) */
 psf_status psf_batch_results(psf_batch *batch, double *out);
 /* one SIMP iteration without the graph, device seconds of the four phases
  * (filter + conductivities, solve, sensitivities, OC) */

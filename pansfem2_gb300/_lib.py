@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libpansfem2_gb300.so")
 
 PSF_OK, PSF_NOT_CONVERGED, PSF_FELL_BACK, PSF_BAD_INPUT, PSF_CUDA_ERROR, PSF_TIMEOUT, PSF_NOT_FINITE = range(7)
+PSF_KERNEL_PCG_CSR, PSF_KERNEL_OPT = 0, 1
 STATUS_NAMES = ["OK", "NOT_CONVERGED", "FELL_BACK", "BAD_INPUT", "CUDA_ERROR", "TIMEOUT", "NOT_FINITE"]
 
 SOLVERS = {
@@ -27,7 +28,8 @@ SOLVERS = {
 
 # every symbol declared in include/pansfem2_gpu.h
 EXPORTS = [
-    "psf_create", "psf_destroy", "psf_last_error", "psf_kernel_launches", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
+    "psf_create", "psf_destroy", "psf_last_error", "psf_kernel_launches", "psf_set_launch_shape",
+    "psf_get_launch_shape", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
     "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_solve",
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_sensitivity_filter",
     "psf_compliance_sensitivity",
@@ -151,6 +153,8 @@ def load(path=LIB_PATH):
         "psf_fem_reaction": [vp, dp, dp],
         "psf_fem_timings": [vp, dp, dp, dp],
         "psf_kernel_launches": [C.POINTER(C.c_longlong)],
+        "psf_set_launch_shape": [vp, C.c_int, C.c_int, C.c_int, C.c_int],
+        "psf_get_launch_shape": [vp, C.c_int, ip, ip, ip],
         "psf_fem_set_body_force": [vp, C.c_double, C.c_double],
         "psf_fem_set_edge_loads": [vp, C.c_int, C.POINTER(C.c_int32), C.c_double, C.c_double],
         # device pointers and a stream handle

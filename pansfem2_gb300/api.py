@@ -45,6 +45,17 @@ class Problem:
     def __exit__(self, *a):
         self.close()
 
+    # ---------------------------------------------------------------- launch shapes
+    def set_launch_shape(self, kernel, a=0, b=256, c=2):
+        """psf_set_launch_shape: kernel PSF_KERNEL_PCG_CSR (a lanes per row, b threads, c blocks
+        per SM) or PSF_KERNEL_OPT (c blocks per SM)."""
+        check(self.L.psf_set_launch_shape(self.h, int(kernel), int(a), int(b), int(c)))
+
+    def launch_shape(self, kernel):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(self.L.psf_get_launch_shape(self.h, int(kernel), C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     # ---------------------------------------------------------------- set-up
     def _sizes(self):
         ne, nn, nf, nz = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()

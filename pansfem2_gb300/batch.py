@@ -9,7 +9,7 @@ import numpy as np
 from . import _lib as L
 from . import problems as PB
 
-RESULT_FIELDS = ("f", "g", "lambda", "iters", "res", "conv", "passes", "bisect")
+RESULT_FIELDS = ("f", "g", "lambda", "iters", "res", "conv", "passes", "bisect", "f_prev", "done")
 
 
 class HeatBatch:
@@ -75,7 +75,7 @@ class HeatBatch:
         return dict(zip(("filter_moduli", "solve", "sens", "oc"), out))
 
     def results(self):
-        out = np.zeros((self.n, 8))
+        out = np.zeros((self.n, len(RESULT_FIELDS)))
         L.check(L.load().psf_batch_results(self._h, L.ptr(out)))
         return {k: out[:, i] for i, k in enumerate(RESULT_FIELDS)}
 

@@ -87,7 +87,9 @@ struct Args {
 };
 
 // per-instance outputs
-enum { O_F = 0, O_G, O_LAMBDA, O_ITERS, O_RES, O_CONV, O_PASSES, O_BISECT, kOut = 8 };
+// O_CONV: the solve reached its residual; O_FPREV: the compliance of the last update;
+// O_DONE: IsConvergence held (OC.h:67-73), so the design is no longer updated
+enum { O_F = 0, O_G, O_LAMBDA, O_ITERS, O_RES, O_CONV, O_PASSES, O_BISECT, O_FPREV, O_DONE, kOut = 10 };
 
 constexpr int kThreads = 512;
 
@@ -739,6 +741,16 @@ __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Arg
     __shared__ double s_tot;
     const Team T = team(A);
     const Inst &I = A.inst[T.idx];
+    // IsConvergence (OC.h:67-73) before the update, as the samples test it (sample :188-191): a
+    // converged instance keeps its design (the samples leave their loop there)
+    {
+        double *o = A.out + (long long)T.idx * kOut;
+        const double f = o[O_F], fp = o[O_FPREV];
+        if (o[O_DONE] != 0.0 || fabs(f - fp) / (f + fp) < 1.0e-5) {
+            if (T.tid == 0) o[O_DONE] = 1.0;
+            return;
+        }
+    }
     const int n = I.n;
     const long long ne = (long long)n * n;
     const long long nc = (ne + kChunk - 1) / kChunk;
@@ -792,6 +804,7 @@ __global__ void __launch_bounds__(kThreads) oc_batch(const __grid_constant__ Arg
         double *o = A.out + (long long)T.idx * kOut;
         o[O_LAMBDA] = lambda;
         o[O_BISECT] = steps;
+        o[O_FPREV] = o[O_F];
     }
 }
 
@@ -1114,6 +1127,7 @@ psf_status psf_batch_begin(psf_batch *b, const psf_simp_params *prm) {
     PSF_CUDA(cudaMemcpy(a.wsum, ws.data(), sizeof(double) * ws.size(), cudaMemcpyHostToDevice));
     PSF_CUDA(cudaMemcpy(a.s, s0.data(), sizeof(double) * s0.size(), cudaMemcpyHostToDevice));
     PSF_CUDA(cudaMemset(a.x, 0, sizeof(double) * b->nv_tot));
+    PSF_CUDA(cudaMemset(a.out, 0, sizeof(double) * b->ninst * psf::batch::kOut));   // f_prev = 0, not done
     PSF_CUDA(cudaFuncSetAttribute(psf::batch::solve_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)b->smem));
     if (b->exec) cudaGraphExecDestroy(b->exec);

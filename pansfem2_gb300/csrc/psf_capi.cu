@@ -42,6 +42,43 @@ psf_status psf_kernel_launches(long long *n) {
     return PSF_OK;
 }
 
+psf_status psf_set_launch_shape(psf_ctx *h, int kernel, int a, int b, int c) {
+    if (!h) { set_error("psf_set_launch_shape: null context"); return PSF_BAD_INPUT; }
+    Ctx *x = &h->c;
+    if (c < 1 || c > 8) { set_error("psf_set_launch_shape: blocks per SM must be in [1, 8]"); return PSF_BAD_INPUT; }
+    if (kernel == PSF_KERNEL_PCG_CSR) {
+        if ((a != 4 && a != 8 && a != 16) || (b != 256 && b != 512 && b != 1024)) {
+            set_error("psf_set_launch_shape: PCG lanes per row must be 4, 8 or 16 and threads 256, 512 or 1024");
+            return PSF_BAD_INPUT;
+        }
+        x->pcg_lanes = a;
+        x->pcg_threads = b;
+        x->pcg_blocks_per_sm = c;
+        return PSF_OK;
+    }
+    if (kernel == PSF_KERNEL_OPT) {
+        x->opt_blocks_per_sm = c;
+        return PSF_OK;
+    }
+    set_error("psf_set_launch_shape: unknown kernel family");
+    return PSF_BAD_INPUT;
+}
+
+psf_status psf_get_launch_shape(const psf_ctx *h, int kernel, int *a, int *b, int *c) {
+    if (!h || !a || !b || !c) { set_error("psf_get_launch_shape: null argument"); return PSF_BAD_INPUT; }
+    const Ctx *x = &h->c;
+    if (kernel == PSF_KERNEL_PCG_CSR) {
+        *a = x->pcg_lanes; *b = x->pcg_threads; *c = x->pcg_blocks_per_sm;
+        return PSF_OK;
+    }
+    if (kernel == PSF_KERNEL_OPT) {
+        *a = 0; *b = 256; *c = x->opt_blocks_per_sm;
+        return PSF_OK;
+    }
+    set_error("psf_get_launch_shape: unknown kernel family");
+    return PSF_BAD_INPUT;
+}
+
 psf_status psf_create(psf_ctx **out, int kind, int nx, int ny, int nz, double lx, double ly, double lz, double V,
                       double t) {
     if (!out) { set_error("psf_create: null output"); return PSF_BAD_INPUT; }
@@ -91,11 +128,11 @@ psf_status psf_create(psf_ctx **out, int kind, int nx, int ny, int nz, double lx
     A(dzalloc(c, &c->Dn, c->ndofs));
     A(dzalloc(c, &c->Dnf, c->ndofs));
     A(dzalloc(c, &c->Dl1f, c->ndofs));
-    A(dzalloc(c, &c->w64[0], 5 * c->ndofs));
+    A(dzalloc(c, &c->w64[0], 7 * c->ndofs));   // the CSR PCG's workspace (7 vectors)
     for (int k = 1; k < 8; k++) A(dzalloc(c, &c->w64[k], c->ndofs));
     for (int k = 0; k < 8; k++) A(dzalloc(c, &c->w32[k], c->ndofs));
     A(dzalloc(c, &c->gs, 1));
-    A(dzalloc(c, &c->partials, (size_t)(kMaxRed + 2) * 8192));
+    A(dzalloc(c, &c->partials, (size_t)kPartialSlots * 8192));   // grid_sync partials for up to 8192 blocks
     A(dzalloc(c, &c->scal, 64));
     A(dzalloc(c, &c->filt_wsum, c->ne));
     A(dzalloc(c, &c->filt_vw, c->ne));

@@ -3,10 +3,12 @@
 // Persistent kernels synchronise their blocks with grid_sync(), a barrier on
 // global-memory atomics whose wait is bounded: after kSpinLimit polls it sets
 // PSF_TIMEOUT in the status word and every block returns, so a wait can never
-// hang the GPU.  The last block to arrive also folds the per-block partial
-// sums of the phase (fixed order: deterministic) before it releases the
-// others, so a reduction costs one barrier.  These kernels are launched with
-// cudaLaunchCooperativeKernel, which guarantees that all blocks are resident.
+// hang the GPU.  A barrier can fold per-block partial sums: every block writes
+// its partials, arrives, waits for all arrivals, and then reduces all blocks'
+// partials itself in one fixed order, so every block holds the same,
+// deterministic sums without a second round through one releasing block.
+// These kernels are launched with cudaLaunchCooperativeKernel, which
+// guarantees that all blocks are resident.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,16 +30,34 @@ inline long long launches() { return g_launches; }
 
 constexpr int kMaxRed = 6;                    // values reduced by one grid_sync
 constexpr long long kSpinLimit = 1ll << 23;   // polls (x >= 64 ns each): ~1 s bound
+// partial sums a grid_sync needs: two alternating sets (the phase parity) of kMaxRed + 1
+// values per block, so a block that has left a barrier never overwrites the partials a
+// slower block is still reading
+constexpr int kPartialSlots = 2 * (kMaxRed + 1);
 
-// one slot of per-block partials for up to kMaxRed sums (and one max)
+// the barrier's global state (reset to zero before every launch)
 struct GridSync {
-    unsigned int count;       // arrivals in the current phase
-    unsigned int gen;         // phase generation (release flag)
+    unsigned int count;       // arrivals since the launch (phase p completes at count = (p + 1) * blocks)
+    unsigned int gen;         // unused
     int status;               // psf_status set by a device-side failure
     int pad;
-    double result[kMaxRed];   // reduced values of the last phase
-    double result_max;
+    double result[kMaxRed];   // unused
+    double result_max;        // unused
 };
+
+// per-block barrier state: the block's phase and the reduced values of its last grid_sync
+struct GridBlockState {
+    unsigned int phase;
+    int ok;
+    double res[kMaxRed + 1];
+};
+static __shared__ GridBlockState s_grid;
+
+// every kernel that calls grid_sync calls this first (all threads)
+__device__ __forceinline__ void grid_sync_init() {
+    if (threadIdx.x == 0) s_grid.phase = 0;
+    __syncthreads();
+}
 
 // explicit single-rounding a*b + c, so that values recomputed in two places agree bit for bit
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
@@ -91,86 +111,97 @@ __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ void red_release_add(unsigned int *p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ int ld_volatile_int(const int *p) {
     return *(const volatile int *)p;
 }
 
 // Grid-wide barrier with a fused reduction.
-//   partials: [NV][gridDim.x] doubles; this block's values in v[] (thread 0)
+//   partials: kPartialSlots * gridDim.x doubles; this block's values in v[] (thread 0)
 //   and pmax (thread 0) for an optional max over blocks (NMAX = 0 or 1).
-// On return every thread of every block sees gs->result[0..NV) and
-// gs->result_max.  Returns false if any block recorded a failure; callers
+// On return every thread of every block sees gs_result(gs, 0..NV) and
+// gs_result_max(gs), the same values in every block (partials summed in block
+// order by one warp per block: lane l adds blocks l, l + 32, ... in order, then
+// an xor butterfly).  Returns false if any block recorded a failure; callers
 // then return at once.
 template <int NV, int NMAX>
 __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV > 0 ? NV : 1],
                           double pmax) {
-    __shared__ int s_last;
-    __shared__ unsigned int s_gen;
-    __shared__ int s_ok;
-    __shared__ double s_red[32 * (NV > 0 ? NV : 1)];
     const unsigned int nb = gridDim.x;
-    __syncthreads();
+    __syncthreads();   // thread 0 holds the block's values; every thread has read the last results
     if (threadIdx.x == 0) {
+        const unsigned int ph = s_grid.phase;
+        double *slot = partials + (size_t)(ph & 1u) * (kMaxRed + 1) * nb;
 #pragma unroll
-        for (int k = 0; k < NV; k++) partials[(size_t)k * nb + blockIdx.x] = v[k];
-        if (NMAX) partials[(size_t)NV * nb + blockIdx.x] = pmax;
-        unsigned int g = ld_acquire(&gs->gen);
-        __threadfence();
-        unsigned int arrived = atomicAdd(&gs->count, 1u);
-        s_last = (arrived == nb - 1);
-        s_gen = g;
-    }
-    __syncthreads();
-    if (s_last) {
-        // last block: every thread loads a strided share of the partials (one
-        // L2 round trip instead of nb/32 dependent ones), fixed-order tree sum,
-        // publish, release
-        __threadfence();
-        if (NV > 0) {
-            double acc[NV > 0 ? NV : 1];
-#pragma unroll
-            for (int k = 0; k < NV; k++) {
-                acc[k] = 0.0;
-                for (unsigned int b = threadIdx.x; b < nb; b += blockDim.x)
-                    acc[k] += __ldcg(&partials[(size_t)k * nb + b]);
-            }
-            block_sum<(NV > 0 ? NV : 1)>(acc, s_red);
-            if (threadIdx.x == 0) {
-#pragma unroll
-                for (int k = 0; k < NV; k++) gs->result[k] = acc[k];
-            }
-        }
-        if (NMAX) {
-            double m = -INFINITY;
-            for (unsigned int b = threadIdx.x; b < nb; b += blockDim.x)
-                m = fmax(m, __ldcg(&partials[(size_t)NV * nb + b]));
-            m = block_max(m, s_red);
-            if (threadIdx.x == 0) gs->result_max = m;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            gs->count = 0;
-            __threadfence();
-            atomicAdd(&gs->gen, 1u);
-            s_ok = 1;
-        }
-    } else if (threadIdx.x == 0) {
-        const unsigned int g = s_gen;
+        for (int k = 0; k < NV; k++) slot[(size_t)k * nb + blockIdx.x] = v[k];
+        if (NMAX) slot[(size_t)NV * nb + blockIdx.x] = pmax;
+        red_release_add(&gs->count, 1u);   // arrival, ordered after the partial stores
+        const unsigned int target = (ph + 1u) * nb;
         long long spins = 0;
         int ok = 1;
-        while (ld_acquire(&gs->gen) == g) {
+        for (;;) {
+            const unsigned int c = ld_acquire(&gs->count);
+            const int st = ld_volatile_int(&gs->status);
+            if (st != 0) { ok = 0; break; }
+            if (c >= target) break;
             if (spins > 256) __nanosleep(32);   // tight polling first, then back off
-            if (++spins > kSpinLimit || ld_volatile_int(&gs->status) != 0) {
+            if (++spins > kSpinLimit) {
                 atomicCAS(&gs->status, 0, (int)PSF_TIMEOUT);
                 ok = 0;
                 break;
             }
         }
-        __threadfence();
-        s_ok = ok;
+        s_grid.ok = ok;
+        s_grid.phase = ph + 1u;
     }
     __syncthreads();
-    return s_ok && ld_volatile_int(&gs->status) == 0;
+    if (!s_grid.ok) return false;
+    if (NV + NMAX > 0) {
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            const double *slot = partials + (size_t)((s_grid.phase - 1u) & 1u) * (kMaxRed + 1) * nb;
+            if (NV > 0) {
+                // every lane adds its blocks in ascending order for each value; the loads of
+                // several blocks and values are in flight together
+                double acc[NV > 0 ? NV : 1];
+#pragma unroll
+                for (int k = 0; k < NV; k++) acc[k] = 0.0;
+#pragma unroll 4
+                for (unsigned int b = lane; b < nb; b += 32) {
+#pragma unroll
+                    for (int k = 0; k < NV; k++) acc[k] += __ldcg(slot + (size_t)k * nb + b);
+                }
+#pragma unroll
+                for (int k = 0; k < NV; k++) {
+                    double a = acc[k];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                    if (lane == 0) s_grid.res[k] = a;
+                }
+            }
+            if (NMAX) {
+                double m = -INFINITY;
+                for (unsigned int b = lane; b < nb; b += 32) m = fmax(m, __ldcg(slot + (size_t)NV * nb + b));
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+                if (lane == 0) s_grid.res[kMaxRed] = m;
+            }
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// reduced values of this block's last grid_sync
+__device__ __forceinline__ double gs_result(const GridSync *, int k) { return s_grid.res[k]; }
+__device__ __forceinline__ double gs_result_max(const GridSync *) { return s_grid.res[kMaxRed]; }
+
+// plain barrier (no reduction)
+__device__ __forceinline__ bool grid_barrier(GridSync *gs, double *partials) {
+    double v[1] = {0.0};
+    return grid_sync<0, 0>(gs, partials, v, 0.0);
 }
 
 // ------------------------------------------------------------------ canonical sums
@@ -194,15 +225,6 @@ __device__ __forceinline__ double warp_canonical_sum(const double *v, long long 
     return warp_xor_sum(acc);
 }
 
-// reduced values of the last grid_sync, read past L1 (the slot is rewritten every phase)
-__device__ __forceinline__ double gs_result(const GridSync *gs, int k) { return __ldcg(&gs->result[k]); }
-__device__ __forceinline__ double gs_result_max(const GridSync *gs) { return __ldcg(&gs->result_max); }
-
-// plain barrier (no reduction)
-__device__ __forceinline__ bool grid_barrier(GridSync *gs, double *partials) {
-    double v[1] = {0.0};
-    return grid_sync<0, 0>(gs, partials, v, 0.0);
-}
 
 }  // namespace psf
 

@@ -691,7 +691,7 @@ psf_status psf_fem_solve(psf_fem *h, int solver, int itmax, double eps, double *
     const long long n = f->nfree, nt = f->nn * f->nd;
     double *x = nullptr, *w = nullptr, *u = nullptr;
     PSF_CHECK(fem_alloc(f, (void **)&x, sizeof(double) * (n + 1)));
-    PSF_CHECK(fem_alloc(f, (void **)&w, sizeof(double) * 6 * (n + 1)));
+    PSF_CHECK(fem_alloc(f, (void **)&w, sizeof(double) * 7 * (n + 1)));   // the CSR PCG's workspace
     PSF_CHECK(fem_alloc(f, (void **)&u, sizeof(double) * nt));
     c->ksec = 0.0;
     c->klaunch = 0;

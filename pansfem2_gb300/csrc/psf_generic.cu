@@ -130,7 +130,7 @@ psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, c
     PSF_CUDA(cudaMallocAsync((void **)&dd, sizeof(double) * (nnz + 1), s));
     PSF_CUDA(cudaMallocAsync((void **)&db, sizeof(double) * (n + 1), s));
     PSF_CUDA(cudaMallocAsync((void **)&dx, sizeof(double) * (n + 1), s));
-    PSF_CUDA(cudaMallocAsync((void **)&w, sizeof(double) * 6 * (n + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&w, sizeof(double) * 7 * (n + 1), s));
     PSF_CUDA(cudaMemcpyAsync(dp, indptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(di, indices, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
     PSF_CUDA(cudaMemcpyAsync(dd, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));

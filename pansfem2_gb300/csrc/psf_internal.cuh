@@ -20,6 +20,9 @@ namespace psf {
 //   element fields: element id ny*i + j (3D: (ny*i + j)*nz + k), ne entries.
 //   CSR (free x free): int32 indptr/indices, FP64 values (FP32 copy for the
 //                  mixed-precision path), the diagonal position per row.
+// default launch shape of the CSR PCG kernel: lanes per row, threads per block, blocks per SM
+constexpr int kPcgDefaultLanes = 4, kPcgDefaultThreads = 1024, kPcgDefaultBlocksPerSm = 1;
+
 template <class T>
 struct DevBuf {
     T *p = nullptr;
@@ -78,6 +81,9 @@ struct Ctx {
     GridSync *gs = nullptr;
     double *partials = nullptr;
     int coop_blocks = 0;         // resident blocks for the persistent kernels
+    // launch shapes (psf_set_launch_shape; the autotuner picks them per workload)
+    int pcg_lanes = kPcgDefaultLanes, pcg_threads = kPcgDefaultThreads, pcg_blocks_per_sm = kPcgDefaultBlocksPerSm;
+    int opt_blocks_per_sm = 2;   // OC / MMA / CONLIN persistent kernels (256 threads)
 
     // filter (structured stencil)
     int filt_r = 0;              // stencil half width in elements

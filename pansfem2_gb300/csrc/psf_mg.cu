@@ -1,14 +1,20 @@
 // psf_mg.cu -- geometric multigrid preconditioned CG in FP32 inside FP64
 // iterative refinement (PSF_SOLVE_IR_MG_F32).
 //
-// Hierarchy: the structured grid is halved per axis while every axis stays
-// even and the level has more than kCoarseDofs dofs.  Coarse operators are
+// Hierarchy: the structured grid is coarsened by 2 per axis (a coarse axis of
+// ceil(n/2) elements) while every axis has at least 2 elements and the level
+// has more than kCoarseDofs dofs.  Coarse node I sits on fine node 2I; on an odd
+// axis the last coarse node lies one fine element beyond the grid (a ghost
+// node), and the last coarse element holds one fine child along that axis, the
+// missing one counting as an element of zero stiffness.  Coarse operators are
 // Galerkin products built element by element: bilinear (trilinear)
 // prolongation restricted to one coarse element depends only on that
 // element's nodes, so A_c = P^T A_f P is the sum over coarse elements of
 // K_c = sum_children P_c^T K_child P_c.  Element matrices are stored per coarse
 // element (FP32), with the rows / columns of fixed dofs zeroed at every level;
-// a coarse node is fixed where its coincident fine node is.
+// a coarse node is fixed where its coincident fine node is (a ghost node never
+// is; where its only fine neighbour is fixed its row is empty and the smoother
+// and the coarsest solve treat it as an identity row).
 //
 // Cycle: V(2,2) with degree-2 Chebyshev smoothing on the l1-Jacobi scaled operator,
 // full restriction R = P^T, and an
@@ -229,6 +235,8 @@ __global__ void galerkin_kernel(MgLev F, MgLev Cc, int fine_lev, KeF Ke) {
             int a, b, c;
             corner_of(ch, a, b, c);
             const int fi = 2 * ci + a, fj = 2 * cj + b, fk = T::is3d ? 2 * ck + c : 0;
+            // a child beyond an odd fine axis does not exist (zero stiffness)
+            if (fi >= F.nx || fj >= F.ny || (T::is3d && fk >= F.nz)) continue;
             // child matrix (masked at the fine level)
             float Kf[nk * nk];
             const long long fe = lelem<KIND>(F, fi, fj, fk);
@@ -296,8 +304,9 @@ __global__ void coarse_fixed_kernel(MgLev F, MgLev Cc) {
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < Cc.nnodes; n += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         lnode_ijk<KIND>(Cc, n, i, j, k);
-        const long long m = lnode<KIND>(F, 2 * i, 2 * j, 2 * k);
-        for (int s = 0; s < T::nd; s++) Cc.fixed[n * T::nd + s] = F.fixed[m * T::nd + s];
+        const bool ghost = 2 * i > F.nx || 2 * j > F.ny || (T::is3d && 2 * k > F.nz);
+        const long long m = ghost ? 0 : lnode<KIND>(F, 2 * i, 2 * j, 2 * k);
+        for (int s = 0; s < T::nd; s++) Cc.fixed[n * T::nd + s] = ghost ? 0 : F.fixed[m * T::nd + s];
     }
 }
 
@@ -815,6 +824,7 @@ __device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *
 
 template <int KIND>
 __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
+    grid_sync_init();
     using T = KT<KIND>;
     __shared__ double sm[32 * 4];
     __shared__ Block0View B0;
@@ -954,6 +964,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
 // caller, as for the FP64 kernel.
 template <int KIND>
 __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
+    grid_sync_init();
     using T = KT<KIND>;
     using dw::D;
     __shared__ double sm[32 * 4];
@@ -1097,6 +1108,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_apply_kernel(MgFcgArgs A, co
                                                                  const int *flags) {
     using T = KT<KIND>;
     if (flags && *(volatile const int *)flags) return;
+    grid_sync_init();
     __shared__ double sm[32 * 4];
     __shared__ Block0View B0;
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -1210,9 +1222,9 @@ static psf_status mg_build_hierarchy(Ctx *c) {
     while (nl < kMaxLev) {
         const MgLev &F = H->L[nl - 1];
         if (nl > 1 && F.ndofs <= kCoarseDofs) break;
-        if ((F.nx & 1) || (F.ny & 1) || (is3d && (F.nz & 1)) || F.nx < 2 || F.ny < 2 || (is3d && F.nz < 2)) break;
+        if (F.nx < 2 || F.ny < 2 || (is3d && F.nz < 2)) break;
         MgLev &Cc = H->L[nl];
-        Cc.nx = F.nx / 2; Cc.ny = F.ny / 2; Cc.nz = is3d ? F.nz / 2 : 0;
+        Cc.nx = (F.nx + 1) / 2; Cc.ny = (F.ny + 1) / 2; Cc.nz = is3d ? (F.nz + 1) / 2 : 0;
         Cc.nnodes = is3d ? (long long)(Cc.nx + 1) * (Cc.ny + 1) * (Cc.nz + 1) : (long long)(Cc.nx + 1) * (Cc.ny + 1);
         Cc.ndofs = Cc.nnodes * nd;
         Cc.ne = is3d ? (long long)Cc.nx * Cc.ny * Cc.nz : (long long)Cc.nx * Cc.ny;
@@ -1231,9 +1243,9 @@ static psf_status mg_build_hierarchy(Ctx *c) {
         PSF_CHECK(mg_alloc(H, c, (void **)&L.r, sizeof(float) * L.ndofs));
         PSF_CHECK(mg_alloc(H, c, (void **)&L.b, sizeof(float) * L.ndofs));
     }
-    if (nl < 2) { set_error("multigrid needs at least one even coarsening of the grid"); return PSF_BAD_INPUT; }
+    if (nl < 2) { set_error("multigrid needs a grid of at least 2 elements per axis"); return PSF_BAD_INPUT; }
     H->nc = (int)H->L[nl - 1].ndofs;
-    if (H->nc > 4096) { set_error("multigrid coarsest level too large for the dense solve (grid not divisible enough)"); return PSF_BAD_INPUT; }
+    if (H->nc > 4096) { set_error("multigrid coarsest level too large for the dense solve (an axis of 1 element stops the coarsening: aspect ratio too large)"); return PSF_BAD_INPUT; }
     PSF_CHECK(mg_alloc(H, c, (void **)&H->Ac, sizeof(double) * (size_t)H->nc * H->nc));
     return PSF_OK;
 }

@@ -9,7 +9,7 @@
 // must not be bypassed.  For them this entry point takes inputs and outputs
 // already in device memory and keeps its scratch (Krylov vectors, diagonal
 // positions, reduction slots, the validation flag) in one fixed file-scope
-// device array, g_noalloc_scratch, sized for kNoallocMaxRows rows (~11.6 MB).
+// device array, g_noalloc_scratch, sized for kNoallocMaxRows rows (~15.8 MB).
 //
 // The driver allocates that array, and the code of the kernels the solve
 // launches, when it loads their modules.  With lazy module loading (the CUDA
@@ -32,17 +32,17 @@ constexpr long long kNoallocMaxRows = 262144;   // PSF_NOALLOC_MAX_ROWS
 constexpr int kNoallocMaxBlocks = 1024;
 
 // scratch layout (bytes, each part 256-byte aligned)
-constexpr size_t kOffW = 0;                                                        // 5 * rows doubles
-constexpr size_t kOffDiag = kOffW + 5 * kNoallocMaxRows * sizeof(double);          // rows ints
+constexpr size_t kOffW = 0;                                                        // 7 * rows doubles
+constexpr size_t kOffDiag = kOffW + 7 * kNoallocMaxRows * sizeof(double);          // rows ints
 constexpr size_t kOffPart = kOffDiag + kNoallocMaxRows * sizeof(int);              // partial sums
-constexpr size_t kOffSync = kOffPart + (size_t)(kMaxRed + 2) * kNoallocMaxBlocks * sizeof(double);
+constexpr size_t kOffSync = kOffPart + (size_t)kPartialSlots * kNoallocMaxBlocks * sizeof(double);
 constexpr size_t kOffOut = kOffSync + 256;   // out[0..3] solver results, [4..5] true residual sums
 constexpr size_t kOffFlag = kOffOut + 128;   // CSR validation flag (int)
 constexpr size_t kScratchBytes = kOffOut + 256;
 static_assert(sizeof(GridSync) <= 256, "grid sync slot exceeds its scratch part");
 static_assert(kOffDiag % 256 == 0 && kOffPart % 256 == 0 && kOffSync % 256 == 0, "scratch parts misaligned");
 constexpr int kResBlocks = 512;   // blocks of the true-residual pass (partials fit the partials part)
-static_assert(2 * kResBlocks <= (kMaxRed + 2) * kNoallocMaxBlocks, "residual partials exceed their part");
+static_assert(2 * kResBlocks <= kPartialSlots * kNoallocMaxBlocks, "residual partials exceed their part");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 

@@ -203,6 +203,7 @@ struct OcArgs {
 };
 
 __global__ void __launch_bounds__(256) oc_kernel(const __grid_constant__ Stencil S, OcArgs A) {
+    grid_sync_init();
     __shared__ double sm[32];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -254,6 +255,7 @@ __global__ void __launch_bounds__(256) oc_kernel(const __grid_constant__ Stencil
 // so both take the same bisection branches on the same inputs.  Against the reference's
 // expression the trial designs differ by rounding only.
 __global__ void __launch_bounds__(256) oc_fact_kernel(OcArgs A) {
+    grid_sync_init();
     __shared__ double s_tot;
     const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long gw = gtid >> 5, nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -356,6 +358,7 @@ __device__ __forceinline__ double mu_(double a, double b) { return __dmul_rn(a, 
 
 template <bool kConlin>
 __global__ void __launch_bounds__(256) mma_kernel(MmaArgs A) {
+    grid_sync_init();
     __shared__ double sm[32 * 4];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -788,7 +791,8 @@ static bool opt_use_dw() {
 static int coop_blocks_for(Ctx *c, const void *fn, int threads, long long work) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1) return 0;
-    int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
+    const int bps = c->opt_blocks_per_sm;   // psf_set_launch_shape(PSF_KERNEL_OPT)
+    int blocks = c->num_sms * (per_sm < bps ? per_sm : bps);
     long long need = (work + threads - 1) / threads;
     if (blocks > need) blocks = (int)need;
     return blocks < 1 ? 1 : blocks;

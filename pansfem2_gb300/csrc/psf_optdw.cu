@@ -56,6 +56,7 @@ __device__ __forceinline__ void dw_add_to(D &acc, D v) { acc = dw::add(acc, v); 
 
 template <bool kConlin>
 __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
+    grid_sync_init();
     __shared__ double sm[32 * 4];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -371,7 +372,8 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
 static int coop_blocks_dw(Ctx *c, const void *fn, int threads, long long work) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1) return 0;
-    int blocks = c->num_sms * (per_sm < 2 ? per_sm : 2);
+    const int bps = c->opt_blocks_per_sm;   // psf_set_launch_shape(PSF_KERNEL_OPT)
+    int blocks = c->num_sms * (per_sm < bps ? per_sm : bps);
     long long need = (work + threads - 1) / threads;
     if (blocks > need) blocks = (int)need;
     return blocks < 1 ? 1 : blocks;

@@ -174,6 +174,7 @@ struct PcgArgs {
 
 template <class T, int KIND>
 __global__ void __launch_bounds__(256) pcg_ebe_kernel(PcgArgs<T> A) {
+    grid_sync_init();
     constexpr int nd = ndof_of<KIND>();
     __shared__ double sm[32 * 2];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -270,12 +271,14 @@ __global__ void __launch_bounds__(256) pcg_ebe_kernel(PcgArgs<T> A) {
 }
 
 // ------------------------------------------------------------------ persistent Jacobi PCG on the CSR (FP64)
+// Workspace (7 * rows doubles, from w): zpA, zpB = (z, p) pairs of 2 * rows each, then r, Ap, D.
 struct PcgCsrArgs {
     long long rows;
     int jacobi;                      // 1: ScalingCG (z = r / D), 0: CG (CG.h:123-154, z = r)
     const int *indptr, *indices, *diag;   // diag[i] = position of (i, i), -1 when absent
     const double *data, *b;
-    double *x, *r, *z, *pA, *pB, *Ap;
+    double *x, *r, *Ap, *D;
+    double2 *zpA, *zpB;              // (z, p) of the current / next iteration
     int itmax;
     double eps;
     GridSync *gs;
@@ -283,29 +286,50 @@ struct PcgCsrArgs {
     double *out;
 };
 
-// GetDiagonal (CG.h:397-404): CSR::get(i, i), zero when the entry is absent
-__device__ __forceinline__ double csr_diag(const PcgCsrArgs &A, long long i) {
-    if (!A.jacobi) return 1.0;
-    const int d = A.diag[i];
-    return d >= 0 ? A.data[d] : 0.0;
+// the workspace split (zp pairs first: 16-byte aligned for any row count)
+__host__ __device__ inline void pcg_csr_carve(PcgCsrArgs &a, double *w, long long n) {
+    a.zpA = (double2 *)w;
+    a.zpB = (double2 *)(w + 2 * n);
+    a.r = w + 4 * n;
+    a.Ap = w + 5 * n;
+    a.D = w + 6 * n;
 }
 
-// ScalingCG (CG.h:419-453): x0 = 0, r = b, z = r / D (division, CG.h:412), p = z;
-// the recurrence residual ||r|| < eps ||b|| stops it (CG.h:443-448).
-__global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
+
+// ScalingCG (CG.h:419-453): x0 = 0, r = b, z = r / D (GetDiagonal :397-404 with the division
+// of Scaling :408-415), p = z; the recurrence residual ||r|| < eps ||b|| stops it (:443-448).
+// One iteration is two phases and two grid barriers (each folding its dot products):
+//   product  p = z + beta p_prev formed on the fly from one 16-byte gather of the (z, p_prev)
+//            pair per stored entry, Ap = A p, p.Ap; the row's p is stored for the update;
+//   update   x += alpha p, r -= alpha Ap, z = r / D, z.r and r.r.
+// The CSR arrays are read once per iteration with streaming (evict-first) loads, so the
+// vectors (8 bytes per row each) stay in L2; a lane's loads of a row are issued before their
+// products.  Sums run in lane / tree order (the reference sums rows left to right and dot
+// products sequentially: the results agree to rounding).
+// Launch shape: LANES lanes per CSR row in the product (32 / LANES rows per warp), THREADS
+// threads per block; blocks per SM is chosen at launch (psf_set_launch_shape, autotuned).
+template <int LANES, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsrArgs A) {
+    constexpr int kPcgRowLanes = LANES;
+    grid_sync_init();
     __shared__ double sm[32 * 2];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long rows = A.rows;
     {
         double acc[2] = {0.0, 0.0};
-        for (long long i = tid; i < A.rows; i += stride) {
+        for (long long i = tid; i < rows; i += stride) {
             const double bv = A.b[i];
-            const double D = csr_diag(A, i);
+            double D = 1.0;
+            if (A.jacobi) {
+                const int d = A.diag[i];
+                D = d >= 0 ? A.data[d] : 0.0;   // CSR::get(i, i): zero when the entry is absent
+            }
+            A.D[i] = D;
             A.x[i] = 0.0;
             A.r[i] = bv;
             const double zv = bv / D;
-            A.z[i] = zv;
-            A.pA[i] = 0.0;
+            A.zpA[i] = make_double2(zv, 0.0);
             acc[0] += zv * bv;
             acc[1] += bv * bv;
         }
@@ -315,26 +339,56 @@ __global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
     double zr = gs_result(A.gs, 0);
     const double bnorm = sqrt(gs_result(A.gs, 1));
     double beta = 0.0, rr = 0.0;
-    double *pp = A.pA, *pn = A.pB;
+    double2 *cur = A.zpA, *nxt = A.zpB;
     int it = 0, conv = 0;
-    const int sub = threadIdx.x & 3;
-    const long long rstride = stride >> 2;
+    const int lane = threadIdx.x & 31, sub = lane & (kPcgRowLanes - 1);
+    const long long rows_per_warp = 32 / kPcgRowLanes;
+    const long long gw = tid >> 5, nw = stride >> 5;
+    // entries a lane handles per round (slots): one round covers 20 (4 lanes), 24 (8) or 32 (16)
+    // entries of a row, so a 2D row (at most 18) takes one round and its loads are all in flight
+    // at once: the indices and values, then the gathers, then the products
+    constexpr int SL = kPcgRowLanes == 4 ? 5 : (kPcgRowLanes == 8 ? 3 : 2);
     for (; it < A.itmax; it++) {
         double pAp[1] = {0.0};
-        // four lanes per row; warp-uniform loop bound (8 rows per warp)
-        for (long long base = (tid >> 5) << 3; base < A.rows; base += rstride) {
-            const long long i = base + ((threadIdx.x & 31) >> 2);
+        long long base = gw * rows_per_warp;
+        // the row bounds are fetched one pass ahead
+        int rs_n = 0, re_n = 0;
+        {
+            const long long i0 = base + lane / kPcgRowLanes;
+            if (i0 < rows) { rs_n = __ldg(A.indptr + i0); re_n = __ldg(A.indptr + i0 + 1); }
+        }
+        for (; base < rows; base += nw * rows_per_warp) {
+            const long long i = base + lane / kPcgRowLanes;
+            const int rs = rs_n, re = re_n;
+            {
+                const long long i1 = i + nw * rows_per_warp;
+                if (i1 < rows) { rs_n = __ldg(A.indptr + i1); re_n = __ldg(A.indptr + i1 + 1); }
+            }
             double v = 0.0;
-            if (i < A.rows)
-                for (int q = A.indptr[i] + sub; q < A.indptr[i + 1]; q += 4) {
-                    const int jc = A.indices[q];
-                    v += A.data[q] * fma(beta, pp[jc], A.z[jc]);
+            if (i < rows) {
+                for (int q = rs + sub; q < re; q += SL * kPcgRowLanes) {
+                    int j[SL];
+                    double a[SL];
+#pragma unroll
+                    for (int t = 0; t < SL; t++) {
+                        const int qt = q + t * kPcgRowLanes;
+                        const bool h = qt < re;
+                        j[t] = h ? __ldcs(A.indices + qt) : -1;
+                        a[t] = h ? __ldcs(A.data + qt) : 0.0;
+                    }
+                    double2 g[SL];
+#pragma unroll
+                    for (int t = 0; t < SL; t++) g[t] = j[t] >= 0 ? cur[j[t]] : make_double2(0.0, 0.0);
+#pragma unroll
+                    for (int t = 0; t < SL; t++) v += a[t] * fma(beta, g[t].y, g[t].x);
                 }
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            v += __shfl_xor_sync(0xffffffffu, v, 2);
-            if (sub == 0 && i < A.rows) {
-                const double pv = fma(beta, pp[i], A.z[i]);
-                pn[i] = pv;
+            }
+#pragma unroll
+            for (int o = 1; o < kPcgRowLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (sub == 0 && i < rows) {
+                const double2 gi = cur[i];
+                const double pv = fma(beta, gi.y, gi.x);
+                reinterpret_cast<double *>(nxt)[2 * i + 1] = pv;
                 A.Ap[i] = v;
                 pAp[0] += pv * v;
             }
@@ -343,12 +397,13 @@ __global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
         if (!grid_sync<1, 0>(A.gs, A.partials, pAp, 0.0)) return;
         const double alpha = zr / gs_result(A.gs, 0);
         double acc[2] = {0.0, 0.0};
-        for (long long i = tid; i < A.rows; i += stride) {
-            A.x[i] = A.x[i] + alpha * pn[i];
+        double *nxt_d = reinterpret_cast<double *>(nxt);
+        for (long long i = tid; i < rows; i += stride) {
+            A.x[i] = A.x[i] + alpha * nxt_d[2 * i + 1];
             const double rv = A.r[i] + (-alpha) * A.Ap[i];
             A.r[i] = rv;
-            const double zv = rv / csr_diag(A, i);
-            A.z[i] = zv;
+            const double zv = rv / A.D[i];
+            nxt_d[2 * i] = zv;
             acc[0] += zv * rv;
             acc[1] += rv * rv;
         }
@@ -358,7 +413,7 @@ __global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
         rr = gs_result(A.gs, 1);
         beta = zr1 / zr;
         zr = zr1;
-        double *t = pp; pp = pn; pn = t;
+        double2 *t = cur; cur = nxt; nxt = t;
         if (sqrt(rr) < A.eps * bnorm) { it++; conv = 1; break; }
         if (!isfinite(rr)) { it++; break; }
     }
@@ -367,8 +422,32 @@ __global__ void __launch_bounds__(256) pcg_csr_kernel(PcgCsrArgs A) {
         A.out[1] = rr;
         A.out[2] = bnorm * bnorm;
         A.out[3] = conv;
-        // the final x lives in A.x; p buffers swapped in registers only
     }
+}
+
+// the instantiated shapes: lanes per row {4, 8, 16} x threads per block {256, 512, 1024}
+static const void *pcg_csr_fn(int lanes, int threads) {
+#define PSF_PCG_SHAPE(L, T) \
+    if (lanes == L && threads == T) return (const void *)pcg_csr_kernel<L, T>;
+    PSF_PCG_SHAPE(4, 256) PSF_PCG_SHAPE(4, 512) PSF_PCG_SHAPE(4, 1024)
+    PSF_PCG_SHAPE(8, 256) PSF_PCG_SHAPE(8, 512) PSF_PCG_SHAPE(8, 1024)
+    PSF_PCG_SHAPE(16, 256) PSF_PCG_SHAPE(16, 512) PSF_PCG_SHAPE(16, 1024)
+#undef PSF_PCG_SHAPE
+    return nullptr;
+}
+
+// blocks of a persistent launch: blocks_per_sm per SM (at most what fits), at most one block
+// per `work_per_block` units of work, at least one
+static psf_status persistent_blocks(const void *fn, int threads, int sms, int blocks_per_sm, long long work,
+                                    long long work_per_block, int *blocks) {
+    int per_sm = 0;
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0));
+    if (per_sm < 1) { set_error("persistent kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
+    long long b = (long long)sms * (per_sm < blocks_per_sm ? per_sm : blocks_per_sm);
+    const long long need = (work + work_per_block - 1) / work_per_block;
+    if (b > need) b = need;
+    *blocks = (int)(b < 1 ? 1 : b);
+    return PSF_OK;
 }
 
 // ------------------------------------------------------------------ host side
@@ -517,22 +596,20 @@ psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *ind
     a.b = b;
     a.x = x;
     const long long n = rows;
-    a.r = w; a.z = w + n; a.pA = w + 2 * n; a.pB = w + 3 * n; a.Ap = w + 4 * n;
+    pcg_csr_carve(a, w, n);
     a.itmax = itmax;
     a.eps = eps;
     a.gs = c->gs;
     a.partials = c->partials;
     a.out = c->scal + 12;
-    int per_sm = 0;
-    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_csr_kernel, 256, 0));
-    if (per_sm < 1) { set_error("persistent PCG kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
-    int blocks = c->num_sms * (per_sm < 4 ? per_sm : 4);
-    long long need = (n * 4 + 255) / 256;
-    if (blocks > need) blocks = (int)need;
-    if (blocks < 1) blocks = 1;
+    const void *fn = pcg_csr_fn(c->pcg_lanes, c->pcg_threads);
+    if (!fn) { set_error("PCG launch shape not instantiated"); return PSF_BAD_INPUT; }
+    int blocks = 0;
+    PSF_CHECK(persistent_blocks(fn, c->pcg_threads, c->num_sms, c->pcg_blocks_per_sm, n,
+                                c->pcg_threads / c->pcg_lanes, &blocks));
     void *args[] = {&a};
     PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
-    PSF_CHECK(launch_coop(c, (const void *)pcg_csr_kernel, blocks, 256, args));
+    PSF_CHECK(launch_coop(c, fn, blocks, c->pcg_threads, args));
     PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
     PSF_CHECK(read_sync_status(c));
     PSF_CHECK(add_kernel_time(c));
@@ -582,6 +659,7 @@ __device__ __forceinline__ void csr_rows4(const BicgArgs &A, const double *__res
 // BiCGSTAB of the reference (x0 = 0, shadow residual rd = r0, stop on ||r|| < eps ||b||),
 // one persistent launch with five grid phases per iteration
 __global__ void __launch_bounds__(256) bicgstab_csr_kernel(BicgArgs A) {
+    grid_sync_init();
     __shared__ double sm[32 * 2];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -702,25 +780,23 @@ psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr,
     a.indptr = indptr; a.indices = indices; a.diag = diag; a.data = data;
     a.b = b;
     a.x = x;
-    a.r = w; a.z = w + rows; a.pA = w + 2 * rows; a.pB = w + 3 * rows; a.Ap = w + 4 * rows;
+    pcg_csr_carve(a, w, rows);
     a.itmax = itmax;
     a.eps = eps;
     a.gs = gs;
     a.partials = partials;
     a.out = out;
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0;
     PSF_CUDA(cudaGetDevice(&dev));
     PSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_csr_kernel, 256, 0));
-    if (per_sm < 1) { set_error("persistent PCG kernel does not fit on an SM"); return PSF_CUDA_ERROR; }
-    int blocks = sms * (per_sm < 4 ? per_sm : 4);
-    const long long need = (rows * 4 + 255) / 256;
-    if (blocks > need) blocks = (int)need;
+    const void *fn = pcg_csr_fn(kPcgDefaultLanes, kPcgDefaultThreads);
+    int blocks = 0;
+    PSF_CHECK(persistent_blocks(fn, kPcgDefaultThreads, sms, kPcgDefaultBlocksPerSm, rows,
+                                kPcgDefaultThreads / kPcgDefaultLanes, &blocks));
     if (blocks > max_blocks) blocks = max_blocks;
-    if (blocks < 1) blocks = 1;
     PSF_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), s));
     void *args[] = {&a};
-    PSF_CUDA(cudaLaunchCooperativeKernel((const void *)pcg_csr_kernel, dim3(blocks), dim3(256), args, 0, s));
+    PSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPcgDefaultThreads), args, 0, s));
     note_launch();
     return PSF_OK;
 }
@@ -728,7 +804,7 @@ psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr,
 // loads the module of the persistent PCG kernel (its code and static data), without a launch
 psf_status pcg_csr_load_module() {
     cudaFuncAttributes fa;
-    PSF_CUDA(cudaFuncGetAttributes(&fa, pcg_csr_kernel));
+    PSF_CUDA(cudaFuncGetAttributes(&fa, pcg_csr_fn(kPcgDefaultLanes, kPcgDefaultThreads)));
     return PSF_OK;
 }
 
