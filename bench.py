@@ -488,6 +488,82 @@ def learned_metric(nx, ny):
     return f"SIMP iters/s at {size} DOF ({nx}x{ny} MBB), resid 1e-8: learned FCG vs Jacobi PCG"
 
 
+def harvest_and_train(nx, ny, pairs, train_steps, seed=0):
+    """Training pairs harvested from the method's own multigrid FCG solves along seeded SIMP runs
+    of the nx x ny MBB beam (volume fraction uniform in [0.3, 0.6], point loads on the right
+    edge, designs of the first iterations), then the U-Net trained on the GPU (scale-free energy
+    loss, Adam).  Returns (network, harvest seconds, training seconds, loss history)."""
+    import pansfem2_gb300 as P
+    from pansfem2_gb300 import learned as Ln
+    from pansfem2_gb300 import problems as PB
+    H, W = nx + 1, ny + 1
+    rng = np.random.default_rng(seed)
+    ts = Ln.TrainSet(H, W, pairs)
+    t0 = time.perf_counter()
+    runs, iters_per_run = 8, 24
+    per_design = max(1, pairs // (runs * (iters_per_run // 2)))
+    while len(ts) < pairs:
+        pr = PB.mbb_q4(nx, ny, vf=float(rng.uniform(0.3, 0.6)), load_right=int(rng.integers(ny // 4, ny + 1)))
+        with P.Problem(pr) as prob:
+            prob.setup_bc()
+            prob.attach_learned(None, pre_mg=True, nu_post=1, use_net=False)
+            prob.simp_begin(solver="ir_mg_f32", cg_eps=1e-8, warm_start=True)
+            for k in range(iters_per_run):
+                prob.simp_step()
+                if k % 2 == 1 and len(ts) < pairs:
+                    prob.harvest(ts, min(per_design, pairs - len(ts)), iters=[0, 1, 2, 3, 4, 6, 8, 12, 16])
+    t_harvest = time.perf_counter() - t0
+    net = Ln.UNet(H, W, batch=8, seed=3)
+    t0 = time.perf_counter()
+    hist = Ln.train(net, ts, train_steps, batch=8, lr=1e-3, seed=5, loss="angle")
+    t_train = time.perf_counter() - t0
+    ts.close()
+    return net, t_harvest, t_train, hist
+
+
+def learned_leg(pr, nx, ny, warmup, steps, eps, fp64_value, fp64_iters, mg_value, pairs=400, train_steps=1500):
+    """The learned preconditioner on the headline problem: the U-Net is trained on a 512 x 256
+    beam (harvest + training on the GPU, timed and reported), and, being fully convolutional,
+    its parameters run on this grid; the learned flexible CG then runs the same SIMP window as
+    the headline (W warm-up iterations, K timed), with the Jacobi PCG fallback after twice the
+    plain FP64 PCG's iteration count on a stall."""
+    import pansfem2_gb300 as P
+    from pansfem2_gb300 import learned as Ln
+    tnx, tny = 512, 256
+    net_t, t_h, t_t, hist = harvest_and_train(tnx, tny, pairs, train_steps)
+    net = Ln.UNet(nx + 1, ny + 1, batch=1, seed=3)
+    net.set_params(net_t.get_params())
+    net.out_scale = net_t.out_scale
+    net_t.close()
+    limit = int(2 * fp64_iters) if fp64_iters else 0
+    with P.Problem(pr) as prob:
+        prob.setup_bc()
+        prob.attach_learned(net, pre_mg=True, nu_post=1, fallback_after=limit)
+        prob.simp_begin(solver="ir_learned_f32", cg_eps=eps, warm_start=True)
+        for _ in range(warmup):
+            prob.simp_step()
+        prob.sync()
+        l0 = P.kernel_launches()
+        infos = [prob.simp_step() for _ in range(steps)]
+        nl = P.kernel_launches() - l0
+    net.close()
+    t = sum(sum(i["phase_seconds"]) for i in infos)
+    v = steps / t
+    return {"solver": "ir_learned_f32", "value": v, "unit": UNIT,
+            "krylov_iterations": int(sum(i["solve"]["iterations"] for i in infos)),
+            "fell_back": int(sum(i["solve"]["fell_back"] for i in infos)),
+            "fallback_after": limit, "true_residual_max": max(i["solve"]["rel_residual"] for i in infos),
+            "f_last": infos[-1]["f"], "kernel_launches": int(nl),
+            "training": {"grid": f"{tnx}x{tny}", "pairs": pairs, "adam_steps": train_steps, "harvest_s": t_h,
+                         "train_s": t_t, "loss_first": float(np.mean(hist[:20])),
+                         "loss_last": float(np.mean(hist[-100:]))},
+            "vs_fp64_gpu_pcg": v / fp64_value if fp64_value else None,
+            "vs_multigrid_fcg": v / mg_value if mg_value else None,
+            "note": "U-Net (4 levels, 16->128 channels, bf16, tcgen05 convolutions) after one V-cycle in each "
+                    "flexible-CG preconditioner application; trained on the GPU by the project's kernels on pairs "
+                    "from the method's own solves; FP64 true residual decides"}
+
+
 def bench_learned2d(args, rank, world):
     """The learned preconditioner end to end at 512x256: training pairs harvested from
     seeded SIMP runs (vf uniform in [0.3, 0.6], point loads on the right edge, designs
@@ -497,31 +573,10 @@ def bench_learned2d(args, rank, world):
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     import pansfem2_gb300 as P
-    from pansfem2_gb300 import learned as Ln
     from pansfem2_gb300 import problems as PB
     P.load()
     nx, ny = args.nx or 512, args.ny or 256
-    H, W = nx + 1, ny + 1
-    rng = np.random.default_rng(rank)
-    ts = Ln.TrainSet(H, W, args.pairs)
-    t0 = time.perf_counter()
-    runs, iters_per_run = 8, 24
-    per_design = max(1, args.pairs // (runs * (iters_per_run // 2)))
-    while len(ts) < args.pairs:
-        pr = PB.mbb_q4(nx, ny, vf=float(rng.uniform(0.3, 0.6)), load_right=int(rng.integers(ny // 4, ny + 1)))
-        with P.Problem(pr) as prob:
-            prob.setup_bc()
-            prob.attach_learned(None, pre_mg=True, nu_post=1, use_net=False)
-            prob.simp_begin(solver="ir_mg_f32", cg_eps=1e-8, warm_start=True)
-            for k in range(iters_per_run):
-                prob.simp_step()
-                if k % 2 == 1 and len(ts) < args.pairs:
-                    prob.harvest(ts, min(per_design, args.pairs - len(ts)), iters=[0, 1, 2, 3, 4, 6, 8, 12, 16])
-    t_harvest = time.perf_counter() - t0
-    net = Ln.UNet(H, W, batch=8, seed=3)
-    t0 = time.perf_counter()
-    hist = Ln.train(net, ts, args.train_steps, batch=8, lr=1e-3, seed=5, loss="angle")
-    t_train = time.perf_counter() - t0
+    net, t_harvest, t_train, hist = harvest_and_train(nx, ny, args.pairs, args.train_steps, seed=rank)
     pr = PB.mbb_q4(nx, ny)
     res = {}
     clocks = None
@@ -551,7 +606,7 @@ def bench_learned2d(args, rank, world):
            "ms_per_step": 1e3 / res["ir_learned_f32"]["value"], "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "bf16 network / f32 cycle / f64 FCG", "data": "synthetic",
            "config": {"workload": f"MBB half beam {nx}x{ny} Q4, MMA, R=3, vf=0.4; U-Net 4 levels 16->128",
-                      "pairs": len(ts), "train_steps": args.train_steps, "residual": f"FP64 relative {args.eps:g}"},
+                      "pairs": args.pairs, "train_steps": args.train_steps, "residual": f"FP64 relative {args.eps:g}"},
            "clocks": clocks, "gpu_launches": res["ir_learned_f32"]["kernel_launches"],
            "training": {"harvest_s": t_harvest, "train_s": t_train, "loss": "angle",
                         "loss_first": float(hist[:20].mean()), "loss_last": float(hist[-100:].mean())},
@@ -703,6 +758,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-vtk", action="store_true", help="skip the VTK export of the final state")
+    ap.add_argument("--no-learned", action="store_true", help="mbb2d: skip the learned-preconditioner block")
     ap.add_argument("--warm-start", type=int, default=1)
     ap.add_argument("--workload", default="mbb2d", choices=["mbb2d", "h8", "heat_batch", "c1", "learned2d", "fem_q4"])
     ap.add_argument("--pairs", type=int, default=4000, help="learned2d: training pairs")
@@ -933,6 +989,12 @@ def main():
             "warm_start_gain_of_fp64_pcg": t_base_few / t_warm,
             "note": "value / fp64_gpu_pcg = solver_gain_both_cold x warm_start_gain_of_this_solver; the FP64 PCG "
                     "path itself cold-starts every solve (CG.h:423, x0 = 0)"}
+
+    # ---- the learned preconditioner on the same window (rank 0)
+    if rank == 0 and not args.no_learned and args.workload == "mbb2d":
+        fp = out.get("fp64_gpu_pcg", {})
+        out["learned"] = learned_leg(pr, pr["nx"], pr["ny"], args.warmup, args.steps, args.eps, fp.get("value"),
+                                     fp.get("krylov_iterations_per_solve"), value)
 
     # ---- parity with the oracle at this size and the CPU baseline (rank 0 at N=1 only): the
     #      first K SIMP iterations from the uniform start, on the device (the product path, same

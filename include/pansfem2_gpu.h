@@ -84,6 +84,12 @@ psf_status psf_kernel_launches(long long *n);
 #define PSF_KERNEL_OPT 1
 psf_status psf_set_launch_shape(psf_ctx *ctx, int kernel, int a, int b, int c);
 psf_status psf_get_launch_shape(const psf_ctx *ctx, int kernel, int *a, int *b, int *c);
+/* Diagnostic of the bounded device waits (no counterpart in the reference): a cooperative
+ * launch of `blocks` blocks in which the last block never arrives at a grid barrier (the
+ * arrival is a flag nothing sets); the others poll at most spin_limit times (1 .. 2^23; the
+ * solvers use 2^23, about a second), record PSF_TIMEOUT and return.  Returns the status the
+ * host read back (PSF_TIMEOUT) and leaves the context usable.  Nothing faults or hangs. */
+psf_status psf_diag_barrier_timeout(psf_ctx *ctx, int blocks, int64_t spin_limit);
 /* sizes: elements, nodes, dofs per node, free dofs (after psf_set_dirichlet), CSR nnz (after psf_build_csr) */
 psf_status psf_sizes(const psf_ctx *ctx, int64_t *ne, int64_t *nnodes, int *ndof, int64_t *nfree,
                      int64_t *nnz);
@@ -281,7 +287,9 @@ psf_status psf_csr_spmv(int n, const int32_t *indptr, const int32_t *indices, co
 /* ScalingCG (CG.h:419-453; solver PSF_SOLVE_CSR_JACOBI_F64) or CG (CG.h:123-154;
  * PSF_SOLVE_CSR_CG_F64) on host CSR arrays: x0 = 0, stop when the recurrence
  * residual drops below eps*||b||, last iterate returned with PSF_NOT_CONVERGED
- * after itmax iterations.  x has n entries. */
+ * after itmax iterations.  x has n entries.  Where the reference divides by a zero
+ * diagonal and lets inf / NaN run, ScalingCG returns PSF_BAD_INPUT; a non-finite
+ * residual (non-finite entries) returns PSF_NOT_FINITE. */
 psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, const double *data,
                          const double *b, int solver, int itmax, double eps, double *x,
                          psf_solve_info *info);

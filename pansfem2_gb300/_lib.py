@@ -29,7 +29,7 @@ SOLVERS = {
 # every symbol declared in include/pansfem2_gpu.h
 EXPORTS = [
     "psf_create", "psf_destroy", "psf_last_error", "psf_kernel_launches", "psf_set_launch_shape",
-    "psf_get_launch_shape", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
+    "psf_get_launch_shape", "psf_diag_barrier_timeout", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
     "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_solve",
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_sensitivity_filter",
     "psf_compliance_sensitivity",
@@ -155,6 +155,7 @@ def load(path=LIB_PATH):
         "psf_kernel_launches": [C.POINTER(C.c_longlong)],
         "psf_set_launch_shape": [vp, C.c_int, C.c_int, C.c_int, C.c_int],
         "psf_get_launch_shape": [vp, C.c_int, ip, ip, ip],
+        "psf_diag_barrier_timeout": [vp, C.c_int, C.c_int64],
         "psf_fem_set_body_force": [vp, C.c_double, C.c_double],
         "psf_fem_set_edge_loads": [vp, C.c_int, C.POINTER(C.c_int32), C.c_double, C.c_double],
         # device pointers and a stream handle

@@ -64,6 +64,15 @@ psf_status psf_set_launch_shape(psf_ctx *h, int kernel, int a, int b, int c) {
     return PSF_BAD_INPUT;
 }
 
+psf_status psf_diag_barrier_timeout(psf_ctx *h, int blocks, int64_t spin_limit) {
+    if (!h) { set_error("psf_diag_barrier_timeout: null context"); return PSF_BAD_INPUT; }
+    if (spin_limit < 1 || spin_limit > (1ll << 23)) {
+        set_error("psf_diag_barrier_timeout: spin_limit must be in [1, 2^23]");
+        return PSF_BAD_INPUT;
+    }
+    return diag_barrier_timeout(&h->c, blocks, (long long)spin_limit);
+}
+
 psf_status psf_get_launch_shape(const psf_ctx *h, int kernel, int *a, int *b, int *c) {
     if (!h || !a || !b || !c) { set_error("psf_get_launch_shape: null argument"); return PSF_BAD_INPUT; }
     const Ctx *x = &h->c;
@@ -566,7 +575,16 @@ psf_status psf_simp_step_host(psf_ctx *h, const double *s_in, double *s_out, dou
                               psf_iter_info *info) {
     CTX_CHECK(h);
     Ctx *c = &h->c;
-    if (s_in) PSF_CHECK(h2d(c, c->s, s_in, sizeof(double) * c->ne));
+    if (s_in) {
+        // a non-finite design entry would run through the filter, the moduli and the solve as NaN
+        // (the reference lets it); it is rejected before any device work
+        for (long long e = 0; e < c->ne; e++)
+            if (!std::isfinite(s_in[e])) {
+                set_error("psf_simp_step_host: non-finite design entry " + std::to_string(e));
+                return PSF_NOT_FINITE;
+            }
+        PSF_CHECK(h2d(c, c->s, s_in, sizeof(double) * c->ne));
+    }
     // keep the pre-update densities for rho_out: psf_simp_step overwrites s only
     psf_status st = psf_simp_step(h, info);
     if (st != PSF_OK && st != PSF_NOT_CONVERGED && st != PSF_FELL_BACK) return st;

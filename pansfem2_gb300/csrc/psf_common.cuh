@@ -128,7 +128,7 @@ __device__ __forceinline__ int ld_volatile_int(const int *p) {
 // then return at once.
 template <int NV, int NMAX>
 __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV > 0 ? NV : 1],
-                          double pmax) {
+                          double pmax, long long spin_limit = kSpinLimit) {
     const unsigned int nb = gridDim.x;
     __syncthreads();   // thread 0 holds the block's values; every thread has read the last results
     if (threadIdx.x == 0) {
@@ -147,7 +147,7 @@ __device__ bool grid_sync(GridSync *gs, double *partials, const double (&v)[NV >
             if (st != 0) { ok = 0; break; }
             if (c >= target) break;
             if (spins > 256) __nanosleep(32);   // tight polling first, then back off
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 atomicCAS(&gs->status, 0, (int)PSF_TIMEOUT);
                 ok = 0;
                 break;

@@ -204,6 +204,7 @@ psf_status learned_free(Ctx *c);                                                
 void vtk_free(Ctx *c);                                                                 // psf_vtk.cu
 psf_status learned_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_learned.cu
 psf_status residual64_pub(Ctx *c, const double *b, const double *x, double *r, double *rnorm, double *bnorm);  // psf_solve.cu
+psf_status diag_barrier_timeout(Ctx *c, int blocks, long long spin_limit);                                   // psf_solve.cu
 psf_status bicgstab_csr_any(Ctx *c, long long rows, const int *indptr, const int *indices, const double *data,
                             const double *b, double *x, double *const v[6], int itmax, double eps, int *iters,
                             double *rr, double *bb, int *conv);                                           // psf_solve.cu

@@ -30,8 +30,9 @@ psf_status read_sync_status(Ctx *c) {
     PSF_CUDA(cudaMemcpyAsync(&st, &c->gs->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     PSF_CUDA(cudaStreamSynchronize(c->stream));
     if (st != 0) {
-        set_error(st == PSF_TIMEOUT ? "device-side grid barrier wait exceeded its limit"
-                                    : "device-side failure in a persistent kernel");
+        set_error(st == PSF_TIMEOUT     ? "device-side grid barrier wait exceeded its limit"
+                  : st == PSF_BAD_INPUT ? "zero or non-finite diagonal entry (the Jacobi scaling divides by it)"
+                                        : "device-side failure in a persistent kernel");
         return (psf_status)st;
     }
     return PSF_OK;

@@ -17,6 +17,7 @@
 // exists to do it at start-up: it loads the modules of every kernel the solve
 // launches and looks up the array's address, and allocates nothing afterwards.
 // Every GPU that loads the modules holds the array until the process exits.
+#include <cmath>
 #include <string>
 
 #include "psf_internal.cuh"
@@ -191,7 +192,11 @@ extern "C" psf_status psf_csr_solve_noalloc(int n, int64_t nnz, const int32_t *d
     PSF_CUDA(cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, s));
     PSF_CUDA(cudaMemcpyAsync(&st, &gs->status, sizeof(int), cudaMemcpyDeviceToHost, s));
     PSF_CUDA(cudaStreamSynchronize(s));
-    if (st != 0) { set_error("device-side grid barrier wait exceeded its limit"); return (psf_status)st; }
+    if (st != 0) {
+        set_error(st == PSF_TIMEOUT ? "device-side grid barrier wait exceeded its limit"
+                                    : "zero or non-finite diagonal entry (the Jacobi scaling divides by it)");
+        return (psf_status)st;
+    }
     if (info) {
         psf_solve_info inf{};
         inf.iterations = (int)h[0];
@@ -199,6 +204,10 @@ extern "C" psf_status psf_csr_solve_noalloc(int n, int64_t nnz, const int32_t *d
         inf.rel_residual_recurrence = h[2] > 0 ? sqrt(h[1] / h[2]) : 0.0;
         inf.rel_residual = h[5] > 0 ? sqrt(h[4] / h[5]) : 0.0;
         *info = inf;
+    }
+    if (!std::isfinite(h[1]) || !std::isfinite(h[2])) {
+        set_error("non-finite residual (non-finite matrix or right-hand side entries)");
+        return PSF_NOT_FINITE;
     }
     return h[3] != 0.0 ? PSF_OK : PSF_NOT_CONVERGED;
 }

@@ -324,6 +324,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsr
             if (A.jacobi) {
                 const int d = A.diag[i];
                 D = d >= 0 ? A.data[d] : 0.0;   // CSR::get(i, i): zero when the entry is absent
+                // the reference divides by it (CG.h:412) and lets inf / NaN run; here the solve stops
+                if (!(D != 0.0) || !isfinite(D)) atomicCAS(&A.gs->status, 0, (int)PSF_BAD_INPUT);
             }
             A.D[i] = D;
             A.x[i] = 0.0;
@@ -557,7 +559,38 @@ static psf_status run_pcg_ebe(Ctx *c, PcgArgs<T> &a, int *iters, double *rr, dou
     *rr = h[1];
     *bb = h[2];
     *conv = (int)h[3];
+    if (!std::isfinite(h[1]) || !std::isfinite(h[2])) {
+        set_error("non-finite residual (non-finite matrix or right-hand side entries)");
+        return PSF_NOT_FINITE;
+    }
     return PSF_OK;
+}
+
+// A diagnostic of the bounded device waits: block absent_block never arrives at the barrier (its
+// arrival is the flag nothing sets); the others give up after spin_limit polls, record PSF_TIMEOUT
+// and return, so the host reads the status and the context stays usable.
+__global__ void barrier_timeout_probe(GridSync *gs, double *partials, int absent_block, long long spin_limit) {
+    grid_sync_init();
+    if ((int)blockIdx.x == absent_block) return;
+    double v[1] = {0.0};
+    grid_sync<0, 0>(gs, partials, v, 0.0, spin_limit);
+}
+
+psf_status diag_barrier_timeout(Ctx *c, int blocks, long long spin_limit) {
+    int per_sm = 0;
+    PSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, barrier_timeout_probe, 128, 0));
+    if (blocks < 2 || blocks > c->num_sms * per_sm) {
+        set_error("psf_diag_barrier_timeout: blocks must be in [2, resident blocks]");
+        return PSF_BAD_INPUT;
+    }
+    GridSync *gs = c->gs;
+    double *partials = c->partials;
+    int absent = blocks - 1;
+    void *args[] = {&gs, &partials, &absent, &spin_limit};
+    PSF_CHECK(launch_coop(c, (const void *)barrier_timeout_probe, blocks, 128, args));
+    const psf_status st = read_sync_status(c);
+    PSF_CHECK(reset_sync(c));
+    return st;
 }
 
 template <class T>
@@ -620,6 +653,10 @@ psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *ind
     *rr = h[1];
     *bb = h[2];
     *conv = (int)h[3];
+    if (!std::isfinite(h[1]) || !std::isfinite(h[2])) {
+        set_error("non-finite residual (non-finite matrix or right-hand side entries)");
+        return PSF_NOT_FINITE;
+    }
     return PSF_OK;
 }
 

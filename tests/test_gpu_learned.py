@@ -11,7 +11,12 @@ Ablation (what the trained network gains over the method without it):
   beats the untrained one on the held-out pairs;
 * whole solves: the FCG iteration counts of the cycle with the trained network,
   with an untrained one and without a network, all to the FP64 true residual
-  1e-8, are recorded (printed with -s); every variant must reach the residual.
+  1e-8, are recorded (printed with -s); every variant must reach the residual,
+  and the trained correction may cost at most twice the iterations of the cycle
+  without it (it does not reduce them: the negative result is recorded with its
+  experiment matrix in the design notes);
+* a stall (a limit below the iterations the learned FCG needs) falls back to the
+  FP64 Jacobi PCG, which still reaches the FP64 residual.
 """
 import numpy as np
 import pytest
@@ -90,6 +95,9 @@ def test_ablation_solves_reach_fp64_residual(trained, gpu):
         assert np.linalg.norm(u - u_mg) <= 1e-5 * np.linalg.norm(u_mg), name
         its[name] = info["iterations"]
     print("FCG iterations to FP64 1e-8:", its)
+    # the measured relation (no gain in whole solves; recorded with the experiment matrix in the design
+    # notes): the trained correction costs at most twice the iterations of the cycle without it
+    assert its["trained network"] <= 2 * its["cycle without network"], its
 
 
 def test_learned_simp_trajectory_matches_multigrid(trained, gpu):
@@ -115,3 +123,17 @@ def test_learned_simp_trajectory_matches_multigrid(trained, gpu):
     fb, rb = runs["ir_learned_f32"]
     assert np.max(np.abs(fa - fb) / np.abs(fa)) < 1e-6
     assert np.max(np.abs(ra - rb)) < 1e-6
+
+
+def test_stall_falls_back_to_fp64_jacobi_pcg(trained, gpu):
+    """A stall limit below what the learned flexible CG needs (3 iterations) hands the solve to the
+    FP64 Jacobi PCG from the current iterate: the solve reports the fallback and still reaches the
+    FP64 true residual, with the multigrid solver's answer."""
+    prob, net, _, _, _ = trained
+    prob.attach_learned(net, pre_mg=True, nu_post=1, fallback_after=3)
+    u, info = prob.solve("ir_learned_f32", itmax=100000, eps=1e-8)
+    assert info["fell_back"] == 1, info
+    assert info["rel_residual"] < 1e-8 and info["iterations"] > 3, info
+    u_mg, _ = prob.solve("ir_mg_f32", itmax=20000, eps=1e-10)
+    assert np.linalg.norm(u - u_mg) <= 1e-5 * np.linalg.norm(u_mg)
+    prob.attach_learned(net, pre_mg=True, nu_post=1)
