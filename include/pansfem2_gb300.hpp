@@ -129,6 +129,54 @@ template <class T>
 std::vector<T> CG(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps) {
     return detail::csr_solve(A, b, itrmax, eps, PSF_SOLVE_CSR_CG_F64);
 }
+// BiCGSTAB (CG.h:158-193)
+template <class T>
+std::vector<T> BiCGSTAB(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps) {
+    return detail::csr_solve(A, b, itrmax, eps, PSF_SOLVE_CSR_BICGSTAB_F64);
+}
+// BiCGSTAB2 (CG.h:196-253)
+template <class T>
+std::vector<T> BiCGSTAB2(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps) {
+    return detail::csr_solve(A, b, itrmax, eps, PSF_SOLVE_CSR_BICGSTAB2_F64);
+}
+// ScalingBiCGSTAB (CG.h:457-495)
+template <class T>
+std::vector<T> ScalingBiCGSTAB(CSR<T> &A, const std::vector<T> &b, int itrmax, T eps) {
+    return detail::csr_solve(A, b, itrmax, eps, PSF_SOLVE_CSR_SCALING_BICGSTAB_F64);
+}
+// ILU0 (CG.h:257-284): the factor on A's pattern, computed on the GPU
+template <class T>
+CSR<T> ILU0(CSR<T> &A) {
+    std::vector<T> m(A.Data().size());
+    check(psf_csr_ilu0(A.ROWS, A.Indptr().data(), A.Indices().data(), A.Data().data(), nullptr, nullptr, m.data(),
+                       nullptr), false);
+    return CSR<T>(A.ROWS, A.COLS, A.Indptr(), A.Indices(), m);
+}
+// PreILU0 (CG.h:288-315): U^-1 L^-1 b with the factor M
+template <class T>
+std::vector<T> PreILU0(CSR<T> &M, std::vector<T> &b) {
+    std::vector<T> v(b.size());
+    check(psf_csr_ilu0(M.ROWS, M.Indptr().data(), M.Indices().data(), M.Data().data(), M.Data().data(), b.data(),
+                       nullptr, v.data()), false);
+    return v;
+}
+// ILU0CG (CG.h:319-352) and ILU0BiCGSTAB (CG.h:356-391) with the factor M of ILU0(A)
+template <class T>
+std::vector<T> ILU0CG(CSR<T> &A, CSR<T> &M, const std::vector<T> &b, int itrmax, T eps) {
+    std::vector<T> x(b.size());
+    psf_solve_info info;
+    check(psf_csr_solve_ilu0(A.ROWS, A.Indptr().data(), A.Indices().data(), A.Data().data(), M.Data().data(),
+                             b.data(), PSF_SOLVE_CSR_ILU0_CG_F64, itrmax, eps, x.data(), &info));
+    return x;
+}
+template <class T>
+std::vector<T> ILU0BiCGSTAB(CSR<T> &A, CSR<T> &M, std::vector<T> &b, int itrmax, T eps) {
+    std::vector<T> x(b.size());
+    psf_solve_info info;
+    check(psf_csr_solve_ilu0(A.ROWS, A.Indptr().data(), A.Indices().data(), A.Data().data(), M.Data().data(),
+                             b.data(), PSF_SOLVE_CSR_ILU0_BICGSTAB_F64, itrmax, eps, x.data(), &info));
+    return x;
+}
 
 // ------------------------------------------------------------------ structured-grid problem
 // SquareMesh<T>(lx, ly, nx, ny) (SquareMesh.h:19-45) or its 3D analogue, with
@@ -317,16 +365,42 @@ private:
     T iota_, lmin_, lmax_, leps_, move_, prev_ = T();
 };
 
-// ------------------------------------------------------------------ MMA (MMA.h:18-509), m = 1
+// ------------------------------------------------------------------ MMA (MMA.h:18-509)
+// One constraint with uniform bounds (the SIMP samples) runs on the Problem's device state
+// (psf_mma_init / psf_mma_update); any other m <= 4 or per-variable bounds run on a device MMA
+// object of their own (psf_mma_create / psf_mma_update_host).
 template <class T>
 class MMA {
 public:
+    // the reference's signature (MMA.h:20-22): a device MMA object of its own
+    MMA(int n, int m, T a0, std::vector<T> a, std::vector<T> c, std::vector<T> d, const std::vector<T> &xmin,
+        const std::vector<T> &xmax)
+        : MMA(nullptr, n, m, a0, a, c, d, xmin, xmax) {}
+    // on a Problem: m = 1 with uniform bounds runs on the Problem's device state
     MMA(Problem &p, int n, int m, T a0, std::vector<T> a, std::vector<T> c, std::vector<T> d,
         const std::vector<T> &xmin, const std::vector<T> &xmax)
-        : p_(p), n_(n), a0_(a0), a_(a.at(0)), c_(c.at(0)), d_(d.at(0)), xmin_(xmin.at(0)), xmax_(xmax.at(0)) {
-        if (m != 1) throw std::runtime_error("pansfem2_gb300: the device MMA solves m = 1 (one constraint)");
+        : MMA(&p, n, m, a0, a, c, d, xmin, xmax) {}
+    MMA(Problem *p, int n, int m, T a0, std::vector<T> a, std::vector<T> c, std::vector<T> d,
+        const std::vector<T> &xmin, const std::vector<T> &xmax)
+        : p_(p), n_(n), m_(m), a0_(a0), av_(a), cv_(c), dv_(d), xminv_(xmin), xmaxv_(xmax) {
+        if (m < 1 || m > 4) throw std::runtime_error("pansfem2_gb300: the device MMA solves 1 <= m <= 4 constraints");
+        if ((int)a.size() < m || (int)c.size() < m || (int)d.size() < m || (int)xmin.size() < n || (int)xmax.size() < n)
+            throw std::runtime_error("pansfem2_gb300: MMA needs m entries of a, c, d and n of xmin, xmax");
+        bool uniform = true;
+        for (int j = 1; j < n; j++) uniform = uniform && xmin[j] == xmin[0] && xmax[j] == xmax[0];
+        general_ = !(p && m == 1 && uniform);
+        if (general_) {
+            std::vector<double> a64(a.begin(), a.end()), c64(c.begin(), c.end()), d64(d.begin(), d.end()),
+                lo(xmin.begin(), xmin.begin() + n), hi(xmax.begin(), xmax.begin() + n);
+            check(psf_mma_create(n, m, a0, a64.data(), c64.data(), d64.data(), lo.data(), hi.data(), &obj_), false);
+        }
         init();
     }
+    ~MMA() {
+        if (obj_) psf_mma_destroy(obj_);
+    }
+    MMA(const MMA &) = delete;
+    MMA &operator=(const MMA &) = delete;
     void SetParameters(T raa0, T albefa, T move, T asyinit, T asydecr, T asyincr, T epsvalue) {
         raa0_ = raa0; albefa_ = albefa; move_ = move; asyinit_ = asyinit; asydecr_ = asydecr; asyincr_ = asyincr;
         eps_ = epsvalue;
@@ -336,18 +410,33 @@ public:
     void UpdateVariables(std::vector<T> &xk, T f, std::vector<T> dfdx, std::vector<T> g,
                          std::vector<std::vector<T> > dgdx) {
         int newton = 0;
-        check(psf_mma_update(p_.ctx(), xk.data(), f, dfdx.data(), g.at(0), dgdx.at(0).data(), &newton));
+        if (general_) {
+            std::vector<double> x(xk.begin(), xk.begin() + n_), df(dfdx.begin(), dfdx.begin() + n_),
+                gv(g.begin(), g.begin() + m_), dg((size_t)m_ * n_);
+            for (int i = 0; i < m_; i++)
+                for (int j = 0; j < n_; j++) dg[(size_t)i * n_ + j] = dgdx.at(i).at(j);
+            check(psf_mma_update_host(obj_, x.data(), f, df.data(), gv.data(), dg.data(), &newton));
+            for (int j = 0; j < n_; j++) xk[j] = x[j];
+        } else {
+            check(psf_mma_update(p_->ctx(), xk.data(), f, dfdx.data(), g.at(0), dgdx.at(0).data(), &newton));
+        }
         prev_ = f;
     }
 
 private:
     void init() {
-        check(psf_mma_init(p_.ctx(), a0_, a_, c_, d_, xmin_, xmax_, raa0_, albefa_, move_, asyinit_, asydecr_,
-                           asyincr_, eps_), false);
+        if (general_)
+            check(psf_mma_set_parameters(obj_, raa0_, albefa_, move_, asyinit_, asydecr_, asyincr_, eps_), false);
+        else
+            check(psf_mma_init(p_->ctx(), a0_, av_.at(0), cv_.at(0), dv_.at(0), xminv_.at(0), xmaxv_.at(0), raa0_,
+                               albefa_, move_, asyinit_, asydecr_, asyincr_, eps_), false);
     }
-    Problem &p_;
-    int n_;
-    T a0_, a_, c_, d_, xmin_, xmax_;
+    Problem *p_;
+    int n_, m_;
+    T a0_;
+    std::vector<T> av_, cv_, dv_, xminv_, xmaxv_;
+    bool general_ = false;
+    psf_mma *obj_ = nullptr;
     T raa0_ = 1.0e-5, albefa_ = 0.1, move_ = 0.5, asyinit_ = 0.5, asydecr_ = 0.7, asyincr_ = 1.2, eps_ = 1.0e-5;
     T prev_ = T();
 };
@@ -360,6 +449,10 @@ public:
            const std::vector<T> &xmin, const std::vector<T> &xmax)
         : p_(p), n_(n), a0_(a0), a_(a.at(0)), c_(c.at(0)), d_(d.at(0)), xmin_(xmin.at(0)), xmax_(xmax.at(0)) {
         if (m != 1) throw std::runtime_error("pansfem2_gb300: the device CONLIN solves m = 1 (one constraint)");
+        for (int j = 1; j < n && j < (int)xmin.size() && j < (int)xmax.size(); j++)
+            if (xmin[j] != xmin[0] || xmax[j] != xmax[0])
+                throw std::runtime_error("pansfem2_gb300: the device CONLIN takes uniform bounds (xmin, xmax the same "
+                                         "for every variable)");
         init();
     }
     void SetParameters(T move, T epsvalue) {

@@ -46,7 +46,11 @@ typedef enum {
     PSF_SOLVE_IR_MG_F32 = 3,      /* FP32 multigrid-preconditioned flexible CG inside FP64 refinement */
     PSF_SOLVE_CSR_CG_F64 = 4,     /* CG (CG.h:123-154) on the CSR */
     PSF_SOLVE_CSR_BICGSTAB_F64 = 5, /* BiCGSTAB (CG.h:158-193) on the CSR */
-    PSF_SOLVE_IR_LEARNED_F32 = 6  /* FP32 FCG preconditioned by the learned grid U-Net inside FP64 refinement */
+    PSF_SOLVE_IR_LEARNED_F32 = 6, /* FP32 FCG preconditioned by the learned grid U-Net inside FP64 refinement */
+    PSF_SOLVE_CSR_SCALING_BICGSTAB_F64 = 7, /* ScalingBiCGSTAB (CG.h:457-495), psf_csr_solve */
+    PSF_SOLVE_CSR_BICGSTAB2_F64 = 8,        /* BiCGSTAB2 (CG.h:196-253), psf_csr_solve */
+    PSF_SOLVE_CSR_ILU0_CG_F64 = 9,          /* ILU0 + ILU0CG (CG.h:257-284, :319-352), psf_csr_solve(_ilu0) */
+    PSF_SOLVE_CSR_ILU0_BICGSTAB_F64 = 10    /* ILU0 + ILU0BiCGSTAB (CG.h:356-391), psf_csr_solve(_ilu0) */
 } psf_solver;
 
 typedef struct psf_ctx psf_ctx;
@@ -172,6 +176,22 @@ psf_status psf_mma_init(psf_ctx *ctx, double a0, double a, double c, double d, d
 psf_status psf_mma_update(psf_ctx *ctx, double *x, double f, const double *dfdx, double g,
                           const double *dgdx, int *newton_steps);
 
+/* MMA<T> (MMA.h:18-509) as a standalone object for any n and 1 <= m <= 4
+ * constraints, with per-variable bounds: MMA(n, m, a0, a, c, d, xmin, xmax)
+ * (MMA.h:64-90; a, c, d have m entries, xmin and xmax n), SetParameters (MMA.h:92-100),
+ * UpdateVariables (MMA.h:116-419) on host arrays: x (n, in / out), dfdx (n), g (m), dgdx
+ * (m x n, row i = constraint i).  The state (asymptotes, history) stays on the device.
+ * n > m: the (m+1) Newton system, one persistent launch; n <= m: the (n+1) system, one
+ * thread.  IsConvergence (MMA.h:107-113) is the caller's comparison of f values. */
+typedef struct psf_mma psf_mma;
+psf_status psf_mma_create(int n, int m, double a0, const double *a, const double *c, const double *d,
+                          const double *xmin, const double *xmax, psf_mma **out);
+psf_status psf_mma_set_parameters(psf_mma *mma, double raa0, double albefa, double move, double asyinit,
+                                  double asydecr, double asyincr, double epsvalue);
+psf_status psf_mma_update_host(psf_mma *mma, double *x, double f, const double *dfdx, const double *g,
+                               const double *dgdx, int *newton_steps);
+psf_status psf_mma_destroy(psf_mma *mma);
+
 /* CONLIN (CONLIN.h:17-455) for m = 1: the constructor's a0, a, c, d, xmin, xmax
  * (CONLIN.h:55-67) and SetParameters(move, epsvalue) (CONLIN.h:71-74).  The
  * approximation has q_j / x_j terms, so 0 < xmin < xmax is required. */
@@ -287,12 +307,25 @@ psf_status psf_csr_spmv(int n, const int32_t *indptr, const int32_t *indices, co
 /* ScalingCG (CG.h:419-453; solver PSF_SOLVE_CSR_JACOBI_F64) or CG (CG.h:123-154;
  * PSF_SOLVE_CSR_CG_F64) on host CSR arrays: x0 = 0, stop when the recurrence
  * residual drops below eps*||b||, last iterate returned with PSF_NOT_CONVERGED
- * after itmax iterations.  x has n entries.  Where the reference divides by a zero
+ * after itmax iterations.  x has n entries.  Also the solvers 7-10 (ScalingBiCGSTAB,
+ * BiCGSTAB2, ILU0CG, ILU0BiCGSTAB).  Where the reference divides by a zero
  * diagonal and lets inf / NaN run, ScalingCG returns PSF_BAD_INPUT; a non-finite
  * residual (non-finite entries) returns PSF_NOT_FINITE. */
 psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, const double *data,
                          const double *b, int solver, int itmax, double eps, double *x,
                          psf_solve_info *info);
+/* The solvers PSF_SOLVE_CSR_ILU0_CG_F64 / _ILU0_BICGSTAB_F64 with a given ILU(0)
+ * factor m on the matrix's pattern (ILU0CG(A, M, b, ...), CG.h:319; ILU0BiCGSTAB,
+ * CG.h:356), m = NULL factoring A here.  The triangular solves run level by level. */
+psf_status psf_csr_solve_ilu0(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                              const double *m, const double *b, int solver, int itmax, double eps, double *x,
+                              psf_solve_info *info);
+/* ILU0 (CG.h:257-284) of a CSR matrix on its own pattern: m_out (nnz values, optional)
+ * receives the factor (m_in given: used as the factor instead); with b and v_out,
+ * PreILU0 (CG.h:288-315) v = U^-1 L^-1 b.  Level-scheduled on the device, each row's
+ * sums in the reference's order (bit-exact). */
+psf_status psf_csr_ilu0(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                        const double *m_in, const double *b, double *m_out, double *v_out);
 /* DensityFilter::GetFilteredVariables / GetFilteredSensitivitis (DensityFilter.h:44-71)
  * with explicit neighbour lists: out_i = sum_k w[k]*in[idx[k]] / sum_k w[k] over
  * k in [ptr[i], ptr[i+1]), summed in list order. */
@@ -308,7 +341,7 @@ psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const 
  * pointers (CSR arrays of n rows and nnz stored entries, b, x); the call makes
  * no cudaMalloc / cudaFree and calls no allocating library routine.  Its
  * scratch lives in one fixed file-scope device array sized for
- * PSF_NOALLOC_MAX_ROWS rows (about 15.8 MB); larger n is rejected with
+ * PSF_NOALLOC_MAX_ROWS rows (about 16.1 MB); larger n is rejected with
  * PSF_BAD_INPUT.
  *
  * Set-up: the driver allocates that array, and the code of the kernels the

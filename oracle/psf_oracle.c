@@ -839,6 +839,63 @@ int orc_ilu0_cg(const orc_csr *A, const orc_csr *M, const double *b, int itmax, 
     return ret;
 }
 
+/* the preconditioned BiCGSTAB loop of ScalingBiCGSTAB (CG.h:457-495) and ILU0BiCGSTAB
+ * (CG.h:356-391): M(v) is the preconditioner; p starts as M(r) for the scaling variant
+ * (CG.h:463) and as r for the ILU(0) one (CG.h:362), as the reference writes them */
+static int precond_bicgstab(const orc_csr *A, const double *b, int itmax, double eps, double *x,
+                            void (*M)(const void *, const double *, double *), const void *ctx, int p_scaled) {
+    long n = A->rows;
+    size_t sz = sizeof(double) * n;
+    double *r = xmalloc(sz), *rd = xmalloc(sz), *p = xmalloc(sz), *Mp = xmalloc(sz), *AMp = xmalloc(sz),
+           *s = xmalloc(sz), *Ms = xmalloc(sz), *AMs = xmalloc(sz);
+    for (long i = 0; i < n; i++) x[i] = 0.0;
+    orc_spmv(A, x, AMp);
+    for (long i = 0; i < n; i++) r[i] = b[i] - AMp[i];
+    memcpy(rd, r, sz);
+    if (p_scaled) M(ctx, r, p);
+    else memcpy(p, r, sz);
+    double rdr = dot(rd, r, n);
+    double bnorm = sqrt(dot(b, b, n));
+    int ret = -1;
+    for (int k = 0; k < itmax; ++k) {
+        M(ctx, p, Mp);
+        orc_spmv(A, Mp, AMp);
+        double alpha = rdr / dot(rd, AMp, n);
+        double ma = -alpha;
+        for (long i = 0; i < n; i++) s[i] = 1.0 * r[i] + ma * AMp[i];
+        M(ctx, s, Ms);
+        orc_spmv(A, Ms, AMs);
+        double omega = dot(AMs, s, n) / dot(AMs, AMs, n);
+        for (long i = 0; i < n; i++) x[i] = 1.0 * x[i] + alpha * Mp[i] + omega * Ms[i];
+        double mo = -omega;
+        for (long i = 0; i < n; i++) r[i] = 1.0 * s[i] + mo * AMs[i];
+        double rdr1 = dot(rd, r, n);
+        double beta = alpha / omega * rdr1 / rdr;
+        double mbo = -beta * omega;
+        for (long i = 0; i < n; i++) p[i] = beta * p[i] + 1.0 * r[i] + mbo * AMp[i];
+        rdr = rdr1;
+        if (sqrt(dot(r, r, n)) < eps * bnorm) { ret = k + 1; break; }
+    }
+    free(r); free(rd); free(p); free(Mp); free(AMp); free(s); free(Ms); free(AMs);
+    return ret;
+}
+
+static void scaling_apply(const void *ctx, const double *v, double *out) {   /* Scaling :408-415 */
+    const orc_csr *A = (const orc_csr *)ctx;
+    for (int i = 0; i < A->rows; i++) out[i] = v[i] / orc_csr_get(A, i, i);
+}
+static void ilu0_apply(const void *ctx, const double *v, double *out) { orc_pre_ilu0((const orc_csr *)ctx, v, out); }
+
+/* ScalingBiCGSTAB (CG.h:457-495) */
+int orc_scaling_bicgstab(const orc_csr *A, const double *b, int itmax, double eps, double *x) {
+    return precond_bicgstab(A, b, itmax, eps, x, scaling_apply, A, 1);
+}
+
+/* ILU0BiCGSTAB (CG.h:356-391) with the factor M of ILU0 */
+int orc_ilu0_bicgstab(const orc_csr *A, const orc_csr *M, const double *b, int itmax, double eps, double *x) {
+    return precond_bicgstab(A, b, itmax, eps, x, ilu0_apply, M, 0);
+}
+
 double orc_true_residual(const orc_csr *A, const double *b, const double *x) {
     long n = A->rows;
     double *Ax = xmalloc(sizeof(double) * n);

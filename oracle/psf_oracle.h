@@ -82,6 +82,9 @@ int orc_scaling_cg(const orc_csr *A, const double *b, int itmax, double eps, dou
 int orc_cg(const orc_csr *A, const double *b, int itmax, double eps, double *x);         /* :123-154 */
 int orc_bicgstab(const orc_csr *A, const double *b, int itmax, double eps, double *x);   /* :158-193 */
 int orc_bicgstab2(const orc_csr *A, const double *b, int itmax, double eps, double *x);  /* :197-253 */
+int orc_scaling_bicgstab(const orc_csr *A, const double *b, int itmax, double eps, double *x);   /* :457-495 */
+int orc_ilu0_bicgstab(const orc_csr *A, const orc_csr *M, const double *b, int itmax, double eps,
+                      double *x);                                                          /* :356-391 */
 int orc_ilu0(const orc_csr *A, orc_csr *M);                                              /* :257-284 */
 void orc_pre_ilu0(const orc_csr *M, const double *b, double *v);                         /* :288-315 */
 int orc_ilu0_cg(const orc_csr *A, const orc_csr *M, const double *b, int itmax, double eps,

@@ -31,7 +31,8 @@ def _lib(fast=False):
     lib = C.CDLL(path)
     lib.orc_assemble.restype = C.c_int
     lib.orc_renumber.restype = C.c_int
-    for fn in ("orc_scaling_cg", "orc_cg", "orc_bicgstab", "orc_bicgstab2", "orc_ilu0_cg",
+    for fn in ("orc_scaling_cg", "orc_cg", "orc_bicgstab", "orc_bicgstab2", "orc_ilu0_cg", "orc_scaling_bicgstab",
+               "orc_ilu0_bicgstab",
                "orc_mma_update", "orc_simp_run", "orc_get_threads"):
         getattr(lib, fn).restype = C.c_int
     for fn in ("orc_true_residual", "orc_compliance_sens", "orc_oc_update", "orc_csr_get"):
@@ -165,15 +166,16 @@ def spmv(indptr, indices, data, x, fast=False):
 
 
 def solve(kind, indptr, indices, data, b, itmax=100000, eps=1e-10, fast=False):
-    """kind in {'scaling_cg', 'cg', 'bicgstab', 'bicgstab2', 'ilu0_cg'}; returns (x, iters)."""
+    """kind in {'scaling_cg', 'cg', 'bicgstab', 'bicgstab2', 'scaling_bicgstab', 'ilu0_cg',
+    'ilu0_bicgstab'}; returns (x, iters)."""
     A = _csr_struct(indptr, indices, data)
     b = f64(b)
     x = np.zeros(A.rows)
     L = _lib(fast)
-    if kind == "ilu0_cg":
+    if kind in ("ilu0_cg", "ilu0_bicgstab"):
         M = CSR()
         L.orc_ilu0(C.byref(A), C.byref(M))
-        it = L.orc_ilu0_cg(C.byref(A), C.byref(M), P(b), itmax, C.c_double(eps), P(x))
+        it = getattr(L, "orc_" + kind)(C.byref(A), C.byref(M), P(b), itmax, C.c_double(eps), P(x))
         L.orc_csr_free(C.byref(M))
     else:
         it = getattr(L, "orc_" + kind)(C.byref(A), P(b), itmax, C.c_double(eps), P(x))

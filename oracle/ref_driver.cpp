@@ -251,6 +251,8 @@ static int run_simp() {
             std::vector<double> Fc = F;
             out.d("ilu_apply_F", PreILU0(M, Fc));
             out.d("sol_ilu0cg", ILU0CG(Kmod, M, F, cg_itmax, cg_eps));
+            out.d("sol_scalingbicgstab", ScalingBiCGSTAB(Kmod, F, cg_itmax, cg_eps));
+            out.d("sol_ilu0bicgstab", ILU0BiCGSTAB(Kmod, M, F, cg_itmax, cg_eps));
         }
         std::vector<double> result = ScalingCG(Kmod, F, cg_itmax, cg_eps);
         Disassembling(u, result, nodetoglobal);

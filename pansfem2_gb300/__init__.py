@@ -6,4 +6,4 @@ the C++ host mirror of the reference's template API is include/pansfem2_gb300.hp
 """
 from . import problems  # noqa: F401
 from ._lib import PsfError, SOLVERS, kernel_launches, load  # noqa: F401
-from .api import Problem  # noqa: F401
+from .api import DeviceMMA, Problem  # noqa: F401

@@ -24,6 +24,10 @@ SOLVERS = {
     "csr_cg_f64": 4,
     "csr_bicgstab_f64": 5,
     "ir_learned_f32": 6,
+    "csr_scaling_bicgstab_f64": 7,
+    "csr_bicgstab2_f64": 8,
+    "csr_ilu0_cg_f64": 9,
+    "csr_ilu0_bicgstab_f64": 10,
 }
 
 # every symbol declared in include/pansfem2_gpu.h
@@ -36,7 +40,8 @@ EXPORTS = [
     "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_conlin_init", "psf_conlin_update",
     "psf_heaviside_forward", "psf_heaviside_backward", "psf_simp_begin", "psf_simp_step",
     "psf_simp_step_host", "psf_simp_fields", "psf_device_ptr", "psf_sync",
-    "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc",
+    "psf_csr_spmv", "psf_csr_solve", "psf_list_filter", "psf_csr_solve_noalloc", "psf_csr_solve_ilu0",
+    "psf_csr_ilu0",
     "psf_fem_create", "psf_fem_destroy", "psf_fem_set_dirichlet", "psf_fem_set_loads", "psf_fem_assemble",
     "psf_fem_get_system", "psf_fem_solve", "psf_fem_reaction", "psf_fem_set_body_force", "psf_fem_set_edge_loads",
     "psf_fem_timings",
@@ -46,7 +51,7 @@ EXPORTS = [
     "psf_learned_attach", "psf_learned_apply", "psf_trainset_create", "psf_trainset_destroy", "psf_trainset_size",
     "psf_learned_harvest", "psf_learned_train", "psf_learned_eval", "psf_export_vtk", "psf_export_wait",
     "psf_batch_create", "psf_batch_destroy", "psf_batch_begin", "psf_batch_step", "psf_batch_results",
-    "psf_batch_profile",
+    "psf_batch_profile", "psf_mma_create", "psf_mma_set_parameters", "psf_mma_update_host", "psf_mma_destroy",
     "psf_batch_fields",
 ]
 
@@ -159,6 +164,9 @@ def load(path=LIB_PATH):
         "psf_fem_set_body_force": [vp, C.c_double, C.c_double],
         "psf_fem_set_edge_loads": [vp, C.c_int, C.POINTER(C.c_int32), C.c_double, C.c_double],
         # device pointers and a stream handle
+        "psf_csr_solve_ilu0": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, dp, C.c_int, C.c_int,
+                               C.c_double, dp, C.POINTER(SolveInfo)],
+        "psf_csr_ilu0": [C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp, dp, dp, dp],
         "psf_csr_solve_noalloc": [C.c_int, C.c_int64, vp, vp, vp, vp, vp, C.c_int, C.c_double, vp,
                                   C.POINTER(SolveInfo)],
         # learned preconditioner network
@@ -189,6 +197,10 @@ def load(path=LIB_PATH):
         "psf_batch_profile": [vp, dp],
         "psf_batch_fields": [vp, C.c_int, dp, dp, dp],
         "psf_export_wait": [vp],
+        "psf_mma_create": [C.c_int, C.c_int, C.c_double, dp, dp, dp, dp, dp, C.POINTER(C.c_void_p)],
+        "psf_mma_set_parameters": [vp] + [C.c_double] * 7,
+        "psf_mma_update_host": [vp, dp, C.c_double, dp, dp, dp, ip],
+        "psf_mma_destroy": [vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -287,6 +287,52 @@ class Problem:
                                          0 if it is None else len(it)))
 
 
+class DeviceMMA:
+    """MMA<T>(n, m, a0, a, c, d, xmin, xmax) (MMA.h:18-509) on the device for any n and
+    1 <= m <= 4, per-variable bounds (psf_mma_*)."""
+
+    def __init__(self, n, m, a0, a, c, d, xmin, xmax):
+        self.L = load()
+        self.n, self.m = int(n), int(m)
+        h = C.c_void_p()
+        xmin = f64(np.broadcast_to(np.asarray(xmin, float), (self.n,)))
+        xmax = f64(np.broadcast_to(np.asarray(xmax, float), (self.n,)))
+        check(self.L.psf_mma_create(self.n, self.m, float(a0), ptr(f64(a)), ptr(f64(c)), ptr(f64(d)), ptr(xmin),
+                                    ptr(xmax), C.byref(h)))
+        self.h = h
+        self.prev = 0.0
+        self.eps = 1.0e-5
+
+    def set_parameters(self, raa0, albefa, move, asyinit, asydecr, asyincr, eps):
+        self.eps = float(eps)
+        check(self.L.psf_mma_set_parameters(self.h, raa0, albefa, move, asyinit, asydecr, asyincr, eps))
+
+    def is_convergence(self, f):
+        """IsConvergence (MMA.h:107-113)."""
+        return abs(f - self.prev) / (f + self.prev) < self.eps
+
+    def update(self, x, f, dfdx, g, dgdx):
+        """UpdateVariables (MMA.h:116-419); returns (new x, Newton steps)."""
+        x = f64(x).copy()
+        nt = C.c_int()
+        check(self.L.psf_mma_update_host(self.h, ptr(x), float(f), ptr(f64(dfdx)), ptr(f64(g)),
+                                         ptr(f64(np.asarray(dgdx, float).reshape(-1))), C.byref(nt)),
+              allow=(PSF_OK, PSF_NOT_CONVERGED))
+        self.prev = float(f)
+        return x, nt.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.psf_mma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def run_simp(pr, iters, solver="csr_jacobi_f64", **kw):
     """Runs `iters` SIMP iterations on the device; returns per-iteration infos and final fields."""
     with Problem(pr) as P:

@@ -20,8 +20,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 if not os.path.exists(NVCC):
     NVCC = "nvcc"
 
-SOURCES = ["psf_element.cu", "psf_mesh.cu", "psf_solve.cu", "psf_opt.cu", "psf_optdw.cu", "psf_mg.cu", "psf_capi.cu", "psf_generic.cu", "psf_fem.cu", "psf_noalloc.cu", "psf_unet.cu", "psf_learned.cu", "psf_vtk.cu", "psf_batch.cu"]
-PER_FILE = {"psf_element.cu": ["--fmad=false"], "psf_fem.cu": ["--fmad=false"]}
+SOURCES = ["psf_element.cu", "psf_mesh.cu", "psf_solve.cu", "psf_opt.cu", "psf_optdw.cu", "psf_mg.cu", "psf_capi.cu", "psf_generic.cu", "psf_fem.cu", "psf_noalloc.cu", "psf_unet.cu", "psf_learned.cu", "psf_vtk.cu", "psf_batch.cu", "psf_mmagen.cu", "psf_krylov.cu"]
+PER_FILE = {"psf_element.cu": ["--fmad=false"], "psf_fem.cu": ["--fmad=false"], "psf_krylov.cu": ["--fmad=false"]}
 
 
 def _compile(src, verbose):

@@ -28,7 +28,7 @@ inline void note_launch(long long n = 1) { g_launches += n; }
 inline long long launches() { return g_launches; }
 
 
-constexpr int kMaxRed = 6;                    // values reduced by one grid_sync
+constexpr int kMaxRed = 20;                   // values reduced by one grid_sync (the m = 4 MMA needs 19)
 constexpr long long kSpinLimit = 1ll << 23;   // polls (x >= 64 ns each): ~1 s bound
 // partial sums a grid_sync needs: two alternating sets (the phase parity) of kMaxRed + 1
 // values per block, so a block that has left a barrier never overwrites the partials a

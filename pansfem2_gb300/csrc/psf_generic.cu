@@ -2,6 +2,7 @@
 // an arbitrary CSR matrix (CSR<T> of CSR.h) and explicit neighbour lists
 // (DensityFilter of DensityFilter.h).  They run on a process-wide internal
 // context (stream, grid-sync slot) created on first use on the current device.
+#include <cmath>
 #include <mutex>
 
 #include "psf_internal.cuh"
@@ -10,6 +11,11 @@ namespace psf {
 psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *indices, const int *diag,
                        const double *data, const double *b, double *x, double *w, int jacobi, int itmax, double eps,
                        int *iters, double *rr, double *bb, int *conv);  // psf_solve.cu
+psf_status krylov_csr_solve(Ctx *c, int solver, int n, long long nnz, const int *h_ip, const int *h_ix, const int *ip,
+                            const int *ix, const double *a, const double *m_given, const double *b, double *x,
+                            int itmax, double eps, int *iters, double *rr, double *bb, int *conv);   // psf_krylov.cu
+psf_status krylov_ilu0(Ctx *c, int n, long long nnz, const int *h_ip, const int *h_ix, const int *ip, const int *ix,
+                       const double *a, const double *m_given, const double *b, double *m_out, double *v_out);
 
 namespace {
 // position of (i, i) in row i (binary search over the sorted columns), -1 when absent
@@ -109,12 +115,62 @@ psf_status psf_csr_spmv(int n, const int32_t *indptr, const int32_t *indices, co
     return PSF_OK;
 }
 
+static bool krylov_solver(int solver) {
+    return solver == PSF_SOLVE_CSR_SCALING_BICGSTAB_F64 || solver == PSF_SOLVE_CSR_BICGSTAB2_F64 ||
+           solver == PSF_SOLVE_CSR_ILU0_CG_F64 || solver == PSF_SOLVE_CSR_ILU0_BICGSTAB_F64;
+}
+
+// the solvers of psf_krylov.cu on host CSR arrays (m: a given ILU(0) factor or NULL)
+static psf_status krylov_host(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                              const double *m, const double *b, int solver, int itmax, double eps, double *x,
+                              psf_solve_info *info) {
+    Ctx *c;
+    PSF_CHECK(generic_ctx(&c));
+    const long long nnz = indptr[n];
+    int *dp = nullptr, *di = nullptr;
+    double *dd = nullptr, *dm = nullptr, *db = nullptr, *dx = nullptr;
+    cudaStream_t s = c->stream;
+    PSF_CUDA(cudaMallocAsync((void **)&dp, sizeof(int) * (n + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&di, sizeof(int) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dd, sizeof(double) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dm, sizeof(double) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&db, sizeof(double) * (n + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dx, sizeof(double) * (n + 1), s));
+    PSF_CUDA(cudaMemcpyAsync(dp, indptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+    PSF_CUDA(cudaMemcpyAsync(di, indices, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+    PSF_CUDA(cudaMemcpyAsync(dd, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+    if (m) PSF_CUDA(cudaMemcpyAsync(dm, m, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+    PSF_CUDA(cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    int it = 0, conv = 0;
+    double rr = 0, bb = 0;
+    psf_status st = krylov_csr_solve(c, solver, n, nnz, indptr, indices, dp, di, dd, m ? dm : nullptr, db, dx, itmax,
+                                     eps, &it, &rr, &bb, &conv);
+    if (st == PSF_OK) st = cuda_status(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "copy");
+    for (void *p : {(void *)dp, (void *)di, (void *)dd, (void *)dm, (void *)db, (void *)dx}) cudaFreeAsync(p, s);
+    PSF_CUDA(cudaStreamSynchronize(s));
+    if (st != PSF_OK) return st;
+    if (!std::isfinite(rr) || !std::isfinite(bb)) {
+        set_error("non-finite residual (non-finite matrix or right-hand side entries)");
+        return PSF_NOT_FINITE;
+    }
+    if (info) {
+        psf_solve_info inf{};
+        inf.iterations = it;
+        inf.outer_iterations = 1;
+        inf.rel_residual_recurrence = bb > 0 ? sqrt(rr / bb) : 0.0;
+        inf.rel_residual = -1.0;   // not computed on this path
+        *info = inf;
+    }
+    return conv ? PSF_OK : PSF_NOT_CONVERGED;
+}
+
 psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, const double *data, const double *b,
                          int solver, int itmax, double eps, double *x, psf_solve_info *info) {
     if (!csr_ok(n, indptr, indices, data) || !b || !x) { set_error("psf_csr_solve: invalid CSR arrays"); return PSF_BAD_INPUT; }
+    if (itmax < 1 || !(eps > 0)) { set_error("psf_csr_solve: itmax >= 1 and eps > 0 required"); return PSF_BAD_INPUT; }
+    if (krylov_solver(solver)) return krylov_host(n, indptr, indices, data, nullptr, b, solver, itmax, eps, x, info);
     if (solver != PSF_SOLVE_CSR_JACOBI_F64 && solver != PSF_SOLVE_CSR_CG_F64 && solver != PSF_SOLVE_CSR_BICGSTAB_F64) {
-        set_error("psf_csr_solve: solver must be PSF_SOLVE_CSR_JACOBI_F64, PSF_SOLVE_CSR_CG_F64 or "
-                  "PSF_SOLVE_CSR_BICGSTAB_F64");
+        set_error("psf_csr_solve: solver must be one of the PSF_SOLVE_CSR_* kinds");
         return PSF_BAD_INPUT;
     }
     if (itmax < 1 || !(eps > 0)) { set_error("psf_csr_solve: itmax >= 1 and eps > 0 required"); return PSF_BAD_INPUT; }
@@ -167,6 +223,57 @@ psf_status psf_csr_solve(int n, const int32_t *indptr, const int32_t *indices, c
         *info = inf;
     }
     return conv ? PSF_OK : PSF_NOT_CONVERGED;
+}
+
+psf_status psf_csr_solve_ilu0(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                              const double *m, const double *b, int solver, int itmax, double eps, double *x,
+                              psf_solve_info *info) {
+    if (!csr_ok(n, indptr, indices, data) || !b || !x) {
+        set_error("psf_csr_solve_ilu0: invalid CSR arrays");
+        return PSF_BAD_INPUT;
+    }
+    if (solver != PSF_SOLVE_CSR_ILU0_CG_F64 && solver != PSF_SOLVE_CSR_ILU0_BICGSTAB_F64) {
+        set_error("psf_csr_solve_ilu0: solver must be PSF_SOLVE_CSR_ILU0_CG_F64 or PSF_SOLVE_CSR_ILU0_BICGSTAB_F64");
+        return PSF_BAD_INPUT;
+    }
+    if (itmax < 1 || !(eps > 0)) { set_error("psf_csr_solve_ilu0: itmax >= 1 and eps > 0 required"); return PSF_BAD_INPUT; }
+    return krylov_host(n, indptr, indices, data, m, b, solver, itmax, eps, x, info);
+}
+
+psf_status psf_csr_ilu0(int n, const int32_t *indptr, const int32_t *indices, const double *data,
+                        const double *m_in, const double *b, double *m_out, double *v_out) {
+    if (!csr_ok(n, indptr, indices, data) || (!m_out && !(b && v_out))) {
+        set_error("psf_csr_ilu0: invalid arrays");
+        return PSF_BAD_INPUT;
+    }
+    Ctx *c;
+    PSF_CHECK(generic_ctx(&c));
+    const long long nnz = indptr[n];
+    int *dp = nullptr, *di = nullptr;
+    double *dd = nullptr, *dmi = nullptr, *dmo = nullptr, *db = nullptr, *dv = nullptr;
+    cudaStream_t s = c->stream;
+    PSF_CUDA(cudaMallocAsync((void **)&dp, sizeof(int) * (n + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&di, sizeof(int) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dd, sizeof(double) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dmi, sizeof(double) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dmo, sizeof(double) * (nnz + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&db, sizeof(double) * (n + 1), s));
+    PSF_CUDA(cudaMallocAsync((void **)&dv, sizeof(double) * (n + 1), s));
+    PSF_CUDA(cudaMemcpyAsync(dp, indptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+    PSF_CUDA(cudaMemcpyAsync(di, indices, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+    PSF_CUDA(cudaMemcpyAsync(dd, data, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+    if (m_in) PSF_CUDA(cudaMemcpyAsync(dmi, m_in, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+    if (b) PSF_CUDA(cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    psf_status st = krylov_ilu0(c, n, nnz, indptr, indices, dp, di, dd, m_in ? dmi : nullptr, b ? db : nullptr, dmo,
+                                (b && v_out) ? dv : nullptr);
+    if (st == PSF_OK && m_out)
+        st = cuda_status(cudaMemcpyAsync(m_out, dmo, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s), "copy");
+    if (st == PSF_OK && b && v_out)
+        st = cuda_status(cudaMemcpyAsync(v_out, dv, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "copy");
+    for (void *p : {(void *)dp, (void *)di, (void *)dd, (void *)dmi, (void *)dmo, (void *)db, (void *)dv})
+        cudaFreeAsync(p, s);
+    PSF_CUDA(cudaStreamSynchronize(s));
+    return st;
 }
 
 psf_status psf_list_filter(int n, const int32_t *ptr, const int32_t *idx, const double *w, const double *in,

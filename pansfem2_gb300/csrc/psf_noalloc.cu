@@ -9,7 +9,7 @@
 // must not be bypassed.  For them this entry point takes inputs and outputs
 // already in device memory and keeps its scratch (Krylov vectors, diagonal
 // positions, reduction slots, the validation flag) in one fixed file-scope
-// device array, g_noalloc_scratch, sized for kNoallocMaxRows rows (~15.8 MB).
+// device array, g_noalloc_scratch, sized for kNoallocMaxRows rows (~16.1 MB).
 //
 // The driver allocates that array, and the code of the kernels the solve
 // launches, when it loads their modules.  With lazy module loading (the CUDA

@@ -806,7 +806,7 @@ psf_status bicgstab_csr_any(Ctx *c, long long rows, const int *indptr, const int
 
 // Cooperative launch of pcg_csr_kernel (ScalingCG) on caller-owned device
 // buffers and the caller's stream, without a context and without allocating:
-// w holds 5*rows doubles, gs is zeroed here, partials holds (kMaxRed+2)*blocks
+// w holds 7*rows doubles, gs is zeroed here, partials holds kPartialSlots*blocks
 // doubles, out receives iterations, |r|^2, |b|^2, converged.
 psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr, const int *indices, const int *diag,
                               const double *data, const double *b, double *x, double *w, int itmax, double eps,

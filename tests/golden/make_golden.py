@@ -58,12 +58,21 @@ def read_vtk_vectors(path, name):
 
 def main():
     from oracle.build import REFERENCE_ROOT
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else REFERENCE_ROOT
+    # usage: make_golden.py [path-to-PANSFEM2] [--only CASE]  (--only: regenerate one SIMP case and stop)
+    argv = sys.argv[1:]
+    only = None
+    if "--only" in argv:
+        k = argv.index("--only")
+        only = argv[k + 1]
+        argv = argv[:k] + argv[k + 2:]
+    ref_root = argv[0] if argv else REFERENCE_ROOT
     obuild.build()
     if not obuild.build_reference(ref_root):
         raise SystemExit(f"reference tree not found at {ref_root}")
     tmp = os.path.join(ROOT, "oracle", "_ref", "dump.bin")
     for name, (args, iters, keep) in CASES.items():
+        if only is not None and name != only:
+            continue
         subprocess.run([os.path.join(REF, "ref_driver"), "simp", f"out={tmp}", f"iters={iters}"] + args,
                        check=True, stdout=subprocess.DEVNULL)
         d = read_dump(tmp)
@@ -73,6 +82,8 @@ def main():
         d["iters"] = np.array([iters], np.int32)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(f"{name}: {sorted(d)}")
+    if only is not None:
+        return
     # iteration 0 of the 12x6 cantilever written by the reference's own VTK writer
     vtk = os.path.join(HERE, "ref_cantilever_12x6_it0.vtk")
     subprocess.run([os.path.join(REF, "ref_driver"), "simp", f"out={tmp}", "iters=1", "kind=0", "nx=12", "ny=6",

@@ -77,11 +77,12 @@ def test_simp_trajectory_bitexact(name):
 
 
 def test_solver_suite_bitexact():
-    """CG, BiCGSTAB, BiCGSTAB2, ILU0 (factor + apply) and ILU0CG of CG.h."""
+    """CG, BiCGSTAB, BiCGSTAB2, ScalingBiCGSTAB, ILU0 (factor + apply), ILU0CG and ILU0BiCGSTAB of CG.h."""
     g, pr = load("cantilever_12x6_oc"), CASES["cantilever_12x6_oc"]()
     ipr, ind, dat, F = g["indptr"], g["indices"], g["data"], g["F0"]
     for kind, key in (("cg", "sol_cg"), ("bicgstab", "sol_bicgstab"), ("bicgstab2", "sol_bicgstab2"),
-                      ("ilu0_cg", "sol_ilu0cg")):
+                      ("ilu0_cg", "sol_ilu0cg"), ("scaling_bicgstab", "sol_scalingbicgstab"),
+                      ("ilu0_bicgstab", "sol_ilu0bicgstab")):
         x, it = O.solve(kind, ipr, ind, dat, F, eps=1e-10)
         assert same(g[key], x), kind
     mi, mj, md = O.ilu0(ipr, ind, dat)
