@@ -80,7 +80,9 @@ const char *psf_last_error(void);
 psf_status psf_kernel_launches(long long *n);
 /* Launch shape of a persistent kernel family of this context (no counterpart in the
  * reference; the autotuner pansfem2_gb300/autotune.py times candidates on the workload and
- * sets the fastest).  kernel = PSF_KERNEL_PCG_CSR: a = lanes per CSR row (4, 8, 16),
+ * sets the fastest).  kernel = PSF_KERNEL_PCG_CSR: a = lanes per CSR row (4, 8, 16), or 1
+ * for one lane per row on a sliced copy of the CSR that the context builds before each solve
+ * (slices of 32 rows stored column by column, about 12 bytes per stored entry; the default),
  * b = threads per block (256, 512, 1024), c = blocks per SM (1-8).  kernel = PSF_KERNEL_OPT
  * (the OC / MMA / CONLIN kernels, 256 threads): c = blocks per SM (1-8), a and b ignored.
  * Blocks per SM are capped by what fits.  Results agree to rounding across shapes. */

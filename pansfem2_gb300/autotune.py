@@ -11,7 +11,7 @@ Tuned today:
                  CTAs per instance shorten the largest instances' critical path
                  (one SM's bandwidth and FP64 rate bound a lone CTA); fewer leave
                  room for more instances at once.
-  pcg            lanes per CSR row, threads per block and blocks per SM of the
+  pcg            lanes per CSR row (1: one lane per row on the sliced copy), threads per block and blocks per SM of the
                  persistent FP64 CSR PCG (psf_set_launch_shape PSF_KERNEL_PCG_CSR),
                  timed on the Problem's own assembled system.
   opt            blocks per SM of the persistent OC / MMA / CONLIN kernels
@@ -84,7 +84,7 @@ def pick(key, candidates, timer, log=None):
     return tuple(_CACHE[key]["best"]), times
 
 
-PCG_CANDIDATES = ((4, 256, 4), (4, 512, 2), (4, 1024, 1), (8, 256, 4), (8, 1024, 1), (16, 1024, 1))
+PCG_CANDIDATES = ((1, 256, 4), (1, 512, 2), (1, 1024, 1), (4, 512, 2), (4, 1024, 1), (8, 1024, 1))
 
 
 def tune_pcg(prob, candidates=PCG_CANDIDATES, iters=300, log=None):

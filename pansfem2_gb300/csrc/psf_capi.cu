@@ -47,8 +47,9 @@ psf_status psf_set_launch_shape(psf_ctx *h, int kernel, int a, int b, int c) {
     Ctx *x = &h->c;
     if (c < 1 || c > 8) { set_error("psf_set_launch_shape: blocks per SM must be in [1, 8]"); return PSF_BAD_INPUT; }
     if (kernel == PSF_KERNEL_PCG_CSR) {
-        if ((a != 4 && a != 8 && a != 16) || (b != 256 && b != 512 && b != 1024)) {
-            set_error("psf_set_launch_shape: PCG lanes per row must be 4, 8 or 16 and threads 256, 512 or 1024");
+        if ((a != 1 && a != 4 && a != 8 && a != 16) || (b != 256 && b != 512 && b != 1024)) {
+            set_error("psf_set_launch_shape: PCG lanes per row must be 1 (sliced copy), 4, 8 or 16 and threads "
+                      "256, 512 or 1024");
             return PSF_BAD_INPUT;
         }
         x->pcg_lanes = a;
@@ -172,7 +173,7 @@ psf_status psf_destroy(psf_ctx *h) {
     learned_free(c);
     for (void *p : c->allocs) cudaFree(p);
     for (void *p : {(void *)c->g2n, (void *)c->indptr, (void *)c->indices, (void *)c->diag, (void *)c->data,
-                    (void *)c->F, (void *)c->u})
+                    (void *)c->F, (void *)c->u, (void *)c->sell_ptr, (void *)c->sell_col, (void *)c->sell_val})
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);

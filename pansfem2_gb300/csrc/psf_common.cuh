@@ -96,6 +96,34 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
         }
     }
 }
+// The same sums with about a fifth of the FP64 additions (the FP64 pipe is narrow on GB300):
+// every thread stores its values, then warp 0 adds the block's values per lane in four fixed
+// chains and finishes with one shuffle tree.  smem holds NV * blockDim.x doubles (blockDim.x a
+// multiple of 32); the results are in warp 0.
+template <int NV>
+__device__ __forceinline__ void block_sum_wide(double (&v)[NV], double *smem) {
+    const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, nw = nt >> 5;
+    __syncthreads();   // the previous use of smem is over
+#pragma unroll
+    for (int k = 0; k < NV; k++) smem[k * nt + t] = v[k];
+    __syncthreads();
+    if (t < 32) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            const double *s = smem + k * nt + lane;
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            int w = 0;
+            for (; w + 4 <= nw; w += 4) {
+                a0 += s[32 * w];
+                a1 += s[32 * (w + 1)];
+                a2 += s[32 * (w + 2)];
+                a3 += s[32 * (w + 3)];
+            }
+            for (; w < nw; w++) a0 += s[32 * w];
+            v[k] = warp_sum((a0 + a1) + (a2 + a3));
+        }
+    }
+}
 __device__ __forceinline__ double block_max(double v, double *smem) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     v = warp_max(v);

@@ -21,7 +21,10 @@ namespace psf {
 //   CSR (free x free): int32 indptr/indices, FP64 values (FP32 copy for the
 //                  mixed-precision path), the diagonal position per row.
 // default launch shape of the CSR PCG kernel: lanes per row, threads per block, blocks per SM
+// (the allocation-free entry point, which reads the CSR as it is); a context's solves default
+// to one lane per row on the sliced copy of the CSR (kPcgSliced)
 constexpr int kPcgDefaultLanes = 4, kPcgDefaultThreads = 1024, kPcgDefaultBlocksPerSm = 1;
+constexpr int kPcgSliced = 1;
 
 template <class T>
 struct DevBuf {
@@ -82,7 +85,14 @@ struct Ctx {
     double *partials = nullptr;
     int coop_blocks = 0;         // resident blocks for the persistent kernels
     // launch shapes (psf_set_launch_shape; the autotuner picks them per workload)
-    int pcg_lanes = kPcgDefaultLanes, pcg_threads = kPcgDefaultThreads, pcg_blocks_per_sm = kPcgDefaultBlocksPerSm;
+    int pcg_lanes = kPcgSliced, pcg_threads = kPcgDefaultThreads, pcg_blocks_per_sm = kPcgDefaultBlocksPerSm;
+    // sliced copy of the CSR for the one-lane-per-row PCG (grown on demand, refilled per solve):
+    // slices of 32 rows, slice s holds its rows' entries column-major from slot sell_ptr[s]
+    int *sell_ptr = nullptr;     // slices + 1 slot offsets, then the slot total
+    long long sell_ptr_cap = 0;
+    int *sell_col = nullptr;
+    double *sell_val = nullptr;
+    long long sell_cap = 0;
     int opt_blocks_per_sm = 2;   // OC / MMA / CONLIN persistent kernels (256 threads)
 
     // filter (structured stencil)

@@ -271,14 +271,15 @@ __global__ void __launch_bounds__(256) pcg_ebe_kernel(PcgArgs<T> A) {
 }
 
 // ------------------------------------------------------------------ persistent Jacobi PCG on the CSR (FP64)
-// Workspace (7 * rows doubles, from w): zpA, zpB = (z, p) pairs of 2 * rows each, then r, Ap, D.
+// Workspace (5 * rows doubles from w): r, z, p, Ap and the reciprocal diagonal.
 struct PcgCsrArgs {
     long long rows;
     int jacobi;                      // 1: ScalingCG (z = r / D), 0: CG (CG.h:123-154, z = r)
     const int *indptr, *indices, *diag;   // diag[i] = position of (i, i), -1 when absent
     const double *data, *b;
-    double *x, *r, *Ap, *D;
-    double2 *zpA, *zpB;              // (z, p) of the current / next iteration
+    double *x, *r, *z, *p, *Ap, *Dinv;
+    const int *sell_ptr, *sell_col;   // the sliced copy (one lane per row), else unused
+    const double *sell_val;
     int itmax;
     double eps;
     GridSync *gs;
@@ -286,33 +287,39 @@ struct PcgCsrArgs {
     double *out;
 };
 
-// the workspace split (zp pairs first: 16-byte aligned for any row count)
 __host__ __device__ inline void pcg_csr_carve(PcgCsrArgs &a, double *w, long long n) {
-    a.zpA = (double2 *)w;
-    a.zpB = (double2 *)(w + 2 * n);
-    a.r = w + 4 * n;
-    a.Ap = w + 5 * n;
-    a.D = w + 6 * n;
+    a.r = w;
+    a.z = w + n;
+    a.p = w + 2 * n;
+    a.Ap = w + 3 * n;
+    a.Dinv = w + 4 * n;
 }
 
-
-// ScalingCG (CG.h:419-453): x0 = 0, r = b, z = r / D (GetDiagonal :397-404 with the division
-// of Scaling :408-415), p = z; the recurrence residual ||r|| < eps ||b|| stops it (:443-448).
-// One iteration is two phases and two grid barriers (each folding its dot products):
-//   product  p = z + beta p_prev formed on the fly from one 16-byte gather of the (z, p_prev)
-//            pair per stored entry, Ap = A p, p.Ap; the row's p is stored for the update;
-//   update   x += alpha p, r -= alpha Ap, z = r / D, z.r and r.r.
-// The CSR arrays are read once per iteration with streaming (evict-first) loads, so the
-// vectors (8 bytes per row each) stay in L2; a lane's loads of a row are issued before their
-// products.  Sums run in lane / tree order (the reference sums rows left to right and dot
-// products sequentially: the results agree to rounding).
+// ScalingCG (CG.h:419-453): x0 = 0, r = b, z = r / D (GetDiagonal :397-404, Scaling :408-415),
+// p = z; the recurrence residual ||r|| < eps ||b|| stops it (:443-448).
+// On GB300 this iteration is bound by the FP64 pipe, not by HBM (a capture of the previous
+// form, which formed p = z + beta p_prev inside the product, showed the FP64 pipe 85% busy
+// and DRAM at 19%), so the FP64 work is kept to the minimum: one FMA per stored entry in the
+// product, and the Jacobi scaling as a multiplication by the reciprocal diagonal (computed
+// once; it differs from the reference's division by at most one rounding).  Three phases per
+// iteration:
+//   P  p = z + beta p (own rows)                                   -> barrier
+//   S  Ap = A p (LANES lanes per row, every load of a row's entries in flight at once), p.Ap
+//                                                                  -> barrier + 1 sum
+//   U  x += alpha p, r -= alpha Ap, z = r / D, z.r and r.r         -> barrier + 2 sums
+// The CSR arrays are read with streaming (evict-first) loads, so the vectors stay in L2.
 // Launch shape: LANES lanes per CSR row in the product (32 / LANES rows per warp), THREADS
 // threads per block; blocks per SM is chosen at launch (psf_set_launch_shape, autotuned).
+// LANES = 1 reads the sliced copy instead (sell_fill_kernel): a warp owns a slice of 32 rows,
+// each lane one row, and the warp's loads of the k-th entries of its rows are one contiguous
+// 128-byte (columns) and 256-byte (values) segment.  Without the lane reduction and the slot
+// padding of the multi-lane form, the product costs one FMA per stored entry, summed in the
+// CSR order of the row (the order of CSR::operator* at CSR.h:108-122).
 template <int LANES, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsrArgs A) {
     constexpr int kPcgRowLanes = LANES;
     grid_sync_init();
-    __shared__ double sm[32 * 2];
+    __shared__ double sm[2 * THREADS];
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long rows = A.rows;
@@ -320,28 +327,29 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsr
         double acc[2] = {0.0, 0.0};
         for (long long i = tid; i < rows; i += stride) {
             const double bv = A.b[i];
-            double D = 1.0;
+            double Di = 1.0;
             if (A.jacobi) {
                 const int d = A.diag[i];
-                D = d >= 0 ? A.data[d] : 0.0;   // CSR::get(i, i): zero when the entry is absent
+                const double D = d >= 0 ? A.data[d] : 0.0;   // CSR::get(i, i): zero when the entry is absent
                 // the reference divides by it (CG.h:412) and lets inf / NaN run; here the solve stops
                 if (!(D != 0.0) || !isfinite(D)) atomicCAS(&A.gs->status, 0, (int)PSF_BAD_INPUT);
+                Di = 1.0 / D;
             }
-            A.D[i] = D;
+            A.Dinv[i] = Di;
             A.x[i] = 0.0;
             A.r[i] = bv;
-            const double zv = bv / D;
-            A.zpA[i] = make_double2(zv, 0.0);
+            const double zv = bv * Di;
+            A.z[i] = zv;
+            A.p[i] = 0.0;
             acc[0] += zv * bv;
             acc[1] += bv * bv;
         }
-        block_sum<2>(acc, sm);
+        block_sum_wide<2>(acc, sm);
         if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
     }
     double zr = gs_result(A.gs, 0);
     const double bnorm = sqrt(gs_result(A.gs, 1));
     double beta = 0.0, rr = 0.0;
-    double2 *cur = A.zpA, *nxt = A.zpB;
     int it = 0, conv = 0;
     const int lane = threadIdx.x & 31, sub = lane & (kPcgRowLanes - 1);
     const long long rows_per_warp = 32 / kPcgRowLanes;
@@ -351,10 +359,44 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsr
     // at once: the indices and values, then the gathers, then the products
     constexpr int SL = kPcgRowLanes == 4 ? 5 : (kPcgRowLanes == 8 ? 3 : 2);
     for (; it < A.itmax; it++) {
+        // ---- P
+        for (long long i = tid; i < rows; i += stride) A.p[i] = fma(beta, A.p[i], A.z[i]);
+        if (!grid_barrier(A.gs, A.partials)) return;
+        // ---- S
         double pAp[1] = {0.0};
+        if constexpr (LANES == 1) {
+            constexpr int U = 6;   // entries in flight per lane (a 2D row of 18 entries: three rounds)
+            const long long nsl = (rows + 31) >> 5;
+            for (long long sl = gw; sl < nsl; sl += nw) {
+                const long long i = (sl << 5) + lane;
+                const int s0 = __ldg(A.sell_ptr + sl), s1 = __ldg(A.sell_ptr + sl + 1);
+                double v = 0.0;
+                // s1 - s0 is a multiple of 32, so the bounds below are the same in every lane
+                for (int q = s0; q < s1; q += 32 * U) {
+                    int j[U];
+                    double a[U];
+#pragma unroll
+                    for (int t = 0; t < U; t++) {
+                        const int qt = q + 32 * t + lane;
+                        const bool h = q + 32 * t < s1;
+                        j[t] = h ? __ldcs(A.sell_col + qt) : 0;
+                        a[t] = h ? __ldcs(A.sell_val + qt) : 0.0;
+                    }
+                    double g[U];
+#pragma unroll
+                    for (int t = 0; t < U; t++) g[t] = q + 32 * t < s1 ? A.p[j[t]] : 0.0;
+#pragma unroll
+                    for (int t = 0; t < U; t++)
+                        if (q + 32 * t < s1) v = fma(a[t], g[t], v);
+                }
+                if (i < rows) {
+                    A.Ap[i] = v;
+                    pAp[0] = fma(A.p[i], v, pAp[0]);
+                }
+            }
+        } else {
         long long base = gw * rows_per_warp;
-        // the row bounds are fetched one pass ahead
-        int rs_n = 0, re_n = 0;
+        int rs_n = 0, re_n = 0;   // the row bounds are fetched one pass ahead
         {
             const long long i0 = base + lane / kPcgRowLanes;
             if (i0 < rows) { rs_n = __ldg(A.indptr + i0); re_n = __ldg(A.indptr + i0 + 1); }
@@ -378,44 +420,41 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsr
                         j[t] = h ? __ldcs(A.indices + qt) : -1;
                         a[t] = h ? __ldcs(A.data + qt) : 0.0;
                     }
-                    double2 g[SL];
+                    double g[SL];
 #pragma unroll
-                    for (int t = 0; t < SL; t++) g[t] = j[t] >= 0 ? cur[j[t]] : make_double2(0.0, 0.0);
+                    for (int t = 0; t < SL; t++) g[t] = j[t] >= 0 ? A.p[j[t]] : 0.0;
 #pragma unroll
-                    for (int t = 0; t < SL; t++) v += a[t] * fma(beta, g[t].y, g[t].x);
+                    for (int t = 0; t < SL; t++) v = fma(a[t], g[t], v);
                 }
             }
 #pragma unroll
             for (int o = 1; o < kPcgRowLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (sub == 0 && i < rows) {
-                const double2 gi = cur[i];
-                const double pv = fma(beta, gi.y, gi.x);
-                reinterpret_cast<double *>(nxt)[2 * i + 1] = pv;
                 A.Ap[i] = v;
-                pAp[0] += pv * v;
+                pAp[0] += A.p[i] * v;
             }
         }
-        block_sum<1>(pAp, sm);
+        }
+        block_sum_wide<1>(pAp, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, pAp, 0.0)) return;
         const double alpha = zr / gs_result(A.gs, 0);
+        // ---- U
         double acc[2] = {0.0, 0.0};
-        double *nxt_d = reinterpret_cast<double *>(nxt);
         for (long long i = tid; i < rows; i += stride) {
-            A.x[i] = A.x[i] + alpha * nxt_d[2 * i + 1];
-            const double rv = A.r[i] + (-alpha) * A.Ap[i];
+            A.x[i] = fma(alpha, A.p[i], A.x[i]);
+            const double rv = fma(-alpha, A.Ap[i], A.r[i]);
             A.r[i] = rv;
-            const double zv = rv / A.D[i];
-            nxt_d[2 * i] = zv;
+            const double zv = rv * A.Dinv[i];
+            A.z[i] = zv;
             acc[0] += zv * rv;
             acc[1] += rv * rv;
         }
-        block_sum<2>(acc, sm);
+        block_sum_wide<2>(acc, sm);
         if (!grid_sync<2, 0>(A.gs, A.partials, acc, 0.0)) return;
         const double zr1 = gs_result(A.gs, 0);
         rr = gs_result(A.gs, 1);
         beta = zr1 / zr;
         zr = zr1;
-        double2 *t = cur; cur = nxt; nxt = t;
         if (sqrt(rr) < A.eps * bnorm) { it++; conv = 1; break; }
         if (!isfinite(rr)) { it++; break; }
     }
@@ -431,6 +470,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) pcg_csr_kernel(PcgCsr
 static const void *pcg_csr_fn(int lanes, int threads) {
 #define PSF_PCG_SHAPE(L, T) \
     if (lanes == L && threads == T) return (const void *)pcg_csr_kernel<L, T>;
+    PSF_PCG_SHAPE(1, 256) PSF_PCG_SHAPE(1, 512) PSF_PCG_SHAPE(1, 1024)
     PSF_PCG_SHAPE(4, 256) PSF_PCG_SHAPE(4, 512) PSF_PCG_SHAPE(4, 1024)
     PSF_PCG_SHAPE(8, 256) PSF_PCG_SHAPE(8, 512) PSF_PCG_SHAPE(8, 1024)
     PSF_PCG_SHAPE(16, 256) PSF_PCG_SHAPE(16, 512) PSF_PCG_SHAPE(16, 1024)
@@ -618,6 +658,118 @@ static psf_status pcg_ebe(Ctx *c, const double *b, double bscale, const double *
     }
 }
 
+// ------------------------------------------------------------------ sliced copy of the CSR
+// Slice s (rows 32s .. 32s+31) is as wide as its longest row; entry k of row 32s + l sits at
+// slot sell_ptr[s] + 32k + l.  Short rows are padded with column = the row, value 0, so the
+// padded products add exact zeros.
+
+// width of every slice (one thread per slice)
+__global__ void sell_width_kernel(long long rows, long long nsl, const int *__restrict__ indptr, int *__restrict__ width) {
+    for (long long sl = blockIdx.x * (long long)blockDim.x + threadIdx.x; sl < nsl;
+         sl += (long long)gridDim.x * blockDim.x) {
+        const long long i0 = sl << 5, i1 = i0 + 32 < rows ? i0 + 32 : rows;
+        int w = 0;
+        for (long long i = i0; i < i1; i++) {
+            const int l = indptr[i + 1] - indptr[i];
+            w = l > w ? l : w;
+        }
+        width[sl] = w;
+    }
+}
+
+// exclusive scan of 32 * width into ptr[0 .. nsl] (one block of 1024 threads, chunked)
+__global__ void __launch_bounds__(1024) sell_scan_kernel(long long nsl, int *__restrict__ ptr) {
+    __shared__ long long warp_tot[32];
+    __shared__ long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (long long b = 0; b < nsl; b += 1024) {
+        const long long sl = b + threadIdx.x;
+        const long long w = sl < nsl ? 32ll * ptr[sl] : 0;
+        long long x = w;   // inclusive scan in the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            long long t = warp_tot[lane], u = t;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(0xffffffffu, u, o);
+                if (lane >= o) u += y;
+            }
+            warp_tot[lane] = u - t;   // exclusive over the warps
+        }
+        __syncthreads();
+        const long long excl = carry + warp_tot[wid] + x - w;
+        __syncthreads();
+        if (sl < nsl) ptr[sl] = (int)excl;
+        if (threadIdx.x == 1023) carry = excl + w;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) ptr[nsl] = carry > 0x7fffffffll ? -1 : (int)carry;   // -1: too many slots
+}
+
+// the columns and values (one thread per row slot of a slice)
+__global__ void sell_fill_kernel(long long rows, long long nsl, const int *__restrict__ indptr,
+                                 const int *__restrict__ indices, const double *__restrict__ data,
+                                 const int *__restrict__ ptr, int *__restrict__ col, double *__restrict__ val) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (nsl << 5);
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long sl = t >> 5;
+        const int l = (int)(t & 31);
+        const int s0 = ptr[sl], wd = (ptr[sl + 1] - s0) >> 5;
+        const bool live = t < rows;
+        const int rs = live ? indptr[t] : 0, len = live ? indptr[t + 1] - rs : 0;
+        const int self = (int)(live ? t : rows - 1);
+        for (int k = 0; k < wd; k++) {
+            const bool h = k < len;
+            col[s0 + 32 * k + l] = h ? indices[rs + k] : self;
+            val[s0 + 32 * k + l] = h ? data[rs + k] : 0.0;
+        }
+    }
+}
+
+// builds the context's sliced copy of a device CSR (storage grown on demand)
+static psf_status sell_prepare(Ctx *c, long long rows, const int *indptr, const int *indices, const double *data) {
+    const long long nsl = (rows + 31) >> 5;
+    if (c->sell_ptr_cap < nsl + 1) {
+        if (c->sell_ptr) cudaFreeAsync(c->sell_ptr, c->stream);
+        c->sell_ptr = nullptr;
+        c->sell_ptr_cap = 0;
+        PSF_CUDA(cudaMallocAsync((void **)&c->sell_ptr, sizeof(int) * (nsl + 1), c->stream));
+        c->sell_ptr_cap = nsl + 1;
+    }
+    const int gw = grid_for(nsl, 256, 4096);
+    (sell_width_kernel<<<gw, 256, 0, c->stream>>>(rows, nsl, indptr, c->sell_ptr), note_launch());
+    PSF_CUDA(cudaGetLastError());
+    (sell_scan_kernel<<<1, 1024, 0, c->stream>>>(nsl, c->sell_ptr), note_launch());
+    PSF_CUDA(cudaGetLastError());
+    int total = 0;
+    PSF_CUDA(cudaMemcpyAsync(&total, c->sell_ptr + nsl, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    PSF_CUDA(cudaStreamSynchronize(c->stream));
+    if (total < 0) { set_error("sliced CSR copy exceeds 2^31 slots"); return PSF_BAD_INPUT; }
+    if (c->sell_cap < total) {
+        if (c->sell_col) cudaFreeAsync(c->sell_col, c->stream);
+        if (c->sell_val) cudaFreeAsync(c->sell_val, c->stream);
+        c->sell_col = nullptr;
+        c->sell_val = nullptr;
+        c->sell_cap = 0;
+        PSF_CUDA(cudaMallocAsync((void **)&c->sell_col, sizeof(int) * total, c->stream));
+        PSF_CUDA(cudaMallocAsync((void **)&c->sell_val, sizeof(double) * total, c->stream));
+        c->sell_cap = total;
+    }
+    (sell_fill_kernel<<<grid_for(nsl << 5, 256, 65536), 256, 0, c->stream>>>(rows, nsl, indptr, indices, data,
+                                                                            c->sell_ptr, c->sell_col, c->sell_val),
+     note_launch());
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
+}
+
 // Jacobi PCG (jacobi = 1) or CG (jacobi = 0) on any device CSR; w holds 5*rows doubles
 psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *indices, const int *diag,
                        const double *data, const double *b, double *x, double *w, int jacobi, int itmax, double eps,
@@ -630,6 +782,13 @@ psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *ind
     a.x = x;
     const long long n = rows;
     pcg_csr_carve(a, w, n);
+    a.sell_ptr = nullptr; a.sell_col = nullptr; a.sell_val = nullptr;
+    // the solve's time includes building the sliced copy
+    PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
+    if (c->pcg_lanes == kPcgSliced) {
+        PSF_CHECK(sell_prepare(c, rows, indptr, indices, data));
+        a.sell_ptr = c->sell_ptr; a.sell_col = c->sell_col; a.sell_val = c->sell_val;
+    }
     a.itmax = itmax;
     a.eps = eps;
     a.gs = c->gs;
@@ -641,7 +800,6 @@ psf_status pcg_csr_any(Ctx *c, long long rows, const int *indptr, const int *ind
     PSF_CHECK(persistent_blocks(fn, c->pcg_threads, c->num_sms, c->pcg_blocks_per_sm, n,
                                 c->pcg_threads / c->pcg_lanes, &blocks));
     void *args[] = {&a};
-    PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
     PSF_CHECK(launch_coop(c, fn, blocks, c->pcg_threads, args));
     PSF_CUDA(cudaEventRecord(c->evk1, c->stream));
     PSF_CHECK(read_sync_status(c));
@@ -806,7 +964,7 @@ psf_status bicgstab_csr_any(Ctx *c, long long rows, const int *indptr, const int
 
 // Cooperative launch of pcg_csr_kernel (ScalingCG) on caller-owned device
 // buffers and the caller's stream, without a context and without allocating:
-// w holds 7*rows doubles, gs is zeroed here, partials holds kPartialSlots*blocks
+// w holds at least 5*rows doubles, gs is zeroed here, partials holds kPartialSlots*blocks
 // doubles, out receives iterations, |r|^2, |b|^2, converged.
 psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr, const int *indices, const int *diag,
                               const double *data, const double *b, double *x, double *w, int itmax, double eps,
@@ -818,6 +976,7 @@ psf_status pcg_csr_launch_raw(cudaStream_t s, long long rows, const int *indptr,
     a.b = b;
     a.x = x;
     pcg_csr_carve(a, w, rows);
+    a.sell_ptr = nullptr; a.sell_col = nullptr; a.sell_val = nullptr;
     a.itmax = itmax;
     a.eps = eps;
     a.gs = gs;

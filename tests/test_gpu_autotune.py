@@ -30,7 +30,7 @@ def test_tune_pcg_sets_and_reuses_the_shape(gpu, tmp_path, monkeypatch):
                                                key=lambda kv: kv[1])[0]
         assert prob.launch_shape(_lib.PSF_KERNEL_PCG_CSR) == best
         sols = []
-        for shape in ((4, 256, 4), (8, 512, 2), (16, 1024, 1), best):
+        for shape in ((1, 1024, 1), (4, 256, 4), (8, 512, 2), (16, 1024, 1), best):
             prob.set_launch_shape(_lib.PSF_KERNEL_PCG_CSR, *shape)
             u, info = prob.solve("csr_jacobi_f64", eps=1e-10)
             assert info["status"] == 0

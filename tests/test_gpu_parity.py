@@ -117,6 +117,29 @@ def test_solve_matches_oracle(gpu, name, solver):
         assert rel(u, g["result0"]) < TOL_U
 
 
+@pytest.mark.parametrize("shape", [(1, 1024, 1), (1, 256, 4), (4, 1024, 1), (8, 512, 2), (16, 256, 4)])
+@pytest.mark.parametrize("name", ["cantilever_12x6_oc", "cantilever_h8_6x3x3_oc", "cantilever_60x30_oc"])
+def test_fp64_pcg_launch_shapes_match_oracle(gpu, name, shape):
+    """Every launch shape of the FP64 CSR PCG: one lane per row on the sliced copy (row
+    counts that are not multiples of 32, 3D rows of 81 entries) and 4 / 8 / 16 lanes per row on
+    the CSR itself."""
+    from pansfem2_gb300 import _lib
+    g, pr = load(name), CASES[name]()
+    coords, conn, dim = geometry(pr)
+    ne = PB.counts(pr)[0]
+    rho0 = O.density_filter(*O.neighbors(O.centroids(conn, coords, dim), pr["R"]), np.full(ne, pr["rho0"]))
+    E = pr["E1"] * np.power(rho0, pr["p"]) + pr["E0"] * (1.0 - np.power(rho0, pr["p"]))
+    with gpu.Problem(pr) as P:
+        P.setup_bc()
+        P.assemble(E)
+        P.set_launch_shape(_lib.PSF_KERNEL_PCG_CSR, *shape)
+        assert P.launch_shape(_lib.PSF_KERNEL_PCG_CSR) == shape
+        u, info = P.solve("csr_jacobi_f64", eps=1e-10)
+        assert info["status"] == 0, info
+        assert info["rel_residual"] < 1e-9
+        assert rel(u, g["result0"]) < TOL_U
+
+
 @pytest.mark.parametrize("name", ["cantilever_12x6_oc", "mbb_16x8_mma", "cantilever_h8_6x3x3_oc"])
 def test_filter_forward_backward(gpu, name):
     g, pr = load(name), CASES[name]()

@@ -69,7 +69,8 @@ def test_noalloc_matches_existing_entry_point_twice(env, case):
         ref, rinfo = generic.csr_solve(ip, ix, d, b, "csr_jacobi_f64", eps=1e-10)
         st, x, info = call_noalloc(torch, lib, ip, ix, d, b)
         assert st == lib.PSF_OK, lib.load().psf_last_error()
-        assert info.iterations == rinfo["iterations"]
+        # the same ScalingCG; the context's solve sums its rows in a different order (sliced copy)
+        assert abs(info.iterations - rinfo["iterations"]) <= max(2, rinfo["iterations"] // 50)
         assert rel(x, ref) < TOL_U
         # the FP64 true residual of the result, as the other solve entry points report it
         assert 0.0 < info.rel_residual < 1e-9, info.rel_residual
