@@ -77,26 +77,29 @@ def mg_levels(pr, coarse_dofs=40):
 def bytes_per_krylov_iteration(solver, pr, nnz, nfree):
     """Algorithmic HBM bytes of one Krylov iteration (every array a phase
     touches counted once per phase).
-    Jacobi PCG: operator + 11 vector passes (x, p, r, Ap, D read; x, r write;
-    r, D, p read; p write).
+    Jacobi PCG (three phases): the operator, 12 B per stored entry, and 14
+    vector passes (p = z + beta p: z, p read, p written; A p: p gathered, p
+    read, Ap written; update: x, p, Ap, r, 1/D read, x, r, z written).
     Multigrid FCG (ir_mg_f32): Krylov phases on 8-byte double-word vectors,
-    132 B/dof + 8 B/element (V-cycle input 20, z and dot products 28, p 20,
-    q = K p 16 + E, x/r update 48), the FP32
-    level-0 V(2,2) work 72 B/dof + 16 B/element, and per coarse level four
-    stencil applications (9 blocks in 2D, 27 in 3D, of nd x nd floats per
-    node) plus 72 B/dof of level vectors."""
+    125 B/dof + 8 B/element (z and dot products: the cycle's result, q, r, p
+    28; p and q = rs K x - beta q_prev: x, p, q read, p, q written 36 + E;
+    update: x, p, r, q, D, fixed read, x, r, the next cycle's input and first
+    sweep written 61), the fused level-0 V(2,2) work 34 B/dof + 8 B/element
+    (each fused phase reads its level's vectors, diagonal, flags and moduli
+    once), and per coarse level four stencil applications (9 blocks in 2D, 27
+    in 3D, of nd x nd floats per node) plus 34 B/dof of level vectors."""
     from pansfem2_gb300 import problems as PB
     ne, nnodes, nd = PB.counts(pr)
     ndofs = nnodes * nd
     if solver == "csr_jacobi_f64":
-        return 12 * nnz + 20 * nfree + 11 * 8 * nfree
+        return 12 * nnz + 14 * 8 * nfree
     if solver == "ebe_jacobi_f64":
         return 8 * ne + 16 * ndofs + 11 * 8 * ndofs
     if solver == "ir_mg_f32":
         nb = 27 if pr["kind"] == PB.H8_SOLID else 9
-        outer = 132 * ndofs + 8 * ne
-        level0 = 72 * ndofs + 16 * ne
-        coarse = sum(4 * nb * nd * nd * 4 * n + 72 * nd * n for n in mg_levels(pr)[1:-1])
+        outer = 125 * ndofs + 8 * ne
+        level0 = 34 * ndofs + 8 * ne
+        coarse = sum(4 * nb * nd * nd * 4 * n + 34 * nd * n for n in mg_levels(pr)[1:-1])
         return outer + level0 + coarse
     # FP32 inner Jacobi iterations
     return 4 * ne + 8 * ndofs + 11 * 4 * ndofs

@@ -129,6 +129,11 @@ psf_status psf_assemble(psf_ctx *ctx, const double *E_e, double *data_out, doubl
 psf_status psf_spmv(psf_ctx *ctx, const double *x, double *y);
 /* y = K x matrix-free (element-by-element with Ke(E=1) scaled by E_e), same K. */
 psf_status psf_ebe_matvec(psf_ctx *ctx, const double *x, double *y);
+/* z = M^-1 r with M^-1 one V(2,2)-cycle of the geometric multigrid that preconditions
+ * PSF_SOLVE_IR_MG_F32 (no counterpart in the reference; the hierarchy is built for the
+ * current moduli): z = |r| V(r / |r|) in FP32, returned in FP64.  Host vectors of length
+ * nfree. */
+psf_status psf_mg_precondition(psf_ctx *ctx, const double *r, double *z);
 
 /* Solve K u = F for the current E_e / loads (ScalingCG signature: itmax, eps;
  * CG.h:420).  u_out (nfree) is the reduced solution, optional.  For the

@@ -34,7 +34,7 @@ SOLVERS = {
 EXPORTS = [
     "psf_create", "psf_destroy", "psf_last_error", "psf_kernel_launches", "psf_set_launch_shape",
     "psf_get_launch_shape", "psf_diag_barrier_timeout", "psf_sizes", "psf_set_dirichlet", "psf_set_loads",
-    "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_solve",
+    "psf_element_matrix", "psf_build_csr", "psf_assemble", "psf_spmv", "psf_ebe_matvec", "psf_mg_precondition", "psf_solve",
     "psf_filter_setup", "psf_filter_forward", "psf_filter_backward", "psf_sensitivity_filter",
     "psf_compliance_sensitivity",
     "psf_oc_update", "psf_mma_init", "psf_mma_update", "psf_conlin_init", "psf_conlin_update",
@@ -124,6 +124,7 @@ def load(path=LIB_PATH):
         "psf_assemble": [vp, dp, dp, dp],
         "psf_spmv": [vp, dp, dp],
         "psf_ebe_matvec": [vp, dp, dp],
+        "psf_mg_precondition": [vp, dp, dp],
         "psf_solve": [vp, C.c_int, C.c_int, C.c_double, dp, C.POINTER(SolveInfo)],
         "psf_filter_setup": [vp, C.c_double],
         "psf_filter_forward": [vp, dp, dp],

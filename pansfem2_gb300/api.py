@@ -121,6 +121,13 @@ class Problem:
         check(self.L.psf_ebe_matvec(self.h, ptr(x), ptr(y)))
         return y
 
+    def mg_precondition(self, r):
+        """z = one multigrid V-cycle applied to r (psf_mg_precondition), reduced vectors."""
+        r = f64(r)
+        z = np.zeros(self.nfree)
+        check(self.L.psf_mg_precondition(self.h, ptr(r), ptr(z)))
+        return z
+
     def solve(self, solver="csr_jacobi_f64", itmax=100000, eps=1e-10):
         u = np.zeros(self.nfree)
         info = SolveInfo()

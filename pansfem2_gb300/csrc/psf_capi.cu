@@ -280,6 +280,19 @@ psf_status psf_ebe_matvec(psf_ctx *h, const double *x, double *y) {
     return d2h_sync(c, y, xr, sizeof(double) * c->nfree);
 }
 
+psf_status psf_mg_precondition(psf_ctx *h, const double *r, double *z) {
+    CTX_CHECK(h);
+    Ctx *c = &h->c;
+    if (!c->have_bc) { set_error("psf_mg_precondition: call psf_set_dirichlet and set the moduli first"); return PSF_BAD_INPUT; }
+    if (!r || !z) { set_error("psf_mg_precondition: null vector"); return PSF_BAD_INPUT; }
+    double *dx = c->w64[6], *dy = c->w64[7], *xr = c->w64[5];
+    PSF_CHECK(h2d(c, xr, r, sizeof(double) * c->nfree));
+    PSF_CHECK(scatter_reduced(c, xr, dx));
+    PSF_CHECK(mg_precondition(c, dx, dy));
+    PSF_CHECK(gather_reduced(c, dy, xr));
+    return d2h_sync(c, z, xr, sizeof(double) * c->nfree);
+}
+
 psf_status psf_solve(psf_ctx *h, int solver, int itmax, double eps, double *u_out, psf_solve_info *info) {
     CTX_CHECK(h);
     Ctx *c = &h->c;

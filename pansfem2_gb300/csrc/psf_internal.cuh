@@ -210,6 +210,7 @@ psf_status mma_dw_update(Ctx *c, bool conlin, double *x, const double *dfdx, dou
                          int *newton, bool *capped, bool *done);
 psf_status moduli_from_rho(Ctx *c, const double *rho, double E1, double E0, double p, double *E_dev);
 psf_status mg_free(Ctx *c);
+psf_status mg_precondition(Ctx *c, const double *r, double *z);   // psf_mg.cu
 psf_status learned_free(Ctx *c);                                                       // psf_learned.cu
 void vtk_free(Ctx *c);                                                                 // psf_vtk.cu
 psf_status learned_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *info);  // psf_learned.cu

@@ -76,6 +76,9 @@ struct MgHier {
     unsigned long long *trace = nullptr;   // phase timestamps (PSF_MG_TRACE)
     float2 *xw = nullptr, *rw = nullptr, *pw = nullptr, *qw = nullptr, *Ew = nullptr;   // double-word FCG
     long long npad = 0;
+    float *tbuf = nullptr;       // private buffers of the fused grid levels
+    size_t tbuf_bytes = 0;
+    size_t max_dyn = 0;          // dynamic shared memory the solver kernels may take
 };
 
 // ------------------------------------------------------------------ geometry helpers
@@ -116,8 +119,75 @@ __device__ __forceinline__ long long lelem(const MgLev &L, int i, int j, int k) 
     return KT<KIND>::is3d ? ((long long)L.ny * i + j) * L.nz + k : (long long)L.ny * i + j;
 }
 
+// the nd values of node m of a node-major vector (one 8-byte load for two dofs)
+template <int ND>
+__device__ __forceinline__ void load_node(const float *__restrict__ v, long long m, float *o) {
+    if constexpr (ND == 2) {
+        const float2 t = *reinterpret_cast<const float2 *>(v + 2 * m);
+        o[0] = t.x;
+        o[1] = t.y;
+    } else {
+#pragma unroll
+        for (int b = 0; b < ND; b++) o[b] = v[m * ND + b];
+    }
+}
+
+// 2D level 0: the 3 x 3 node neighbourhood of node (i, j) (u[a][b] = node (clamp(i + a - 1),
+// clamp(j + b - 1))) and the moduli of its four elements
+template <int ND>
+struct L0Gather {
+    float u[3][3][ND];
+    float E[2][2];
+};
+template <int KIND, class LD>
+__device__ __forceinline__ void l0_gather(const MgLev &L, LD ld, int i, int j, L0Gather<KT<KIND>::nd> &g) {
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int mi = min(max(i + a - 1, 0), L.nx), mj = min(max(j + b - 1, 0), L.ny);
+            ld(lnode<KIND>(L, mi, mj, 0), mi, mj, 0, g.u[a][b]);
+        }
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++) g.E[ci][cj] = L.Ep[(long long)(i + ci) * (L.ny + 2) + (j + cj)];
+}
+// y = sum over the four elements of E_e (Ke0 u_e) rows of the node, element by element
+template <int KIND>
+__device__ __forceinline__ void l0_compute(const KeF &Ke, const L0Gather<KT<KIND>::nd> &g, float *y) {
+    using T = KT<KIND>;
+#pragma unroll
+    for (int a = 0; a < T::nd; a++) y[a] = 0.f;
+#pragma unroll
+    for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+        for (int cj = 0; cj < 2; cj++) {
+            const int li = corner_q(1 - ci, 1 - cj, 0);
+            float ue[T::nk];
+#pragma unroll
+            for (int q = 0; q < T::nen; q++) {
+                int qi, qj, qk;
+                corner_of(q, qi, qj, qk);
+#pragma unroll
+                for (int b = 0; b < T::nd; b++) ue[q * T::nd + b] = g.u[ci + qi][cj + qj][b];
+            }
+            const float Ee = g.E[ci][cj];
+#pragma unroll
+            for (int a = 0; a < T::nd; a++) {
+                float acc = 0.f;
+                const int row = (li * T::nd + a) * T::nk;
+#pragma unroll
+                for (int l = 0; l < T::nk; l++) acc += Ke.v[row + l] * ue[l];
+                y[a] += Ee * acc;
+            }
+        }
+}
+
 // y = (A_l v)(node) for the ndof dofs of node (i,j,k); level 0 uses E*Ke0, coarse levels their
-// element matrices.  The vector is read through ld(m, mi, mj, mk, b): node m = (mi, mj, mk), dof b.
+// element matrices.  The vector is read through ld(m, mi, mj, mk, out): the nd values of node
+// m = (mi, mj, mk).  In 2D the 3 x 3 node neighbourhood is read once and shared by the four
+// elements (the sums are the same as element by element).
 template <int KIND, class LD>
 __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF &Ke, LD ld, int i, int j, int k,
                                              float *y) {
@@ -139,14 +209,19 @@ __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF 
                               mk = T::is3d ? min(max(k + dk, 0), L.nz) : 0;
                     const long long m = lnode<KIND>(L, mi, mj, mk);
                     float vb[T::nd];
-#pragma unroll
-                    for (int b = 0; b < T::nd; b++) vb[b] = ld(m, mi, mj, mk, b);
+                    ld(m, mi, mj, mk, vb);
 #pragma unroll
                     for (int a = 0; a < T::nd; a++)
 #pragma unroll
                         for (int b = 0; b < T::nd; b++)
                             y[a] += L.S[((long long)(slot * T::nd + a) * T::nd + b) * L.nnodes + n] * vb[b];
                 }
+        return;
+    }
+    if constexpr (!T::is3d) {
+        L0Gather<T::nd> g;
+        l0_gather<KIND>(L, ld, i, j, g);
+        l0_compute<KIND>(Ke, g, y);
         return;
     }
 #pragma unroll
@@ -156,7 +231,6 @@ __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF 
 #pragma unroll
             for (int ck = 0; ck < (T::is3d ? 2 : 1); ck++) {
                 const int ei = i - 1 + ci, ej = j - 1 + cj, ek = T::is3d ? k - 1 + ck : 0;
-                const bool inside = ei >= 0 && ei < L.nx && ej >= 0 && ej < L.ny && (!T::is3d || (ek >= 0 && ek < L.nz));
                 const int li = corner_q(1 - ci, 1 - cj, T::is3d ? 1 - ck : 0);
                 float ue[T::nk];
 #pragma unroll
@@ -165,31 +239,17 @@ __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF 
                     corner_of(q, qi, qj, qk);
                     const int ni = min(max(ei + qi, 0), L.nx), nj = min(max(ej + qj, 0), L.ny),
                               nk2 = T::is3d ? min(max(ek + qk, 0), L.nz) : 0;
-                    const long long m = lnode<KIND>(L, ni, nj, nk2);
-#pragma unroll
-                    for (int b = 0; b < T::nd; b++) ue[q * T::nd + b] = ld(m, ni, nj, nk2, b);
+                    ld(lnode<KIND>(L, ni, nj, nk2), ni, nj, nk2, ue + q * T::nd);
                 }
-                if (lev == 0) {
-                    const float Ee = L.Ep[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
-                                                  : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
+                const float Ee = L.Ep[T::is3d ? ((long long)(ei + 1) * (L.ny + 2) + (ej + 1)) * (L.nz + 2) + (ek + 1)
+                                              : (long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
 #pragma unroll
-                    for (int a = 0; a < T::nd; a++) {
-                        float acc = 0.f;
-                        const int row = (li * T::nd + a) * T::nk;
+                for (int a = 0; a < T::nd; a++) {
+                    float acc = 0.f;
+                    const int row = (li * T::nd + a) * T::nk;
 #pragma unroll
-                        for (int l = 0; l < T::nk; l++) acc += Ke.v[row + l] * ue[l];
-                        y[a] += Ee * acc;
-                    }
-                } else if (inside) {
-                    const float *Kel = L.K + lelem<KIND>(L, ei, ej, ek) * (T::nk * T::nk);
-#pragma unroll
-                    for (int a = 0; a < T::nd; a++) {
-                        float acc = 0.f;
-                        const float *row = Kel + (li * T::nd + a) * T::nk;
-#pragma unroll
-                        for (int l = 0; l < T::nk; l++) acc += row[l] * ue[l];
-                        y[a] += acc;
-                    }
+                    for (int l = 0; l < T::nk; l++) acc += Ke.v[row + l] * ue[l];
+                    y[a] += Ee * acc;
                 }
             }
 }
@@ -197,8 +257,8 @@ __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF 
 template <int KIND>
 __device__ __forceinline__ void apply_node(const MgLev &L, int lev, const KeF &Ke, const float *__restrict__ v, int i,
                                            int j, int k, float *y) {
-    apply_node_f<KIND>(L, lev, Ke, [v](long long m, int, int, int, int b) { return v[m * KT<KIND>::nd + b]; }, i, j, k,
-                       y);
+    apply_node_f<KIND>(L, lev, Ke, [v](long long m, int, int, int, float *o) { load_node<KT<KIND>::nd>(v, m, o); },
+                       i, j, k, y);
 }
 
 // interpolation weight of coarse corner q at fine position (fx, fy, fz) in {0, 1/2, 1}
@@ -450,6 +510,7 @@ struct MgFcgArgs {
     double *out;              // iterations, |r|^2, |b|^2, converged, V-cycles
     unsigned long long *trace;   // optional: [0] = count, then %globaltimer after each sync of one iteration
     int trace_iter;
+    int trace_steps;             // also after the block-level steps of the fused phases (block 0's view)
     // block 0's shared-memory levels: lsm (>= lsmall; nlev = none), byte offsets into dynamic
     // shared memory of S, D, x, xt, b, r, fixed per level, of the coarsest inverse (-1 = global)
     int lsm;
@@ -459,6 +520,17 @@ struct MgFcgArgs {
         // double-word Krylov vectors (mg_fcg_dw_kernel): x, r, p, q as FP32 pairs, padded moduli
     float2 *xw, *rw, *pw, *qw, *Ew;
     long long npad;           // padded moduli entries
+    // fused grid levels (levels < lsmall with fuse[l] = 1): block b owns tile b of the level's
+    // node grid, tg[l] tiles per axis of ts[l] nodes; tbuf holds two private buffers of
+    // tbuf_half floats per block (the tile grown by two nodes per side)
+    int fuse[kMaxLev];
+    int tg[kMaxLev][3], ts[kMaxLev][3];
+    float *tbuf;
+    long long tbuf_half;
+    // levels with tsm[l] = 1 keep the two buffers in dynamic shared memory from byte tsm_off
+    // (tsm_half floats each) instead
+    int tsm[kMaxLev];
+    int tsm_off, tsm_half;
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -466,11 +538,20 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
-// block 0 / thread 0 stamps the time after a grid sync of the traced iteration
+// block 0 / thread 0 stamps the time after a grid sync of the traced iteration (the count
+// is kept in shared memory: a global read-back would add its latency to every stamp)
+__shared__ unsigned int s_trace_n;
+__device__ __forceinline__ void trace_init() {
+    if (threadIdx.x == 0) s_trace_n = 0;
+}
 __device__ __forceinline__ void stamp(const MgFcgArgs &A, bool on) {
     if (on && A.trace && blockIdx.x == 0 && threadIdx.x == 0) {
-        const unsigned long long n = A.trace[0];
-        if (n < 1000) { A.trace[1 + n] = global_ns(); A.trace[0] = n + 1; }
+        const unsigned int n = s_trace_n;
+        if (n < 1000) {
+            A.trace[1 + n] = global_ns();
+            A.trace[0] = n + 1;
+            s_trace_n = n + 1;
+        }
     }
 }
 
@@ -672,6 +753,306 @@ __device__ void block0_levels(const MgFcgArgs &A, Block0View &V, unsigned char *
     __syncthreads();
 }
 
+// ------------------------------------------------------------------ fused grid levels
+// A grid level's down-leg (second pre-sweep, residual, restriction) and up-leg (prolongation,
+// two post-sweeps) each run as one grid phase instead of three: every block takes a tile of
+// the level's nodes, grown by two nodes per side, and computes the intermediate sweeps on the
+// grown tile into block-private buffers, the outer rings redundantly (each ring is the
+// neighbourhood the next step reads).  Every node gets the same arithmetic as in the
+// three-phase form, so the cycle's result is identical bit for bit; the grid barriers of a
+// V-cycle fall from 6 per grid level to 2.
+struct Box {
+    int i0, i1, j0, j1, k0, k1;   // half-open node ranges
+};
+
+template <int KIND>
+__device__ __forceinline__ bool own_box(const MgFcgArgs &A, int l, Box &b) {
+    const int *tg = A.tg[l], *ts = A.ts[l];
+    if ((int)blockIdx.x >= tg[0] * tg[1] * tg[2]) return false;
+    int q = blockIdx.x;
+    const int bk = q % tg[2];
+    q /= tg[2];
+    const int bj = q % tg[1], bi = q / tg[1];
+    const MgLev &L = A.L[l];
+    b.i0 = bi * ts[0]; b.i1 = min(b.i0 + ts[0], L.nx + 1);
+    b.j0 = bj * ts[1]; b.j1 = min(b.j0 + ts[1], L.ny + 1);
+    if (KT<KIND>::is3d) { b.k0 = bk * ts[2]; b.k1 = min(b.k0 + ts[2], L.nz + 1); }
+    else { b.k0 = 0; b.k1 = 1; }
+    return b.i0 < b.i1 && b.j0 < b.j1 && b.k0 < b.k1;
+}
+
+template <int KIND>
+__device__ __forceinline__ Box grow(const Box &b, int h, const MgLev &L) {
+    Box g;
+    g.i0 = max(b.i0 - h, 0); g.i1 = min(b.i1 + h, L.nx + 1);
+    g.j0 = max(b.j0 - h, 0); g.j1 = min(b.j1 + h, L.ny + 1);
+    if (KT<KIND>::is3d) { g.k0 = max(b.k0 - h, 0); g.k1 = min(b.k1 + h, L.nz + 1); }
+    else { g.k0 = 0; g.k1 = 1; }
+    return g;
+}
+
+__device__ __forceinline__ int box_vol(const Box &b) { return (b.i1 - b.i0) * (b.j1 - b.j0) * (b.k1 - b.k0); }
+__device__ __forceinline__ void box_ijk(const Box &b, int t, int &i, int &j, int &k) {
+    const int nk = b.k1 - b.k0, nj = b.j1 - b.j0;
+    k = b.k0 + t % nk;
+    t /= nk;
+    j = b.j0 + t % nj;
+    i = b.i0 + t / nj;
+}
+__device__ __forceinline__ int box_at(const Box &b, int i, int j, int k) {
+    return ((i - b.i0) * (b.j1 - b.j0) + (j - b.j0)) * (b.k1 - b.k0) + (k - b.k0);
+}
+__device__ __forceinline__ bool box_has(const Box &b, int i, int j, int k) {
+    return i >= b.i0 && i < b.i1 && j >= b.j0 && j < b.j1 && k >= b.k0 && k < b.k1;
+}
+
+// the block's two private buffers of level l
+__device__ __forceinline__ void tile_buffers(const MgFcgArgs &A, int l, float *&PX, float *&PR) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    if (A.tsm[l]) {
+        PX = (float *)(dsm + A.tsm_off);
+        PR = PX + A.tsm_half;
+    } else {
+        PX = A.tbuf + (size_t)blockIdx.x * 2 * A.tbuf_half;
+        PR = PX + A.tbuf_half;
+    }
+}
+
+// down-leg of grid level l as one phase (ends with the grid barrier)
+template <int KIND>
+__device__ bool down_fused(const MgFcgArgs &A, int l, bool tr) {
+    using T = KT<KIND>;
+    constexpr int nd = T::nd;
+    const MgLev &L = A.L[l];
+    const MgLev &Cc = A.L[l + 1];
+    Box own;
+    if (own_box<KIND>(A, l, own)) {
+        const Box g2 = grow<KIND>(own, 2, L), g1 = grow<KIND>(own, 1, L);
+        float *PX, *PR;
+        tile_buffers(A, l, PX, PR);
+        const float c2 = A.sm_c2, c3 = A.sm_c3;
+        // second pre-sweep (from the first sweep in L.x) on the tile + 2 rings; own nodes to L.xt
+        for (int t = threadIdx.x, nv = box_vol(g2); t < nv; t += blockDim.x) {
+            int i, j, k;
+            box_ijk(g2, t, i, j, k);
+            const long long n = lnode<KIND>(L, i, j, k);
+            float y[nd];
+            apply_node<KIND>(L, l, A.Ke, L.x, i, j, k, y);
+            const bool mine = box_has(own, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) {
+                const long long q = n * nd + s;
+                const float xv = L.x[q];
+                const float x2 = L.fixed[q] ? 0.f : xv + c2 * (xv - 0.f) + c3 * (L.b[q] - y[s]) / L.D[q];
+                PX[t * nd + s] = x2;
+                if (mine) L.xt[q] = x2;
+            }
+        }
+        __syncthreads();
+        stamp(A, tr && A.trace_steps);
+        // residual on the tile + 1 ring
+        auto ldx = [&](long long, int mi, int mj, int mk, float *o) { load_node<nd>(PX, box_at(g2, mi, mj, mk), o); };
+        for (int t = threadIdx.x, nv = box_vol(g1); t < nv; t += blockDim.x) {
+            int i, j, k;
+            box_ijk(g1, t, i, j, k);
+            const long long n = lnode<KIND>(L, i, j, k);
+            float y[nd];
+            apply_node_f<KIND>(L, l, A.Ke, ldx, i, j, k, y);
+            const int o = box_at(g2, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) {
+                const long long q = n * nd + s;
+                PR[o * nd + s] = L.fixed[q] ? 0.f : L.b[q] - y[s];
+            }
+        }
+        __syncthreads();
+        stamp(A, tr && A.trace_steps);
+        // restriction to the coarse nodes on the tile (a ghost coarse node beyond an odd axis
+        // belongs to the last tile of that axis)
+        Box cb;
+        cb.i0 = (own.i0 + 1) >> 1; cb.i1 = own.i1 == L.nx + 1 ? Cc.nx + 1 : (own.i1 + 1) >> 1;
+        cb.j0 = (own.j0 + 1) >> 1; cb.j1 = own.j1 == L.ny + 1 ? Cc.ny + 1 : (own.j1 + 1) >> 1;
+        if (T::is3d) { cb.k0 = (own.k0 + 1) >> 1; cb.k1 = own.k1 == L.nz + 1 ? Cc.nz + 1 : (own.k1 + 1) >> 1; }
+        else { cb.k0 = 0; cb.k1 = 1; }
+        const bool first = l + 1 < A.nlev - 1;
+        for (int t = threadIdx.x, nv = cb.i1 > cb.i0 && cb.j1 > cb.j0 && cb.k1 > cb.k0 ? box_vol(cb) : 0; t < nv;
+             t += blockDim.x) {
+            int i, j, k;
+            box_ijk(cb, t, i, j, k);
+            float acc[nd];
+#pragma unroll
+            for (int s = 0; s < nd; s++) acc[s] = 0.f;
+            for (int di = -1; di <= 1; di++)
+                for (int dj = -1; dj <= 1; dj++)
+                    for (int dk = (T::is3d ? -1 : 0); dk <= (T::is3d ? 1 : 0); dk++) {
+                        const int fi = 2 * i + di, fj = 2 * j + dj, fk = 2 * k + dk;
+                        if (fi < 0 || fi > L.nx || fj < 0 || fj > L.ny || (T::is3d && (fk < 0 || fk > L.nz))) continue;
+                        const float w = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * (dk ? 0.5f : 1.f);
+                        const int o = box_at(g2, fi, fj, fk);
+#pragma unroll
+                        for (int s = 0; s < nd; s++) acc[s] += w * PR[o * nd + s];
+                    }
+            const long long n = lnode<KIND>(Cc, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) {
+                const long long q = n * nd + s;
+                const float bv = Cc.fixed[q] ? 0.f : acc[s];
+                Cc.b[q] = bv;
+                Cc.x[q] = first ? A.omega * bv / Cc.D[q] : 0.f;   // first sweep from zero
+            }
+        }
+    }
+    if (A.trace_steps) {
+        __syncthreads();
+        stamp(A, tr);
+    }
+    if (!grid_barrier(A.gs, A.partials)) return false;
+    stamp(A, tr);
+    return true;
+}
+
+// up-leg of grid level l as one phase: x = xt + P x_c and two post-sweeps, the result in L.x
+// of the own nodes; on(q, x) sees every own dof's result.  Ends with the grid barrier when
+// `barrier` (the caller's next phase reads other blocks' nodes).
+template <int KIND, class ON>
+__device__ bool up_fused(const MgFcgArgs &A, int l, bool tr, bool barrier, ON on) {
+    using T = KT<KIND>;
+    constexpr int nd = T::nd;
+    const MgLev &L = A.L[l];
+    const MgLev &Cc = A.L[l + 1];
+    Box own;
+    if (own_box<KIND>(A, l, own)) {
+        const Box g2 = grow<KIND>(own, 2, L), g1 = grow<KIND>(own, 1, L);
+        float *PX, *PR;
+        tile_buffers(A, l, PX, PR);
+        // x = xt + P x_c on the tile + 2 rings
+        for (int t = threadIdx.x, nv = box_vol(g2); t < nv; t += blockDim.x) {
+            int i, j, k;
+            box_ijk(g2, t, i, j, k);
+            const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+            const int hi = i & 1, hj = j & 1, hk = k & 1;
+            float acc[nd];
+#pragma unroll
+            for (int s = 0; s < nd; s++) acc[s] = 0.f;
+            for (int a = 0; a <= hi; a++)
+                for (int b = 0; b <= hj; b++)
+                    for (int c = 0; c <= (T::is3d ? hk : 0); c++) {
+                        const float w = (hi ? 0.5f : 1.f) * (hj ? 0.5f : 1.f) * ((T::is3d && hk) ? 0.5f : 1.f);
+                        const long long m = lnode<KIND>(Cc, ci + a, cj + b, ck + c);
+#pragma unroll
+                        for (int s = 0; s < nd; s++) acc[s] += w * Cc.x[m * nd + s];
+                    }
+            const long long n = lnode<KIND>(L, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) {
+                const long long q = n * nd + s;
+                PX[t * nd + s] = L.fixed[q] ? 0.f : L.xt[q] + acc[s];
+            }
+        }
+        __syncthreads();
+        stamp(A, tr && A.trace_steps);
+        // post-smoothing step 1 on the tile + 1 ring
+        auto ldx = [&](long long, int mi, int mj, int mk, float *o) { load_node<nd>(PX, box_at(g2, mi, mj, mk), o); };
+        for (int t = threadIdx.x, nv = box_vol(g1); t < nv; t += blockDim.x) {
+            int i, j, k;
+            box_ijk(g1, t, i, j, k);
+            const long long n = lnode<KIND>(L, i, j, k);
+            float y[nd];
+            apply_node_f<KIND>(L, l, A.Ke, ldx, i, j, k, y);
+            const int o = box_at(g2, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) {
+                const long long q = n * nd + s;
+                const float xv = PX[o * nd + s];
+                PR[o * nd + s] = L.fixed[q] ? 0.f : xv + 0.f * (xv - 0.f) + A.omega * (L.b[q] - y[s]) / L.D[q];
+            }
+        }
+        __syncthreads();
+        stamp(A, tr && A.trace_steps);
+        // post-smoothing step 2 on the own nodes -> L.x
+        auto ldt = [&](long long, int mi, int mj, int mk, float *o) { load_node<nd>(PR, box_at(g2, mi, mj, mk), o); };
+        const float c2 = A.sm_c2, c3 = A.sm_c3;
+        for (int t = threadIdx.x, nv = box_vol(own); t < nv; t += blockDim.x) {
+            int i, j, k;
+            box_ijk(own, t, i, j, k);
+            const long long n = lnode<KIND>(L, i, j, k);
+            float y[nd];
+            apply_node_f<KIND>(L, l, A.Ke, ldt, i, j, k, y);
+            const int o = box_at(g2, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) {
+                const long long q = n * nd + s;
+                const float xv = PR[o * nd + s], xp = PX[o * nd + s];
+                L.x[q] = L.fixed[q] ? 0.f : xv + c2 * (xv - xp) + c3 * (L.b[q] - y[s]) / L.D[q];
+            }
+        }
+        // the caller's view of the result, in a second pass over the same nodes in the same
+        // thread order (each thread reads back what it wrote)
+        for (int t = threadIdx.x, nv = box_vol(own); t < nv; t += blockDim.x) {
+            int i, j, k;
+            box_ijk(own, t, i, j, k);
+            const long long n = lnode<KIND>(L, i, j, k);
+#pragma unroll
+            for (int s = 0; s < nd; s++) on(n * nd + s, L.x[n * nd + s]);
+        }
+    }
+    if (A.trace_steps) {
+        __syncthreads();
+        stamp(A, tr);
+    }
+    if (barrier) {
+        if (!grid_barrier(A.gs, A.partials)) return false;
+        stamp(A, tr);
+    }
+    return true;
+}
+
+// V(2,2)-cycle with the grid levels fused where fuse[l] is set (the others run as three
+// phases each); on(q, x) sees the level-0 result of every dof this thread wrote, with no
+// barrier after the last sweep (the caller's reduction follows).
+template <int KIND, class ON>
+__device__ bool vcycle_fused(const MgFcgArgs &A, const Block0View &V, long long tid, long long stride, bool tr, ON on) {
+    const int nl = A.nlev, ls = A.lsmall;
+    for (int l = 0; l < ls; l++) {
+        if (A.fuse[l]) {
+            if (!down_fused<KIND>(A, l, tr)) return false;
+        } else if (!down_level<KIND>(A, A.L, l, tid, stride, true, tr)) {
+            return false;
+        }
+    }
+    if (blockIdx.x == 0) {
+        const long long bt = threadIdx.x, bs = blockDim.x;
+        const bool tb = tr && A.trace_steps;
+        for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, V.L, l, bt, bs, false, tb);
+        coarsest_solve(A, V.L, V.Ainv, bt, bs);
+        __syncthreads();
+        stamp(A, tb);
+        for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, V.L, l, bt, bs, false, tb);
+    }
+    if (!grid_barrier(A.gs, A.partials)) return false;
+    stamp(A, tr);
+    auto none = [](long long, float) {};
+    for (int l = ls - 1; l >= 1; l--) {
+        if (A.fuse[l]) {
+            if (!up_fused<KIND>(A, l, tr, true, none)) return false;
+        } else if (!up_level<KIND>(A, A.L, l, tid, stride, true, tr)) {
+            return false;
+        }
+    }
+    if (ls >= 1 && A.fuse[0]) return up_fused<KIND>(A, 0, tr, false, on);
+    if (ls >= 1 && !up_level<KIND>(A, A.L, 0, tid, stride, true, tr)) return false;
+    // level 0 unfused (or the cycle is the coarsest solve alone): the last node loop wrote
+    // the own dofs in the grid-stride order
+    const MgLev &L0 = A.L[0];
+    for (long long n = tid; n < L0.nnodes; n += stride)
+#pragma unroll
+        for (int s = 0; s < KT<KIND>::nd; s++) {
+            const long long q = n * KT<KIND>::nd + s;
+            on(q, L0.x[q]);
+        }
+    return true;
+}
+
 template <int KIND>
 __device__ bool vcycle(const MgFcgArgs &A, const Block0View &V, long long tid, long long stride, bool tr) {
     const int nl = A.nlev, ls = A.lsmall;
@@ -803,6 +1184,68 @@ __device__ __forceinline__ void applydw_core(const MgFcgArgs &A, LD vload, long 
             }
 }
 
+// The same product for an FP32 vector x (exact in double words with a zero low part): the
+// low-order term is lo * x alone, and in 2D the 3 x 3 node neighbourhood is read once.
+// Per element the terms are summed in the same order as above.
+template <int KIND>
+__device__ __forceinline__ void applydw_x32(const MgFcgArgs &A, const float *__restrict__ x, long long n, dw::D *y) {
+    using T = KT<KIND>;
+    if constexpr (T::is3d) {
+        applydw_core<KIND>(A, [x](long long t) { return make_float2(x[t], 0.f); }, n, y);
+    } else {
+        const MgLev &L = A.L[0];
+        int i, j, k;
+        lnode_ijk<KIND>(L, n, i, j, k);
+        float u[3][3][T::nd];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                const int mi = min(max(i + a - 1, 0), L.nx), mj = min(max(j + b - 1, 0), L.ny);
+                load_node<T::nd>(x, lnode<KIND>(L, mi, mj, 0), u[a][b]);
+            }
+#pragma unroll
+        for (int a = 0; a < T::nd; a++) y[a] = dw::from_float(0.f);
+#pragma unroll
+        for (int ci = 0; ci < 2; ci++)
+#pragma unroll
+            for (int cj = 0; cj < 2; cj++) {
+                const int ei = i - 1 + ci, ej = j - 1 + cj;
+                const int li = corner_q(1 - ci, 1 - cj, 0);
+                const float2 Ev = A.Ew[(long long)(ei + 1) * (L.ny + 2) + (ej + 1)];
+                if (Ev.x == 0.f) continue;
+                float ps[T::nd], cs[T::nd];
+#pragma unroll
+                for (int a = 0; a < T::nd; a++) ps[a] = cs[a] = 0.0f;
+#pragma unroll
+                for (int q = 0; q < T::nen; q++) {
+                    int qi, qj, qk;
+                    corner_of(q, qi, qj, qk);
+#pragma unroll
+                    for (int b = 0; b < T::nd; b++) {
+                        const float uv = u[ci + qi][cj + qj][b];
+                        const int l = q * T::nd + b;
+#pragma unroll
+                        for (int a = 0; a < T::nd; a++) {
+                            const int kk = (li * T::nd + a) * T::nk + l;
+                            float pe, se;
+                            const float pr = dw::two_prod(A.Kds.hi[kk], uv, pe);
+                            ps[a] = dw::two_sum(ps[a], pr, se);
+                            cs[a] += se + pe + A.Kds.lo[kk] * uv;
+                        }
+                    }
+                }
+                const dw::D Ed = dw::make(Ev.x, Ev.y);
+#pragma unroll
+                for (int a = 0; a < T::nd; a++) {
+                    float sl;
+                    const float sh = dw::fast_two_sum(ps[a], cs[a], sl);
+                    y[a] = dw::add(y[a], dw::mul(Ed, dw::make(sh, sl)));
+                }
+            }
+    }
+}
+
 template <int KIND>
 __device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *__restrict__ v, long long n,
                                               float2 *__restrict__ out) {
@@ -825,6 +1268,7 @@ __device__ __forceinline__ dw::D applydw_node(const MgFcgArgs &A, const float2 *
 template <int KIND>
 __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
     grid_sync_init();
+    trace_init();
     using T = KT<KIND>;
     __shared__ double sm[32 * 4];
     __shared__ Block0View B0;
@@ -965,6 +1409,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_kernel(MgFcgArgs A) {
 template <int KIND>
 __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
     grid_sync_init();
+    trace_init();
     using T = KT<KIND>;
     using dw::D;
     __shared__ double sm[32 * 4];
@@ -1006,9 +1451,12 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
     double rr = gs_result(A.gs, 1);
     double rn = sqrt(rr), pq_prev = 1.0;
     int it = 0, conv = (rn <= A.eps * bnorm) ? 1 : 0, cycles = 0;
-    for (; !conv && it < A.itmax; it++) {
-        // ---- preconditioner: one FP32 V-cycle on r / |r|
-        const float sc = (float)(1.0 / rn);
+    // The cycle's input is r scaled by 1 / rs, rs the residual norm known when r was formed (the
+    // current one before the first cycle, the previous one after), so the input is formed in
+    // the update phase that forms r; z = rs V(r / rs).
+    double rs = rn;
+    if (!conv) {
+        const float sc = (float)(1.0 / rs);
         for (long long n = tid; n < L0.nnodes; n += stride)
 #pragma unroll
             for (int s = 0; s < T::nd; s++) {
@@ -1018,43 +1466,54 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
                 L0.b[t] = bv;
                 L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
             }
+        if (!grid_barrier(A.gs, A.partials)) return;
+    }
+    for (; !conv && it < A.itmax; it++) {
         const bool tr = it == A.trace_iter;
         stamp(A, tr);
-        if (!grid_barrier(A.gs, A.partials)) return;
-        stamp(A, tr);
-        if (!vcycle<KIND>(A, B0, tid, stride, tr)) return;
-        cycles++;
-        // ---- z = |r| V(r/|r|) (own dofs of L0.x); z.q_prev, z.r, p_prev.r
-        const D rnD = dw::from_double(rn);
+        // ---- preconditioner: one FP32 V-cycle; z = rs x (never stored); z.q_prev, z.r, p_prev.r
+        const D rsD = dw::from_double(rs);
         D a3[3] = {dw::from_float(0.f), dw::from_float(0.f), dw::from_float(0.f)};
-        for (long long n = tid; n < L0.nnodes; n += stride)
-#pragma unroll
-            for (int s = 0; s < T::nd; s++) {
-                const long long t = n * T::nd + s;
-                const D zv = dw::mulf(rnD, L0.x[t]);
-                a3[0] = dw::add(a3[0], dw::mul(zv, ld(Q, t)));
-                a3[1] = dw::add(a3[1], dw::mul(zv, ld(R, t)));
-                a3[2] = dw::add(a3[2], dw::mul(ld(P, t), ld(R, t)));
-            }
+        auto on = [&](long long t, float xv) {
+            const D zv = dw::mulf(rsD, xv);
+            a3[0] = dw::add(a3[0], dw::mul(zv, ld(Q, t)));
+            a3[1] = dw::add(a3[1], dw::mul(zv, ld(R, t)));
+            a3[2] = dw::add(a3[2], dw::mul(ld(P, t), ld(R, t)));
+        };
+        if (!vcycle_fused<KIND>(A, B0, tid, stride, tr, on)) return;
+        cycles++;
         double s3[3] = {0.0, 0.0, 0.0};
         dw::block_sum_dw<3>(a3, s3, sm);
+        if (A.trace_steps) {
+            __syncthreads();
+            stamp(A, tr);
+        }
         if (!grid_sync<3, 0>(A.gs, A.partials, s3, 0.0)) return;
         stamp(A, tr);
         const double beta = it > 0 ? gs_result(A.gs, 0) / pq_prev : 0.0;
         const double pr = gs_result(A.gs, 1) - beta * gs_result(A.gs, 2);
         const D betaD = dw::from_double(beta);
-        // ---- p = z - beta p_prev (own dofs)
-        for (long long n = tid; n < L0.nnodes; n += stride)
+        // ---- p = z - beta p_prev and q = K p = rs K x - beta q_prev (K applied to the cycle's
+        //      FP32 result, exact in double words), p.q
+        D pqd[1] = {dw::from_float(0.f)};
+        const float *X0 = L0.x;
+        for (long long n = tid; n < L0.nnodes; n += stride) {
+            D y[T::nd];
+            applydw_x32<KIND>(A, X0, n, y);
 #pragma unroll
             for (int s = 0; s < T::nd; s++) {
                 const long long t = n * T::nd + s;
-                st(P, t, dw::sub(dw::mulf(rnD, L0.x[t]), dw::mul(betaD, ld(P, t))));
+                const D pv = dw::sub(dw::mulf(rsD, X0[t]), dw::mul(betaD, ld(P, t)));
+                const D qv = L0.fixed[t] ? dw::from_float(0.f) : dw::sub(dw::mul(rsD, y[s]), dw::mul(betaD, ld(Q, t)));
+                st(P, t, pv);
+                st(Q, t, qv);
+                pqd[0] = dw::add(pqd[0], dw::mul(pv, qv));
             }
-        if (!grid_barrier(A.gs, A.partials)) return;
-        stamp(A, tr);
-        // ---- q = K p (double words), p.q
-        D pqd[1] = {dw::from_float(0.f)};
-        for (long long n = tid; n < L0.nnodes; n += stride) pqd[0] = dw::add(pqd[0], applydw_node<KIND>(A, P, n, Q));
+        }
+        if (A.trace_steps) {
+            __syncthreads();
+            stamp(A, tr);
+        }
         double pq[1] = {0.0};
         dw::block_sum_dw<1>(pqd, pq, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, pq, 0.0)) return;
@@ -1062,21 +1521,55 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_fcg_dw_kernel(MgFcgArgs A) {
         const double pqv = gs_result(A.gs, 0);
         if (!(pqv > 0.0)) { it++; break; }
         const D alphaD = dw::from_double(pr / pqv);
-        // ---- x += alpha p, r -= alpha q, |r|^2
+        // ---- x += alpha p, r -= alpha q, |r|^2; the next cycle's input r / |r_prev| and its
+        //      first sweep
+        const float sc = (float)(1.0 / rn);
         D rad[1] = {dw::from_float(0.f)};
-        for (long long n = tid; n < L0.nnodes; n += stride)
+        // two nodes per pass, every load of both issued before the arithmetic
+        for (long long n0 = tid; n0 < L0.nnodes; n0 += 2 * stride) {
+            constexpr int nd = T::nd;
+            const bool two = n0 + stride < L0.nnodes;
+            float2 xv[2][nd], pv[2][nd], rv[2][nd], qv[2][nd];
+            float dv[2][nd];
+            unsigned char fx[2][nd];
 #pragma unroll
-            for (int s = 0; s < T::nd; s++) {
-                const long long t = n * T::nd + s;
-                st(X, t, dw::add(ld(X, t), dw::mul(alphaD, ld(P, t))));
-                const D rv = dw::sub(ld(R, t), dw::mul(alphaD, ld(Q, t)));
-                st(R, t, rv);
-                rad[0] = dw::add(rad[0], dw::sq(rv));
+            for (int h = 0; h < 2; h++)
+#pragma unroll
+                for (int s = 0; s < nd; s++) {
+                    const long long t = (n0 + (h ? stride : 0)) * nd + s;
+                    const bool on = h == 0 || two;
+                    xv[h][s] = on ? X[t] : make_float2(0.f, 0.f);
+                    pv[h][s] = on ? P[t] : make_float2(0.f, 0.f);
+                    rv[h][s] = on ? R[t] : make_float2(0.f, 0.f);
+                    qv[h][s] = on ? Q[t] : make_float2(0.f, 0.f);
+                    dv[h][s] = on ? L0.D[t] : 1.f;
+                    fx[h][s] = on ? L0.fixed[t] : 1;
+                }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (h == 1 && !two) break;
+#pragma unroll
+                for (int s = 0; s < nd; s++) {
+                    const long long t = (n0 + (h ? stride : 0)) * nd + s;
+                    st(X, t, dw::add(dw::make(xv[h][s].x, xv[h][s].y), dw::mul(alphaD, dw::make(pv[h][s].x, pv[h][s].y))));
+                    const D r1 = dw::sub(dw::make(rv[h][s].x, rv[h][s].y), dw::mul(alphaD, dw::make(qv[h][s].x, qv[h][s].y)));
+                    st(R, t, r1);
+                    rad[0] = dw::add(rad[0], dw::sq(r1));
+                    const float bv = fx[h][s] ? 0.f : r1.h * sc + r1.l * sc;
+                    L0.b[t] = bv;
+                    L0.x[t] = fx[h][s] ? 0.f : A.omega * bv / dv[h][s];
+                }
             }
+        }
+        if (A.trace_steps) {
+            __syncthreads();
+            stamp(A, tr);
+        }
         double ra[1] = {0.0};
         dw::block_sum_dw<1>(rad, ra, sm);
         if (!grid_sync<1, 0>(A.gs, A.partials, ra, 0.0)) return;
         stamp(A, tr);
+        rs = rn;
         rr = gs_result(A.gs, 0);
         rn = sqrt(rr);
         pq_prev = pqv;
@@ -1139,17 +1632,23 @@ __global__ void __launch_bounds__(kMgThreads, 1) mg_apply_kernel(MgFcgArgs A, co
             L0.x[t] = L0.fixed[t] ? 0.f : A.omega * bv / L0.D[t];
         }
     if (!grid_barrier(A.gs, A.partials)) return;
-    if (!vcycle<KIND>(A, B0, tid, stride, false)) return;
-    for (long long t = tid; t < L0.ndofs; t += stride) xo[t] = L0.fixed[t] ? 0.0f : (float)(rn * (double)L0.x[t]);
+    vcycle_fused<KIND>(A, B0, tid, stride, false,
+                       [&](long long t, float xv) { xo[t] = L0.fixed[t] ? 0.0f : (float)(rn * (double)xv); });
 }
 
 // ------------------------------------------------------------------ host side
-constexpr long long kSmallLevelNodes = 4096;   // levels at most this large run in one block
+// levels at most this large run in one block: on the 1025 x 513-node MBB grid, block 0 from
+// the 561-node level on takes 230 us per FCG iteration, from the 2,145-node level 267 us,
+// from the 153-node level 242 us (a level on the grid costs two or six barriers, a level in
+// block 0 runs one SM's worth of threads)
+constexpr long long kSmallLevelNodes = 1024;
 
-// first level (>= 1) that block 0 runs alone
+// first level (>= 1) that block 0 runs alone (PSF_MG_SMALL_NODES overrides the size)
 static int mg_small_level(const MgHier *H) {
+    const char *e = getenv("PSF_MG_SMALL_NODES");
+    const long long lim = e && *e ? atoll(e) : kSmallLevelNodes;
     for (int l = 1; l < H->nlev - 1; l++)
-        if (H->L[l].nnodes <= kSmallLevelNodes) return l;
+        if (H->L[l].nnodes <= lim) return l;
     return H->nlev - 1;
 }
 
@@ -1271,14 +1770,23 @@ static psf_status mg_setup_t(Ctx *c, MgHier *H) {
     (dense_fix_identity<<<grid_for(n, 128), 128, 0, c->stream>>>(H->Ac, Lc.fixed, n), ::psf::note_launch());
     (gauss_jordan_kernel<<<1, 1024, 0, c->stream>>>(H->Ac, n), ::psf::note_launch());
     PSF_CUDA(cudaGetLastError());
-    // the solver kernels may use up to kMaxDynSmem of dynamic shared memory (block 0's levels);
-    // set here, outside any stream capture of their launches
-    PSF_CUDA(cudaFuncSetAttribute((const void *)mg_fcg_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kMaxDynSmem));
-    PSF_CUDA(cudaFuncSetAttribute((const void *)mg_fcg_dw_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kMaxDynSmem));
-    PSF_CUDA(cudaFuncSetAttribute((const void *)mg_apply_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kMaxDynSmem));
+    // the solver kernels may use all the dynamic shared memory a block can opt into (block 0's
+    // levels, the fused levels' buffers); set here, outside any stream capture of their launches
+    int dev = 0, optin = 0;
+    PSF_CUDA(cudaGetDevice(&dev));
+    PSF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    size_t max_dyn = (size_t)optin;
+    const void *fns[3] = {(const void *)mg_fcg_kernel<KIND>, (const void *)mg_fcg_dw_kernel<KIND>,
+                          (const void *)mg_apply_kernel<KIND>};
+    for (const void *fn : fns) {
+        cudaFuncAttributes fa;
+        PSF_CUDA(cudaFuncGetAttributes(&fa, fn));
+        max_dyn = std::min(max_dyn, (size_t)optin - fa.sharedSizeBytes);
+    }
+    max_dyn &= ~(size_t)15;
+    for (const void *fn : fns)
+        PSF_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn));
+    H->max_dyn = max_dyn;
     return PSF_OK;
 }
 
@@ -1320,6 +1828,77 @@ static void mg_smoother(MgFcgArgs *a) {
     }
 }
 
+// Tiles of the fused grid levels for a launch of `blocks` blocks: per level the tile grid
+// (at most one tile per block) whose grown tile (two rings) is smallest; a level is fused
+// when that grown tile holds at most 1.35x (level 0) or 3x (coarser levels, whose phases
+// are short and barrier-bound) the own nodes.  PSF_MG_FUSE=0 runs every level in three
+// phases, =2 fuses every grid level.
+// The buffers of a fused level go to dynamic shared memory, after block 0's levels
+// (*smem bytes on entry, the launch's total on return), where both fit in max_dyn bytes.
+static psf_status mg_tiles(Ctx *c, MgHier *H, MgFcgArgs *a, int blocks, size_t max_dyn, size_t *smem) {
+    const bool is3d = c->kind == PSF_H8_SOLID;
+    const char *e = getenv("PSF_MG_FUSE");
+    const int mode = e && *e ? atoi(e) : 1;
+    long long half = 0, half_sm = 0;
+    const size_t off = (*smem + 15) & ~(size_t)15;
+    const size_t avail = max_dyn > off ? max_dyn - off : 0;
+    for (int l = 0; l < kMaxLev; l++) {
+        a->fuse[l] = 0;
+        a->tsm[l] = 0;
+        for (int d = 0; d < 3; d++) a->tg[l][d] = a->ts[l][d] = 1;
+    }
+    for (int l = 0; l < a->lsmall && l < H->nlev - 1; l++) {
+        const MgLev &L = H->L[l];
+        const long long N[3] = {L.nx + 1, L.ny + 1, is3d ? L.nz + 1 : 1};
+        long long best = -1;
+        int bt[3] = {1, 1, 1};
+        for (long long ti = 1; ti <= blocks && ti <= N[0]; ti++)
+            for (long long tj = 1; ti * tj <= blocks && tj <= N[1]; tj++)
+                for (long long tk = 1; ti * tj * tk <= blocks && tk <= N[2]; tk++) {
+                    const long long si = (N[0] + ti - 1) / ti, sj = (N[1] + tj - 1) / tj, sk = (N[2] + tk - 1) / tk;
+                    const long long cost = (si + 4) * (sj + 4) * (is3d ? sk + 4 : 1);
+                    if (best < 0 || cost < best) {
+                        best = cost;
+                        bt[0] = (int)ti; bt[1] = (int)tj; bt[2] = (int)tk;
+                    }
+                }
+        const long long s0 = (N[0] + bt[0] - 1) / bt[0], s1 = (N[1] + bt[1] - 1) / bt[1], s2 = (N[2] + bt[2] - 1) / bt[2];
+        const double ratio = (double)best / (double)(s0 * s1 * s2);
+        const bool f = mode == 0 ? false : (mode == 2 ? true : ratio <= (l == 0 ? 1.35 : 3.0));
+        a->fuse[l] = f ? 1 : 0;
+        a->tg[l][0] = bt[0]; a->tg[l][1] = bt[1]; a->tg[l][2] = bt[2];
+        a->ts[l][0] = (int)s0; a->ts[l][1] = (int)s1; a->ts[l][2] = (int)s2;
+        if (!f) continue;
+        const long long need = ((best * c->ndof) + 3) & ~3ll;   // floats per buffer, 16-byte multiple
+        if ((size_t)need * 2 * sizeof(float) <= avail) {
+            a->tsm[l] = 1;
+            half_sm = std::max(half_sm, need);
+        } else {
+            half = std::max(half, need);
+        }
+    }
+    half = (half + 31) & ~31ll;
+    const size_t bytes = (size_t)blocks * 2 * (size_t)half * sizeof(float);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    PSF_CUDA(cudaStreamIsCapturing(c->stream, &cap));
+    if (bytes > H->tbuf_bytes && cap != cudaStreamCaptureStatusNone) {
+        // no allocation inside a stream capture: the levels that would need global buffers
+        // run in three phases
+        for (int l = 0; l < kMaxLev; l++)
+            if (a->fuse[l] && !a->tsm[l]) a->fuse[l] = 0;
+        half = 0;
+    } else if (bytes > H->tbuf_bytes) {
+        PSF_CHECK(mg_alloc(H, c, (void **)&H->tbuf, bytes));
+        H->tbuf_bytes = bytes;
+    }
+    a->tbuf = H->tbuf;
+    a->tbuf_half = half;
+    a->tsm_off = (int)off;
+    a->tsm_half = (int)half_sm;
+    if (half_sm > 0) *smem = off + (size_t)half_sm * 2 * sizeof(float);
+    return PSF_OK;
+}
+
 template <int KIND>
 static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h, bool dwords, size_t smem) {
     const void *fn = dwords ? (const void *)mg_fcg_dw_kernel<KIND> : (const void *)mg_fcg_kernel<KIND>;
@@ -1330,6 +1909,7 @@ static psf_status mg_fcg_t(Ctx *c, MgFcgArgs &a, double *h, bool dwords, size_t 
     long long need = (c->nnodes + kMgThreads - 1) / kMgThreads;
     if (blocks > need) blocks = (int)need;
     if (blocks < 1) blocks = 1;
+    PSF_CHECK(mg_tiles(c, (MgHier *)c->mg, &a, blocks, ((MgHier *)c->mg)->max_dyn, &smem));
     void *args[] = {&a};
     PSF_CUDA(cudaEventRecord(c->evk0, c->stream));
     PSF_CHECK(launch_coop(c, fn, blocks, kMgThreads, args, smem));
@@ -1377,6 +1957,7 @@ psf_status mg_solve(Ctx *c, int itmax, double eps, bool warm, psf_solve_info *in
     const char *trace_path = getenv("PSF_MG_TRACE");
     a->trace = nullptr;
     a->trace_iter = 2;
+    a->trace_steps = getenv("PSF_MG_TRACE_STEPS") ? 1 : 0;
     if (trace_path && *trace_path) {
         if (!H->trace) PSF_CHECK(mg_alloc(H, c, (void **)&H->trace, sizeof(unsigned long long) * 1001));
         PSF_CUDA(cudaMemsetAsync(H->trace, 0, sizeof(unsigned long long) * 1001, c->stream));
@@ -1477,6 +2058,7 @@ static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, con
     a->partials = c->partials;
     a->trace = nullptr;
     a->trace_iter = -1;
+    a->trace_steps = 0;
     int per_sm = 0;
     psf_status st = cuda_status(
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_apply_kernel<KIND>, kMgThreads, smem), "occupancy");
@@ -1489,11 +2071,30 @@ static psf_status mg_apply_t(Ctx *c, const double *r, float *r32, float *xo, con
         const long long need = (c->nnodes + kMgThreads - 1) / kMgThreads;
         if (blocks > need) blocks = (int)need;
         if (blocks < 1) blocks = 1;
+        size_t sm2 = smem;
+        st = mg_tiles(c, H, a, blocks, H->max_dyn, &sm2);
         void *args[] = {a, (void *)&r, (void *)&r32, (void *)&xo, (void *)&flags};
-        st = launch_coop(c, (const void *)mg_apply_kernel<KIND>, blocks, kMgThreads, args, smem);
+        if (st == PSF_OK) st = launch_coop(c, (const void *)mg_apply_kernel<KIND>, blocks, kMgThreads, args, sm2);
     }
     delete a;
     return st;
+}
+
+__global__ void widen_kernel(long long n, const float *__restrict__ a, double *__restrict__ b) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        b[t] = (double)a[t];
+}
+
+psf_status mg_apply(Ctx *c, const double *r, float *r32, float *xo, const int *flags);
+
+// z = |r| V(r / |r|) for a nodal r (fixed dofs zero): one V-cycle of the current design's
+// hierarchy, the preconditioner of PSF_SOLVE_IR_MG_F32 on its own
+psf_status mg_precondition(Ctx *c, const double *r, double *z) {
+    PSF_CHECK(mg_prepare(c));
+    PSF_CHECK(mg_apply(c, r, c->w32[0], c->w32[1], nullptr));
+    (widen_kernel<<<grid_for(c->ndofs, 256, 65536), 256, 0, c->stream>>>(c->ndofs, c->w32[1], z), note_launch());
+    PSF_CUDA(cudaGetLastError());
+    return PSF_OK;
 }
 
 psf_status mg_apply(Ctx *c, const double *r, float *r32, float *xo, const int *flags) {
