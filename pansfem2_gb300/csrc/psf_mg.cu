@@ -1829,10 +1829,13 @@ static void mg_smoother(MgFcgArgs *a) {
 }
 
 // Tiles of the fused grid levels for a launch of `blocks` blocks: per level the tile grid
-// (at most one tile per block) whose grown tile (two rings) is smallest; a level is fused
-// when that grown tile holds at most 1.35x (level 0) or 3x (coarser levels, whose phases
-// are short and barrier-bound) the own nodes.  PSF_MG_FUSE=0 runs every level in three
-// phases, =2 fuses every grid level.
+// (at most one tile per block) whose grown tile (two rings) is smallest.  In 2D every grid
+// level is fused (1025 x 513-node MBB: 209.5 us per FCG iteration, 221.2 us with the
+// 65 x 33-node level in three phases, 270 us with none fused; 513 x 513-node heat sink: 105,
+// 113 and 136 us); in 3D, where the rings are thicker in proportion, a level is fused when its
+// grown tile holds at most 1.35x (level 0) or 3x (coarser levels) the own nodes (65 x 33 x 33
+// nodes: 245 us either way, 254 us with every level fused).  PSF_MG_FUSE=0 runs every level in
+// three phases, =2 fuses every grid level, =3 applies the size rule in 2D too.
 // The buffers of a fused level go to dynamic shared memory, after block 0's levels
 // (*smem bytes on entry, the launch's total on return), where both fit in max_dyn bytes.
 static psf_status mg_tiles(Ctx *c, MgHier *H, MgFcgArgs *a, int blocks, size_t max_dyn, size_t *smem) {
@@ -1864,7 +1867,8 @@ static psf_status mg_tiles(Ctx *c, MgHier *H, MgFcgArgs *a, int blocks, size_t m
                 }
         const long long s0 = (N[0] + bt[0] - 1) / bt[0], s1 = (N[1] + bt[1] - 1) / bt[1], s2 = (N[2] + bt[2] - 1) / bt[2];
         const double ratio = (double)best / (double)(s0 * s1 * s2);
-        const bool f = mode == 0 ? false : (mode == 2 ? true : ratio <= (l == 0 ? 1.35 : 3.0));
+        const bool by_size = ratio <= (l == 0 ? 1.35 : 3.0);
+        const bool f = mode == 0 ? false : (mode == 2 || (mode == 1 && !is3d) ? true : by_size);
         a->fuse[l] = f ? 1 : 0;
         a->tg[l][0] = bt[0]; a->tg[l][1] = bt[1]; a->tg[l][2] = bt[2];
         a->ts[l][0] = (int)s0; a->ts[l][1] = (int)s1; a->ts[l][2] = (int)s2;

@@ -60,9 +60,9 @@ def test_fused_cycle_is_bit_identical(gpu, name):
         prob.setup_bc()
         prob.assemble(E)
         r = np.random.default_rng(1).standard_normal(prob.nfree)
-        z = {m: with_mode(m, lambda: prob.mg_precondition(r)) for m in (0, 1, 2)}
+        z = {m: with_mode(m, lambda: prob.mg_precondition(r)) for m in (0, 1, 2, 3)}
     assert np.all(np.isfinite(z[0])) and np.linalg.norm(z[0]) > 0
-    for m in (1, 2):
+    for m in (1, 2, 3):
         assert np.array_equal(z[m], z[0]), (m, float(np.max(np.abs(z[m] - z[0]))))
 
 
