@@ -222,8 +222,7 @@ __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF 
         L0Gather<T::nd> g;
         l0_gather<KIND>(L, ld, i, j, g);
         l0_compute<KIND>(Ke, g, y);
-        return;
-    }
+    } else {
 #pragma unroll
     for (int ci = 0; ci < 2; ci++)
 #pragma unroll
@@ -252,6 +251,7 @@ __device__ __forceinline__ void apply_node_f(const MgLev &L, int lev, const KeF 
                     y[a] += Ee * acc;
                 }
             }
+    }
 }
 
 template <int KIND>
@@ -1007,12 +1007,40 @@ __device__ bool up_fused(const MgFcgArgs &A, int l, bool tr, bool barrier, ON on
     return true;
 }
 
+// Block 0's part of the cycle: the levels from lsmall down and back up, with block barriers.
+// When the interface level lsmall sits in shared memory its right-hand side and first sweep
+// (written by the grid phases) are copied in first and its result copied out at the end.
+template <int KIND>
+__device__ void block0_part(const MgFcgArgs &A, const Block0View &V, bool tb) {
+    const int nl = A.nlev, ls = A.lsmall;
+    const long long bt = threadIdx.x, bs = blockDim.x;
+    const bool in_smem = A.lsm <= ls;
+    if (in_smem) {
+        const MgLev &G = A.L[ls], &S = V.L[ls];
+        for (long long t = bt; t < G.ndofs; t += bs) {
+            S.b[t] = G.b[t];
+            S.x[t] = G.x[t];
+        }
+        __syncthreads();
+    }
+    for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, V.L, l, bt, bs, false, tb);
+    coarsest_solve(A, V.L, V.Ainv, bt, bs);
+    __syncthreads();
+    stamp(A, tb);
+    for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, V.L, l, bt, bs, false, tb);
+    if (in_smem) {
+        __syncthreads();
+        const MgLev &G = A.L[ls], &S = V.L[ls];
+        for (long long t = bt; t < G.ndofs; t += bs) G.x[t] = S.x[t];
+    }
+}
+
 // V(2,2)-cycle with the grid levels fused where fuse[l] is set (the others run as three
 // phases each); on(q, x) sees the level-0 result of every dof this thread wrote, with no
 // barrier after the last sweep (the caller's reduction follows).
 template <int KIND, class ON>
 __device__ bool vcycle_fused(const MgFcgArgs &A, const Block0View &V, long long tid, long long stride, bool tr, ON on) {
-    const int nl = A.nlev, ls = A.lsmall;
+    const int ls = A.lsmall;
     for (int l = 0; l < ls; l++) {
         if (A.fuse[l]) {
             if (!down_fused<KIND>(A, l, tr)) return false;
@@ -1020,15 +1048,7 @@ __device__ bool vcycle_fused(const MgFcgArgs &A, const Block0View &V, long long 
             return false;
         }
     }
-    if (blockIdx.x == 0) {
-        const long long bt = threadIdx.x, bs = blockDim.x;
-        const bool tb = tr && A.trace_steps;
-        for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, V.L, l, bt, bs, false, tb);
-        coarsest_solve(A, V.L, V.Ainv, bt, bs);
-        __syncthreads();
-        stamp(A, tb);
-        for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, V.L, l, bt, bs, false, tb);
-    }
+    if (blockIdx.x == 0) block0_part<KIND>(A, V, tr && A.trace_steps);
     if (!grid_barrier(A.gs, A.partials)) return false;
     stamp(A, tr);
     auto none = [](long long, float) {};
@@ -1055,16 +1075,10 @@ __device__ bool vcycle_fused(const MgFcgArgs &A, const Block0View &V, long long 
 
 template <int KIND>
 __device__ bool vcycle(const MgFcgArgs &A, const Block0View &V, long long tid, long long stride, bool tr) {
-    const int nl = A.nlev, ls = A.lsmall;
+    const int ls = A.lsmall;
     for (int l = 0; l < ls; l++)
         if (!down_level<KIND>(A, A.L, l, tid, stride, true, tr)) return false;
-    if (blockIdx.x == 0) {
-        const long long bt = threadIdx.x, bs = blockDim.x;
-        for (int l = ls; l < nl - 1; l++) down_level<KIND>(A, V.L, l, bt, bs, false, false);
-        coarsest_solve(A, V.L, V.Ainv, bt, bs);
-        __syncthreads();
-        for (int l = nl - 2; l >= ls; l--) up_level<KIND>(A, V.L, l, bt, bs, false, false);
-    }
+    if (blockIdx.x == 0) block0_part<KIND>(A, V, false);
     if (!grid_barrier(A.gs, A.partials)) return false;
     stamp(A, tr);
     for (int l = ls - 1; l >= 0; l--)
@@ -1654,9 +1668,10 @@ static int mg_small_level(const MgHier *H) {
 
 constexpr size_t kMaxDynSmem = 200 * 1024;   // the MG kernels' dynamic shared memory limit (set once per setup)
 
-// Block 0's shared-memory levels: from the coarsest level up, as many whole levels below
-// lsmall (the interface level the grid phases write and read stays global) and the
-// coarsest inverse as fit in PSF_MG_SMEM_KB (default 160) KB of dynamic shared memory.
+// Block 0's shared-memory levels: from the coarsest level up, as many whole levels from
+// lsmall on and the coarsest inverse as fit in PSF_MG_SMEM_KB (default 160) KB of dynamic
+// shared memory.  The interface level lsmall, which the grid phases write and read in global
+// memory, is copied in and out around block 0's part of the cycle.
 // Fills a->lsm, a->smo, a->smo_ainv; returns the bytes.
 static size_t mg_block0_layout(const Ctx *c, const MgHier *H, MgFcgArgs *a) {
     const int nd = c->ndof;
@@ -1675,8 +1690,12 @@ static size_t mg_block0_layout(const Ctx *c, const MgHier *H, MgFcgArgs *a) {
     size_t total = ainv;
     if (total > budget) return 0;
     int lsm = H->nlev;
-    // level lsmall itself stays in global memory: the grid phases write and read it
-    for (int l = H->nlev - 1; l > a->lsmall; l--) {
+    // the interface level lsmall joins them only when PSF_MG_SMEM_IFACE=1: its 80 KB of
+    // stencil at 1024x512 cost the grid phases more L1 than block 0 gains (236.6 vs 209.5 us
+    // per FCG iteration)
+    const char *ei = getenv("PSF_MG_SMEM_IFACE");
+    const int lo = (ei && *ei == '1') ? a->lsmall : a->lsmall + 1;
+    for (int l = H->nlev - 1; l >= lo && l >= 1; l--) {
         if (total + level_bytes(l) > budget) break;
         total += level_bytes(l);
         lsm = l;
@@ -1845,6 +1864,8 @@ static psf_status mg_tiles(Ctx *c, MgHier *H, MgFcgArgs *a, int blocks, size_t m
     long long half = 0, half_sm = 0;
     const size_t off = (*smem + 15) & ~(size_t)15;
     const size_t avail = max_dyn > off ? max_dyn - off : 0;
+    const char *ets = getenv("PSF_MG_TILE_SMEM");
+    const bool tile_smem = !(ets && *ets == '0');   // 0: the tile buffers in global memory
     for (int l = 0; l < kMaxLev; l++) {
         a->fuse[l] = 0;
         a->tsm[l] = 0;
@@ -1874,7 +1895,7 @@ static psf_status mg_tiles(Ctx *c, MgHier *H, MgFcgArgs *a, int blocks, size_t m
         a->ts[l][0] = (int)s0; a->ts[l][1] = (int)s1; a->ts[l][2] = (int)s2;
         if (!f) continue;
         const long long need = ((best * c->ndof) + 3) & ~3ll;   // floats per buffer, 16-byte multiple
-        if ((size_t)need * 2 * sizeof(float) <= avail) {
+        if (tile_smem && (size_t)need * 2 * sizeof(float) <= avail) {
             a->tsm[l] = 1;
             half_sm = std::max(half_sm, need);
         } else {
