@@ -534,9 +534,14 @@ __device__ __forceinline__ double filt(const Args &A, const Inst &I, const doubl
 }
 
 // rho = filter(s), E = kmin + (k0 - kmin) rho^p, g = sum(rho) / (vf n^2) - 1
+// a converged instance (IsConvergence held at an earlier update) keeps its design and its
+// fields, as the samples leave their loop: every phase returns at once for it
+__device__ __forceinline__ bool frozen(const Args &A, int idx) { return A.out[(long long)idx * kOut + O_DONE] != 0.0; }
+
 __global__ void __launch_bounds__(kThreads) filter_moduli_batch(const __grid_constant__ Args A) {
     __shared__ double sm[32];
     const Team T = team(A);
+    if (frozen(A, T.idx)) return;
     const Inst &I = A.inst[T.idx];
     int par = 0;
     const int n = I.n;
@@ -564,6 +569,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
     extern __shared__ double dyn[];
     double *sm = dyn;            // 32 doubles of reduction space, then the coarse inverse workspace
     const Team T = team(A);
+    if (frozen(A, T.idx)) return;
     const Inst &I = A.inst[T.idx];
     int par = 0;
     const int idx = T.idx;
@@ -688,6 +694,7 @@ __global__ void __launch_bounds__(kThreads) solve_batch(const __grid_constant__ 
 __global__ void __launch_bounds__(kThreads) sens_batch(const __grid_constant__ Args A) {
     __shared__ double sm[32];
     const Team T = team(A);
+    if (frozen(A, T.idx)) return;
     const Inst &I = A.inst[T.idx];
     int par = 0;
     const int n = I.n;
