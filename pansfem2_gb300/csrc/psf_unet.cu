@@ -4,12 +4,13 @@
 //
 // Convolutions (3x3, stride 1 or 2, and the transposed forms the backward pass
 // needs) are implicit GEMMs on the 5th-generation tensor cores: one CTA of 128
-// threads computes a 128-pixel x N-channel tile whose fp32 accumulator lives in
+// threads computes an 8 x 16-pixel x N-channel tile whose fp32 accumulator lives in
 // tensor memory.  Each thread stages its pixel's im2col row (64 K values per
 // chunk) into shared memory in the no-swizzle K-major core-matrix layout, the
 // weights arrive pre-packed in the same layout, one thread issues four
 // tcgen05.mma (K = 16 each) per chunk and commits them to the chunk's mbarrier
-// (two stages, so staging chunk s+1 overlaps the MMAs of chunk s), and the
+// (two stages; the loads of chunk s+1 go out into registers while chunk s is
+// stored and its MMAs issued), and the
 // epilogue reads the accumulator with tcgen05.ld, adds the bias, applies ReLU
 // and stores bf16 (or fp32, optionally accumulating, for gradients).  Every
 // mbarrier wait is bounded (about one second), after which the kernel records
@@ -183,6 +184,9 @@ __device__ __forceinline__ bool tap_src(int mode, int oy, int ox, int dy, int dx
     return yi >= 0 && yi < hin && xi >= 0 && xi < win;
 }
 
+constexpr int kTileH = 8, kTileW = 16;   // output pixels of a CTA's tile (128 = the MMA's M)
+constexpr int kConvCarveout = 75;
+
 template <int N>
 __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ ConvArgs a) {
     using S = ConvSmem<N>;
@@ -203,26 +207,31 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(meta + 16);
 
-    const long long P = (long long)a.batch * a.hout * a.wout;
-    const long long p = (long long)blockIdx.x * 128 + tid;
-    const bool pv = p < P;
-    int b = 0, oy = 0, ox = 0;
-    if (pv) {
-        ox = (int)(p % a.wout);
-        const long long q = p / a.wout;
-        oy = (int)(q % a.hout);
-        b = (int)(q / a.hout);
-    }
+    // the CTA's tile: kTileH x kTileW output pixels of one image (2D, so that the 3x3 taps of
+    // the tile's pixels share a small halo in L1); thread tid takes pixel (tid / kTileW,
+    // tid % kTileW) of it, rows past the image edge are zero and not stored
+    const int tiles_x = (a.wout + kTileW - 1) / kTileW, tiles_y = (a.hout + kTileH - 1) / kTileH;
+    long long tq = blockIdx.x;
+    const int tx = (int)(tq % tiles_x);
+    tq /= tiles_x;
+    const int ty = (int)(tq % tiles_y);
+    const int b = (int)(tq / tiles_y);
+    const int oy = ty * kTileH + tid / kTileW, ox = tx * kTileW + tid % kTileW;
+    const bool pv = oy < a.hout && ox < a.wout;
+    const long long p = ((long long)b * a.hout + oy) * a.wout + ox;
     const bf16 *xb = a.x + (size_t)b * a.hin * a.win * a.x_cs + a.x_c0;
     const int K = 9 * a.cin;
     constexpr uint32_t IDESC = idesc_bf16(128, N);
-    bool ok = true;
-    for (int s = 0; s < a.nchunks; s++) {
-        const int st = s & 1;
-        uint8_t *As = smem + st * S::STAGE;
-        uint8_t *Bs = As + S::A;
-        if (s >= 2) ok = mbar_wait(st ? bar1 : bar0, ((s >> 1) - 1) & 1) && ok;
-        // A: this thread's row, 8 core-matrix columns of 8 K values (one tap, 8 channels each)
+    // Chunk s + 1 is loaded into registers while chunk s is stored and its MMAs issued, so one
+    // L2 round trip per chunk (A gather and B together) overlaps the rest of the step.
+    // A: this thread's row, 8 core-matrix columns of 8 K values (one tap, 8 channels each);
+    // B: the packed chunk, already in core-matrix order, N / 16 uint4 per thread.
+    constexpr int kBPer = N / 16;
+    // register sets in flight: two for the narrow layers (chunk s + 2 loads while chunk s is
+    // stored), one where two sets of B would cost too many registers
+    constexpr int kAhead = N <= 64 ? 2 : 1;
+    uint4 ra[kAhead][8], rb[kAhead][kBPer];
+    auto load_chunk = [&](int s, uint4(&va)[8], uint4(&vb)[kBPer]) {
 #pragma unroll
         for (int kc = 0; kc < 8; kc++) {
             const int k = s * 64 + kc * 8;
@@ -233,14 +242,28 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
                 if (tap_src(a.mode, oy, ox, tap / 3 - 1, tap % 3 - 1, a.hin, a.win, yi, xi))
                     v = __ldg(reinterpret_cast<const uint4 *>(xb + ((size_t)yi * a.win + xi) * a.x_cs + ci));
             }
-            *reinterpret_cast<uint4 *>(As + (kc * 128 + tid) * 16) = v;
+            va[kc] = v;
         }
-        // B: the packed chunk is already in core-matrix order
         const uint4 *wsrc = reinterpret_cast<const uint4 *>(a.w + (size_t)s * N * 64);
-        for (int i = tid; i < N * 8; i += 128) reinterpret_cast<uint4 *>(Bs)[i] = __ldg(wsrc + i);
+#pragma unroll
+        for (int j = 0; j < kBPer; j++) vb[j] = __ldg(wsrc + tid + 128 * j);
+    };
+    bool ok = true;
+    // chunk s: wait for the MMAs of chunk s - 2 (its stage), store its registers, send out the
+    // loads of chunk s + kAhead into the same registers, then one thread issues the MMAs
+    auto step = [&](int s, uint4(&va)[8], uint4(&vb)[kBPer]) {
+        const int st = s & 1;
+        uint8_t *As = smem + st * S::STAGE;
+        uint8_t *Bs = As + S::A;
+        if (s >= 2) ok = mbar_wait(st ? bar1 : bar0, ((s >> 1) - 1) & 1) && ok;
+#pragma unroll
+        for (int kc = 0; kc < 8; kc++) *reinterpret_cast<uint4 *>(As + (kc * 128 + tid) * 16) = va[kc];
+#pragma unroll
+        for (int j = 0; j < kBPer; j++) reinterpret_cast<uint4 *>(Bs)[tid + 128 * j] = vb[j];
+        if (s + kAhead < a.nchunks) load_chunk(s + kAhead, va, vb);
         fence_async_smem();
         ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
+        if (!ok) return;
         if (tid == 0) {
             tc_fence_after();
             const uint32_t a0 = sbase + st * S::STAGE, b0 = a0 + S::A;
@@ -251,6 +274,16 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
                 tc_mma(tmem, ad, bd, IDESC, (s > 0 || kk > 0) ? 1u : 0u);
             }
             tc_commit(st ? bar1 : bar0);
+        }
+    };
+#pragma unroll
+    for (int h = 0; h < kAhead; h++)
+        if (h < a.nchunks) load_chunk(h, ra[h], rb[h]);
+    for (int s = 0; s < a.nchunks && ok; s += kAhead) {
+#pragma unroll
+        for (int h = 0; h < kAhead; h++) {
+            if (s + h >= a.nchunks || !ok) break;
+            step(s + h, ra[h], rb[h]);
         }
     }
     if (ok) {
@@ -308,10 +341,17 @@ static cudaError_t launch_conv_n(const ConvArgs &a, cudaStream_t st) {
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(conv_mma_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES);
         if (e != cudaSuccess) return e;
+        // shared-memory share of the unified L1 (percent; PSF_CONV_CARVEOUT overrides): fewer
+        // resident CTAs but more L1 for the tap gathers.  A learned FCG solve at 1025 x 513
+        // nodes took 22.3 ms with 75, 25.1 with the driver's choice and with 100, 30.2 with 50.
+        const char *cv = getenv("PSF_CONV_CARVEOUT");
+        e = cudaFuncSetAttribute(conv_mma_kernel<N>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cv && *cv ? atoi(cv) : kConvCarveout);
+        if (e != cudaSuccess) return e;
         attr = true;
     }
-    const long long P = (long long)a.batch * a.hout * a.wout;
-    const unsigned grid = (unsigned)((P + 127) / 128);
+    const long long tiles = (long long)a.batch * ((a.hout + kTileH - 1) / kTileH) * ((a.wout + kTileW - 1) / kTileW);
+    const unsigned grid = (unsigned)tiles;
     if (grid == 0) return cudaSuccess;
     (conv_mma_kernel<N><<<grid, 128, S::BYTES, st>>>(a), ::psf::note_launch());
     return cudaGetLastError();
