@@ -177,11 +177,23 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
             if (ctl != 1) { capped = ctl == 2; break; }
         }
         const D lamD = get(0), epsD = get(2);
-        // ---- phase 1: G, 1/Dx, deltilx and the sums of the Newton system + KKT norm at w
+        // ---- phase 1: G, 1/Dx, deltilx and the sums of the Newton system + KKT norm at w.
+        //      From the second step on it first takes the previous step's accepted trial point,
+        //      x += tau dx (and the same for the multipliers), in the expressions of the trial.
+        const bool pend = l > 0;
+        const D tauA = get(10);
         D a0 = dw::from_float(0.f), a1 = a0, a2 = a0, a3 = a0;
         for (long long j = tid; j < n; j += stride) {
-            const D x = dw::ld(X, j), gsi = dw::ld(GS, j), ita = dw::ld(IT, j), P1 = dw::ld(p1, j),
-                    Q1 = dw::ld(q1, j);
+            D x = dw::ld(X, j), gsi = dw::ld(GS, j), ita = dw::ld(IT, j);
+            if (pend) {
+                x = dw::add(x, dw::mul(tauA, dw::ld(dX, j)));
+                gsi = dw::add(gsi, dw::mul(tauA, dw::ld(dGS, j)));
+                ita = dw::add(ita, dw::mul(tauA, dw::ld(dIT, j)));
+                dw::st(X, j, x);
+                dw::st(GS, j, gsi);
+                dw::st(IT, j, ita);
+            }
+            const D P1 = dw::ld(p1, j), Q1 = dw::ld(q1, j);
             const D plj = dw::add(dw::ld(p0, j), dw::mul(lamD, P1)), qlj = dw::add(dw::ld(q0, j), dw::mul(lamD, Q1));
             const D xa = dw::sub(x, dw::ld(al, j)), bx = dw::sub(dw::ld(be, j), x);
             const D ia = dw::rcp(xa), ib = dw::rcp(bx);
@@ -333,23 +345,19 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
             if (s_ctl[1]) { bail(); return; }
             if (s_ctl[0]) break;
         }
-        // ---- accept the last trial point (the same double-word expressions as the trial)
+        // ---- accept the last trial point: its step length goes to the next phase 1 (or to the
+        //      final pass), which applies it element by element with the trial's expressions
         if (lead) {
             put(10, tau_used);
             y = yp; lam = lp; mu = mp; s = sp; z = zp; zeta = zetap;
             if (dw1 < 0.9 * eps) eps *= 0.1;
         }
-        __syncthreads();
-        {
-            const D tauD = get(10);
-            for (long long j = tid; j < n; j += stride) {
-                dw::st(X, j, dw::add(dw::ld(X, j), dw::mul(tauD, dw::ld(dX, j))));
-                dw::st(GS, j, dw::add(dw::ld(GS, j), dw::mul(tauD, dw::ld(dGS, j))));
-                dw::st(IT, j, dw::add(dw::ld(IT, j), dw::mul(tauD, dw::ld(dIT, j))));
-            }
-        }
+        __syncthreads();   // every thread has read the backtracking's s_ctl before the lead rewrites it
     }
-    // ---- history, asymptotes and the new design (MMA.h:413-418; CONLIN.h:361-364)
+    // ---- history, asymptotes and the new design (MMA.h:413-418; CONLIN.h:361-364), with the
+    //      last accepted step applied to x
+    const bool pend = l > 0;
+    const D tauA = get(10);
     for (long long j = tid; j < n; j += stride) {
         if constexpr (!kConlin) {
             A.xkm2[j] = A.xkm1[j];
@@ -357,7 +365,9 @@ __global__ void __launch_bounds__(256) mma_dw_kernel(MmaDwArgs A) {
             A.L[j] = A.Lnew[j];
             A.U[j] = A.Unew[j];
         }
-        A.xk[j] = dw::to_double(dw::ld(X, j));
+        D x = dw::ld(X, j);
+        if (pend) x = dw::add(x, dw::mul(tauA, dw::ld(dX, j)));
+        A.xk[j] = dw::to_double(x);
     }
     if (tid == 0) {
         A.out[0] = l;
