@@ -185,6 +185,7 @@ __device__ __forceinline__ bool tap_src(int mode, int oy, int ox, int dy, int dx
 }
 
 constexpr int kTileH = 8, kTileW = 16;   // output pixels of a CTA's tile (128 = the MMA's M)
+constexpr int kTapGroups = 512;          // 8-wide K groups in the per-CTA (tap, channel) table
 constexpr int kConvCarveout = 75;
 
 template <int N>
@@ -222,6 +223,17 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
     const bf16 *xb = a.x + (size_t)b * a.hin * a.win * a.x_cs + a.x_c0;
     const int K = 9 * a.cin;
     constexpr uint32_t IDESC = idesc_bf16(128, N);
+    // (tap, channel) of each 8-wide K group, computed once per CTA: the gathers then need no
+    // integer division (layers of up to kTapGroups / 8 chunks; wider ones divide inline)
+    __shared__ uint32_t s_tap[kTapGroups];
+    const bool tab = a.nchunks * 8 <= kTapGroups;
+    if (tab) {
+        for (int gi = tid; gi < a.nchunks * 8; gi += 128) {
+            const int k = gi * 8, tap = k / a.cin;
+            s_tap[gi] = (uint32_t)tap | ((uint32_t)(k - tap * a.cin) << 4);
+        }
+        __syncthreads();
+    }
     // Chunk s + 1 is loaded into registers while chunk s is stored and its MMAs issued, so one
     // L2 round trip per chunk (A gather and B together) overlaps the rest of the step.
     // A: this thread's row, 8 core-matrix columns of 8 K values (one tap, 8 channels each);
@@ -237,7 +249,15 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
             const int k = s * 64 + kc * 8;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (pv && k < K) {
-                const int tap = k / a.cin, ci = k - tap * a.cin;
+                int tap, ci;
+                if (tab) {
+                    const uint32_t e = s_tap[s * 8 + kc];
+                    tap = (int)(e & 15u);
+                    ci = (int)(e >> 4);
+                } else {
+                    tap = k / a.cin;
+                    ci = k - tap * a.cin;
+                }
                 int yi, xi;
                 if (tap_src(a.mode, oy, ox, tap / 3 - 1, tap % 3 - 1, a.hin, a.win, yi, xi))
                     v = __ldg(reinterpret_cast<const uint4 *>(xb + ((size_t)yi * a.win + xi) * a.x_cs + ci));
