@@ -234,8 +234,8 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
         }
         __syncthreads();
     }
-    // Chunk s + 1 is loaded into registers while chunk s is stored and its MMAs issued, so one
-    // L2 round trip per chunk (A gather and B together) overlaps the rest of the step.
+    // The next chunks are loaded into registers while chunk s is stored and its MMAs issued, so
+    // the L2 round trips of the gathers (A and B together) overlap the rest of the steps.
     // A: this thread's row, 8 core-matrix columns of 8 K values (one tap, 8 channels each);
     // B: the packed chunk, already in core-matrix order, N / 16 uint4 per thread.
     constexpr int kBPer = N / 16;
@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
         for (int j = 0; j < kBPer; j++) vb[j] = __ldg(wsrc + tid + 128 * j);
     };
     bool ok = true;
+    int issued = 0;   // chunks whose MMAs were issued (the same in every thread)
     // chunk s: wait for the MMAs of chunk s - 2 (its stage), store its registers, send out the
     // loads of chunk s + kAhead into the same registers, then one thread issues the MMAs
     auto step = [&](int s, uint4(&va)[8], uint4(&vb)[kBPer]) {
@@ -284,6 +285,7 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
         fence_async_smem();
         ok = __syncthreads_and(ok) != 0;
         if (!ok) return;
+        issued = s + 1;
         if (tid == 0) {
             tc_fence_after();
             const uint32_t a0 = sbase + st * S::STAGE, b0 = a0 + S::A;
@@ -346,8 +348,10 @@ __global__ void __launch_bounds__(128) conv_mma_kernel(const __grid_constant__ C
                     if (j < n) dst[j] = (a.accumulate ? dst[j] : 0.0f) + v[j];
             }
         }
-    } else if (tid == 0) {
-        atomicExch(a.err, 1);
+    } else {
+        if (tid == 0) atomicExch(a.err, 1);
+        // a wait gave up: wait (bounded again) for the MMAs already issued before TMEM is freed
+        if (issued > 0) mbar_wait(((issued - 1) & 1) ? bar1 : bar0, ((issued - 1) >> 1) & 1);
     }
     tc_fence_before();
     __syncthreads();
