@@ -367,7 +367,7 @@ static cudaError_t launch_conv_n(const ConvArgs &a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         // shared-memory share of the unified L1 (percent; PSF_CONV_CARVEOUT overrides): fewer
         // resident CTAs but more L1 for the tap gathers.  A learned FCG solve at 1025 x 513
-        // nodes took 22.3 ms with 75, 25.1 with the driver's choice and with 100, 30.2 with 50.
+        // nodes took 22.3 ms with 75, 25.1 with the CUDA driver's default and with 100, 30.2 with 50.
         const char *cv = getenv("PSF_CONV_CARVEOUT");
         e = cudaFuncSetAttribute(conv_mma_kernel<N>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cv && *cv ? atoi(cv) : kConvCarveout);
